@@ -1,0 +1,382 @@
+"""Benchmark: PSV forward, heterogeneous, 4096 x 4096, nt = 4000 (the HBM-bound
+headline workload), in Gcell-updates/s on one GB300.
+
+A step is one complete forward simulation (4000 time steps of the fused
+velocity+stress kernel over 16.8 M cells, plus receiver traces).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nt NT]
+
+value  device throughput: model, sources and receivers resident in HBM; CUDA
+       events on the engine's stream around K forward runs.
+e2e    the reference-facing C ABI with host buffers: per step
+       seiswg_solver_new (INI text + model files in a VFS, uploaded to the GPU)
+       + seiswg_solver_run_forward (traces copied back as .npy bytes).
+--impl reference  the CPU oracle (a restatement of the reference's WGSL
+       kernels; the WGSL itself has no CPU path here) on all host cores, on a
+       bounded sample of the same workload.
+N > 1: independent replicas, one per GPU (shots are independent; no
+       collective on the data path); value = total cell-updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Gcell-updates/s"
+BYTES_PER_CELL = {"sh": 32, "psv": 52, "spin": 96}  # algorithmic bytes per cell-update
+
+
+# ---------------------------------------------------------------------------
+# Workload: PSV forward, heterogeneous, 4096^2 (seeded synthetic model)
+# ---------------------------------------------------------------------------
+def make_workload(nx=4096, nz=4096, nt=4000, seed=0):
+    from scipy.ndimage import gaussian_filter
+
+    dx = dz = 5.0
+    rng = np.random.default_rng(seed)
+    p = gaussian_filter(rng.standard_normal((nx, nz)).astype(np.float32), 20.0)
+    p *= np.float32(0.05 / np.abs(p).max())
+    depth_km = (np.arange(nz, dtype=np.float32) * np.float32(dz) / np.float32(1000.0))[None, :]
+    vp = ((np.float32(2000.0) + np.float32(600.0) * depth_km) * (np.float32(1.0) + p)).astype(np.float32)
+    vs = (vp / np.float32(math.sqrt(3.0))).astype(np.float32)
+    rho = (np.float32(310.0) * vp ** np.float32(0.25)).astype(np.float32)
+    dt = float(np.float32(0.3 * dx / float(vp.max())))
+    w = 40
+    src = dict(i=nx // 2, j=w + 10, f0=15.0, t0=0.1, ang=90.0, amp=1.0e10)
+    rec_i = np.round(np.linspace(0, nx - 1, 256)).astype(np.int32)  # 256 receivers on the top row
+    rec_j = np.zeros(256, np.int32)
+    return dict(nx=nx, nz=nz, nt=nt, dx=dx, dz=dz, dt=dt, vp=vp, vs=vs, rho=rho, w=w, alpha=0.015, src=src,
+                rec_i=rec_i, rec_j=rec_j)
+
+
+def workload_config(W, nt):
+    return {"workload": f"PSV forward, heterogeneous {W['nx']}x{W['nz']}, nt={nt}",
+            "grid": [W["nx"], W["nz"]], "nt": nt, "dx_m": W["dx"], "dt_s": W["dt"],
+            "physics": "psv", "abs_width": W["w"], "receivers": int(W["rec_i"].size),
+            "source": "Ricker f0=15 Hz t0=0.1 s angle 90 at (nx/2, w+10)",
+            "model": "vp=2000+600*depth_km, Gaussian-filtered (sigma 20) +-5% perturbation, seed 0; "
+                     "vs=vp/sqrt(3); rho=310*vp^0.25",
+            "l2": "state+model 8 x 67 MB > 129 MB L2 (no flush needed)",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def _traffic(kernel, nx, nz):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, scaled
+    to nx*nz cells; None when no capture is recorded."""
+    path = os.path.join(ROOT, "profiles", "traffic.txt")
+    try:
+        for ln in open(path):
+            f = ln.split()
+            if len(f) >= 3 and f[0] == kernel:
+                return float(f[1]) * (nx * nz) / float(f[2])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_oracle_rate(W, nt_sample):
+    """FP32 oracle (reference operation order, OpenMP) on the full grid for
+    nt_sample steps; returns (Gcell/s, seconds, threads)."""
+    from oracle import oracle as O
+
+    s = O.Setup(W["nx"], W["nz"], nt_sample, W["dx"], W["dz"], W["dt"], sh=False, psv=True,
+                abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=W["w"],
+                abs_alpha=W["alpha"])
+    sr = W["src"]
+    stf = O.stf_table([(0, 0, sr["f0"], sr["t0"], sr["ang"], sr["amp"])], nt_sample, W["dt"], 32)
+    o = O.FD2DOracle(s, [sr["i"] * W["nz"] + sr["j"]], stf, W["rec_i"] * W["nz"] + W["rec_j"], 32)
+    o.set_field("LAM", W["vp"])
+    o.set_field("MU", W["vs"])
+    o.set_field("RHO", W["rho"])
+    o.init_model()
+    t0 = time.perf_counter()
+    o.run_forward(-1)
+    dtm = time.perf_counter() - t0
+    return W["nx"] * W["nz"] * nt_sample / dtm / 1e9, dtm, O.num_threads()
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    W = make_workload(nx=args.grid, nz=args.grid, nt=args.nt)
+    rates = []
+    for _ in range(args.warmup):
+        cpu_oracle_rate(W, 2)
+    for _ in range(args.steps):
+        r, dtm, thr = cpu_oracle_rate(W, args.ref_sample)
+        rates.append(r)
+    val = float(np.median(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dtm * 1e3 * args.nt / args.ref_sample,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(W, args.nt),
+        "cpu_baseline": {"value": val, "unit": METRIC, "cores": thr, "kind": "port",
+                         "sample": f"full {W['nx']}x{W['nz']} grid, {args.ref_sample} of {args.nt} steps per "
+                                   f"step (FP32 oracle restating fd2d.wgsl, OpenMP)"},
+        "e2e": {"value": val, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import seiswg_gb300 as sw
+
+    dist = world > 1
+    if dist:
+        import torch
+        import torch.distributed as tdist
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    W = make_workload(nx=args.grid, nz=args.grid, nt=args.nt)
+    nx, nz, nt = W["nx"], W["nz"], W["nt"]
+    sr = W["src"]
+    stf = sw.ricker(nt, W["dt"], sr["f0"], sr["t0"], sr["ang"], sr["amp"])[:, None, :]
+
+    # ---- device-resident throughput --------------------------------------
+    sim = sw.Sim(nx, nz, nt, W["dx"], W["dz"], W["dt"], sh=False, psv=True, abs_left=True, abs_right=True,
+                 abs_bottom=True, abs_top=True, abs_width=W["w"], abs_alpha=W["alpha"])
+    if args.chunk_rows:
+        sim.set_option("chunk_rows", args.chunk_rows)
+    sim.upload_model("vp", W["vp"])
+    sim.upload_model("vs", W["vs"])
+    sim.upload_model("rho", W["rho"])
+    sim.prepare()
+    sim.set_sources([sr["i"]], [sr["j"]], stf)
+    sim.set_receivers(W["rec_i"], W["rec_j"])
+    stream = torch.cuda.ExternalStream(sim.stream)
+    for _ in range(args.warmup):
+        sim.forward(0, sync=False)
+    sim.synchronize()
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = sim.launches
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.forward(0, sync=False)
+        ev1.record(stream)
+        ev1.synchronize()
+    sim.synchronize()
+    torch.cuda.synchronize()
+    launches = sim.launches - l0
+    ms = ev0.elapsed_time(ev1)
+    tr = sim.traces()
+    finite = bool(np.isfinite(tr).all())
+    sim.close()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+        tdist.barrier()
+
+    cells = float(nx) * nz * nt
+    ms_per_step = ms / args.steps
+    value = world * cells * args.steps / (ms / 1e3) / 1e9
+    # Dominant kernel: one psv step launch per time step; its average duration
+    # is the timed region over nt launches (memsets and the trace kernel are
+    # < 0.1 % of it; see the launch list under profiles/).
+    launch_s = ms_per_step / 1e3 / nt
+    achieved = BYTES_PER_CELL["psv"] * nx * nz / launch_s / 1e9
+    peak, peak_kind = _peaks()
+    traffic = _traffic("psv_step_kernel", nx, nz)
+
+    # ---- end to end through the reference-facing C ABI ---------------------
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(args, W, stf)
+        if dist:
+            t = torch.tensor([e2e["seconds"]], device="cuda")
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            e2e["seconds"] = float(t.item())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r, dtm, thr = cpu_oracle_rate(W, args.ref_sample)
+        cpu = {"value": r, "unit": METRIC, "cores": thr, "kind": "port",
+               "sample": f"full {nx}x{nz} grid, {args.ref_sample} of {nt} steps (FP32 oracle restating "
+                         f"fd2d.wgsl, OpenMP), {dtm:.1f} s"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(W, nt),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "psv_step_kernel", "bytes_per_cell_update": BYTES_PER_CELL["psv"],
+                         "peak_source": peak_kind},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "traces_finite": finite,
+        }
+        if e2e:
+            line["e2e"] = {"value": world * cells * args.e2e_steps / e2e["seconds"] / 1e9, "unit": METRIC,
+                           "h2d_bytes_per_step": e2e["h2d"], "d2h_bytes_per_step": e2e["d2h"],
+                           "api": "seiswg_config_load_str + seiswg_solver_new + seiswg_solver_run_forward"}
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+
+
+def run_e2e(args, W, stf):
+    """Reference-facing API with host buffers: INI + model files in a VFS."""
+    import seiswg_gb300 as sw
+
+    nx, nz, nt = W["nx"], W["nz"], W["nt"]
+    x = np.repeat(np.arange(nx, dtype=np.float32) * np.float32(W["dx"]), nz)
+    z = np.tile(np.arange(nz, dtype=np.float32) * np.float32(W["dz"]), nx)
+
+    def mbin(a):
+        a = np.ascontiguousarray(a, np.float32).reshape(-1)
+        return np.array([a.size], np.int32).tobytes() + a.tobytes()
+
+    vfs = sw.Vfs({"m/proc000000_x.bin": mbin(x), "m/proc000000_z.bin": mbin(z),
+                  "m/proc000000_vp.bin": mbin(W["vp"]), "m/proc000000_vs.bin": mbin(W["vs"]),
+                  "m/proc000000_rho.bin": mbin(W["rho"])})
+    sr = W["src"]
+    vfs["sources.dat"] = (f"{sr['i'] * W['dx']} {sr['j'] * W['dz']} 0 {sr['f0']} {sr['t0']} {sr['ang']} "
+                          f"{sr['amp']}\n").encode()
+    vfs["stations.dat"] = "".join(f"{i * W['dx']} {j * W['dz']}\n" for i, j in
+                                  zip(W["rec_i"], W["rec_j"])).encode()
+    ini = (f"[workflow]\nmode = forward\n[solver]\nsh = no\npsv = yes\nnt = {nt}\ndt = {W['dt']!r}\n"
+           f"abs_top = yes\nabs_bottom = yes\nabs_left = yes\nabs_right = yes\nabs_width = {W['w']}\n"
+           f"abs_alpha = {W['alpha']}\ncombine_sources = yes\n[path]\noutput = out\nmodel_init = m\n"
+           f"sources = sources.dat\nstations = stations.dat\n")
+    cfg = sw.Config.from_str(ini, "")
+    h2d = 3 * nx * nz * 4 + 3 * nt * 4 + 2 * 256 * 4
+    d2h = 5 * 256 * nt * 4
+
+    def one():
+        s = sw.Solver(cfg, vfs, write_files=False)
+        out = s.run_forward()
+        s.close()
+        return out
+
+    one()  # warm-up (context, allocator)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        out = one()
+    sec = time.perf_counter() - t0
+    assert any(k.endswith("ux_000000.npy") for k in out)
+    return {"seconds": sec, "h2d": h2d, "d2h": d2h}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nt", type=int, default=4000)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--ref-sample", type=int, default=40, help="oracle steps in the CPU sample")
+    ap.add_argument("--chunk-rows", type=int, default=0)
+    ap.add_argument("--grid", type=int, default=4096, help="grid edge (4096 = the headline workload)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch.distributed as tdist
+
+        tdist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world)
+    finally:
+        if world > 1:
+            import torch.distributed as tdist
+
+            tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/*
+ * seiswg.h -- C ABI of the GB300 (sm_103a) implementation of seiswg's 2-D
+ * staggered-grid finite-difference path.
+ *
+ * The reference exposes this path through its Rust host API and, one level
+ * down, through the WGSL kernel interface.  Both levels are mirrored here
+ * with plain pointers and sizes:
+ *
+ *   reference                                     this header
+ *   config::load            (src/config.rs:118)   seiswg_config_load
+ *   config::load_from_str   (src/config.rs:132)   seiswg_config_load_str
+ *   Vfs = HashMap<String, Vec<u8>> (src/solver.rs:15)   seiswg_vfs_*
+ *   Solver::new             (src/solver.rs:578)   seiswg_solver_new
+ *   Solver::run_forward     (src/solver.rs:941)   seiswg_solver_run_forward
+ *   Solver::run_adjoint     (src/solver.rs:1298)  seiswg_solver_run_adjoint
+ *   fields/idata/obs/stf bindings and the per-step kernel chain
+ *     (shaders/fd2d.wgsl:123-127, src/solver.rs:984-1044)   seiswg_sim_*
+ *   ricker                  (src/solver.rs:350)   seiswg_ricker
+ *   compute_waveform_misfit (src/solver.rs:432)   seiswg_waveform_misfit
+ *   make_npy_bytes          (src/solver.rs:270)   seiswg_npy_encode
+ *   grid inference          (src/solver.rs:646-656) seiswg_infer_grid
+ *
+ * Conventions
+ *   - Every function returns SEISWG_OK (0) or an error code; the message of
+ *     the last failure on the calling thread is seiswg_last_error().  The
+ *     reference's anyhow::Result context strings map to these messages.
+ *   - Inputs are caller-owned and copied in; outputs are written to
+ *     caller-provided buffers or to a seiswg_vfs the caller frees.
+ *   - Grids are indexed k = i*nz + j (z contiguous), as in the reference.
+ *   - One handle is used by one host thread at a time.  Device work runs on
+ *     the handle's CUDA stream (its own, or the one passed at creation).
+ */
+#ifndef SEISWG_H
+#define SEISWG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEISWG_OK 0
+#define SEISWG_EINVAL 1    /* invalid argument or input data */
+#define SEISWG_EIO 2       /* a file or VFS entry is missing or unreadable */
+#define SEISWG_ECUDA 3     /* CUDA runtime failure (no device, out of memory, launch error) */
+#define SEISWG_EINTERNAL 4
+
+/* Message of the last failed call on this thread ("" after a success). */
+const char* seiswg_last_error(void);
+const char* seiswg_version(void);
+
+/* ---- virtual file system (src/solver.rs:15, lookups :236-267) ------------ */
+typedef struct seiswg_vfs seiswg_vfs;
+seiswg_vfs* seiswg_vfs_new(void);
+void seiswg_vfs_free(seiswg_vfs* vfs);
+/* Inserts (or replaces) `key` with a copy of `len` bytes. */
+int seiswg_vfs_insert(seiswg_vfs* vfs, const char* key, const void* data, size_t len);
+/* Borrowed view of an entry; valid until the entry is replaced or freed. */
+int seiswg_vfs_get(const seiswg_vfs* vfs, const char* key, const void** data, size_t* len);
+size_t seiswg_vfs_size(const seiswg_vfs* vfs);
+/* Key of the index-th entry in sorted order, or NULL past the end. */
+const char* seiswg_vfs_key(const seiswg_vfs* vfs, size_t index);
+
+/* ---- configuration (src/config.rs) ---------------------------------------- */
+typedef struct seiswg_config seiswg_config;
+/* config::load: reads an INI file; paths resolve relative to its directory. */
+int seiswg_config_load(const char* path, seiswg_config** out);
+/* config::load_from_str: INI text with paths resolved against base_dir. */
+int seiswg_config_load_str(const char* ini_text, const char* base_dir, seiswg_config** out);
+void seiswg_config_free(seiswg_config* cfg);
+/* Reads one parsed value as text: "workflow", "solver.<key>", "path.<key>"
+ * (e.g. "solver.nt", "path.output").  Fails when the key is unset. */
+int seiswg_config_get(const seiswg_config* cfg, const char* key, char* buf, size_t buflen);
+
+/* ---- solver (src/solver.rs:194-1530) -------------------------------------- */
+typedef struct seiswg_solver seiswg_solver;
+/* Solver::new: loads the model, sources and stations (VFS first, then disk),
+ * infers the grid, builds the Ricker STF table and uploads everything. */
+int seiswg_solver_new(const seiswg_config* cfg, const seiswg_vfs* vfs, seiswg_solver** out);
+/* Native builds of the reference write outputs to disk as well as returning
+ * them (the default here too); 0 returns them only. */
+int seiswg_solver_set_write_files(seiswg_solver* s, int on);
+/* Solver::run_forward: traces (uy/ux/uz/ry/yi .npy, raw vy/vx/vz) and
+ * snapshots (proc<it>_<field>.bin, "snapshot/..." entries) into `out`. */
+int seiswg_solver_run_forward(seiswg_solver* s, seiswg_vfs* out);
+/* Solver::run_adjoint: observed uy traces from `vfs` (or disk); writes
+ * proc000000_kmu.bin and gradient_kmu.bin into `out`. */
+int seiswg_solver_run_adjoint(seiswg_solver* s, const seiswg_vfs* vfs, seiswg_vfs* out);
+int seiswg_solver_info(const seiswg_solver* s, int32_t* nx, int32_t* nz, float* dx, float* dz, int32_t* nsrc,
+                       int32_t* nrec);
+/* Total waveform misfit of the last run_adjoint (solver.rs:1503). */
+double seiswg_solver_total_misfit(const seiswg_solver* s);
+/* The simulation handle the solver drives (borrowed; owned by the solver). */
+struct seiswg_sim* seiswg_solver_sim(seiswg_solver* s);
+void seiswg_solver_free(seiswg_solver* s);
+
+/* ---- simulation operator (the kernel-level interface) -------------------- */
+typedef struct seiswg_sim seiswg_sim;
+typedef struct {
+  int32_t nx, nz, nt;
+  float dx, dz, dt;
+  int32_t sh, psv, spin;
+  int32_t abs_left, abs_right, abs_bottom, abs_top;
+  int32_t abs_width;
+  float abs_alpha;
+} seiswg_sim_desc;
+
+/* stream: a cudaStream_t to run on, or NULL for a stream of the handle's own. */
+int seiswg_sim_create(const seiswg_sim_desc* desc, void* stream, seiswg_sim** out);
+void seiswg_sim_free(seiswg_sim* sim);
+/* Model fields, n = nx*nz values: "vp", "vs", "rho" (converted to Lame
+ * parameters by seiswg_sim_prepare, fd2d.wgsl:188-201) or "lambda", "mu",
+ * "nu", "j", "lambda_c", "mu_c", "nu_c", "rho" for spin models. */
+int seiswg_sim_upload_model(seiswg_sim* sim, const char* name, const float* host, size_t n);
+/* vps2lm, mu_c+nu_c and the absorbing taper (fd2d.wgsl:188-235). */
+int seiswg_sim_prepare(seiswg_sim* sim);
+/* Sources at cells (i[s], j[s]); stf_xyz is [3][n][nt] (x, y, z components). */
+int seiswg_sim_set_sources(seiswg_sim* sim, int32_t n, const int32_t* i, const int32_t* j, const float* stf_xyz);
+int seiswg_sim_set_receivers(seiswg_sim* sim, int32_t n, const int32_t* i, const int32_t* j);
+/* One forward run from rest: all nt steps of source isrc (-1: all sources).
+ * Snapshots of `nfields` fields ("vy", "vx", "vz", "vyc", "sxy", ...) after
+ * every step it > 0 with it % snap_every == 0 go to snaps_out
+ * [nsnap][nfields][nx*nz] (snap_every = 0: none).  sync = 0 returns once
+ * the run is queued on the stream (only without snapshots). */
+int seiswg_sim_forward(seiswg_sim* sim, int32_t isrc, int32_t snap_every, int32_t nfields,
+                       const char* const* fields, float* snaps_out, int32_t sync);
+/* Receiver traces of the last run, [5][nrec][nt]: x, y, z, yi, yc
+ * (the reference's obs buffer, fd2d.wgsl:110-114). */
+int seiswg_sim_traces(seiswg_sim* sim, float* host);
+/* Current wavefield component, nx*nz values. */
+int seiswg_sim_state(seiswg_sim* sim, const char* field, float* host);
+/* Reference adjoint, one shot at a time (solver.rs:1380-1498). */
+int seiswg_sim_kernel_clear(seiswg_sim* sim);
+int seiswg_sim_adjoint_forward(seiswg_sim* sim, int32_t isrc, int32_t adj_interval);
+int seiswg_sim_adjoint_backward(seiswg_sim* sim, const float* adstf, int32_t adj_interval);
+int seiswg_sim_kernel_smooth(seiswg_sim* sim, float sigma);
+int seiswg_sim_kernel(seiswg_sim* sim, float* host);
+/* Options: "graphs" (0/1), "chunk_rows" (rows per warp march). */
+int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
+int seiswg_sim_synchronize(seiswg_sim* sim);
+/* Number of kernels this handle has launched (graph nodes count per replay). */
+uint64_t seiswg_sim_launches(const seiswg_sim* sim);
+void* seiswg_sim_stream(const seiswg_sim* sim);
+size_t seiswg_sim_device_bytes(const seiswg_sim* sim);
+
+/* ---- host-side numerics of the reference ---------------------------------- */
+/* [3][nt] Ricker STF of one source (solver.rs:350-356, 721-733). */
+int seiswg_ricker(int32_t nt, float dt, float f0, float t0, float ang_deg, float amp, float* out);
+/* Misfit and time-reversed adjoint source (solver.rs:432-467). */
+int seiswg_waveform_misfit(const float* syn, const float* obs, int32_t nrec, int32_t nt, float dt, float* adstf,
+                           double* misfit);
+/* .npy v1 bytes of a [nrows][ncols] f32 array (solver.rs:270-285).  With
+ * out == NULL only *len is set. */
+int seiswg_npy_encode(const float* data, size_t nrows, size_t ncols, void* out, size_t* len);
+/* nx, nz, dx, dz from coordinate arrays (solver.rs:646-656). */
+int seiswg_infer_grid(const float* x, const float* z, size_t npt, int32_t* nx, int32_t* nz, float* dx, float* dz);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEISWG_H */

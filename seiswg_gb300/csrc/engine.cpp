@@ -1,0 +1,653 @@
+// engine.cpp -- device storage, time loop and reference adjoint of one
+// simulation.  See engine.h.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <tuple>
+
+namespace seiswg {
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    throw CudaError(std::string("CUDA error ") + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ") in " +
+                    what);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Arena
+// ---------------------------------------------------------------------------
+Arena::~Arena() {
+  if (base_) cudaFree(base_);
+}
+
+void Arena::commit() {
+  if (base_ || plan_ == 0) return;
+  SW_CUDA(cudaMalloc(reinterpret_cast<void**>(&base_), plan_));
+}
+
+void* Arena::take(size_t bytes) {
+  size_t b = (bytes + 255) & ~size_t(255);
+  if (!base_ || used_ + b > plan_) throw std::logic_error("arena overflow");
+  void* p = base_ + used_;
+  used_ += b;
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// Sim
+// ---------------------------------------------------------------------------
+namespace {
+int round_up(int x, int m) { return (x + m - 1) / m * m; }
+}  // namespace
+
+Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
+  if (d.nx < 5 || d.nz < 5) throw std::invalid_argument("grid must be at least 5 x 5");
+  if (d.nt < 0) throw std::invalid_argument("nt must be >= 0");
+  if (!(d.dx > 0) || !(d.dz > 0)) throw std::invalid_argument("dx and dz must be positive");
+  if (!d.sh && !d.psv) throw std::invalid_argument("neither sh nor psv is enabled");
+  if (!stream_) {
+    SW_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    own_stream_ = true;
+  }
+  // A warp strip reads columns [j0-4, j0+124) with j0 <= nz-117 (fd_common.cuh).
+  ld_ = round_up(std::max(128, d.nz + 12), 32);
+  const size_t rows_alloc = size_t(d.nx) + 2 * kHaloRows;
+  field_elems_ = rows_alloc * size_t(ld_);
+  const size_t fb = field_elems_ * sizeof(float);
+
+  int nstate = (d.sh ? 3 : 0) + (d.psv ? 5 : 0) + (d.psv && d.spin ? 4 : 0);
+  int nmodel = 3 + (d.psv && d.spin ? 5 : 0);
+  for (int q = 0; q < 2 * nstate + nmodel; ++q) arena_.reserve(fb);
+  arena_.reserve(rows_alloc * sizeof(float));
+  arena_.reserve(size_t(ld_) * sizeof(float));
+  arena_.reserve(size_t(ld_) * sizeof(float));
+  arena_.commit();
+
+  for (int b = 0; b < 2; ++b) {
+    State& s = st_[b];
+    if (d.sh) { s.vy = alloc_field(); s.sxy = alloc_field(); s.szy = alloc_field(); }
+    if (d.psv) {
+      s.vx = alloc_field(); s.vz = alloc_field(); s.sxx = alloc_field(); s.szz = alloc_field(); s.sxz = alloc_field();
+      if (d.spin) { s.vyc = alloc_field(); s.syx = alloc_field(); s.syy = alloc_field(); s.syz = alloc_field(); }
+    }
+  }
+  rho_ = alloc_field(); lam_ = alloc_field(); mu_ = alloc_field();
+  if (d.psv && d.spin) { nu_ = alloc_field(); jm_ = alloc_field(); muc_ = alloc_field(); nuc_ = alloc_field(); mc_ = alloc_field(); }
+  taper_x_ = static_cast<float*>(arena_.take(rows_alloc * sizeof(float))) + kHaloRows;
+  taper_zb_ = static_cast<float*>(arena_.take(size_t(ld_) * sizeof(float))) + kHaloCols;
+  taper_zt_ = static_cast<float*>(arena_.take(size_t(ld_) * sizeof(float))) + kHaloCols;
+  // Zero everything; density and micro-inertia halos hold 1 so that the
+  // (never used) halo velocities stay finite.
+  zero_state();
+  for (float* f : {lam_, mu_, nu_, muc_, nuc_, mc_})
+    if (f) SW_CUDA(cudaMemsetAsync(f - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
+  for (float* f : {rho_, jm_})
+    if (f) SW_CUDA(launch_fill_rows(f - kHaloCols, -kHaloRows, d.nx + kHaloRows, ld_, 1.0f, stream_));
+
+  geom_.nx = d.nx;
+  geom_.nz = d.nz;
+  geom_.ld = ld_;
+  geom_.nstrips = (d.nz + kStripCols - 1) / kStripCols;
+  geom_.dt = d.dt;
+  geom_.rdx = float(1.0 / double(8.0f * d.dx));  // 1 / (8.0 * dx), fd2d.wgsl:156
+  geom_.rdz = float(1.0 / double(8.0f * d.dz));
+  den_x_ = 8.0f * d.dx;
+  den_z_ = 8.0f * d.dz;
+  set_chunk_rows(64);
+  use_graphs_ = (size_t(d.nx) * d.nz <= (size_t(1) << 20));
+}
+
+Sim::~Sim() {
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  cudaFree(stf_);
+  cudaFree(adstf_);
+  cudaFree(inj_dev_[0]);
+  cudaFree(inj_dev_[1]);
+  cudaFree(probes_);
+  cudaFree(probe_acc_);
+  cudaFree(probe_hist_);
+  cudaFree(tr_idx_);
+  cudaFree(obs_);
+  cudaFree(fwd_store_);
+  if (kmu_) cudaFree(kmu_ - size_t(kHaloRows) * ld_ - kHaloCols);
+  if (tmp_) cudaFree(tmp_ - size_t(kHaloRows) * ld_ - kHaloCols);
+  if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+void Sim::set_chunk_rows(int lx) {
+  if (lx < 4) lx = 4;
+  geom_.lx = lx;
+  geom_.nchunks = (d_.nx + lx - 1) / lx;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+float* Sim::alloc_field() { return field_ptr(static_cast<float*>(arena_.take(field_elems_ * sizeof(float)))); }
+
+void Sim::zero_state() {
+  const size_t fb = field_elems_ * sizeof(float);
+  for (int b = 0; b < 2; ++b) {
+    const State& s = st_[b];
+    for (float* f : {s.vy, s.sxy, s.szy, s.vx, s.vz, s.sxx, s.szz, s.sxz, s.vyc, s.syx, s.syy, s.syz})
+      if (f) SW_CUDA(cudaMemsetAsync(f - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
+  }
+}
+
+void Sim::synchronize() const { SW_CUDA(cudaStreamSynchronize(stream_)); }
+
+void Sim::upload_model(ModelField f, const float* host) {
+  float* dst = nullptr;
+  switch (f) {
+    case ModelField::VP: dst = lam_; vps_input_ = true; break;
+    case ModelField::VS: dst = mu_; vps_input_ = true; break;
+    case ModelField::RHO: dst = rho_; break;
+    case ModelField::LAMBDA: dst = lam_; break;
+    case ModelField::MU: dst = mu_; break;
+    case ModelField::NU: dst = nu_; break;
+    case ModelField::J: dst = jm_; break;
+    case ModelField::MU_C: dst = muc_; break;
+    case ModelField::NU_C: dst = nuc_; break;
+    case ModelField::LAMBDA_C: return;  // loaded but unused by the stencil (fd2d.wgsl:428-445)
+  }
+  if (!dst) throw std::invalid_argument("model field not used by this physics");
+  prepared_ = false;
+  SW_CUDA(cudaMemcpy2DAsync(dst, size_t(ld_) * sizeof(float), host, size_t(d_.nz) * sizeof(float),
+                            size_t(d_.nz) * sizeof(float), size_t(d_.nx), cudaMemcpyHostToDevice, stream_));
+}
+
+void Sim::prepare_model() {
+  if (prepared_) throw std::logic_error("prepare_model called twice without a new model upload");
+  if (vps_input_) SW_CUDA(launch_vps2lm(lam_, mu_, rho_, d_.nx, d_.nz, ld_, stream_));
+  if (mc_) SW_CUDA(launch_add_fields(mc_, muc_, nuc_, d_.nx, d_.nz, ld_, stream_));
+  // The step kernels read the buoyancy 1/rho and 1/J.
+  SW_CUDA(launch_reciprocal(rho_, d_.nx, d_.nz, ld_, stream_));
+  if (jm_) SW_CUDA(launch_reciprocal(jm_, d_.nx, d_.nz, ld_, stream_));
+  prepared_ = true;
+
+  // Absorbing taper, set_bound (fd2d.wgsl:205-235): b = ((1*eL)*eR)*eB*eT with
+  // e = exp(-(alpha*d)^2); separable into a row factor (left, right) and two
+  // column factors (bottom, top) applied in the reference's order.
+  const uint32_t w = uint32_t(d_.abs_width), nx = uint32_t(d_.nx), nz = uint32_t(d_.nz);
+  const float a = d_.abs_alpha;
+  std::vector<float> tx(size_t(d_.nx) + 2 * kHaloRows, 1.0f), tb(size_t(ld_), 1.0f), tt(size_t(ld_), 1.0f);
+  for (uint32_t i = 0; i < nx; ++i) {
+    float b = 1.0f;
+    if (d_.abs_left && (i + 1u) < w) { float aw = a * float(w - i - 1u); b *= std::exp(-aw * aw); }
+    if (d_.abs_right && i > (nx - w)) { float aw = a * float(w + i - nx); b *= std::exp(-aw * aw); }
+    tx[kHaloRows + i] = b;
+  }
+  for (uint32_t j = 0; j < nz; ++j) {
+    if (d_.abs_bottom && j > (nz - w)) { float aw = a * float(w + j - nz); tb[kHaloCols + j] = std::exp(-aw * aw); }
+    if (d_.abs_top && (j + 1u) < w) { float aw = a * float(w - j - 1u); tt[kHaloCols + j] = std::exp(-aw * aw); }
+  }
+  SW_CUDA(cudaMemcpyAsync(taper_x_ - kHaloRows, tx.data(), tx.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaMemcpyAsync(taper_zb_ - kHaloCols, tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaMemcpyAsync(taper_zt_ - kHaloCols, tt.data(), tt.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));  // the host vectors die here
+}
+
+void Sim::set_sources(int n, const int* i, const int* j, const float* stf_xyz) {
+  if (n < 0) throw std::invalid_argument("negative source count");
+  for (int s = 0; s < n; ++s)
+    if (i[s] < 0 || i[s] >= d_.nx || j[s] < 0 || j[s] >= d_.nz)
+      throw std::invalid_argument("source " + std::to_string(s) + " lies outside the grid");
+  nsrc_ = n;
+  src_i_.assign(i, i + n);
+  src_j_.assign(j, j + n);
+  cudaFree(stf_);
+  stf_ = nullptr;
+  cudaFree(inj_dev_[0]);
+  inj_dev_[0] = nullptr;
+  inj_cap_[0] = 0;
+  size_t bytes = size_t(3) * n * d_.nt * sizeof(float);
+  if (bytes) {
+    SW_CUDA(cudaMalloc(&stf_, bytes));
+    SW_CUDA(cudaMemcpy(stf_, stf_xyz, bytes, cudaMemcpyHostToDevice));
+  }
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+void Sim::set_receivers(int n, const int* i, const int* j) {
+  if (n < 0) throw std::invalid_argument("negative receiver count");
+  for (int r = 0; r < n; ++r)
+    if (i[r] < 0 || i[r] >= d_.nx || j[r] < 0 || j[r] >= d_.nz)
+      throw std::invalid_argument("receiver " + std::to_string(r) + " lies outside the grid");
+  nrec_ = n;
+  rec_i_.assign(i, i + n);
+  rec_j_.assign(j, j + n);
+  build_probe_tables();
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+// Probes: SH uy (vy) at each receiver; PSV ux (vx), uz (vz); spin uy_c (vy_c)
+// and the 8 displacement samples of the curl stencil (compute_du_grad,
+// fd2d.wgsl:450-456).  One probe per (cell, component); SH probes come first
+// in the device list, then the PSV ones (each kernel walks its own segment).
+void Sim::build_probe_tables() {
+  std::map<std::tuple<int, int, int>, int> index;
+  std::vector<Probe> list;
+  auto probe = [&](int i, int j, int comp) -> int {
+    auto k2 = std::make_tuple(i, j, comp);
+    auto it = index.find(k2);
+    if (it != index.end()) return it->second;
+    int idx = int(list.size());
+    index[k2] = idx;
+    list.push_back(Probe{i, j, comp, idx});
+    return idx;
+  };
+  std::vector<int> tr(size_t(nrec_) * 12, -1);
+  for (int r = 0; r < nrec_; ++r) {
+    const int i = rec_i_[r], j = rec_j_[r];
+    int* t = &tr[size_t(r) * 12];
+    if (d_.sh) t[0] = probe(i, j, kProbeVY);
+    if (d_.psv) {
+      t[1] = probe(i, j, kProbeVX);
+      t[2] = probe(i, j, kProbeVZ);
+      if (d_.spin) {
+        t[3] = probe(i, j, kProbeVYC);
+        if (i >= 1 && i < d_.nx - 2)
+          for (int q = 0; q < 4; ++q) t[4 + q] = probe(i - 1 + q, j, kProbeVZ);
+        if (j >= 1 && j < d_.nz - 2)
+          for (int q = 0; q < 4; ++q) t[8 + q] = probe(i, j - 1 + q, kProbeVX);
+      }
+    }
+  }
+  // SH segment first, then PSV; each sorted by (i, j).
+  std::stable_sort(list.begin(), list.end(), [](const Probe& a, const Probe& b) {
+    int sa = a.comp == kProbeVY ? 0 : 1, sb = b.comp == kProbeVY ? 0 : 1;
+    if (sa != sb) return sa < sb;
+    if (a.i != b.i) return a.i < b.i;
+    return a.j < b.j;
+  });
+  nprobe_ = int(list.size());
+  cudaFree(probes_); probes_ = nullptr;
+  cudaFree(probe_acc_); probe_acc_ = nullptr;
+  cudaFree(probe_hist_); probe_hist_ = nullptr;
+  cudaFree(tr_idx_); tr_idx_ = nullptr;
+  cudaFree(obs_); obs_ = nullptr;
+  if (nprobe_) {
+    SW_CUDA(cudaMalloc(&probes_, list.size() * sizeof(Probe)));
+    SW_CUDA(cudaMemcpy(probes_, list.data(), list.size() * sizeof(Probe), cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMalloc(&probe_acc_, size_t(nprobe_) * sizeof(float)));
+    SW_CUDA(cudaMalloc(&probe_hist_, std::max<size_t>(1, size_t(nprobe_) * d_.nt) * sizeof(float)));
+  }
+  if (nrec_) {
+    SW_CUDA(cudaMalloc(&tr_idx_, tr.size() * sizeof(int) + size_t(nrec_) * 2 * sizeof(int)));
+    std::vector<int> packed(tr);
+    for (int r = 0; r < nrec_; ++r) { packed.push_back(rec_i_[r]); packed.push_back(rec_j_[r]); }
+    SW_CUDA(cudaMemcpy(tr_idx_, packed.data(), packed.size() * sizeof(int), cudaMemcpyHostToDevice));
+    size_t ob = std::max<size_t>(1, size_t(5) * nrec_ * d_.nt) * sizeof(float);
+    SW_CUDA(cudaMalloc(&obs_, ob));
+    SW_CUDA(cudaMemset(obs_, 0, ob));
+  }
+  // Segment boundary: number of SH probes.
+  int nsh = 0;
+  for (const Probe& p : list) nsh += (p.comp == kProbeVY);
+  probe_split_ = nsh;
+}
+
+void Sim::upload_inject(const std::vector<Inject>& list, int which) {
+  int n = int(list.size());
+  if (n > inj_cap_[which]) {
+    cudaFree(inj_dev_[which]);
+    inj_dev_[which] = nullptr;
+    SW_CUDA(cudaMalloc(&inj_dev_[which], size_t(n) * sizeof(Inject)));
+    inj_cap_[which] = n;
+  }
+  inj_n_[which] = n;
+  if (n) SW_CUDA(cudaMemcpy(inj_dev_[which], list.data(), size_t(n) * sizeof(Inject), cudaMemcpyHostToDevice));
+}
+
+float* Sim::state_ptr(StateField f, int b) const {
+  const State& s = st_[b];
+  switch (f) {
+    case StateField::VY: return s.vy;
+    case StateField::SXY: return s.sxy;
+    case StateField::SZY: return s.szy;
+    case StateField::VX: return s.vx;
+    case StateField::VZ: return s.vz;
+    case StateField::SXX: return s.sxx;
+    case StateField::SZZ: return s.szz;
+    case StateField::SXZ: return s.sxz;
+    case StateField::VYC: return s.vyc;
+    case StateField::SYX: return s.syx;
+    case StateField::SYY: return s.syy;
+    case StateField::SYZ: return s.syz;
+  }
+  return nullptr;
+}
+
+void Sim::enqueue_step(int it, int b, const InjectList& inj_in, const ProbeList& probes_in, bool sh_only) {
+  const State& a = st_[b];
+  const State& o = st_[1 - b];
+  InjectList inj = inj_in;
+  inj.it = it;
+  if (d_.sh) {
+    ShStep p{};
+    p.g = geom_;
+    p.vy0 = a.vy; p.sxy0 = a.sxy; p.szy0 = a.szy;
+    p.vy1 = o.vy; p.sxy1 = o.sxy; p.szy1 = o.szy;
+    p.rho = rho_; p.mu = mu_;
+    p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+    p.inj = inj;
+    p.probes = probes_in;
+    p.probes.it = it;
+    if (probes_in.n) p.probes.n = probe_split_;
+    SW_CUDA(launch_sh_step(p, stream_));
+    ++launches_;
+  }
+  if (d_.psv && !sh_only) {
+    PsvStep p{};
+    p.g = geom_;
+    p.vx0 = a.vx; p.vz0 = a.vz; p.sxx0 = a.sxx; p.szz0 = a.szz; p.sxz0 = a.sxz;
+    p.vx1 = o.vx; p.vz1 = o.vz; p.sxx1 = o.sxx; p.szz1 = o.szz; p.sxz1 = o.sxz;
+    p.vyc0 = a.vyc; p.syx0 = a.syx; p.syy0 = a.syy; p.syz0 = a.syz;
+    p.vyc1 = o.vyc; p.syx1 = o.syx; p.syy1 = o.syy; p.syz1 = o.syz;
+    p.rho = rho_; p.lam = lam_; p.mu = mu_; p.nu = nu_; p.jm = jm_; p.mc = mc_;
+    p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+    p.inj = inj;
+    p.probes = probes_in;
+    p.probes.it = it;
+    if (probes_in.n) {
+      p.probes.list = probes_ + probe_split_;
+      p.probes.n = nprobe_ - probe_split_;
+    }
+    SW_CUDA(launch_psv_step(p, d_.spin, stream_));
+    ++launches_;
+  }
+}
+
+void Sim::run_loop(const std::string& key, const std::function<void()>& body) {
+  if (!use_graphs_) {
+    body();
+    return;
+  }
+  auto it = graphs_.find(key);
+  if (it == graphs_.end()) {
+    uint64_t before = launches_;
+    cudaGraph_t g = nullptr;
+    SW_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    try {
+      body();
+    } catch (...) {
+      cudaStreamEndCapture(stream_, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    SW_CUDA(cudaStreamEndCapture(stream_, &g));
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    SW_CUDA(e);
+    it = graphs_.emplace(key, exec).first;
+    graph_nodes_[key] = launches_ - before;
+    launches_ = before;
+  }
+  SW_CUDA(cudaGraphLaunch(it->second, stream_));
+  launches_ += graph_nodes_[key];
+}
+
+void Sim::copy_field_to_host(const float* dev, float* host) const {
+  SW_CUDA(cudaMemcpy2DAsync(host, size_t(d_.nz) * sizeof(float), dev, size_t(ld_) * sizeof(float),
+                            size_t(d_.nz) * sizeof(float), size_t(d_.nx), cudaMemcpyDeviceToHost, stream_));
+}
+
+InjectList Sim::source_injections(int isrc) {
+  if (isrc >= nsrc_) throw std::invalid_argument("source index out of range");
+  std::vector<Inject> list;
+  for (int s = 0; s < nsrc_; ++s)
+    if (isrc < 0 || s == isrc) list.push_back(Inject{src_i_[s], src_j_[s], s, 0});
+  std::stable_sort(list.begin(), list.end(),
+                   [](const Inject& a, const Inject& b) { return a.i != b.i ? a.i < b.i : a.j < b.j; });
+  upload_inject(list, 0);
+  InjectList inj{};
+  inj.list = inj_dev_[0];
+  inj.n = inj_n_[0];
+  inj.nt = d_.nt;
+  inj.val_x = stf_;
+  inj.val_y = stf_ ? stf_ + size_t(nsrc_) * d_.nt : nullptr;
+  inj.val_z = stf_ ? stf_ + size_t(2) * nsrc_ * d_.nt : nullptr;
+  return inj;
+}
+
+ProbeList Sim::probe_list() const {
+  ProbeList pl{};
+  pl.list = probes_;
+  pl.n = nprobe_;
+  pl.nt = d_.nt;
+  pl.acc = probe_acc_;
+  pl.hist = probe_hist_;
+  return pl;
+}
+
+void Sim::enqueue_traces() {
+  if (!nrec_) return;
+  TraceSpec t{};
+  t.nrec = nrec_;
+  t.nt = d_.nt;
+  t.sh = d_.sh;
+  t.psv = d_.psv;
+  t.spin = d_.psv && d_.spin;
+  t.idx = tr_idx_;
+  t.rec_ij = tr_idx_ + size_t(nrec_) * 12;
+  t.nx = d_.nx;
+  t.nz = d_.nz;
+  t.den_x = den_x_;
+  t.den_z = den_z_;
+  t.hist = probe_hist_;
+  t.obs = obs_;
+  SW_CUDA(launch_assemble_traces(t, stream_));
+  ++launches_;
+}
+
+void Sim::run_forward(int isrc, Snapshots* snaps) {
+  InjectList inj = source_injections(isrc);
+  ProbeList pl = probe_list();
+  zero_state();
+  if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
+
+  int every = snaps ? snaps->every : 0;
+  std::vector<int> snap_steps;
+  if (every > 0)
+    for (int it = 1; it < d_.nt; ++it)
+      if (it % every == 0) snap_steps.push_back(it);
+  const size_t nf = snaps ? snaps->fields.size() : 0;
+  const size_t need = snap_steps.size() * nf;
+  if (need > snap_cap_) {
+    cudaFree(snap_store_);
+    snap_store_ = nullptr;
+    SW_CUDA(cudaMalloc(&snap_store_, need * field_elems_ * sizeof(float)));
+    snap_cap_ = need;
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+  }
+  std::vector<float*> snap_src;
+  for (StateField f : (snaps ? snaps->fields : std::vector<StateField>{}))
+    for (int b = 0; b < 2; ++b)
+      if (!state_ptr(f, b)) throw std::invalid_argument("snapshot field not present in this physics");
+
+  std::string key = "fwd/" + std::to_string(inj.n) + "/" + std::to_string(every);
+  for (StateField f : (snaps ? snaps->fields : std::vector<StateField>{})) key += "/" + std::to_string(int(f));
+  const size_t fbytes = field_elems_ * sizeof(float);
+  run_loop(key, [&] {
+    size_t q = 0;
+    for (int it = 0; it < d_.nt; ++it) {
+      enqueue_step(it, it & 1, inj, pl, false);
+      if (every > 0 && it > 0 && it % every == 0) {
+        for (StateField f : snaps->fields) {
+          const float* src = state_ptr(f, (it + 1) & 1) - size_t(kHaloRows) * ld_ - kHaloCols;
+          SW_CUDA(cudaMemcpyAsync(snap_store_ + q * field_elems_, src, fbytes, cudaMemcpyDeviceToDevice, stream_));
+          ++q;
+        }
+      }
+    }
+    enqueue_traces();
+  });
+  cur_buf_ = d_.nt & 1;
+  if (snaps) {
+    snaps->steps = snap_steps;
+    snaps->frames.assign(need, std::vector<float>());
+    for (size_t q = 0; q < need; ++q) {
+      snaps->frames[q].resize(size_t(d_.nx) * d_.nz);
+      copy_field_to_host(snap_store_ + q * field_elems_ + size_t(kHaloRows) * ld_ + kHaloCols,
+                         snaps->frames[q].data());
+    }
+    SW_CUDA(cudaStreamSynchronize(stream_));
+  }
+}
+
+void Sim::download_traces(float* host) const {
+  if (!nrec_) return;
+  SW_CUDA(cudaMemcpyAsync(host, obs_, size_t(5) * nrec_ * d_.nt * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Sim::download_state(StateField f, float* host) const {
+  const float* p = state_ptr(f, cur_buf_);
+  if (!p) throw std::invalid_argument("field not present in this physics");
+  copy_field_to_host(p, host);
+  SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+// ---------------------------------------------------------------------------
+// Reference adjoint
+// ---------------------------------------------------------------------------
+void Sim::clear_kmu() {
+  const size_t fb = field_elems_ * sizeof(float);
+  if (!kmu_) {
+    float* a = nullptr;
+    SW_CUDA(cudaMalloc(&a, fb));
+    kmu_ = field_ptr(a);
+    SW_CUDA(cudaMalloc(&a, fb));
+    tmp_ = field_ptr(a);
+    SW_CUDA(cudaMemsetAsync(tmp_ - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
+  }
+  SW_CUDA(cudaMemsetAsync(kmu_ - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
+}
+
+void Sim::adjoint_forward(int isrc, int adj_interval) {
+  if (adj_interval <= 0) throw std::invalid_argument("adj_interval must be positive");
+  const int nsa = d_.nt / adj_interval;
+  if (nsa == 0) throw std::invalid_argument("adj_interval >= nt");
+  if (!kmu_) clear_kmu();
+  const size_t fb = field_elems_ * sizeof(float);
+  if (fwd_nsa_ != nsa) {
+    cudaFree(fwd_store_);
+    fwd_store_ = nullptr;
+    fwd_bytes_ = size_t(nsa) * fb;
+    SW_CUDA(cudaMalloc(&fwd_store_, fwd_bytes_));
+    fwd_nsa_ = nsa;
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+  }
+  InjectList inj = source_injections(isrc);
+  ProbeList pl = probe_list();
+  zero_state();
+  if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
+  if (!d_.sh) {  // the reference's adjoint loops dispatch SH kernels only (solver.rs:1400)
+    SW_CUDA(cudaMemsetAsync(obs_, 0, size_t(5) * nrec_ * d_.nt * sizeof(float), stream_));
+    return;
+  }
+  std::string key = "adjf/" + std::to_string(inj.n) + "/" + std::to_string(adj_interval);
+  run_loop(key, [&] {
+    for (int it = 0; it < d_.nt; ++it) {
+      enqueue_step(it, it & 1, inj, pl, true);
+      if ((it + 1) % adj_interval == 0) {  // solver.rs:1411-1414
+        const int isa = nsa - (it + 1) / adj_interval;
+        const float* src = st_[(it + 1) & 1].vy - size_t(kHaloRows) * ld_ - kHaloCols;
+        SW_CUDA(cudaMemcpyAsync(fwd_store_ + size_t(isa) * field_elems_, src, fb, cudaMemcpyDeviceToDevice,
+                                stream_));
+      }
+    }
+    enqueue_traces();
+  });
+  cur_buf_ = d_.nt & 1;
+}
+
+void Sim::adjoint_backward(const float* adstf_host, int adj_interval) {
+  const int nsa = d_.nt / adj_interval;
+  if (!d_.sh) return;
+  if (nsa != fwd_nsa_) throw std::logic_error("adjoint_backward without a matching adjoint_forward");
+  if (!adstf_ && nrec_) SW_CUDA(cudaMalloc(&adstf_, size_t(nrec_) * d_.nt * sizeof(float)));
+  if (nrec_)
+    SW_CUDA(cudaMemcpyAsync(adstf_, adstf_host, size_t(nrec_) * d_.nt * sizeof(float), cudaMemcpyHostToDevice,
+                            stream_));
+  std::vector<Inject> list;
+  for (int r = 0; r < nrec_; ++r) list.push_back(Inject{rec_i_[r], rec_j_[r], r, 0});
+  std::stable_sort(list.begin(), list.end(),
+                   [](const Inject& a, const Inject& b) { return a.i != b.i ? a.i < b.i : a.j < b.j; });
+  upload_inject(list, 1);
+  InjectList inj{};
+  inj.list = inj_dev_[1];
+  inj.n = inj_n_[1];
+  inj.nt = d_.nt;
+  inj.val_y = adstf_;
+  ProbeList none{};
+  zero_state();
+  const float ndt = float(adj_interval) * d_.dt;  // solver.rs:1368
+  std::string key = "adjb/" + std::to_string(inj.n) + "/" + std::to_string(adj_interval);
+  run_loop(key, [&] {
+    for (int it = 0; it < d_.nt; ++it) {
+      enqueue_step(it, it & 1, inj, none, true);
+      if (it % adj_interval == 0 && it / adj_interval < nsa) {  // solver.rs:1468-1491
+        const float* fw = fwd_store_ + size_t(it / adj_interval) * field_elems_ + size_t(kHaloRows) * ld_ + kHaloCols;
+        SW_CUDA(launch_imaging_muy(kmu_, st_[(it + 1) & 1].vy, fw, d_.nx, d_.nz, ld_, den_x_, den_z_,
+                                   ndt, stream_));
+        ++launches_;
+      }
+    }
+  });
+  cur_buf_ = d_.nt & 1;
+}
+
+// Gaussian smoothing of kmu (solver.rs:1249-1274; fd2d.wgsl:515-554, 590-609).
+// The reference sums exp(-d^2 / (2 sigma^2)) over the full grid; terms beyond
+// 8 sigma are below 1.3e-14 of the peak and are dropped.  The normaliser
+// gsum(i, j) = sx(i) * sz(j) keeps the reference's full-range sums.
+void Sim::smooth_kmu(float sigma) {
+  if (!kmu_) clear_kmu();
+  if (!(sigma > 0.0f)) return;
+  const int radius = std::min(std::max(d_.nx, d_.nz) - 1, int(std::ceil(8.0 * double(sigma))));
+  std::vector<float> w(size_t(radius) + 1);
+  const double s2 = 2.0 * double(sigma) * double(sigma);
+  for (int q = 0; q <= radius; ++q) w[q] = float(std::exp(-double(q) * double(q) / s2));
+  auto sums = [&](int n) {
+    std::vector<float> out(static_cast<size_t>(n));
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int q = 0; q < n; ++q) s += std::exp(-double(i - q) * double(i - q) / s2);
+      out[i] = float(s);
+    }
+    return out;
+  };
+  std::vector<float> gx = sums(d_.nx), gz = sums(d_.nz);
+  float *dw = nullptr, *dgx = nullptr, *dgz = nullptr;
+  SW_CUDA(cudaMalloc(&dw, (w.size() + gx.size() + gz.size()) * sizeof(float)));
+  dgx = dw + w.size();
+  dgz = dgx + gx.size();
+  SW_CUDA(cudaMemcpyAsync(dw, w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaMemcpyAsync(dgx, gx.data(), gx.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaMemcpyAsync(dgz, gz.data(), gz.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(launch_smooth_x(tmp_, kmu_, dw, radius, d_.nx, d_.nz, ld_, stream_));
+  SW_CUDA(launch_smooth_z(kmu_, tmp_, dw, radius, dgx, dgz, d_.nx, d_.nz, ld_, stream_));
+  launches_ += 2;
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  cudaFree(dw);
+}
+
+void Sim::download_kmu(float* host) const {
+  if (!kmu_) {
+    std::fill(host, host + size_t(d_.nx) * d_.nz, 0.0f);
+    return;
+  }
+  copy_field_to_host(kmu_, host);
+  SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+}  // namespace seiswg

@@ -1,0 +1,184 @@
+// engine.h -- the device-side solver: wavefield and model storage in HBM,
+// the time loop (optionally captured as one CUDA graph), receivers,
+// snapshots and the reference adjoint.  Host code only; kernels are launched
+// through fd_kernels.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <functional>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "fd_kernels.h"
+
+namespace seiswg {
+
+struct CudaError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+void cuda_check(cudaError_t e, const char* what);
+#define SW_CUDA(call) ::seiswg::cuda_check((call), #call)
+
+// Grid and physics of one simulation (the numeric part of the reference's
+// Params uniform, fd2d.wgsl:18-49).
+struct SimDesc {
+  int nx = 0, nz = 0, nt = 0;
+  float dx = 0, dz = 0, dt = 0;
+  bool sh = false, psv = true, spin = false;
+  bool abs_left = false, abs_right = false, abs_bottom = false, abs_top = false;
+  int abs_width = 20;
+  float abs_alpha = 0.015f;
+};
+
+// Model slots the caller can upload (host arrays indexed k = i*nz + j).
+enum class ModelField { VP, VS, RHO, LAMBDA, MU, NU, J, LAMBDA_C, MU_C, NU_C };
+
+// Wavefield components a snapshot can read.
+enum class StateField { VY, SXY, SZY, VX, VZ, SXX, SZZ, SXZ, VYC, SYX, SYY, SYZ };
+
+// Device arena: one cudaMalloc carved into 256-byte aligned pieces.
+class Arena {
+ public:
+  Arena() = default;
+  ~Arena();
+  Arena(const Arena&) = delete;
+  Arena& operator=(const Arena&) = delete;
+  void reserve(size_t bytes) { plan_ += (bytes + 255) & ~size_t(255); }
+  void commit();
+  void* take(size_t bytes);
+  size_t bytes() const { return plan_; }
+
+ private:
+  char* base_ = nullptr;
+  size_t plan_ = 0, used_ = 0;
+};
+
+class Sim {
+ public:
+  Sim(const SimDesc& d, cudaStream_t stream = nullptr);
+  ~Sim();
+  Sim(const Sim&) = delete;
+  Sim& operator=(const Sim&) = delete;
+
+  const SimDesc& desc() const { return d_; }
+  int ld() const { return ld_; }
+  cudaStream_t stream() const { return stream_; }
+
+  // ---- set-up ----
+  void upload_model(ModelField f, const float* host);
+  // vps2lm when the model came as vp/vs (fd2d.wgsl:188-201), mu_c + nu_c,
+  // the absorbing taper factors (fd2d.wgsl:203-235).
+  void prepare_model();
+  // Sources at cells (i, j) with STF table [3][n][nt] (x, y, z components).
+  void set_sources(int n, const int* i, const int* j, const float* stf_xyz);
+  // Receivers at cells (i, j).
+  void set_receivers(int n, const int* i, const int* j);
+  int nsrc() const { return nsrc_; }
+  int nrec() const { return nrec_; }
+
+  // ---- forward ----
+  // One shot (isrc >= 0) or all sources together (isrc = -1), nt steps from
+  // rest.  Snapshots of `snap_fields` after every step it > 0 with
+  // it % snap_every == 0 are copied to host memory.
+  struct Snapshots {
+    int every = 0;
+    std::vector<StateField> fields;
+    std::vector<std::vector<float>> frames;  // [nsnap * fields.size()][npt], k = i*nz + j
+    std::vector<int> steps;
+  };
+  void run_forward(int isrc, Snapshots* snaps = nullptr);
+  // Traces of the last forward run, [5][nrec][nt] (x, y, z, yi, yc).
+  void download_traces(float* host) const;
+  // A wavefield component of the current state.
+  void download_state(StateField f, float* host) const;
+
+  // ---- reference adjoint (solver.rs:1298-1529), SH imaging ----
+  // Adds one shot's contribution to kmu: forward with vy saved every
+  // `adj_interval` steps, adjoint with the time-reversed adjoint source
+  // `adstf` [nrec][nt] injected at the receivers, imaging every interval.
+  // The caller computes the adjoint source from the forward traces.
+  void adjoint_forward(int isrc, int adj_interval);
+  void adjoint_backward(const float* adstf_host, int adj_interval);
+  void clear_kmu();
+  void smooth_kmu(float sigma);
+  void download_kmu(float* host) const;
+
+  // Graph capture of whole time loops (replayed on repeated runs).
+  void set_use_graphs(bool on) { use_graphs_ = on; }
+  void set_chunk_rows(int lx);
+  int chunk_rows() const { return geom_.lx; }
+  uint64_t kernel_launches() const { return launches_; }
+  void synchronize() const;
+
+  size_t device_bytes() const { return arena_.bytes() + (fwd_store_ ? fwd_bytes_ : 0); }
+
+ private:
+  struct State {
+    float *vy = nullptr, *sxy = nullptr, *szy = nullptr;
+    float *vx = nullptr, *vz = nullptr, *sxx = nullptr, *szz = nullptr, *sxz = nullptr;
+    float *vyc = nullptr, *syx = nullptr, *syy = nullptr, *syz = nullptr;
+  };
+  float* field_ptr(float* alloc) const { return alloc + size_t(kHaloRows) * ld_ + kHaloCols; }
+  float* alloc_field();
+  void zero_state();
+  void enqueue_step(int it, int src_buf, const InjectList& inj, const ProbeList& probes, bool sh_only);
+  InjectList source_injections(int isrc);
+  ProbeList probe_list() const;
+  void enqueue_traces();
+  float* state_ptr(StateField f, int buf) const;
+  void build_probe_tables();
+  void upload_inject(const std::vector<Inject>& list, int which);
+  void run_loop(const std::string& key, const std::function<void()>& body);
+  void copy_field_to_host(const float* dev, float* host) const;
+
+  SimDesc d_;
+  cudaStream_t stream_;
+  bool own_stream_ = false;
+  int ld_ = 0;
+  size_t field_elems_ = 0;  // rows_alloc * ld
+  Geom geom_{};
+  Arena arena_;
+  State st_[2];
+  float *rho_ = nullptr, *lam_ = nullptr, *mu_ = nullptr;
+  float *nu_ = nullptr, *jm_ = nullptr, *muc_ = nullptr, *nuc_ = nullptr, *mc_ = nullptr;
+  float *taper_x_ = nullptr, *taper_zb_ = nullptr, *taper_zt_ = nullptr;
+  float *kmu_ = nullptr, *tmp_ = nullptr;
+  bool vps_input_ = false;
+  bool prepared_ = false;
+  float den_x_ = 0, den_z_ = 0;   // 8*dx, 8*dz (reference denominators)
+
+  // sources and receivers
+  int nsrc_ = 0, nrec_ = 0;
+  std::vector<int> src_i_, src_j_, rec_i_, rec_j_;
+  float* stf_ = nullptr;          // [3][nsrc][nt]
+  float* adstf_ = nullptr;        // [nrec][nt]
+  Inject* inj_dev_[2] = {nullptr, nullptr};  // 0: sources, 1: receivers (adjoint)
+  int inj_n_[2] = {0, 0}, inj_cap_[2] = {0, 0};
+  Probe* probes_ = nullptr;
+  int nprobe_ = 0;
+  int probe_split_ = 0;           // SH probes first, then PSV probes
+  float *probe_acc_ = nullptr, *probe_hist_ = nullptr;
+  int *tr_idx_ = nullptr;         // per receiver probe indices (device)
+  float* obs_ = nullptr;          // [5][nrec][nt]
+  int cur_buf_ = 0;               // buffer holding the current state
+  float* snap_store_ = nullptr;   // device snapshot frames
+  size_t snap_cap_ = 0;
+
+  // reference adjoint forward-wavefield store
+  float* fwd_store_ = nullptr;
+  size_t fwd_bytes_ = 0;
+  int fwd_nsa_ = 0;
+
+  bool use_graphs_ = true;
+  std::map<std::string, cudaGraphExec_t> graphs_;
+  std::map<std::string, uint64_t> graph_nodes_;
+  uint64_t launches_ = 0;
+};
+
+}  // namespace seiswg

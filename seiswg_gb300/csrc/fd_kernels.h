@@ -1,0 +1,99 @@
+// fd_kernels.h -- launch interface of the seiswg sm_103a kernels (device
+// pointers only; the engine owns the memory).
+#pragma once
+
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "fd_types.h"
+
+namespace seiswg {
+
+constexpr int kStepWarps = 4;  // warps per CTA of the step kernels
+
+struct InjectList {
+  const Inject* list;  // sorted by (i, j), stable
+  int n;
+  int nt, it;
+  const float* val_x;  // [rows][nt] value tables (may be null when unused)
+  const float* val_y;
+  const float* val_z;
+};
+
+struct ProbeList {
+  const Probe* list;  // sorted by (i, j)
+  int n;
+  int nt, it;
+  float* acc;   // [n] running displacement
+  float* hist;  // [n][nt] displacement after each step
+};
+
+struct ShStep {
+  Geom g;
+  const float *vy0, *sxy0, *szy0;
+  float *vy1, *sxy1, *szy1;
+  const float *rho, *mu;
+  const float *taper_x, *taper_zb, *taper_zt;
+  InjectList inj;
+  ProbeList probes;
+};
+
+struct PsvStep {
+  Geom g;
+  const float *vx0, *vz0, *sxx0, *szz0, *sxz0;
+  float *vx1, *vz1, *sxx1, *szz1, *sxz1;
+  const float *vyc0, *syx0, *syy0, *syz0;
+  float *vyc1, *syx1, *syy1, *syz1;
+  const float *rho, *lam, *mu;
+  const float *nu, *jm, *mc;  // spin: nu, J, mu_c + nu_c
+  const float *taper_x, *taper_zb, *taper_zt;
+  InjectList inj;
+  ProbeList probes;
+};
+
+cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s);
+cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s);
+
+// ---- auxiliary kernels (fd_aux.cu) ----------------------------------------
+
+// Pitched field helpers.  `f` points at element (0, 0).
+cudaError_t launch_fill_rows(float* f, int rows_lo, int rows_hi, int ld, float value, cudaStream_t s);
+// vps2lm (fd2d.wgsl:188-201), in place on the vp / vs slots.
+cudaError_t launch_vps2lm(float* lam_vp, float* mu_vs, const float* rho, int nx, int nz, int ld, cudaStream_t s);
+// out = a + b elementwise over the nx x nz interior.
+cudaError_t launch_add_fields(float* out, const float* a, const float* b, int nx, int nz, int ld,
+                              cudaStream_t s);
+// f = 1/f over the nx x nz interior (buoyancy from density, 1/J).
+cudaError_t launch_reciprocal(float* f, int nx, int nz, int ld, cudaStream_t s);
+
+// Receiver traces from probe histories (save_obs_* of fd2d.wgsl:295-301,
+// 463-492).  For each receiver r: obs[comp][r][it].
+struct TraceSpec {
+  int nrec, nt;
+  int sh, psv, spin;
+  // Probe indices per receiver, [r][12] (-1 when not recorded):
+  //   0 uy (SH), 1 ux, 2 uz (PSV), 3 uy_c (spin),
+  //   4..7 uz at rows i-1..i+2, 8..11 ux at columns j-1..j+2 (spin curl)
+  const int* idx;
+  const int* rec_ij; // [r][2]
+  int nx, nz;
+  float den_x, den_z;
+  const float* hist;
+  float* obs;        // [5][nrec][nt]
+};
+cudaError_t launch_assemble_traces(const TraceSpec& t, cudaStream_t s);
+
+// Imaging condition of the reference adjoint (interaction_muy with div_uy and
+// div_fw, fd2d.wgsl:501-509, 571-588):
+//   kmu += (dx+ vy_adj * dx+ vy_fw + dz+ vy_adj * dz+ vy_fw) * ndt
+cudaError_t launch_imaging_muy(float* kmu, const float* vy_adj, const float* vy_fw, int nx, int nz, int ld,
+                               float den_x, float den_z, float ndt, cudaStream_t s);
+
+// Separable Gaussian smoothing normalised by gsum (fd2d.wgsl:515-554):
+//   tmp = sum_n w[|i-n|] f[n, j];  f = sum_n w[|j-n|] tmp[i, n] / gsum
+cudaError_t launch_smooth_x(float* tmp, const float* f, const float* w, int radius, int nx, int nz, int ld,
+                            cudaStream_t s);
+cudaError_t launch_smooth_z(float* f, const float* tmp, const float* w, int radius, const float* gsum_x,
+                            const float* gsum_z, int nx, int nz, int ld, cudaStream_t s);
+
+}  // namespace seiswg

@@ -1,0 +1,56 @@
+// fd_types.h -- plain data shared by the host engine and the sm_103a stencil
+// kernels.
+//
+// Grid layout in HBM (one allocation per field):
+//   rows i in [-kHaloRows, nx + kHaloRows), row pitch `ld` floats (a multiple
+//   of 32, so every row starts on a 128-byte boundary); column j of row i is
+//   at base[i * ld + j] and the element (0, 0) sits kHaloCols floats into a
+//   row, i.e. 16-byte aligned.  z (j) is the contiguous direction, as in the
+//   reference (fd2d.wgsl:140-145, k = i*nz + j).  Halo rows and columns are
+//   zero and never written; the reference's edge rules (derivatives forced to
+//   zero near the edges, fd2d.wgsl:151-180) are applied by index, so halo
+//   values never reach a result.
+//
+// Work decomposition of the streaming kernels: one warp owns a z-strip of
+// kStripCols output columns and marches down x over a chunk of rows.  Lane L
+// holds the float4 of columns [j0 - 4 + 4L, j0 + 4L); lanes 0 and 31 are the
+// strip's halo, lanes 1..30 own the 120 output columns.  z-derivatives take
+// their neighbours from adjacent lanes with warp shuffles; x-derivatives read
+// register rings of the previous rows.
+#pragma once
+
+#include <cstdint>
+
+namespace seiswg {
+
+constexpr int kHaloRows = 4;
+constexpr int kHaloCols = 4;
+constexpr int kStripCols = 120;
+constexpr unsigned kFull = 0xffffffffu;
+
+// An injection (source or adjoint source) at cell (i, j).  `row` indexes the
+// value tables [row][nt].  Lists are sorted by (i, j), stable in row, so that
+// several injections into one cell add in index order.
+struct Inject {
+  int i, j, row, pad;
+};
+
+// A probe: a cell whose displacement u += v*dt is integrated every step and
+// recorded as a history [idx][nt].  comp: 0 vx, 1 vz, 2 vy, 3 vy_c.
+struct Probe {
+  int i, j, comp, idx;
+};
+
+enum ProbeComp { kProbeVX = 0, kProbeVZ = 1, kProbeVY = 2, kProbeVYC = 3 };
+
+struct Geom {
+  int nx, nz, ld;
+  int lx;        // rows per warp chunk
+  int nstrips;   // warps across z
+  int nchunks;   // warps along x
+  float dt;
+  float rdx;     // 1/(8*dx): reciprocal of the reference's denominator (fd2d.wgsl:156)
+  float rdz;     // 1/(8*dz)
+};
+
+}  // namespace seiswg

@@ -1,0 +1,665 @@
+// host.cpp -- configuration, file formats, VFS and the forward / adjoint
+// workflows of seiswg (src/config.rs, src/solver.rs), over the CUDA engine.
+#include "host.h"
+
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace seiswg {
+
+namespace {
+
+constexpr float kPi = 3.14159265358979323846f;
+
+std::string lower(std::string s) {
+  for (char& c : s) c = char(std::tolower(static_cast<unsigned char>(c)));
+  return s;
+}
+
+std::string trim(const std::string& s) {
+  size_t a = 0, b = s.size();
+  while (a < b && std::isspace(static_cast<unsigned char>(s[a]))) ++a;
+  while (b > a && std::isspace(static_cast<unsigned char>(s[b - 1]))) --b;
+  return s.substr(a, b - a);
+}
+
+std::string fmt6(uint32_t v) {
+  char buf[32];
+  std::snprintf(buf, sizeof buf, "%06u", v);
+  return buf;
+}
+
+bool file_exists(const std::string& p) {
+  struct stat st;
+  return ::stat(p.c_str(), &st) == 0;
+}
+
+void mkdirs(const std::string& path) {
+  if (path.empty()) return;
+  std::string cur;
+  size_t pos = 0;
+  while (pos <= path.size()) {
+    size_t nxt = path.find('/', pos);
+    if (nxt == std::string::npos) nxt = path.size();
+    cur = path.substr(0, nxt);
+    if (!cur.empty() && !file_exists(cur)) {
+      if (::mkdir(cur.c_str(), 0777) != 0 && errno != EEXIST)
+        throw Error("Cannot create directory " + cur + ": " + std::strerror(errno));
+    }
+    pos = nxt + 1;
+  }
+}
+
+Bytes read_file(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error("Cannot read " + path);
+  return Bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+}
+
+// ---- INI (configparser 3.x semantics as used by config.rs) ----------------
+// Sections and keys are case-insensitive; ';' and '#' start a comment; '=' or
+// ':' separate key and value; a key without a delimiter has no value.
+using Ini = std::map<std::string, std::map<std::string, std::pair<bool, std::string>>>;
+
+Ini parse_ini(const std::string& text) {
+  Ini ini;
+  std::string section = "default";
+  std::istringstream in(text);
+  std::string raw;
+  int num = 0;
+  while (std::getline(in, raw)) {
+    ++num;
+    size_t c = raw.find_first_of(";#");
+    std::string line = trim(c == std::string::npos ? raw : raw.substr(0, c));
+    if (line.empty()) continue;
+    if (line[0] == '[') {
+      size_t e = line.rfind(']');
+      if (e == std::string::npos)
+        throw Error("line " + std::to_string(num) + ": Found opening bracket for section name but no closing bracket");
+      section = lower(trim(line.substr(1, e - 1)));
+      continue;
+    }
+    if (line[0] == '=' || line[0] == ':')
+      throw Error("line " + std::to_string(num) + ": Started with a delimiter but no key");
+    size_t d = line.find_first_of("=:");
+    auto& sec = ini[section];
+    if (d == std::string::npos) {
+      sec[lower(line)] = {false, ""};
+    } else {
+      std::string key = lower(trim(line.substr(0, d)));
+      if (key.empty()) throw Error("line " + std::to_string(num) + ": Key cannot be empty");
+      sec[key] = {true, trim(line.substr(d + 1))};
+    }
+  }
+  return ini;
+}
+
+bool ini_get(const Ini& ini, const std::string& sec, const std::string& key, std::string* out) {
+  auto s = ini.find(lower(sec));
+  if (s == ini.end()) return false;
+  auto k = s->second.find(lower(key));
+  if (k == s->second.end() || !k->second.first) return false;
+  *out = k->second.second;
+  return true;
+}
+
+std::string get_required(const Ini& ini, const std::string& sec, const std::string& key) {
+  std::string v;
+  if (!ini_get(ini, sec, key, &v)) throw Error("[" + sec + "] " + key + " is required");
+  return v;
+}
+
+bool get_bool(const Ini& ini, const std::string& sec, const std::string& key, bool def) {
+  std::string v;
+  if (!ini_get(ini, sec, key, &v)) return def;
+  return lower(trim(v)) == "yes";  // config.rs:72-76: only "yes" is true
+}
+
+bool parse_u32(const std::string& s, uint32_t* out) {
+  std::string t = trim(s);
+  if (t.empty()) return false;
+  size_t i = (t[0] == '+') ? 1 : 0;
+  if (i == t.size()) return false;
+  uint64_t v = 0;
+  for (; i < t.size(); ++i) {
+    if (t[i] < '0' || t[i] > '9') return false;
+    v = v * 10 + uint64_t(t[i] - '0');
+    if (v > 0xffffffffull) return false;
+  }
+  *out = uint32_t(v);
+  return true;
+}
+
+bool parse_f32(const std::string& s, float* out) {
+  std::string t = trim(s);
+  if (t.empty()) return false;
+  char* end = nullptr;
+  errno = 0;
+  float v = std::strtof(t.c_str(), &end);
+  if (end != t.c_str() + t.size()) return false;
+  *out = v;
+  return true;
+}
+
+uint32_t get_u32(const Ini& ini, const std::string& sec, const std::string& key) {
+  uint32_t v;
+  if (!parse_u32(get_required(ini, sec, key), &v)) throw Error("[" + sec + "] " + key + " must be an integer");
+  return v;
+}
+
+uint32_t get_u32_or(const Ini& ini, const std::string& sec, const std::string& key, uint32_t def) {
+  std::string s;
+  uint32_t v;
+  return (ini_get(ini, sec, key, &s) && parse_u32(s, &v)) ? v : def;
+}
+
+float get_f32(const Ini& ini, const std::string& sec, const std::string& key) {
+  float v;
+  if (!parse_f32(get_required(ini, sec, key), &v)) throw Error("[" + sec + "] " + key + " must be a float");
+  return v;
+}
+
+float get_f32_or(const Ini& ini, const std::string& sec, const std::string& key, float def) {
+  std::string s;
+  float v;
+  return (ini_get(ini, sec, key, &s) && parse_f32(s, &v)) ? v : def;
+}
+
+// config.rs:105-112: paths are relative to the directory of the config file.
+std::string resolve(const std::string& base, const std::string& raw) {
+  std::string p = trim(raw);
+  if (!p.empty() && p[0] == '/') return p;
+  return path_join(base, p);
+}
+
+Config parse_config(const Ini& ini, const std::string& base) {
+  Config c;
+  c.workflow = lower(trim(get_required(ini, "workflow", "mode")));
+  c.nt = get_u32(ini, "solver", "nt");
+  c.dt = get_f32(ini, "solver", "dt");
+  c.abs_left = get_bool(ini, "solver", "abs_left", false);
+  c.abs_right = get_bool(ini, "solver", "abs_right", false);
+  c.abs_bottom = get_bool(ini, "solver", "abs_bottom", false);
+  c.abs_top = get_bool(ini, "solver", "abs_top", false);
+  c.abs_width = get_u32_or(ini, "solver", "abs_width", 20);
+  c.abs_alpha = get_f32_or(ini, "solver", "abs_alpha", 0.015f);
+  c.sh = get_bool(ini, "solver", "sh", false);
+  c.psv = get_bool(ini, "solver", "psv", true);
+  c.spin = get_bool(ini, "solver", "spin", false);
+  c.threads_per_block = get_u32_or(ini, "solver", "threads_per_block", 128);
+  c.combine_sources = get_bool(ini, "solver", "combine_sources", false);
+  c.save_snapshot = get_u32_or(ini, "solver", "save_snapshot", 0);
+  c.adj_interval = get_u32_or(ini, "solver", "adj_interval", 10);
+  c.smooth = get_f32_or(ini, "solver", "smooth", 5.0f);
+  std::string v;
+  c.output = resolve(base, get_required(ini, "path", "output"));
+  if ((c.has_output_traces = ini_get(ini, "path", "output_traces", &v))) c.output_traces = resolve(base, v);
+  if ((c.has_model_true = ini_get(ini, "path", "model_true", &v))) c.model_true = resolve(base, v);
+  if ((c.has_model_init = ini_get(ini, "path", "model_init", &v))) c.model_init = resolve(base, v);
+  c.sources = resolve(base, get_required(ini, "path", "sources"));
+  c.stations = resolve(base, get_required(ini, "path", "stations"));
+  if ((c.has_traces = ini_get(ini, "path", "traces", &v))) c.traces = resolve(base, v);
+  uint32_t u;
+  if (ini_get(ini, "cuda", "chunk_rows", &v) && parse_u32(v, &u)) c.chunk_rows = int(u);
+  if (ini_get(ini, "cuda", "graphs", &v)) c.graphs = lower(trim(v)) == "yes" ? 1 : 0;
+  return c;
+}
+
+}  // namespace
+
+std::string path_join(const std::string& a, const std::string& b) {
+  if (b.empty()) return a;
+  if (!b.empty() && b[0] == '/') return b;
+  if (a.empty()) return b;
+  if (a.back() == '/') return a + b;
+  return a + "/" + b;
+}
+
+Config config_load(const std::string& path) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw Error("Cannot open " + path + ": No such file or directory");
+  std::string text((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+  size_t slash = path.rfind('/');
+  std::string base = slash == std::string::npos ? std::string() : path.substr(0, slash == 0 ? 1 : slash);
+  return parse_config(parse_ini(text), base);
+}
+
+Config config_load_str(const std::string& text, const std::string& base_dir) {
+  return parse_config(parse_ini(text), base_dir);
+}
+
+// ---- file formats -----------------------------------------------------------
+std::vector<float> parse_model_bin(const Bytes& b, const std::string& what) {
+  if (b.size() < 4) throw Error("Model file too small: " + what);
+  int32_t n;
+  std::memcpy(&n, b.data(), 4);
+  if (n < 0) throw Error("Model file " + what + " has a negative point count");
+  size_t expected = 4 + size_t(n) * 4;
+  if (b.size() < expected)
+    throw Error("Model file " + what + " too short (expected " + std::to_string(expected) + " bytes, got " +
+                std::to_string(b.size()) + ")");
+  std::vector<float> out(static_cast<size_t>(n));
+  std::memcpy(out.data(), b.data() + 4, size_t(n) * 4);
+  return out;
+}
+
+Bytes make_model_bin(const std::vector<float>& d) {
+  Bytes out(4 + d.size() * 4);
+  int32_t n = int32_t(d.size());
+  std::memcpy(out.data(), &n, 4);
+  std::memcpy(out.data() + 4, d.data(), d.size() * 4);
+  return out;
+}
+
+// solver.rs:270-285: header dict padded with spaces so that dict + '\n' is a
+// multiple of 64 bytes.
+Bytes make_npy(const float* data, size_t nrows, size_t ncols) {
+  std::string dict = "{'descr': '<f4', 'fortran_order': False, 'shape': (" + std::to_string(nrows) + ", " +
+                     std::to_string(ncols) + "), }";
+  size_t header_len = (dict.size() + 1 + 63) / 64 * 64;
+  std::string header = dict;
+  while (header.size() < header_len - 1) header.push_back(' ');
+  header.push_back('\n');
+  Bytes out;
+  out.reserve(10 + header_len + nrows * ncols * 4);
+  const char magic[] = "\x93NUMPY\x01\x00";
+  out.insert(out.end(), magic, magic + 8);
+  uint16_t hl = uint16_t(header_len);
+  out.push_back(uint8_t(hl & 0xff));
+  out.push_back(uint8_t(hl >> 8));
+  out.insert(out.end(), header.begin(), header.end());
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(data);
+  out.insert(out.end(), p, p + nrows * ncols * 4);
+  return out;
+}
+
+std::vector<float> parse_npy(const Bytes& b, const std::string& what) {
+  if (b.size() < 10 || std::memcmp(b.data(), "\x93NUMPY", 6) != 0) throw Error("Not a NumPy file: " + what);
+  size_t hl = size_t(b[8]) | (size_t(b[9]) << 8);
+  size_t start = 10 + hl;
+  if (b.size() < start) throw Error("Truncated .npy header in " + what);
+  if ((b.size() - start) % 4 != 0) throw Error("Payload length not a multiple of 4 in " + what);
+  std::vector<float> out(static_cast<size_t>((b.size() - start) / 4));
+  std::memcpy(out.data(), b.data() + start, out.size() * 4);
+  return out;
+}
+
+std::vector<std::vector<double>> parse_table(const std::string& text) {
+  std::vector<std::vector<double>> rows;
+  std::istringstream in(text);
+  std::string line;
+  while (std::getline(in, line)) {
+    std::string t = trim(line);
+    if (t.empty() || t[0] == '#') continue;
+    std::istringstream ls(t);
+    std::string tok;
+    std::vector<double> row;
+    while (ls >> tok) {
+      char* end = nullptr;
+      double v = std::strtod(tok.c_str(), &end);
+      row.push_back(end == tok.c_str() + tok.size() ? v : 0.0);  // unwrap_or(0.0)
+    }
+    rows.push_back(row);
+  }
+  return rows;
+}
+
+void ricker(float t, float f0, float t0, float ang_deg, float amp, float* x, float* y, float* z) {
+  const float a = (kPi * f0) * (kPi * f0);
+  const float d = t - t0;
+  const float stf = -amp * (1.0f - 2.0f * a * d * d) * std::exp(-a * d * d);
+  const float ang = ang_deg * (kPi / 180.0f);  // f32::to_radians
+  *x = stf * std::sin(ang);
+  *y = stf;
+  *z = -stf * std::cos(ang);
+}
+
+double waveform_misfit(const float* syn, const float* obs, int nrec, int nt, float dt, float* adstf) {
+  double misfit = 0.0;
+  const float t_end = float(nt - 1) * dt;
+  const float tw = t_end / 10.0f;
+  const float t_min = tw, t_max = t_end - tw;
+  for (int ir = 0; ir < nrec; ++ir) {
+    for (int it = 0; it < nt; ++it) {
+      const size_t kt = size_t(ir) * nt + it;
+      const size_t akt = size_t(ir) * nt + (nt - 1 - it);
+      const float t = float(it) * dt;
+      float taper = 1.0f;
+      if (t <= t_min) taper = 0.5f + 0.5f * std::cos(kPi * (t_min - t) / tw);
+      else if (t >= t_max) taper = 0.5f + 0.5f * std::cos(kPi * (t_max - t) / tw);
+      const float diff = (syn[kt] - obs[kt]) * taper;
+      misfit += double(diff) * double(diff);
+      adstf[akt] = diff * taper * 2.0f;
+    }
+  }
+  return std::sqrt(misfit);
+}
+
+GridInfo infer_grid(const std::vector<float>& x, const std::vector<float>& z) {
+  if (x.empty() || z.empty() || x.size() != z.size()) throw Error("coordinate files are empty or differ in size");
+  auto extent = [](const std::vector<float>& v) {
+    float lo = v[0], hi = v[0];
+    for (float a : v) { lo = std::min(lo, a); hi = std::max(hi, a); }
+    return hi - lo;
+  };
+  const float lx = extent(x), lz = extent(z);
+  if (!(lx > 0.0f) || !(lz > 0.0f)) throw Error("coordinate extents must be positive");
+  const double npt = double(x.size());
+  GridInfo g;
+  g.nx = int(std::round(std::sqrt(npt * double(lx) / double(lz))));
+  g.nz = int(std::round(std::sqrt(npt * double(lz) / double(lx))));
+  if (g.nx < 2 || g.nz < 2 || size_t(g.nx) * size_t(g.nz) != x.size())
+    throw Error("cannot infer a rectangular grid from the coordinates (nx=" + std::to_string(g.nx) +
+                ", nz=" + std::to_string(g.nz) + ", npt=" + std::to_string(x.size()) + ")");
+  g.dx = lx / float(g.nx - 1);
+  g.dz = lz / float(g.nz - 1);
+  return g;
+}
+
+uint32_t grid_index(float coord, float step) {
+  float r = std::round(coord / step);
+  if (!(r > 0.0f)) return 0;                 // saturating cast: negative and NaN -> 0
+  if (r >= 4294967295.0f) return 0xffffffffu;
+  return uint32_t(r);
+}
+
+void log_info(const std::string& msg) {
+  const char* lvl = std::getenv("SEISWG_LOG");
+  if (lvl && (std::strcmp(lvl, "error") == 0 || std::strcmp(lvl, "warn") == 0 || std::strcmp(lvl, "off") == 0)) return;
+  std::fprintf(stderr, "[seiswg] %s\n", msg.c_str());
+}
+
+// ---- Solver ----------------------------------------------------------------
+Bytes Solver::lookup(const Vfs& vfs, const std::string& path) const {
+  auto it = vfs.find(path);
+  if (it == vfs.end() && path.rfind("./", 0) == 0) it = vfs.find(path.substr(2));
+  if (it != vfs.end()) return it->second;
+  return read_file(path);
+}
+
+void Solver::write_file(const std::string& path, const Bytes& b) const {
+  std::ofstream f(path, std::ios::binary);
+  if (!f) throw Error("Cannot create " + path);
+  f.write(reinterpret_cast<const char*>(b.data()), std::streamsize(b.size()));
+  if (!f) throw Error("Cannot write " + path);
+}
+
+Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
+  const std::string model_dir = cfg.has_model_init ? cfg.model_init : cfg.has_model_true ? cfg.model_true : "";
+  if (!cfg.has_model_init && !cfg.has_model_true) throw Error("No model path in config");
+  const bool spin = cfg.spin;
+  auto load = [&](const std::string& name) {
+    std::string p = path_join(model_dir, "proc000000_" + name + ".bin");
+    return parse_model_bin(lookup(vfs, p), p);
+  };
+  std::vector<float> rho = load("rho");
+  const size_t npt = rho.size();
+  std::vector<float> x = load("x"), z = load("z");
+  if (x.size() != npt || z.size() != npt) throw Error("coordinate files do not match the model size");
+  grid_ = infer_grid(x, z);
+  {
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "Grid: nx=%d nz=%d npt=%zu dx=%.1f dz=%.1f", grid_.nx, grid_.nz, npt, grid_.dx,
+                  grid_.dz);
+    log_info(buf);
+  }
+
+  SimDesc d;
+  d.nx = grid_.nx;
+  d.nz = grid_.nz;
+  d.nt = int(cfg.nt);
+  d.dx = grid_.dx;
+  d.dz = grid_.dz;
+  d.dt = cfg.dt;
+  d.sh = cfg.sh;
+  d.psv = cfg.psv;
+  d.spin = cfg.spin;
+  d.abs_left = cfg.abs_left;
+  d.abs_right = cfg.abs_right;
+  d.abs_bottom = cfg.abs_bottom;
+  d.abs_top = cfg.abs_top;
+  d.abs_width = int(cfg.abs_width);
+  d.abs_alpha = cfg.abs_alpha;
+  sim_.reset(new Sim(d));
+  if (cfg.chunk_rows > 0) sim_->set_chunk_rows(cfg.chunk_rows);
+  if (cfg.graphs >= 0) sim_->set_use_graphs(cfg.graphs == 1);
+
+  auto upload = [&](ModelField f, const std::vector<float>& v, const std::string& what) {
+    if (v.size() != npt) throw Error("model file " + what + " does not match the density size");
+    sim_->upload_model(f, v.data());
+  };
+  upload(ModelField::RHO, rho, "rho");
+  if (spin) {
+    // solver.rs:626-638 and 664-671: spin models carry lambda/mu directly.
+    upload(ModelField::LAMBDA, load("lambda"), "lambda");
+    upload(ModelField::MU, load("mu"), "mu");
+    if (cfg.psv) {
+      upload(ModelField::NU, load("nu"), "nu");
+      upload(ModelField::J, load("j"), "j");
+      (void)load("lambda_c");  // read as the reference does; unused by the stencil
+      upload(ModelField::MU_C, load("mu_c"), "mu_c");
+      upload(ModelField::NU_C, load("nu_c"), "nu_c");
+    }
+  } else {
+    upload(ModelField::VP, load("vp"), "vp");
+    upload(ModelField::VS, load("vs"), "vs");
+  }
+  sim_->prepare_model();
+
+  // Sources (solver.rs:703-733).
+  const int nt = int(cfg.nt);
+  const Bytes src_bytes = lookup(vfs, cfg.sources);
+  auto src_rows = parse_table(std::string(reinterpret_cast<const char*>(src_bytes.data()), src_bytes.size()));
+  std::vector<int> si, sj;
+  for (size_t s = 0; s < src_rows.size(); ++s) {
+    const auto& r = src_rows[s];
+    auto g = [&](size_t q, double def) { return q < r.size() ? r[q] : def; };
+    SourceDesc sd;
+    const float sx = float(g(0, 0.0)), sz = float(g(1, 0.0));
+    sd.f0 = float(g(3, 10.0));
+    sd.t0 = float(g(4, 0.1));
+    sd.ang = float(g(5, 0.0));
+    sd.amp = float(g(6, 1.0e10));
+    uint32_t ix = grid_index(sx, grid_.dx), iz = grid_index(sz, grid_.dz);
+    if (ix >= uint32_t(grid_.nx) || iz >= uint32_t(grid_.nz))
+      throw Error("source " + std::to_string(s) + " at (" + std::to_string(sx) + ", " + std::to_string(sz) +
+                  ") lies outside the grid");
+    sd.i = int(ix);
+    sd.j = int(iz);
+    srcs_.push_back(sd);
+    si.push_back(sd.i);
+    sj.push_back(sd.j);
+  }
+  const size_t nsrc = srcs_.size();
+  std::vector<float> stf(3 * nsrc * size_t(nt));
+  for (size_t s = 0; s < nsrc; ++s) {
+    for (int it = 0; it < nt; ++it) {
+      float a, b, c;
+      ricker(float(it) * cfg.dt, srcs_[s].f0, srcs_[s].t0, srcs_[s].ang, srcs_[s].amp, &a, &b, &c);
+      stf[(0 * nsrc + s) * nt + it] = a;
+      stf[(1 * nsrc + s) * nt + it] = b;
+      stf[(2 * nsrc + s) * nt + it] = c;
+    }
+  }
+  sim_->set_sources(int(nsrc), si.data(), sj.data(), stf.data());
+
+  // Stations (solver.rs:742-751).
+  Bytes st = lookup(vfs, cfg.stations);
+  auto rec_rows = parse_table(std::string(reinterpret_cast<const char*>(st.data()), st.size()));
+  for (size_t r = 0; r < rec_rows.size(); ++r) {
+    const auto& row = rec_rows[r];
+    const float rx = float(row.size() > 0 ? row[0] : 0.0), rz = float(row.size() > 1 ? row[1] : 0.0);
+    uint32_t ix = grid_index(rx, grid_.dx), iz = grid_index(rz, grid_.dz);
+    if (ix >= uint32_t(grid_.nx) || iz >= uint32_t(grid_.nz))
+      throw Error("station " + std::to_string(r) + " at (" + std::to_string(rx) + ", " + std::to_string(rz) +
+                  ") lies outside the grid");
+    rec_i_.push_back(int(ix));
+    rec_j_.push_back(int(iz));
+  }
+  sim_->set_receivers(int(rec_i_.size()), rec_i_.data(), rec_j_.data());
+}
+
+Vfs Solver::run_forward() {
+  Vfs out;
+  const bool sh = cfg_.sh, psv = cfg_.psv, spin = cfg_.spin && cfg_.psv;
+  const int nt = int(cfg_.nt), nrec = this->nrec();
+  const uint32_t snap = cfg_.save_snapshot;
+  const std::string trace_dir = cfg_.has_output_traces ? cfg_.output_traces : path_join(cfg_.output, "traces");
+  if (write_files_) {
+    mkdirs(trace_dir);
+    if (snap > 0) mkdirs(cfg_.output);
+  }
+  std::vector<std::pair<int, int>> runs;
+  if (cfg_.combine_sources) runs.push_back({-1, 0});
+  else for (int s = 0; s < nsrc(); ++s) runs.push_back({s, s});
+
+  std::map<std::string, std::vector<float>> snap_bufs;
+  uint32_t snap_count = 0;
+  std::vector<float> obs(size_t(5) * nrec * nt);
+  for (auto [isrc, idx] : runs) {
+    log_info("Forward run  isrc=" + (isrc < 0 ? std::string("all") : std::to_string(isrc)) + "  (" +
+             std::to_string(nt) + " time steps)");
+    Sim::Snapshots snaps;
+    snaps.every = int(snap);
+    std::vector<std::string> names;
+    if (snap > 0) {
+      if (sh) { snaps.fields.push_back(StateField::VY); names.push_back("vy"); }
+      if (psv) {
+        snaps.fields.push_back(StateField::VX); names.push_back("vx");
+        snaps.fields.push_back(StateField::VZ); names.push_back("vz");
+        if (spin) { snaps.fields.push_back(StateField::VYC); names.push_back("ry"); }
+      }
+    }
+    sim_->run_forward(isrc, snap > 0 ? &snaps : nullptr);
+    // Snapshots (solver.rs:1035-1038, 1144-1176).
+    const size_t nf = snaps.fields.size();
+    for (size_t q = 0; q < snaps.steps.size(); ++q) {
+      for (size_t f = 0; f < nf; ++f) {
+        const std::vector<float>& fr = snaps.frames[q * nf + f];
+        auto& acc = snap_bufs[names[f]];
+        acc.insert(acc.end(), fr.begin(), fr.end());
+        if (write_files_) {
+          const uint8_t* p = reinterpret_cast<const uint8_t*>(fr.data());
+          write_file(path_join(cfg_.output, "proc" + fmt6(uint32_t(snaps.steps[q])) + "_" + names[f] + ".bin"),
+                     Bytes(p, p + fr.size() * 4));
+        }
+      }
+      ++snap_count;
+    }
+    // Traces (solver.rs:1047-1101).
+    sim_->download_traces(obs.data());
+    const size_t nobs = size_t(nrec) * nt;
+    auto emit = [&](const std::string& name, int comp, bool npy) {
+      const float* c = obs.data() + size_t(comp) * nobs;
+      std::string p = path_join(trace_dir, name + "_" + fmt6(uint32_t(idx)) + ".npy");
+      Bytes b = npy ? make_npy(c, size_t(nrec), size_t(nt))
+                    : Bytes(reinterpret_cast<const uint8_t*>(c), reinterpret_cast<const uint8_t*>(c + nobs));
+      if (write_files_) write_file(p, b);
+      out[p] = std::move(b);
+    };
+    if (sh) { emit("uy", 1, true); emit("vy", 1, false); }
+    if (psv) {
+      emit("ux", 0, true); emit("uz", 2, true);
+      emit("vx", 0, false); emit("vz", 2, false);
+      if (spin) { emit("ry", 1, true); emit("yi", 3, true); }
+    }
+    log_info("  -> traces saved to " + trace_dir);
+  }
+  if (snap_count > 0) {
+    Bytes nf(4);
+    std::memcpy(nf.data(), &snap_count, 4);
+    out["snapshot/nframes"] = nf;
+    for (auto& kv : snap_bufs) {
+      const uint8_t* p = reinterpret_cast<const uint8_t*>(kv.second.data());
+      out["snapshot/" + kv.first + ".f32"] = Bytes(p, p + kv.second.size() * 4);
+    }
+  }
+  return out;
+}
+
+Vfs Solver::run_adjoint(const Vfs& vfs) {
+  Vfs out;
+  const bool sh = cfg_.sh;
+  const int nt = int(cfg_.nt), nrec = this->nrec(), nsrc = this->nsrc();
+  const uint32_t adj = cfg_.adj_interval;
+  if (adj == 0) throw Error("adj_interval must be positive");
+  const uint32_t nsa = cfg_.nt / adj;
+  if (nsa == 0) throw Error("adj_interval (" + std::to_string(adj) + ") >= nt (" + std::to_string(nt) + ")");
+  if (write_files_) mkdirs(cfg_.output);
+  if (!cfg_.has_traces) throw Error("config [path] traces is required for the adjoint workflow");
+  const std::string obs_dir = cfg_.traces;
+
+  sim_->clear_kmu();
+  std::vector<std::pair<int, int>> runs;
+  if (cfg_.combine_sources) runs.push_back({-1, 0});
+  else for (int s = 0; s < nsrc; ++s) runs.push_back({s, s});
+
+  misfits_.clear();
+  total_misfit_ = 0.0;
+  std::vector<float> obs(size_t(5) * nrec * nt), adstf(size_t(nrec) * nt, 0.0f);
+  const size_t nobs = size_t(nrec) * nt;
+  for (size_t run = 0; run < runs.size(); ++run) {
+    const int isrc = runs[run].first, ref_idx = runs[run].second;
+    log_info("Adjoint: source " + std::to_string(run + 1) + "/" + std::to_string(runs.size()) + " (" +
+             std::to_string(nt) + " steps, " + std::to_string(nsa) + " checkpoints)...");
+    std::vector<float> ref;
+    if (sh) {
+      std::string p = path_join(obs_dir, "uy_" + fmt6(uint32_t(cfg_.combine_sources ? 0 : ref_idx)) + ".npy");
+      Bytes b;
+      try {
+        b = lookup(vfs, p);
+      } catch (const Error&) {
+        throw Error("Cannot load observed traces " + p);
+      }
+      ref = parse_npy(b, p);
+      if (ref.size() != nobs)
+        throw Error("observed traces " + p + " hold " + std::to_string(ref.size()) + " samples, expected " +
+                    std::to_string(nobs));
+    }
+    sim_->adjoint_forward(isrc, int(adj));
+    double misfit = 0.0;
+    if (sh) {
+      sim_->download_traces(obs.data());
+      misfit = waveform_misfit(obs.data() + nobs, ref.data(), nrec, nt, cfg_.dt, adstf.data());
+    } else {
+      std::fill(adstf.begin(), adstf.end(), 0.0f);
+    }
+    misfits_.push_back(misfit);
+    total_misfit_ += misfit;
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "Adjoint: source %zu misfit = %.6e", run + 1, misfit);
+    log_info(buf);
+    sim_->adjoint_backward(adstf.data(), int(adj));
+  }
+  {
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "Adjoint: total misfit = %.6e", total_misfit_);
+    log_info(buf);
+  }
+  sim_->smooth_kmu(cfg_.smooth);
+  std::vector<float> kmu(size_t(grid_.nx) * grid_.nz);
+  sim_->download_kmu(kmu.data());
+  const std::string kp = path_join(cfg_.output, "proc000000_kmu.bin");
+  const std::string gp = path_join(cfg_.output, "gradient_kmu.bin");
+  const uint8_t* p = reinterpret_cast<const uint8_t*>(kmu.data());
+  Bytes raw(p, p + kmu.size() * 4);
+  Bytes with_header = make_model_bin(kmu);
+  if (write_files_) {
+    write_file(kp, raw);
+    write_file(gp, with_header);
+  }
+  out[kp] = std::move(raw);
+  out[gp] = std::move(with_header);
+  log_info("Adjoint: gradient saved to " + kp);
+  return out;
+}
+
+}  // namespace seiswg
