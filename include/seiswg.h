@@ -136,7 +136,8 @@ int seiswg_sim_adjoint_forward(seiswg_sim* sim, int32_t isrc, int32_t adj_interv
 int seiswg_sim_adjoint_backward(seiswg_sim* sim, const float* adstf, int32_t adj_interval);
 int seiswg_sim_kernel_smooth(seiswg_sim* sim, float sigma);
 int seiswg_sim_kernel(seiswg_sim* sim, float* host);
-/* Options: "graphs" (0/1), "chunk_rows" (rows per warp march). */
+/* Options: "graphs" (0/1), "chunk_rows" (rows per warp march), "loader"
+ * (0: plain loads, 1: TMA bulk-copy row pipeline, the default). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */

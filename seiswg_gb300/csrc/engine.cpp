@@ -97,12 +97,16 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   geom_.rdz = float(1.0 / double(8.0f * d.dz));
   den_x_ = 8.0f * d.dx;
   den_z_ = 8.0f * d.dz;
-  set_chunk_rows(64);
+  geom_.loader = kLoaderBulk;
+  set_chunk_rows(model_chunk_rows());
+  SW_CUDA(cudaMalloc(&err_, sizeof(int)));
+  SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
   use_graphs_ = (size_t(d.nx) * d.nz <= (size_t(1) << 20));
 }
 
 Sim::~Sim() {
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  cudaFree(err_);
   cudaFree(stf_);
   cudaFree(adstf_);
   cudaFree(inj_dev_[0]);
@@ -126,6 +130,41 @@ void Sim::set_chunk_rows(int lx) {
   graphs_.clear();
 }
 
+int Sim::model_chunk_rows() const {
+  int dev = 0, nsm = 0;
+  SW_CUDA(cudaGetDevice(&dev));
+  SW_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int per_sm = step_blocks_per_sm(d_.psv, d_.psv && d_.spin, geom_.loader);
+  if (per_sm < 1) per_sm = 1;
+  const long resident = long(per_sm) * nsm * kStepWarps;
+  const int nstrips = (d_.nz + kStripCols - 1) / kStripCols;
+  int best = 64;
+  double best_cost = 1e300;
+  for (int lx = 8; lx <= 256; ++lx) {
+    const long warps = long(nstrips) * ((d_.nx + lx - 1) / lx);
+    const long waves = (warps + resident - 1) / resident;
+    const double cost = double(waves) * double(std::min(lx, d_.nx) + 5);
+    if (cost < best_cost - 1e-9) { best_cost = cost; best = lx; }
+  }
+  return best;
+}
+
+void Sim::set_loader(int loader) {
+  if (loader != kLoaderDirect && loader != kLoaderBulk) throw std::invalid_argument("unknown loader");
+  geom_.loader = loader;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+void Sim::check_device_error() const {
+  int e = 0;
+  SW_CUDA(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  if (e & kErrWaitTimeout)
+    throw CudaError("a step kernel gave up waiting for its row pipeline (bounded wait expired); "
+                    "results of this run are invalid");
+}
+
 float* Sim::alloc_field() { return field_ptr(static_cast<float*>(arena_.take(field_elems_ * sizeof(float)))); }
 
 void Sim::zero_state() {
@@ -137,7 +176,10 @@ void Sim::zero_state() {
   }
 }
 
-void Sim::synchronize() const { SW_CUDA(cudaStreamSynchronize(stream_)); }
+void Sim::synchronize() const {
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  check_device_error();
+}
 
 void Sim::upload_model(ModelField f, const float* host) {
   float* dst = nullptr;
@@ -338,6 +380,7 @@ void Sim::enqueue_step(int it, int b, const InjectList& inj_in, const ProbeList&
     p.inj = inj;
     p.probes = probes_in;
     p.probes.it = it;
+    p.err = err_;
     if (probes_in.n) p.probes.n = probe_split_;
     SW_CUDA(launch_sh_step(p, stream_));
     ++launches_;
@@ -354,6 +397,7 @@ void Sim::enqueue_step(int it, int b, const InjectList& inj_in, const ProbeList&
     p.inj = inj;
     p.probes = probes_in;
     p.probes.it = it;
+    p.err = err_;
     if (probes_in.n) {
       p.probes.list = probes_ + probe_split_;
       p.probes.n = nprobe_ - probe_split_;
@@ -503,6 +547,7 @@ void Sim::run_forward(int isrc, Snapshots* snaps) {
 }
 
 void Sim::download_traces(float* host) const {
+  check_device_error();
   if (!nrec_) return;
   SW_CUDA(cudaMemcpyAsync(host, obs_, size_t(5) * nrec_ * d_.nt * sizeof(float), cudaMemcpyDeviceToHost, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
@@ -513,6 +558,7 @@ void Sim::download_state(StateField f, float* host) const {
   if (!p) throw std::invalid_argument("field not present in this physics");
   copy_field_to_host(p, host);
   SW_CUDA(cudaStreamSynchronize(stream_));
+  check_device_error();
 }
 
 // ---------------------------------------------------------------------------

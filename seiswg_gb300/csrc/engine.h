@@ -112,6 +112,14 @@ class Sim {
   // Graph capture of whole time loops (replayed on repeated runs).
   void set_use_graphs(bool on) { use_graphs_ = on; }
   void set_chunk_rows(int lx);
+  // Rows per warp chunk from a wave-quantisation model: resident warps come
+  // from the occupancy of the step kernel; the cost of a choice is
+  // ceil(warps / resident) waves x (lx + 5) rows per warp.
+  int model_chunk_rows() const;
+  void set_loader(int loader);  // kLoaderDirect or kLoaderBulk
+  int loader() const { return geom_.loader; }
+  // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
+  void check_device_error() const;
   int chunk_rows() const { return geom_.lx; }
   uint64_t kernel_launches() const { return launches_; }
   void synchronize() const;
@@ -175,6 +183,7 @@ class Sim {
   size_t fwd_bytes_ = 0;
   int fwd_nsa_ = 0;
 
+  int* err_ = nullptr;            // device error word
   bool use_graphs_ = true;
   std::map<std::string, cudaGraphExec_t> graphs_;
   std::map<std::string, uint64_t> graph_nodes_;

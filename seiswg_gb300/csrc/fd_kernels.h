@@ -36,6 +36,7 @@ struct ShStep {
   const float *taper_x, *taper_zb, *taper_zt;
   InjectList inj;
   ProbeList probes;
+  int* err;  // device error word (kErr* bits)
 };
 
 struct PsvStep {
@@ -49,8 +50,13 @@ struct PsvStep {
   const float *taper_x, *taper_zb, *taper_zt;
   InjectList inj;
   ProbeList probes;
+  int* err;
 };
 
+// Dynamic shared memory of one step CTA for a loader (0 for direct loads).
+size_t step_smem_bytes(bool psv, bool spin, int loader);
+// Resident CTAs per SM of the step kernel for a loader (occupancy query).
+int step_blocks_per_sm(bool psv, bool spin, int loader);
 cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s);
 cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s);
 

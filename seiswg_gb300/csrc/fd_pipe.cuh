@@ -1,0 +1,164 @@
+// fd_pipe.cuh -- per-warp row pipeline of the step kernels.
+//
+// Each iteration of a warp's march consumes one "stage": NSEG row segments of
+// 128 floats (512 B, the warp's 32 float4 lanes), one per field, each from a
+// fixed row offset relative to the iteration's row.  Two loaders provide them:
+//
+//   DirectRows  plain 16-byte __ldg loads issued at the top of the iteration.
+//   BulkRows    a ring of S stages in shared memory filled by the TMA engine's
+//               bulk copy (cp.async.bulk ... mbarrier::complete_tx::bytes),
+//               lane 0 issuing S-1 iterations ahead; completion is tracked by
+//               one mbarrier per stage.  Waits are bounded: after kWaitLimit
+//               polls the warp records an error in *err, drains the copies it
+//               issued (again bounded) and leaves its march.
+#pragma once
+
+#include "fd_common.cuh"
+
+namespace seiswg {
+
+constexpr int kSegFloats = 128;  // 32 lanes x float4
+constexpr unsigned kWaitLimit = 1u << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait for the completion of phase `parity`.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (unsigned n = 0; n < kWaitLimit; ++n)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 16-byte aligned global -> shared bulk copy completing on `bar`.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Segment table: base pointer (element (0,0)) and row offset of each field.
+template <int NSEG>
+struct Segs {
+  const float* base[NSEG];
+  int roff[NSEG];
+};
+
+template <int NSEG>
+struct DirectRows {
+  static constexpr int kStages = 0;
+  static constexpr size_t smem_bytes_per_warp() { return 0; }
+  Segs<NSEG> s;
+  size_t ld;
+  int c0, ib;
+  f4 v[NSEG];
+  __device__ DirectRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int, float*, uint64_t*, int)
+      : s(segs), ld(ld_), c0(c0_), ib(ib_) {}
+  __device__ __forceinline__ void start() {}
+  // Loads the stage of iteration k (row i = ib - 1 + k).
+  __device__ __forceinline__ bool acquire(int k) {
+    const int i = ib - 1 + k;
+#pragma unroll
+    for (int q = 0; q < NSEG; ++q) v[q] = ld4(s.base[q] + ptrdiff_t(i + s.roff[q]) * ptrdiff_t(ld) + c0);
+    return true;
+  }
+  __device__ __forceinline__ const f4& seg(int q) const { return v[q]; }
+  __device__ __forceinline__ void release() {}
+  __device__ __forceinline__ void drain(int) {}
+};
+
+template <int NSEG, int S>
+struct BulkRows {
+  static constexpr int kStages = S;
+  static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
+  static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
+  Segs<NSEG> s;
+  size_t ld;
+  int c0, ib, lane, nk, cur;
+  float* buf;      // [S][NSEG][128]
+  uint64_t* bar;   // [S]
+  __device__ BulkRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int lane_, float* buf_,
+                      uint64_t* bar_, int nk_)
+      : s(segs), ld(ld_), c0(c0_), ib(ib_), lane(lane_), nk(nk_), cur(0), buf(buf_), bar(bar_) {}
+
+  __device__ __forceinline__ void issue(int k) {
+    const int st = k % S;
+    const int i = ib - 1 + k;
+    const int col0 = c0 - 4 * lane;  // the warp's first column (16-byte aligned)
+    mbar_expect_tx(&bar[st], kStageBytes);
+#pragma unroll
+    for (int q = 0; q < NSEG; ++q)
+      bulk_g2s(buf + (st * NSEG + q) * kSegFloats, s.base[q] + ptrdiff_t(i + s.roff[q]) * ptrdiff_t(ld) + col0,
+               kSegFloats * sizeof(float), &bar[st]);
+  }
+
+  // Barrier set-up and the first S-1 stages.
+  __device__ __forceinline__ void start() {
+    if (lane == 0) {
+      for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
+      fence_mbar_init();
+      for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
+    }
+    __syncwarp();
+  }
+
+  // Refills the stage consumed in iteration k-1 with iteration k+S-1, then
+  // waits for iteration k and reads the lane's float4 of every segment.
+  __device__ __forceinline__ bool acquire(int k) {
+    if (lane == 0 && k + S - 1 < nk) {
+      fence_proxy_async();  // order the warp's reads of the old stage before the copy
+      issue(k + S - 1);
+    }
+    cur = k % S;
+    return __all_sync(kFull, mbar_wait(&bar[cur], uint32_t(k / S) & 1u));
+  }
+  // The lane's float4 of segment q of the acquired stage.
+  __device__ __forceinline__ f4 seg(int q) const {
+    const float4 t = *reinterpret_cast<const float4*>(buf + (cur * NSEG + q) * kSegFloats + 4 * lane);
+    f4 r;
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    return r;
+  }
+  // All lanes have read the stage; it may be refilled.
+  __device__ __forceinline__ void release() { __syncwarp(); }
+  // After a failed wait at iteration k: wait (bounded) for the copies still
+  // in flight so that none lands after the warp has left.
+  __device__ __forceinline__ void drain(int k) {
+    for (int kk = k; kk < k + S && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
+    __syncwarp();
+  }
+};
+
+}  // namespace seiswg

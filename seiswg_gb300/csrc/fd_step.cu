@@ -9,31 +9,37 @@
 // state field is read once and written once per step, each material field
 // read once: 32 B (SH), 52 B (PSV), 96 B (spin) per cell-update.
 //
+// A warp marches down x over its chunk of rows.  Iteration k handles
+// velocity row i = ib-1+k (stress rows i-2..i+1 in a register ring) and
+// stress row r = i-2 (new velocity rows r-1..r+2 in a register ring).  Row
+// data arrive through a loader (fd_pipe.cuh): plain loads, or a shared-memory
+// ring fed by the TMA bulk-copy engine a few rows ahead.
+//
 // State is ping-ponged between two buffers (read step n, write step n+1):
 // a warp recomputes the velocity of its halo rows/columns from step-n data
-// that its neighbours are overwriting in place otherwise.
+// that its neighbours would otherwise be overwriting in place.
 //
 // Arithmetic follows the reference's expressions operation for operation
 // (built with -fmad=false), except that divisions by 8*dx, rho and J are
 // multiplies by precomputed reciprocals; results track the FP32 reference to
 // rounding (relative L2 ~1e-7 over thousands of steps).
-#include "fd_common.cuh"
 #include "fd_kernels.h"
+#include "fd_pipe.cuh"
 
 namespace seiswg {
 
 namespace {
 
-// Row march bounds and per-lane set-up shared by both kernels.
 struct March {
-  int lane, strip, chunk, ib, ie;
+  int lane, warp, strip, chunk, ib, ie;
   bool active;
 };
 
 __device__ __forceinline__ March march_of(const Geom& g) {
   March m;
   m.lane = threadIdx.x & 31;
-  int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  m.warp = threadIdx.x >> 5;
+  int gw = blockIdx.x * (blockDim.x >> 5) + m.warp;
   m.strip = gw % g.nstrips;
   m.chunk = gw / g.nstrips;
   m.active = m.chunk < g.nchunks;
@@ -44,19 +50,36 @@ __device__ __forceinline__ March march_of(const Geom& g) {
 
 // Adds the injections of row i (sources, or adjoint sources at receivers) to
 // the lane's divergence values.  `ci` is the list cursor, advanced past row i.
-__device__ __forceinline__ void inject_row(const InjectList& inj, int i, int c0, int& ci, f4* ds_x, f4* ds_y,
-                                           f4* ds_z) {
+// Element e of an f4 is selected with unrolled compares: a runtime index
+// into a register array would move the whole array to local memory.
+template <bool X, bool Y, bool Z>
+__device__ __forceinline__ void inject_row(const InjectList& inj, int i, int c0, int& ci, f4& ds_x, f4& ds_y,
+                                           f4& ds_z) {
   while (ci < inj.n && __ldg(&inj.list[ci].i) == i) {
-    int j = __ldg(&inj.list[ci].j);
-    int e = j - c0;
+    const int e = __ldg(&inj.list[ci].j) - c0;
     if (e >= 0 && e < 4) {
-      size_t o = size_t(__ldg(&inj.list[ci].row)) * inj.nt + inj.it;
-      if (ds_x) ds_x->v[e] += __ldg(&inj.val_x[o]);
-      if (ds_y) ds_y->v[e] += __ldg(&inj.val_y[o]);
-      if (ds_z) ds_z->v[e] += __ldg(&inj.val_z[o]);
+      const size_t o = size_t(__ldg(&inj.list[ci].row)) * inj.nt + inj.it;
+      const float ax = X ? __ldg(&inj.val_x[o]) : 0.0f;
+      const float ay = Y ? __ldg(&inj.val_y[o]) : 0.0f;
+      const float az = Z ? __ldg(&inj.val_z[o]) : 0.0f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (q == e) {
+          if (X) ds_x.v[q] += ax;
+          if (Y) ds_y.v[q] += ay;
+          if (Z) ds_z.v[q] += az;
+        }
+      }
     }
     ++ci;
   }
+}
+
+__device__ __forceinline__ float pick4(const f4& a, int e) {
+  float r = a.v[0];
+#pragma unroll
+  for (int q = 1; q < 4; ++q) r = (q == e) ? a.v[q] : r;
+  return r;
 }
 
 // Integrates the displacement of the owned probes of row i and records it.
@@ -77,12 +100,48 @@ __device__ __forceinline__ void probe_row(const ProbeList& pr, int i, const Lane
   }
 }
 
+__device__ __forceinline__ void flag_timeout(int* err) {
+  if ((threadIdx.x & 31) == 0 && err) atomicOr(err, kErrWaitTimeout);
+}
+
+template <int NSEG>
+struct DirectL : DirectRows<NSEG> {
+  using SegsT = Segs<NSEG>;
+  static constexpr uint32_t kStageBytes = 0;
+  using DirectRows<NSEG>::DirectRows;
+};
+
+template <int NSEG>
+struct BulkL : BulkRows<NSEG, kPipeStages> {
+  using SegsT = Segs<NSEG>;
+  using BulkRows<NSEG, kPipeStages>::BulkRows;
+};
+
+// Per-warp slices of the CTA's dynamic shared memory: [warps][S][NSEG][128]
+// floats, then [warps][S] mbarriers.
+template <class Loader>
+__device__ __forceinline__ Loader make_loader(const typename Loader::SegsT& segs, const Geom& g, const March& m,
+                                              const LaneCols& L, unsigned char* smem) {
+  float* buf = nullptr;
+  uint64_t* bar = nullptr;
+  if (Loader::kStages > 0) {
+    const size_t per = size_t(Loader::kStages) * Loader::kStageBytes;
+    buf = reinterpret_cast<float*>(smem + per * m.warp);
+    bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
+  }
+  return Loader(segs, size_t(g.ld), L.c0, m.ib, m.lane, buf, bar, m.ie - m.ib + 3);
+}
+
 }  // namespace
 
 // --------------------------------------------------------------------------
-// SH: state vy, sxy, szy; material rho, mu.  fd2d.wgsl:242-301.
+// SH: state vy, sxy, szy; material 1/rho, mu.  fd2d.wgsl:242-301.
 // --------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) sh_step_kernel(const ShStep p) {
+enum ShSeg { SH_SXY = 0, SH_SZY, SH_VY, SH_RHO, SH_MU, SH_NSEG };
+
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32) sh_step_kernel(const ShStep p) {
+  extern __shared__ __align__(128) unsigned char smem[];
   const Geom& g = p.g;
   const March m = march_of(g);
   if (!m.active) return;
@@ -92,20 +151,37 @@ __global__ void __launch_bounds__(128) sh_step_kernel(const ShStep p) {
   const int c0 = L.c0;
   auto at = [&](auto* base, int i) { return base + ptrdiff_t(i) * ptrdiff_t(ld) + c0; };
 
-  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  typename Loader::SegsT segs;
+  segs.base[SH_SXY] = p.sxy0; segs.roff[SH_SXY] = 1;
+  segs.base[SH_SZY] = p.szy0; segs.roff[SH_SZY] = 1;
+  segs.base[SH_VY] = p.vy0; segs.roff[SH_VY] = 0;
+  segs.base[SH_RHO] = p.rho; segs.roff[SH_RHO] = 0;
+  segs.base[SH_MU] = p.mu; segs.roff[SH_MU] = -2;
+  Loader rows = make_loader<Loader>(segs, g, m, L, smem);
+  rows.start();
 
-  // Rings: sxy rows i-2..i+1, szy rows i-2..i+1, new vy rows i-3..i.
-  f4 xy0 = ld4(at(p.sxy0, m.ib - 3)), xy1 = ld4(at(p.sxy0, m.ib - 2)), xy2 = ld4(at(p.sxy0, m.ib - 1)),
-     xy3 = ld4(at(p.sxy0, m.ib));
-  f4 zy0 = ld4(at(p.szy0, m.ib - 3)), zy1 = ld4(at(p.szy0, m.ib - 2)), zy2 = ld4(at(p.szy0, m.ib - 1)),
-     zy3 = ld4(at(p.szy0, m.ib));
+  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  // Rings: sxy, szy rows i-2..i+1 (slot 3 arrives with iteration k); new vy rows i-3..i.
+  f4 xy0 = ld4(at(p.sxy0, m.ib - 3)), xy1 = ld4(at(p.sxy0, m.ib - 2)), xy2 = ld4(at(p.sxy0, m.ib - 1)), xy3;
+  f4 zy0 = ld4(at(p.szy0, m.ib - 3)), zy1 = ld4(at(p.szy0, m.ib - 2)), zy2 = ld4(at(p.szy0, m.ib - 1)), zy3;
   f4 va, vb, vc, vd;
   int ci = lower_row(p.inj.list, p.inj.n, m.ib - 1);
   int pi = lower_row(p.probes.list, p.probes.n, m.ib);
+  const int nk = m.ie - m.ib + 3;
 
-  for (int i = m.ib - 1; i <= m.ie + 1; ++i) {
-    const f4 vo = ld4(at(p.vy0, i));
-    const f4 rho = ld4(at(p.rho, i));
+  for (int k = 0; k < nk; ++k) {
+    const int i = m.ib - 1 + k;
+    if (!rows.acquire(k)) {
+      flag_timeout(p.err);
+      rows.drain(k);
+      return;
+    }
+    xy3 = rows.seg(SH_SXY);
+    zy3 = rows.seg(SH_SZY);
+    const f4 vo = rows.seg(SH_VY);
+    const f4 rho = rows.seg(SH_RHO);
+    const f4 mu = rows.seg(SH_MU);
+    rows.release();
     const float bxi = __ldg(p.taper_x + i);
     const bool xb = (i >= 2 && i < g.nx - 2);
 
@@ -114,7 +190,7 @@ __global__ void __launch_bounds__(128) sh_step_kernel(const ShStep p) {
     const f4 dz = dz_back(zy2, g.rdz, L.zb);
 #pragma unroll
     for (int e = 0; e < 4; ++e) ds.v[e] = ds.v[e] + dz.v[e];
-    inject_row(p.inj, i, c0, ci, nullptr, &ds, nullptr);  // stf_dsy / adj_dsy
+    inject_row<false, true, false>(p.inj, i, c0, ci, ds, ds, ds);  // stf_dsy / adj_dsy
 
     // add_vy (fd2d.wgsl:268): vy = b * (vy + dt * DSY / rho), with the
     // buoyancy 1/rho stored in place of rho.
@@ -125,7 +201,7 @@ __global__ void __launch_bounds__(128) sh_step_kernel(const ShStep p) {
     }
     if (i >= m.ib && i < m.ie) {
       st4_masked(at(p.vy1, i), vd, L.own);
-      if (p.probes.n) probe_row(p.probes, i, L, pi, dt, [&](int, int e) { return vd.v[e]; });
+      if (p.probes.n) probe_row(p.probes, i, L, pi, dt, [&](int, int e) { return pick4(vd, e); });
     }
 
     // Stress of row r = i-2 from new vy rows r-1..r+2 = (va, vb, vc, vd).
@@ -134,7 +210,6 @@ __global__ void __launch_bounds__(128) sh_step_kernel(const ShStep p) {
       const bool xf = (r >= 1 && r < g.nx - 2);
       const f4 gx = dx4(va, vb, vc, vd, g.rdx, xf);
       const f4 gz = dz_fwd(vb, g.rdz, L.zf);
-      const f4 mu = ld4(at(p.mu, r));
       f4 sx, sz;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -149,20 +224,22 @@ __global__ void __launch_bounds__(128) sh_step_kernel(const ShStep p) {
     va = vb; vb = vc; vc = vd;
     xy0 = xy1; xy1 = xy2; xy2 = xy3;
     zy0 = zy1; zy1 = zy2; zy2 = zy3;
-    if (i <= m.ie) {
-      xy3 = ld4(at(p.sxy0, i + 2));
-      zy3 = ld4(at(p.szy0, i + 2));
-    }
   }
 }
 
 // --------------------------------------------------------------------------
 // PSV (+ micropolar spin): state vx, vz, sxx, szz, sxz (+ vy_c, syx_c, syy_c,
-// syz_c); material rho, lambda, mu (+ nu, J, mu_c+nu_c).
+// syz_c); material 1/rho, lambda, mu (+ nu, 1/J, mu_c+nu_c).
 // fd2d.wgsl:308-399 and 319-339, 405-445.
 // --------------------------------------------------------------------------
-template <bool SPIN>
-__global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
+enum PsvSeg {
+  PV_SXX = 0, PV_SXZ, PV_SZZ, PV_VX, PV_VZ, PV_RHO, PV_LAM, PV_MU, PV_NSEG,
+  PV_SYX = PV_NSEG, PV_SYY, PV_SYZ, PV_VYC, PV_J, PV_NU, PV_MC, PV_NSEG_SPIN
+};
+
+template <bool SPIN, class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32) psv_step_kernel(const PsvStep p) {
+  extern __shared__ __align__(128) unsigned char smem[];
   const Geom& g = p.g;
   const March m = march_of(g);
   if (!m.active) return;
@@ -172,33 +249,70 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
   const int c0 = L.c0;
   auto at = [&](auto* base, int i) { return base + ptrdiff_t(i) * ptrdiff_t(ld) + c0; };
 
-  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  typename Loader::SegsT segs;
+  segs.base[PV_SXX] = p.sxx0; segs.roff[PV_SXX] = 1;
+  segs.base[PV_SXZ] = p.sxz0; segs.roff[PV_SXZ] = 1;
+  segs.base[PV_SZZ] = p.szz0; segs.roff[PV_SZZ] = 1;
+  segs.base[PV_VX] = p.vx0; segs.roff[PV_VX] = 0;
+  segs.base[PV_VZ] = p.vz0; segs.roff[PV_VZ] = 0;
+  segs.base[PV_RHO] = p.rho; segs.roff[PV_RHO] = 0;
+  segs.base[PV_LAM] = p.lam; segs.roff[PV_LAM] = -2;
+  segs.base[PV_MU] = p.mu; segs.roff[PV_MU] = -2;
+  if constexpr (SPIN) {
+    segs.base[PV_SYX] = p.syx0; segs.roff[PV_SYX] = 1;
+    segs.base[PV_SYY] = p.syy0; segs.roff[PV_SYY] = 1;
+    segs.base[PV_SYZ] = p.syz0; segs.roff[PV_SYZ] = 1;
+    segs.base[PV_VYC] = p.vyc0; segs.roff[PV_VYC] = 0;
+    segs.base[PV_J] = p.jm; segs.roff[PV_J] = 0;
+    segs.base[PV_NU] = p.nu; segs.roff[PV_NU] = -2;
+    segs.base[PV_MC] = p.mc; segs.roff[PV_MC] = -2;
+  }
+  Loader rows = make_loader<Loader>(segs, g, m, L, smem);
+  rows.start();
 
-  f4 xx0 = ld4(at(p.sxx0, m.ib - 3)), xx1 = ld4(at(p.sxx0, m.ib - 2)), xx2 = ld4(at(p.sxx0, m.ib - 1)),
-     xx3 = ld4(at(p.sxx0, m.ib));
-  f4 xz0 = ld4(at(p.sxz0, m.ib - 3)), xz1 = ld4(at(p.sxz0, m.ib - 2)), xz2 = ld4(at(p.sxz0, m.ib - 1)),
-     xz3 = ld4(at(p.sxz0, m.ib));
-  f4 zz0 = ld4(at(p.szz0, m.ib - 3)), zz1 = ld4(at(p.szz0, m.ib - 2)), zz2 = ld4(at(p.szz0, m.ib - 1)),
-     zz3 = ld4(at(p.szz0, m.ib));
+  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  f4 xx0 = ld4(at(p.sxx0, m.ib - 3)), xx1 = ld4(at(p.sxx0, m.ib - 2)), xx2 = ld4(at(p.sxx0, m.ib - 1)), xx3;
+  f4 xz0 = ld4(at(p.sxz0, m.ib - 3)), xz1 = ld4(at(p.sxz0, m.ib - 2)), xz2 = ld4(at(p.sxz0, m.ib - 1)), xz3;
+  f4 zz0 = ld4(at(p.szz0, m.ib - 3)), zz1 = ld4(at(p.szz0, m.ib - 2)), zz2 = ld4(at(p.szz0, m.ib - 1)), zz3;
   f4 yx0, yx1, yx2, yx3, yy0, yy1, yy2, yy3, yz0, yz1, yz2, yz3;
-  if (SPIN) {
+  if constexpr (SPIN) {
     yx0 = ld4(at(p.syx0, m.ib - 3)); yx1 = ld4(at(p.syx0, m.ib - 2)); yx2 = ld4(at(p.syx0, m.ib - 1));
-    yx3 = ld4(at(p.syx0, m.ib));
     yy0 = ld4(at(p.syy0, m.ib - 3)); yy1 = ld4(at(p.syy0, m.ib - 2)); yy2 = ld4(at(p.syy0, m.ib - 1));
-    yy3 = ld4(at(p.syy0, m.ib));
     yz0 = ld4(at(p.syz0, m.ib - 3)); yz1 = ld4(at(p.syz0, m.ib - 2)); yz2 = ld4(at(p.syz0, m.ib - 1));
-    yz3 = ld4(at(p.syz0, m.ib));
   }
   f4 xa, xb_, xc, xd;   // new vx rows i-3..i
   f4 za, zb_, zc, zd;   // new vz rows i-3..i
   f4 ya, yb, yc, yd;    // new vy_c rows i-3..i
   int ci = lower_row(p.inj.list, p.inj.n, m.ib - 1);
   int pi = lower_row(p.probes.list, p.probes.n, m.ib);
+  const int nk = m.ie - m.ib + 3;
 
-  for (int i = m.ib - 1; i <= m.ie + 1; ++i) {
-    const f4 vxo = ld4(at(p.vx0, i));
-    const f4 vzo = ld4(at(p.vz0, i));
-    const f4 rho = ld4(at(p.rho, i));
+  for (int k = 0; k < nk; ++k) {
+    const int i = m.ib - 1 + k;
+    if (!rows.acquire(k)) {
+      flag_timeout(p.err);
+      rows.drain(k);
+      return;
+    }
+    xx3 = rows.seg(PV_SXX);
+    xz3 = rows.seg(PV_SXZ);
+    zz3 = rows.seg(PV_SZZ);
+    const f4 vxo = rows.seg(PV_VX);
+    const f4 vzo = rows.seg(PV_VZ);
+    const f4 rho = rows.seg(PV_RHO);
+    const f4 lam = rows.seg(PV_LAM);
+    const f4 mu = rows.seg(PV_MU);
+    f4 vyo, jj, nu, mc;
+    if constexpr (SPIN) {
+      yx3 = rows.seg(PV_SYX);
+      yy3 = rows.seg(PV_SYY);
+      yz3 = rows.seg(PV_SYZ);
+      vyo = rows.seg(PV_VYC);
+      jj = rows.seg(PV_J);
+      nu = rows.seg(PV_NU);
+      mc = rows.seg(PV_MC);
+    }
+    rows.release();
     const float bxi = __ldg(p.taper_x + i);
     const bool xbk = (i >= 2 && i < g.nx - 2);
 
@@ -212,7 +326,7 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
       for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
     }
     f4 dsy;
-    if (SPIN) {
+    if constexpr (SPIN) {
       // div_sy_c (fd2d.wgsl:338), then div_sxyz_c (fd2d.wgsl:326-329)
       dsy = dx4(yx0, yx1, yx2, yx3, g.rdx, xbk);
       const f4 a = dz_back(yz2, g.rdz, L.zb);
@@ -226,32 +340,32 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
         dsy.v[e] += 2.0f * yy2.v[e];
       }
     }
-    inject_row(p.inj, i, c0, ci, &dsx, nullptr, &dsz);  // stf_dsxz, fd2d.wgsl:350-351
+    inject_row<true, false, true>(p.inj, i, c0, ci, dsx, dsx, dsz);  // stf_dsxz, fd2d.wgsl:350-351
 
-    // add_vxz (fd2d.wgsl:362-363)
+    // add_vxz (fd2d.wgsl:362-363), rho holding 1/rho
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const float b = (bxi * tb.v[e]) * tt.v[e];
-      xd.v[e] = b * (vxo.v[e] + dt * dsx.v[e] * rho.v[e]);  // rho holds 1/rho
+      xd.v[e] = b * (vxo.v[e] + dt * dsx.v[e] * rho.v[e]);
       zd.v[e] = b * (vzo.v[e] + dt * dsz.v[e] * rho.v[e]);
     }
-    if (SPIN) {
-      // add_vy_c (fd2d.wgsl:412)
-      const f4 vyo = ld4(at(p.vyc0, i));
-      const f4 jj = ld4(at(p.jm, i));
+    if constexpr (SPIN) {
+      // add_vy_c (fd2d.wgsl:412), jm holding 1/J
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float b = (bxi * tb.v[e]) * tt.v[e];
-        yd.v[e] = b * (vyo.v[e] + dt * dsy.v[e] * jj.v[e]);  // jm holds 1/J
+        yd.v[e] = b * (vyo.v[e] + dt * dsy.v[e] * jj.v[e]);
       }
     }
     if (i >= m.ib && i < m.ie) {
       st4_masked(at(p.vx1, i), xd, L.own);
       st4_masked(at(p.vz1, i), zd, L.own);
-      if (SPIN) st4_masked(at(p.vyc1, i), yd, L.own);
+      if constexpr (SPIN) st4_masked(at(p.vyc1, i), yd, L.own);
       if (p.probes.n)
         probe_row(p.probes, i, L, pi, dt, [&](int comp, int e) {
-          return comp == kProbeVX ? xd.v[e] : comp == kProbeVZ ? zd.v[e] : (SPIN ? yd.v[e] : 0.0f);
+          if constexpr (SPIN)
+            return comp == kProbeVX ? pick4(xd, e) : comp == kProbeVZ ? pick4(zd, e) : pick4(yd, e);
+          return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e);
         });
     }
 
@@ -264,8 +378,6 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
       const f4 dvzdx = dx4(za, zb_, zc, zd, g.rdx, xf);
       const f4 dvxdz = dz_fwd(xb_, g.rdz, L.zf);
       const f4 dvzdz = dz_fwd(zb_, g.rdz, L.zf);
-      const f4 lam = ld4(at(p.lam, r));
-      const f4 mu = ld4(at(p.mu, r));
       f4 sxx, szz, sxz;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -278,12 +390,10 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
       st4_masked(at(p.sxx1, r), sxx, L.own);
       st4_masked(at(p.szz1, r), szz, L.own);
       st4_masked(at(p.sxz1, r), sxz, L.own);
-      if (SPIN) {
+      if constexpr (SPIN) {
         // div_vy_c (fd2d.wgsl:423-424), add_sy_c (fd2d.wgsl:442-444)
         const f4 gx = dx4(ya, yb, yc, yd, g.rdx, xf);
         const f4 gz = dz_fwd(yb, g.rdz, L.zf);
-        const f4 nu = ld4(at(p.nu, r));
-        const f4 mc = ld4(at(p.mc, r));
         f4 syy, syx, syz;
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
@@ -302,21 +412,11 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
     xx0 = xx1; xx1 = xx2; xx2 = xx3;
     xz0 = xz1; xz1 = xz2; xz2 = xz3;
     zz0 = zz1; zz1 = zz2; zz2 = zz3;
-    if (SPIN) {
+    if constexpr (SPIN) {
       ya = yb; yb = yc; yc = yd;
       yx0 = yx1; yx1 = yx2; yx2 = yx3;
       yy0 = yy1; yy1 = yy2; yy2 = yy3;
       yz0 = yz1; yz1 = yz2; yz2 = yz3;
-    }
-    if (i <= m.ie) {
-      xx3 = ld4(at(p.sxx0, i + 2));
-      xz3 = ld4(at(p.sxz0, i + 2));
-      zz3 = ld4(at(p.szz0, i + 2));
-      if (SPIN) {
-        yx3 = ld4(at(p.syx0, i + 2));
-        yy3 = ld4(at(p.syy0, i + 2));
-        yz3 = ld4(at(p.syz0, i + 2));
-      }
     }
   }
 }
@@ -324,22 +424,93 @@ __global__ void __launch_bounds__(128) psv_step_kernel(const PsvStep p) {
 // --------------------------------------------------------------------------
 // Launchers
 // --------------------------------------------------------------------------
-static inline unsigned blocks_for(const Geom& g) {
+namespace {
+
+unsigned blocks_for(const Geom& g) {
   long warps = long(g.nstrips) * g.nchunks;
   return unsigned((warps + kStepWarps - 1) / kStepWarps);
 }
 
-cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s) {
-  sh_step_kernel<<<blocks_for(p.g), kStepWarps * 32, 0, s>>>(p);
+template <class L>
+size_t smem_for() {
+  return L::kStages ? size_t(kStepWarps) * L::smem_bytes_per_warp() : 0;
+}
+
+template <typename K>
+cudaError_t prepare_kernel(K kernel, size_t smem) {
+  // Opt in to more than 48 KB of dynamic shared memory.
+  if (smem > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  return cudaSuccess;
+}
+
+template <class L>
+cudaError_t launch_sh(const ShStep& p, cudaStream_t s) {
+  const size_t smem = smem_for<L>();
+  static const cudaError_t attr = prepare_kernel(sh_step_kernel<L>, smem);
+  if (attr != cudaSuccess) return attr;
+  sh_step_kernel<L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
   return cudaGetLastError();
 }
 
-cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s) {
-  if (spin)
-    psv_step_kernel<true><<<blocks_for(p.g), kStepWarps * 32, 0, s>>>(p);
-  else
-    psv_step_kernel<false><<<blocks_for(p.g), kStepWarps * 32, 0, s>>>(p);
+template <bool SPIN, class L>
+cudaError_t launch_psv(const PsvStep& p, cudaStream_t s) {
+  const size_t smem = smem_for<L>();
+  static const cudaError_t attr = prepare_kernel(psv_step_kernel<SPIN, L>, smem);
+  if (attr != cudaSuccess) return attr;
+  psv_step_kernel<SPIN, L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
   return cudaGetLastError();
+}
+
+}  // namespace
+
+size_t step_smem_bytes(bool psv, bool spin, int loader) {
+  if (loader != kLoaderBulk) return 0;
+  if (!psv) return smem_for<BulkL<SH_NSEG>>();
+  return spin ? smem_for<BulkL<PV_NSEG_SPIN>>() : smem_for<BulkL<PV_NSEG>>();
+}
+
+int step_blocks_per_sm(bool psv, bool spin, int loader) {
+  int n = 0;
+  const int threads = kStepWarps * 32;
+  const size_t smem = step_smem_bytes(psv, spin, loader);
+  cudaError_t e;
+  if (!psv) {
+    e = loader == kLoaderBulk
+            ? (prepare_kernel(sh_step_kernel<BulkL<SH_NSEG>>, smem),
+               cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step_kernel<BulkL<SH_NSEG>>, threads, smem))
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step_kernel<DirectL<SH_NSEG>>, threads, smem);
+  } else if (spin) {
+    e = loader == kLoaderBulk
+            ? (prepare_kernel(psv_step_kernel<true, BulkL<PV_NSEG_SPIN>>, smem),
+               cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<true, BulkL<PV_NSEG_SPIN>>,
+                                                             threads, smem))
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<true, DirectL<PV_NSEG_SPIN>>,
+                                                            threads, smem);
+  } else {
+    e = loader == kLoaderBulk
+            ? (prepare_kernel(psv_step_kernel<false, BulkL<PV_NSEG>>, smem),
+               cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<false, BulkL<PV_NSEG>>, threads,
+                                                             smem))
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<false, DirectL<PV_NSEG>>, threads,
+                                                            smem);
+  }
+  return e == cudaSuccess ? n : 0;
+}
+
+
+cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s) {
+  if (p.g.loader == kLoaderBulk) return launch_sh<BulkL<SH_NSEG>>(p, s);
+  return launch_sh<DirectL<SH_NSEG>>(p, s);
+}
+
+cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s) {
+  if (spin) {
+    if (p.g.loader == kLoaderBulk) return launch_psv<true, BulkL<PV_NSEG_SPIN>>(p, s);
+    return launch_psv<true, DirectL<PV_NSEG_SPIN>>(p, s);
+  }
+  if (p.g.loader == kLoaderBulk) return launch_psv<false, BulkL<PV_NSEG>>(p, s);
+  return launch_psv<false, DirectL<PV_NSEG>>(p, s);
 }
 
 }  // namespace seiswg

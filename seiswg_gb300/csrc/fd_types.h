@@ -51,6 +51,14 @@ struct Geom {
   float dt;
   float rdx;     // 1/(8*dx): reciprocal of the reference's denominator (fd2d.wgsl:156)
   float rdz;     // 1/(8*dz)
+  int loader;    // kLoaderDirect or kLoaderBulk
 };
+
+// Row loaders of the step kernels (fd_pipe.cuh).
+enum { kLoaderDirect = 0, kLoaderBulk = 1 };
+constexpr int kPipeStages = 3;  // shared-memory stages per warp (2 rows in flight)
+
+// Bits of the device error word.
+enum { kErrWaitTimeout = 1 };
 
 }  // namespace seiswg

@@ -412,48 +412,6 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
     log_info(buf);
   }
 
-  SimDesc d;
-  d.nx = grid_.nx;
-  d.nz = grid_.nz;
-  d.nt = int(cfg.nt);
-  d.dx = grid_.dx;
-  d.dz = grid_.dz;
-  d.dt = cfg.dt;
-  d.sh = cfg.sh;
-  d.psv = cfg.psv;
-  d.spin = cfg.spin;
-  d.abs_left = cfg.abs_left;
-  d.abs_right = cfg.abs_right;
-  d.abs_bottom = cfg.abs_bottom;
-  d.abs_top = cfg.abs_top;
-  d.abs_width = int(cfg.abs_width);
-  d.abs_alpha = cfg.abs_alpha;
-  sim_.reset(new Sim(d));
-  if (cfg.chunk_rows > 0) sim_->set_chunk_rows(cfg.chunk_rows);
-  if (cfg.graphs >= 0) sim_->set_use_graphs(cfg.graphs == 1);
-
-  auto upload = [&](ModelField f, const std::vector<float>& v, const std::string& what) {
-    if (v.size() != npt) throw Error("model file " + what + " does not match the density size");
-    sim_->upload_model(f, v.data());
-  };
-  upload(ModelField::RHO, rho, "rho");
-  if (spin) {
-    // solver.rs:626-638 and 664-671: spin models carry lambda/mu directly.
-    upload(ModelField::LAMBDA, load("lambda"), "lambda");
-    upload(ModelField::MU, load("mu"), "mu");
-    if (cfg.psv) {
-      upload(ModelField::NU, load("nu"), "nu");
-      upload(ModelField::J, load("j"), "j");
-      (void)load("lambda_c");  // read as the reference does; unused by the stencil
-      upload(ModelField::MU_C, load("mu_c"), "mu_c");
-      upload(ModelField::NU_C, load("nu_c"), "nu_c");
-    }
-  } else {
-    upload(ModelField::VP, load("vp"), "vp");
-    upload(ModelField::VS, load("vs"), "vs");
-  }
-  sim_->prepare_model();
-
   // Sources (solver.rs:703-733).
   const int nt = int(cfg.nt);
   const Bytes src_bytes = lookup(vfs, cfg.sources);
@@ -489,7 +447,6 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
       stf[(2 * nsrc + s) * nt + it] = c;
     }
   }
-  sim_->set_sources(int(nsrc), si.data(), sj.data(), stf.data());
 
   // Stations (solver.rs:742-751).
   Bytes st = lookup(vfs, cfg.stations);
@@ -504,6 +461,54 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
     rec_i_.push_back(int(ix));
     rec_j_.push_back(int(iz));
   }
+  // Remaining model fields (solver.rs:626-638, 661-675): spin models carry
+  // lambda/mu directly, the others vp/vs.
+  std::vector<std::pair<ModelField, std::vector<float>>> fields;
+  fields.emplace_back(ModelField::RHO, std::move(rho));
+  if (spin) {
+    fields.emplace_back(ModelField::LAMBDA, load("lambda"));
+    fields.emplace_back(ModelField::MU, load("mu"));
+    fields.emplace_back(ModelField::NU, load("nu"));
+    fields.emplace_back(ModelField::J, load("j"));
+    fields.emplace_back(ModelField::LAMBDA_C, load("lambda_c"));  // read as the reference does; unused
+    fields.emplace_back(ModelField::MU_C, load("mu_c"));
+    fields.emplace_back(ModelField::NU_C, load("nu_c"));
+  } else {
+    fields.emplace_back(ModelField::VP, load("vp"));
+    fields.emplace_back(ModelField::VS, load("vs"));
+  }
+  for (const auto& f : fields)
+    if (f.second.size() != npt) throw Error("a model file does not match the density size");
+
+  // All inputs are read and checked; only now is the GPU touched.
+  SimDesc d;
+  d.nx = grid_.nx;
+  d.nz = grid_.nz;
+  d.nt = int(cfg.nt);
+  d.dx = grid_.dx;
+  d.dz = grid_.dz;
+  d.dt = cfg.dt;
+  d.sh = cfg.sh;
+  d.psv = cfg.psv;
+  d.spin = cfg.spin;
+  d.abs_left = cfg.abs_left;
+  d.abs_right = cfg.abs_right;
+  d.abs_bottom = cfg.abs_bottom;
+  d.abs_top = cfg.abs_top;
+  d.abs_width = int(cfg.abs_width);
+  d.abs_alpha = cfg.abs_alpha;
+  sim_.reset(new Sim(d));
+  if (cfg.chunk_rows > 0) sim_->set_chunk_rows(cfg.chunk_rows);
+  if (cfg.graphs >= 0) sim_->set_use_graphs(cfg.graphs == 1);
+  for (const auto& f : fields) {
+    const bool spin_only = f.first == ModelField::NU || f.first == ModelField::J || f.first == ModelField::MU_C ||
+                           f.first == ModelField::NU_C;
+    if (spin_only && !cfg.psv) continue;  // the SH system has no micropolar fields
+    sim_->upload_model(f.first, f.second.data());
+  }
+  sim_->prepare_model();
+
+  sim_->set_sources(int(nsrc), si.data(), sj.data(), stf.data());
   sim_->set_receivers(int(rec_i_.size()), rec_i_.data(), rec_j_.data());
 }
 

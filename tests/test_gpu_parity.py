@@ -33,7 +33,7 @@ _STATE = dict(vy="VY", sxy="SXY", szy="SZY", vx="VX", vz="VZ", sxx="SXX", szz="S
 
 
 def _run_pair(nx, nz, nt, dx, dt, src, rec, model, isrc=-1, snap=0, snap_fields=(), chunk_rows=None,
-              graphs=None, **flags):
+              graphs=None, loader=None, **flags):
     """Runs the same problem on the GPU and in both oracles."""
     import seiswg_gb300 as sw
     from oracle import oracle as O
@@ -48,6 +48,8 @@ def _run_pair(nx, nz, nt, dx, dt, src, rec, model, isrc=-1, snap=0, snap_fields=
             sim.set_option("chunk_rows", chunk_rows)
         if graphs is not None:
             sim.set_option("graphs", graphs)
+        if loader is not None:
+            sim.set_option("loader", loader)
         for k, v in model.items():
             sim.upload_model(k, v)
         sim.prepare()
@@ -106,21 +108,27 @@ def _check(gpu, ref, flags, tol=L2_TOL):
             f"state {f}: rel L2 {e32:.2e} vs FP32 oracle (FP64: {e64:.2e}, FP32 oracle vs FP64 {floor:.2e})"
 
 
-def test_sh_two_strips_all_tapers():
+LOADERS = pytest.mark.parametrize("loader", [0, 1], ids=["direct", "bulk"])
+
+
+@LOADERS
+def test_sh_two_strips_all_tapers(loader):
     nx, nz, nt, dx = 64, 200, 150, 10.0
     flags = dict(sh=True, psv=False, abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=15)
     src = [(30, 100, 20.0, 0.05, 0.0), (31, 121, 15.0, 0.06, 0.0)]
     rec = [(0, 0), (1, 1), (2, 119), (5, 120), (63, 199), (62, 198), (32, 60)]
-    gpu, ref = _run_pair(nx, nz, nt, dx, 1.5e-3, src, rec, _model(nx, nz, 1), chunk_rows=16, **flags)
+    gpu, ref = _run_pair(nx, nz, nt, dx, 1.5e-3, src, rec, _model(nx, nz, 1), chunk_rows=16, loader=loader, **flags)
     _check(gpu, ref, flags)
 
 
-def test_psv_narrow_grid_odd_chunks_no_graphs():
+@LOADERS
+def test_psv_narrow_grid_odd_chunks_no_graphs(loader):
     nx, nz, nt, dx = 150, 37, 160, 10.0
     flags = dict(psv=True, abs_left=True, abs_right=True, abs_bottom=True, abs_width=10)
     src = [(75, 18, 20.0, 0.05, 30.0)]
     rec = [(10, 0), (75, 2), (140, 36), (149, 35), (1, 1)]
-    gpu, ref = _run_pair(nx, nz, nt, dx, 1.5e-3, src, rec, _model(nx, nz, 2), chunk_rows=7, graphs=0, **flags)
+    gpu, ref = _run_pair(nx, nz, nt, dx, 1.5e-3, src, rec, _model(nx, nz, 2), chunk_rows=7, graphs=0,
+                         loader=loader, **flags)
     _check(gpu, ref, flags)
 
 
@@ -133,12 +141,14 @@ def test_psv_top_taper_three_strips():
     _check(gpu, ref, flags)
 
 
-def test_spin_receivers_near_edges():
+@LOADERS
+def test_spin_receivers_near_edges(loader):
     nx, nz, nt, dx = 90, 130, 500, 1.0
     flags = dict(psv=True, spin=True)
     src = [(45, 60, 50.0, 0.024, 0.0)]  # t0 = 1.2/f0: the pulse fires within nt*dt = 0.05 s
     rec = [(0, 60), (1, 60), (88, 60), (87, 60), (45, 0), (45, 1), (45, 128), (45, 127), (60, 100)]
-    gpu, ref = _run_pair(nx, nz, nt, dx, 1e-4, src, rec, _model(nx, nz, 4, spin=True), chunk_rows=24, **flags)
+    gpu, ref = _run_pair(nx, nz, nt, dx, 1e-4, src, rec, _model(nx, nz, 4, spin=True), chunk_rows=24,
+                         loader=loader, **flags)
     _check(gpu, ref, flags)
 
 
