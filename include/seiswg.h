@@ -145,6 +145,26 @@ uint64_t seiswg_sim_launches(const seiswg_sim* sim);
 void* seiswg_sim_stream(const seiswg_sim* sim);
 size_t seiswg_sim_device_bytes(const seiswg_sim* sim);
 
+/* ---- smoothing without device allocation ----------------------------------
+ * No counterpart in the reference.  Smooths an nx*nz float field
+ * (k = i*nz + j) from `in` into `out` -- device buffers the caller owns,
+ * which must not overlap -- with the Gaussian of seiswg_sim_kernel_smooth
+ * (sigma in cells), on `stream` (NULL: the default stream).  It is for
+ * callers that cannot call cudaMalloc: hosts whose device memory all belongs
+ * to their own pool allocator, or code where an allocation (which may
+ * synchronise the device) is not allowed.  It allocates nothing; its scratch
+ * is a fixed array in the library's device image (16 MiB + 64 KiB, held on
+ * every GPU that loads the library until the process exits), which limits the
+ * grid to 4,194,304 cells and 6144 per axis, and sigma to 511; larger
+ * requests fail with SEISWG_EINVAL.  The first call on a device looks up the
+ * scratch address for that device; make that first call before any stream
+ * capture.  All calls on a device share the scratch, so calls that may
+ * overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  Every scratch value a call reads is written
+ * earlier in the same call, so nothing carries over from the previous one.
+ * Returns once the work is queued. */
+int seiswg_smooth_noalloc(const float* in, float* out, int32_t nx, int32_t nz, float sigma, void* stream);
+
 /* ---- host-side numerics of the reference ---------------------------------- */
 /* [3][nt] Ricker STF of one source (solver.rs:350-356, 721-733). */
 int seiswg_ricker(int32_t nt, float dt, float f0, float t0, float ang_deg, float amp, float* out);

@@ -94,6 +94,7 @@ PROTOTYPES = [
     ("seiswg_waveform_misfit", _c_int, [_pf, _pf, _i32, _i32, _f32, _pf, ctypes.POINTER(ctypes.c_double)]),
     ("seiswg_npy_encode", _c_int, [_pf, _sz, _sz, _vp, ctypes.POINTER(_sz)]),
     ("seiswg_infer_grid", _c_int, [_pf, _pf, _sz, _pi, _pi, _pf, _pf]),
+    ("seiswg_smooth_noalloc", _c_int, [_vp, _vp, _i32, _i32, _f32, _vp]),
 ]
 
 
@@ -398,6 +399,13 @@ def npy_encode(a) -> bytes:
     return buf.raw[: n.value]
 
 
+def smooth_noalloc(in_ptr: int, out_ptr: int, nx: int, nz: int, sigma: float, stream: int = 0):
+    """Gaussian smoothing of a device field without device allocation
+    (seiswg_smooth_noalloc): in_ptr/out_ptr are device addresses of nx*nz
+    float32 arrays owned by the caller."""
+    _check(lib().seiswg_smooth_noalloc(in_ptr, out_ptr, nx, nz, sigma, stream or None))
+
+
 def infer_grid(x, z):
     x, z = _f32(x).reshape(-1), _f32(z).reshape(-1)
     nx, nz, dx, dz = _i32(), _i32(), ctypes.c_float(), ctypes.c_float()
@@ -407,4 +415,4 @@ def infer_grid(x, z):
 
 
 __all__ = ["SeiswgError", "Vfs", "Config", "Solver", "Sim", "SimDesc", "ricker", "waveform_misfit",
-           "npy_encode", "infer_grid", "lib", "LIB_PATH", "CLI_PATH", "PROTOTYPES"]
+           "npy_encode", "infer_grid", "smooth_noalloc", "lib", "LIB_PATH", "CLI_PATH", "PROTOTYPES"]

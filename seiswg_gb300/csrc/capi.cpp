@@ -26,8 +26,14 @@ struct seiswg_solver {
 };
 
 namespace {
-
 thread_local std::string g_last_error;
+}  // namespace
+
+namespace seiswg {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace seiswg
+
+namespace {
 
 int fail(int code, const std::string& msg) {
   g_last_error = msg;
