@@ -136,6 +136,20 @@ int seiswg_sim_adjoint_forward(seiswg_sim* sim, int32_t isrc, int32_t adj_interv
 int seiswg_sim_adjoint_backward(seiswg_sim* sim, const float* adstf, int32_t adj_interval);
 int seiswg_sim_kernel_smooth(seiswg_sim* sim, float sigma);
 int seiswg_sim_kernel(seiswg_sim* sim, float* host);
+/* Exact discrete adjoint (no counterpart in the reference, which has only the
+ * SH imaging condition above; SURVEY 8(a) "adjoint" row, extended).  The pair
+ * behaves like an autograd function: forward_op runs source isrc (-1: all)
+ * and stores the wavefield every ckpt_every steps (0: ceil(sqrt(nt))); the
+ * traces are then available through seiswg_sim_traces.  backward_op takes
+ * dJ/dd of the recorded displacement traces, [ncomp][nrec][nt] with ncomp 1
+ * (SH: uy) or 2 (PSV: ux, uz), and accumulates the gradients of J with
+ * respect to lambda, mu and the buoyancy 1/rho, recomputing the forward
+ * states of each checkpoint interval.  SH or PSV, not spin. */
+int seiswg_sim_gradient_clear(seiswg_sim* sim);
+int seiswg_sim_forward_op(seiswg_sim* sim, int32_t isrc, int32_t ckpt_every);
+int seiswg_sim_backward_op(seiswg_sim* sim, const float* adj);
+/* param: "lambda", "mu" or "buoyancy"; nx*nz values. */
+int seiswg_sim_gradient(seiswg_sim* sim, const char* param, float* host);
 /* Options: "graphs" (0/1), "chunk_rows" (rows per warp march), "loader"
  * (0: plain loads, 1: TMA bulk-copy row pipeline, the default). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
@@ -174,6 +188,14 @@ int seiswg_waveform_misfit(const float* syn, const float* obs, int32_t nrec, int
 /* .npy v1 bytes of a [nrows][ncols] f32 array (solver.rs:270-285).  With
  * out == NULL only *len is set. */
 int seiswg_npy_encode(const float* data, size_t nrows, size_t ncols, void* out, size_t* len);
+/* J = sum (taper * (syn - obs))^2 over ntr traces of nt samples, with the
+ * misfit taper of solver.rs:442-459, and adj = dJ/dsyn (not time-reversed;
+ * the reference's adjoint source is adj reversed in time). */
+int seiswg_l2_misfit(const float* syn, const float* obs, int32_t ntr, int32_t nt, float dt, float* adj, double* J);
+/* Chain rule from (lambda, mu, buoyancy) gradients to (vp, vs, rho) for
+ * lambda = rho (vp^2 - 2 vs^2) (0 where vp <= vs), mu = rho vs^2. */
+int seiswg_velocity_gradients(const float* g_lam, const float* g_mu, const float* g_b, const float* vp,
+                              const float* vs, const float* rho, size_t n, float* g_vp, float* g_vs, float* g_rho);
 /* nx, nz, dx, dz from coordinate arrays (solver.rs:646-656). */
 int seiswg_infer_grid(const float* x, const float* z, size_t npt, int32_t* nx, int32_t* nz, float* dx, float* dz);
 

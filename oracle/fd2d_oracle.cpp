@@ -89,6 +89,7 @@ struct OracleBase {
   virtual int run_forward(int isrc, int snap_every, int nfid, const int32_t* fids, double* snaps) = 0;
   virtual int run_adjoint(int nruns, const int32_t* run_isrc, const double* obs_y, int adj_interval,
                           double sigma, double* misfits) = 0;
+  virtual int exact_gradient(int isrc, const double* adj, double* g_lam, double* g_mu, double* g_b) = 0;
 };
 
 template <typename R>
@@ -506,6 +507,140 @@ struct Oracle final : OracleBase {
     smooth(sigma);
     return 0;
   }
+
+  // ---- exact discrete adjoint ---------------------------------------------
+  // The reference has no PSV adjoint and only the imaging-condition SH kernel
+  // (fd2d.wgsl:501-509); this is the gradient of
+  //   J = sum over traces and samples of (misfit taper * (d - obs))^2
+  // with respect to lambda, mu and the buoyancy B = 1/rho, for the forward
+  // scheme above, by reverse-mode differentiation of every step.  `adj` holds
+  // dJ/dd for each recorded sample: PSV [2][nrec][nt] (ux, uz), SH
+  // [1][nrec][nt] (uy).  The transposes of the staggered differences are
+  // applied in scatter form (each forward stencil application pushes its
+  // coefficients back onto its inputs), independently of any closed form.
+  // Not defined for spin.
+  void scatter_x(R* out, int i, size_t k, R g, bool fwd) const {
+    // fwd: diff_x1 taps (k-nz:+1, k:-9, k+nz:+9, k+2nz:-1); else diff_x taps (k-2nz:+1, k-nz:-9, k:+9, k+nz:-1)
+    const R r = g / (R(8) * dx);
+    if (fwd) {
+      if (i < 1 || i >= nx - 2) return;
+      out[k - nz] += r; out[k] -= R(9) * r; out[k + nz] += R(9) * r; out[k + 2 * size_t(nz)] -= r;
+    } else {
+      if (i < 2 || i >= nx - 2) return;
+      out[k - 2 * size_t(nz)] += r; out[k - nz] -= R(9) * r; out[k] += R(9) * r; out[k + nz] -= r;
+    }
+  }
+  void scatter_z(R* out, int j, size_t k, R g, bool fwd) const {
+    const R r = g / (R(8) * dz);
+    if (fwd) {
+      if (j < 1 || j >= nz - 2) return;
+      out[k - 1] += r; out[k] -= R(9) * r; out[k + 1] += R(9) * r; out[k + 2] -= r;
+    } else {
+      if (j < 2 || j >= nz - 2) return;
+      out[k - 2] += r; out[k - 1] -= R(9) * r; out[k] += R(9) * r; out[k + 1] -= r;
+    }
+  }
+
+  int exact_gradient(int isrc, const double* adj, double* g_lam, double* g_mu, double* g_b) override {
+    if (spin || (sh && psv)) return -1;
+    const bool is_sh = sh;
+    const int nf = is_sh ? 3 : 6;
+    // forward, keeping the divergence (with sources) and strains of each step
+    clear_dynamic();
+    clear_obs();
+    std::vector<R> store(size_t(nt) * nf * npt);
+    const int ids_sh[3] = {F_DSY, F_DVYDX, F_DVYDZ};
+    const int ids_psv[6] = {F_DSX, F_DSZ, F_DVXDX, F_DVXDZ, F_DVZDX, F_DVZDZ};
+    for (int it = 0; it < nt; ++it) {
+      forward_step(it, isrc);
+      for (int q = 0; q < nf; ++q) {
+        const R* src = F(is_sh ? ids_sh[q] : ids_psv[q]);
+        std::copy(src, src + npt, store.begin() + (size_t(it) * nf + q) * npt);
+      }
+    }
+    const R* lam = F(F_LAM);
+    const R* mu = F(F_MU);
+    const R* rho = F(F_RHO);
+    const R* bnd = F(F_BOUND);
+    const int ncomp = is_sh ? 1 : 2;
+    // U[c][r][n] = sum_{m >= n} adj[c][r][m]: the adjoint of the displacement
+    // accumulators (d^n = u after step n, u += dt*v every step).
+    std::vector<R> U(size_t(ncomp) * nrec * nt);
+    for (int c = 0; c < ncomp; ++c)
+      for (int r = 0; r < nrec; ++r) {
+        R acc = R(0);
+        for (int n = nt - 1; n >= 0; --n) {
+          acc += R(adj[(size_t(c) * nrec + r) * nt + n]);
+          U[(size_t(c) * nrec + r) * nt + n] = acc;
+        }
+      }
+    std::vector<R> gl(npt, R(0)), gm(npt, R(0)), gb(npt, R(0));
+    const int nv = is_sh ? 1 : 2, ns = is_sh ? 2 : 3;
+    std::vector<std::vector<R>> vb(nv, std::vector<R>(npt, R(0))), V(nv, std::vector<R>(npt));
+    std::vector<std::vector<R>> sb(ns, std::vector<R>(npt, R(0)));
+    std::vector<R> q0(npt), q1(npt);
+    for (int n = nt - 1; n >= 0; --n) {
+      const R* st = store.data() + size_t(n) * nf * npt;
+      for (int a = 0; a < nv; ++a) V[a] = vb[a];
+      for (int r = 0; r < nrec; ++r)
+        for (int c = 0; c < ncomp; ++c) V[c][rec_k[r]] += dt * U[(size_t(c) * nrec + r) * nt + n];
+      // sigma^{n+1} = sigma^n + dt C eps(v^{n+1})
+      for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+          const size_t k = size_t(i) * nz + j;
+          if (is_sh) {
+            const R ex = st[1 * npt + k], ez = st[2 * npt + k];
+            const R mdt = mu[k] * dt;
+            gm[k] += dt * (sb[0][k] * ex + sb[1][k] * ez);
+            scatter_x(V[0].data(), i, k, mdt * sb[0][k], true);
+            scatter_z(V[0].data(), j, k, mdt * sb[1][k], true);
+          } else {
+            const R exx = st[2 * npt + k], exz = st[3 * npt + k], ezx = st[4 * npt + k], ezz = st[5 * npt + k];
+            const R l = lam[k], m = mu[k];
+            const R bxx = sb[0][k], bzz = sb[1][k], bxz = sb[2][k];
+            gl[k] += dt * (bxx + bzz) * (exx + ezz);
+            gm[k] += dt * (R(2) * bxx * exx + R(2) * bzz * ezz + bxz * (exz + ezx));
+            scatter_x(V[0].data(), i, k, dt * ((l + R(2) * m) * bxx + l * bzz), true);  // exx
+            scatter_z(V[1].data(), j, k, dt * (l * bxx + (l + R(2) * m) * bzz), true);  // ezz
+            scatter_z(V[0].data(), j, k, dt * m * bxz, true);                           // exz
+            scatter_x(V[1].data(), i, k, dt * m * bxz, true);                           // ezx
+          }
+        }
+      // v^{n+1} = b (v^n + dt B (div sigma^n + f^n))
+      for (int a = 0; a < nv; ++a)
+        for (size_t k = 0; k < npt; ++k) vb[a][k] = bnd[k] * V[a][k];
+      for (size_t k = 0; k < npt; ++k) {
+        const R B = R(1) / rho[k];
+        if (is_sh) {
+          gb[k] += dt * vb[0][k] * st[k];
+          q0[k] = dt * B * vb[0][k];
+        } else {
+          gb[k] += dt * (vb[0][k] * st[k] + vb[1][k] * st[npt + k]);
+          q0[k] = dt * B * vb[0][k];
+          q1[k] = dt * B * vb[1][k];
+        }
+      }
+      for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < nz; ++j) {
+          const size_t k = size_t(i) * nz + j;
+          if (is_sh) {  // dsy = dx-(sxy) + dz-(szy)
+            scatter_x(sb[0].data(), i, k, q0[k], false);
+            scatter_z(sb[1].data(), j, k, q0[k], false);
+          } else {      // dsx = dx-(sxx) + dz-(sxz); dsz = dx-(sxz) + dz-(szz)
+            scatter_x(sb[0].data(), i, k, q0[k], false);
+            scatter_z(sb[2].data(), j, k, q0[k], false);
+            scatter_x(sb[2].data(), i, k, q1[k], false);
+            scatter_z(sb[1].data(), j, k, q1[k], false);
+          }
+        }
+    }
+    for (size_t k = 0; k < npt; ++k) {
+      if (g_lam) g_lam[k] = double(gl[k]);
+      if (g_mu) g_mu[k] = double(gm[k]);
+      if (g_b) g_b[k] = double(gb[k]);
+    }
+    return 0;
+  }
 };
 
 }  // namespace
@@ -538,6 +673,10 @@ int oracle_run_forward(void* h, int isrc, int snap_every, int nfid, const int32_
 int oracle_run_adjoint(void* h, int nruns, const int32_t* run_isrc, const double* obs_y, int adj_interval,
                        double sigma, double* misfits) {
   return static_cast<OracleBase*>(h)->run_adjoint(nruns, run_isrc, obs_y, adj_interval, sigma, misfits);
+}
+
+int oracle_exact_gradient(void* h, int isrc, const double* adj, double* g_lam, double* g_mu, double* g_b) {
+  return static_cast<OracleBase*>(h)->exact_gradient(isrc, adj, g_lam, g_mu, g_b);
 }
 
 // Ricker source-time function, solver.rs:350-356 and the STF table of

@@ -90,6 +90,8 @@ def lib():
                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float),
                                         ctypes.POINTER(ctypes.c_float)]
         L.oracle_num_threads.restype = ctypes.c_int
+        L.oracle_exact_gradient.restype = ctypes.c_int
+        L.oracle_exact_gradient.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -302,6 +304,50 @@ class FD2DOracle:
         if rc != 0:
             raise ValueError("adj_interval >= nt")
         return mis
+
+
+    def exact_gradient(self, adj, isrc=-1):
+        """(g_lambda, g_mu, g_buoyancy) of J for the adjoint source `adj` = dJ/dd
+        ([2][nrec][nt] ux, uz for PSV; [1][nrec][nt] uy for SH)."""
+        a = np.ascontiguousarray(adj, np.float64).reshape(-1)
+        gl = np.zeros(self.npt)
+        gm = np.zeros(self.npt)
+        gb = np.zeros(self.npt)
+        rc = lib().oracle_exact_gradient(self._h, isrc, _dptr(a), _dptr(gl), _dptr(gm), _dptr(gb))
+        if rc != 0:
+            raise ValueError("exact gradient is defined for SH or PSV without spin")
+        shp = (self.s.nx, self.s.nz)
+        return gl.reshape(shp), gm.reshape(shp), gb.reshape(shp)
+
+
+def misfit_taper(nt, dt):
+    """The cosine taper of solver.rs:442-459, in float64."""
+    t = np.arange(nt) * dt
+    t_end = (nt - 1) * dt
+    tw = t_end / 10.0
+    tau = np.ones(nt)
+    lo, hi = t <= tw, t >= t_end - tw
+    tau[lo] = 0.5 + 0.5 * np.cos(np.pi * (tw - t[lo]) / tw)
+    tau[hi] = 0.5 + 0.5 * np.cos(np.pi * ((t_end - tw) - t[hi]) / tw)
+    return tau
+
+
+def l2_misfit(syn, obs, dt):
+    """J = sum (taper * (syn - obs))^2 over traces and samples, and dJ/dsyn."""
+    tau = misfit_taper(syn.shape[-1], dt)
+    d = (np.asarray(syn, np.float64) - np.asarray(obs, np.float64)) * tau
+    return float((d * d).sum()), 2.0 * d * tau
+
+
+def lame_to_velocity_gradients(g_lam, g_mu, g_b, vp, vs, rho):
+    """Chain rule through lambda = rho (vp^2 - 2 vs^2) (0 where vp <= vs),
+    mu = rho vs^2, B = 1/rho (fd2d.wgsl:188-201)."""
+    vp, vs, rho = (np.asarray(a, np.float64) for a in (vp, vs, rho))
+    live = vp > vs
+    g_vp = np.where(live, g_lam * 2.0 * rho * vp, 0.0)
+    g_vs = np.where(live, g_lam * (-4.0 * rho * vs), 0.0) + g_mu * 2.0 * rho * vs
+    g_rho = np.where(live, g_lam * (vp * vp - 2.0 * vs * vs), 0.0) + g_mu * vs * vs - g_b / (rho * rho)
+    return g_vp, g_vs, g_rho
 
 
 def num_threads():

@@ -85,6 +85,10 @@ PROTOTYPES = [
     ("seiswg_sim_adjoint_backward", _c_int, [_vp, _pf, _i32]),
     ("seiswg_sim_kernel_smooth", _c_int, [_vp, _f32]),
     ("seiswg_sim_kernel", _c_int, [_vp, _pf]),
+    ("seiswg_sim_gradient_clear", _c_int, [_vp]),
+    ("seiswg_sim_forward_op", _c_int, [_vp, _i32, _i32]),
+    ("seiswg_sim_backward_op", _c_int, [_vp, _pf]),
+    ("seiswg_sim_gradient", _c_int, [_vp, _cp, _pf]),
     ("seiswg_sim_set_option", _c_int, [_vp, _cp, ctypes.c_int64]),
     ("seiswg_sim_synchronize", _c_int, [_vp]),
     ("seiswg_sim_launches", ctypes.c_uint64, [_vp]),
@@ -95,6 +99,8 @@ PROTOTYPES = [
     ("seiswg_npy_encode", _c_int, [_pf, _sz, _sz, _vp, ctypes.POINTER(_sz)]),
     ("seiswg_infer_grid", _c_int, [_pf, _pf, _sz, _pi, _pi, _pf, _pf]),
     ("seiswg_smooth_noalloc", _c_int, [_vp, _vp, _i32, _i32, _f32, _vp]),
+    ("seiswg_l2_misfit", _c_int, [_pf, _pf, _i32, _i32, _f32, _pf, ctypes.POINTER(ctypes.c_double)]),
+    ("seiswg_velocity_gradients", _c_int, [_pf, _pf, _pf, _pf, _pf, _pf, _sz, _pf, _pf, _pf]),
 ]
 
 
@@ -335,6 +341,24 @@ class Sim:
         _check(lib().seiswg_sim_kernel(self._h, _fp(out)))
         return out
 
+    # -- exact adjoint ---------------------------------------------------
+    def gradient_clear(self):
+        _check(lib().seiswg_sim_gradient_clear(self._h))
+
+    def forward_op(self, isrc: int = -1, ckpt_every: int = 0):
+        """Forward run storing checkpoints; traces via traces()."""
+        _check(lib().seiswg_sim_forward_op(self._h, isrc, ckpt_every))
+
+    def backward_op(self, adj):
+        """Reverse sweep for dJ/dd, [ncomp][nrec][nt] (SH: uy; PSV: ux, uz)."""
+        a = _f32(adj).reshape(-1)
+        _check(lib().seiswg_sim_backward_op(self._h, _fp(a)))
+
+    def gradient(self, param: str):
+        out = np.zeros((self.nx, self.nz), np.float32)
+        _check(lib().seiswg_sim_gradient(self._h, param.encode(), _fp(out)))
+        return out
+
     def set_option(self, key: str, value: int):
         _check(lib().seiswg_sim_set_option(self._h, key.encode(), int(value)))
 
@@ -406,6 +430,27 @@ def smooth_noalloc(in_ptr: int, out_ptr: int, nx: int, nz: int, sigma: float, st
     _check(lib().seiswg_smooth_noalloc(in_ptr, out_ptr, nx, nz, sigma, stream or None))
 
 
+def l2_misfit(syn, obs, dt: float):
+    """(J, dJ/dsyn) of J = sum (taper (syn - obs))^2; syn/obs [..., nt]."""
+    s, o = _f32(syn), _f32(obs)
+    nt = s.shape[-1]
+    ntr = s.size // nt
+    adj = np.zeros_like(s)
+    J = ctypes.c_double()
+    _check(lib().seiswg_l2_misfit(_fp(s), _fp(o), ntr, nt, dt, _fp(adj), ctypes.byref(J)))
+    return J.value, adj
+
+
+def velocity_gradients(g_lam, g_mu, g_b, vp, vs, rho):
+    """(g_vp, g_vs, g_rho) from gradients with respect to lambda, mu, 1/rho."""
+    arrs = [_f32(a).reshape(-1) for a in (g_lam, g_mu, g_b, vp, vs, rho)]
+    n = arrs[0].size
+    outs = [np.zeros(n, np.float32) for _ in range(3)]
+    _check(lib().seiswg_velocity_gradients(*[_fp(a) for a in arrs], n, *[_fp(o) for o in outs]))
+    shp = np.shape(g_lam)
+    return tuple(o.reshape(shp) for o in outs)
+
+
 def infer_grid(x, z):
     x, z = _f32(x).reshape(-1), _f32(z).reshape(-1)
     nx, nz, dx, dz = _i32(), _i32(), ctypes.c_float(), ctypes.c_float()
@@ -415,4 +460,4 @@ def infer_grid(x, z):
 
 
 __all__ = ["SeiswgError", "Vfs", "Config", "Solver", "Sim", "SimDesc", "ricker", "waveform_misfit",
-           "npy_encode", "infer_grid", "smooth_noalloc", "lib", "LIB_PATH", "CLI_PATH", "PROTOTYPES"]
+           "npy_encode", "infer_grid", "smooth_noalloc", "l2_misfit", "velocity_gradients", "lib", "LIB_PATH", "CLI_PATH", "PROTOTYPES"]

@@ -1,6 +1,7 @@
 // capi.cpp -- the extern "C" boundary declared in include/seiswg.h.
 #include "../../include/seiswg.h"
 
+#include <cmath>
 #include <cstring>
 #include <new>
 #include <string>
@@ -381,6 +382,31 @@ int seiswg_sim_kernel(seiswg_sim* s, float* host) {
   });
 }
 
+int seiswg_sim_gradient_clear(seiswg_sim* s) {
+  return guarded([&] { sim_of(s).gradient_clear(); });
+}
+
+int seiswg_sim_forward_op(seiswg_sim* s, int32_t isrc, int32_t ckpt_every) {
+  return guarded([&] { sim_of(s).forward_op(isrc, ckpt_every); });
+}
+
+int seiswg_sim_backward_op(seiswg_sim* s, const float* adj) {
+  return guarded([&] {
+    if (!adj && sim_of(s).nrec() > 0) throw std::invalid_argument("null adjoint source");
+    sim_of(s).backward_op(adj);
+  });
+}
+
+int seiswg_sim_gradient(seiswg_sim* s, const char* param, float* host) {
+  return guarded([&] {
+    if (!param || !host) throw std::invalid_argument("null argument");
+    std::string p = param;
+    int which = p == "lambda" ? 0 : p == "mu" ? 1 : p == "buoyancy" ? 2 : -1;
+    if (which < 0) throw std::invalid_argument("gradient parameter must be lambda, mu or buoyancy");
+    sim_of(s).download_gradient(which, host);
+  });
+}
+
 int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
   return guarded([&] {
     seiswg::Sim& sim = sim_of(s);
@@ -428,6 +454,43 @@ int seiswg_npy_encode(const float* data, size_t nrows, size_t ncols, void* out, 
     }
     *len = b.size();
   });
+}
+
+int seiswg_l2_misfit(const float* syn, const float* obs, int32_t ntr, int32_t nt, float dt, float* adj, double* J) {
+  if (ntr < 0 || nt < 2 || !syn || !obs || !adj || !J) return fail(SEISWG_EINVAL, "seiswg_l2_misfit: bad argument");
+  // Taper of solver.rs:442-459 (in double here).
+  const double t_end = double(nt - 1) * double(dt), tw = t_end / 10.0, pi = 3.14159265358979323846;
+  double sum = 0.0;
+  for (int it = 0; it < nt; ++it) {
+    const double t = double(it) * double(dt);
+    double tau = 1.0;
+    if (t <= tw) tau = 0.5 + 0.5 * std::cos(pi * (tw - t) / tw);
+    else if (t >= t_end - tw) tau = 0.5 + 0.5 * std::cos(pi * ((t_end - tw) - t) / tw);
+    for (int r = 0; r < ntr; ++r) {
+      const size_t k = size_t(r) * nt + it;
+      const double d = (double(syn[k]) - double(obs[k])) * tau;
+      sum += d * d;
+      adj[k] = float(2.0 * d * tau);
+    }
+  }
+  *J = sum;
+  g_last_error.clear();
+  return SEISWG_OK;
+}
+
+int seiswg_velocity_gradients(const float* g_lam, const float* g_mu, const float* g_b, const float* vp,
+                              const float* vs, const float* rho, size_t n, float* g_vp, float* g_vs, float* g_rho) {
+  if (!g_lam || !g_mu || !g_b || !vp || !vs || !rho || !g_vp || !g_vs || !g_rho)
+    return fail(SEISWG_EINVAL, "seiswg_velocity_gradients: null argument");
+  for (size_t k = 0; k < n; ++k) {
+    const double a = vp[k], b = vs[k], r = rho[k], gl = g_lam[k], gm = g_mu[k], gb = g_b[k];
+    const bool live = a > b;  // vps2lm sets lambda to 0 otherwise (fd2d.wgsl:196-200)
+    g_vp[k] = float(live ? gl * 2.0 * r * a : 0.0);
+    g_vs[k] = float((live ? gl * (-4.0 * r * b) : 0.0) + gm * 2.0 * r * b);
+    g_rho[k] = float((live ? gl * (a * a - 2.0 * b * b) : 0.0) + gm * b * b - gb / (r * r));
+  }
+  g_last_error.clear();
+  return SEISWG_OK;
 }
 
 int seiswg_infer_grid(const float* x, const float* z, size_t npt, int32_t* nx, int32_t* nz, float* dx, float* dz) {

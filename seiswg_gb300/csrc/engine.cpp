@@ -117,6 +117,12 @@ Sim::~Sim() {
   cudaFree(tr_idx_);
   cudaFree(obs_);
   cudaFree(fwd_store_);
+  cudaFree(ck_store_);
+  cudaFree(seg_store_);
+  cudaFree(adj_store_);
+  cudaFree(u_tab_);
+  for (float* g : {g_lam_, g_mu_, g_b_})
+    if (g) cudaFree(g - size_t(kHaloRows) * ld_ - kHaloCols);
   if (kmu_) cudaFree(kmu_ - size_t(kHaloRows) * ld_ - kHaloCols);
   if (tmp_) cudaFree(tmp_ - size_t(kHaloRows) * ld_ - kHaloCols);
   if (own_stream_) cudaStreamDestroy(stream_);
@@ -237,6 +243,7 @@ void Sim::set_sources(int n, const int* i, const int* j, const float* stf_xyz) {
   for (int s = 0; s < n; ++s)
     if (i[s] < 0 || i[s] >= d_.nx || j[s] < 0 || j[s] >= d_.nz)
       throw std::invalid_argument("source " + std::to_string(s) + " lies outside the grid");
+  SW_CUDA(cudaStreamSynchronize(stream_));  // queued work may still read the old tables
   nsrc_ = n;
   src_i_.assign(i, i + n);
   src_j_.assign(j, j + n);
@@ -248,7 +255,8 @@ void Sim::set_sources(int n, const int* i, const int* j, const float* stf_xyz) {
   size_t bytes = size_t(3) * n * d_.nt * sizeof(float);
   if (bytes) {
     SW_CUDA(cudaMalloc(&stf_, bytes));
-    SW_CUDA(cudaMemcpy(stf_, stf_xyz, bytes, cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMemcpyAsync(stf_, stf_xyz, bytes, cudaMemcpyHostToDevice, stream_));
+    SW_CUDA(cudaStreamSynchronize(stream_));
   }
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
@@ -259,6 +267,7 @@ void Sim::set_receivers(int n, const int* i, const int* j) {
   for (int r = 0; r < n; ++r)
     if (i[r] < 0 || i[r] >= d_.nx || j[r] < 0 || j[r] >= d_.nz)
       throw std::invalid_argument("receiver " + std::to_string(r) + " lies outside the grid");
+  SW_CUDA(cudaStreamSynchronize(stream_));
   nrec_ = n;
   rec_i_.assign(i, i + n);
   rec_j_.assign(j, j + n);
@@ -315,7 +324,7 @@ void Sim::build_probe_tables() {
   cudaFree(obs_); obs_ = nullptr;
   if (nprobe_) {
     SW_CUDA(cudaMalloc(&probes_, list.size() * sizeof(Probe)));
-    SW_CUDA(cudaMemcpy(probes_, list.data(), list.size() * sizeof(Probe), cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMemcpyAsync(probes_, list.data(), list.size() * sizeof(Probe), cudaMemcpyHostToDevice, stream_));
     SW_CUDA(cudaMalloc(&probe_acc_, size_t(nprobe_) * sizeof(float)));
     SW_CUDA(cudaMalloc(&probe_hist_, std::max<size_t>(1, size_t(nprobe_) * d_.nt) * sizeof(float)));
   }
@@ -323,27 +332,33 @@ void Sim::build_probe_tables() {
     SW_CUDA(cudaMalloc(&tr_idx_, tr.size() * sizeof(int) + size_t(nrec_) * 2 * sizeof(int)));
     std::vector<int> packed(tr);
     for (int r = 0; r < nrec_; ++r) { packed.push_back(rec_i_[r]); packed.push_back(rec_j_[r]); }
-    SW_CUDA(cudaMemcpy(tr_idx_, packed.data(), packed.size() * sizeof(int), cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMemcpyAsync(tr_idx_, packed.data(), packed.size() * sizeof(int), cudaMemcpyHostToDevice, stream_));
     size_t ob = std::max<size_t>(1, size_t(5) * nrec_ * d_.nt) * sizeof(float);
     SW_CUDA(cudaMalloc(&obs_, ob));
-    SW_CUDA(cudaMemset(obs_, 0, ob));
+    SW_CUDA(cudaMemsetAsync(obs_, 0, ob, stream_));
   }
+  SW_CUDA(cudaStreamSynchronize(stream_));  // the host tables above die here
   // Segment boundary: number of SH probes.
   int nsh = 0;
   for (const Probe& p : list) nsh += (p.comp == kProbeVY);
   probe_split_ = nsh;
 }
 
+// Uploads on the engine's stream, so that work already queued that reads the
+// previous list finishes first (a legacy-stream copy would not wait for it).
 void Sim::upload_inject(const std::vector<Inject>& list, int which) {
   int n = int(list.size());
   if (n > inj_cap_[which]) {
+    SW_CUDA(cudaStreamSynchronize(stream_));
     cudaFree(inj_dev_[which]);
     inj_dev_[which] = nullptr;
     SW_CUDA(cudaMalloc(&inj_dev_[which], size_t(n) * sizeof(Inject)));
     inj_cap_[which] = n;
   }
   inj_n_[which] = n;
-  if (n) SW_CUDA(cudaMemcpy(inj_dev_[which], list.data(), size_t(n) * sizeof(Inject), cudaMemcpyHostToDevice));
+  if (n)
+    SW_CUDA(cudaMemcpyAsync(inj_dev_[which], list.data(), size_t(n) * sizeof(Inject), cudaMemcpyHostToDevice,
+                            stream_));
 }
 
 float* Sim::state_ptr(StateField f, int b) const {
@@ -366,8 +381,11 @@ float* Sim::state_ptr(StateField f, int b) const {
 }
 
 void Sim::enqueue_step(int it, int b, const InjectList& inj_in, const ProbeList& probes_in, bool sh_only) {
-  const State& a = st_[b];
-  const State& o = st_[1 - b];
+  enqueue_step_states(it, st_[b], st_[1 - b], inj_in, probes_in, sh_only);
+}
+
+void Sim::enqueue_step_states(int it, const State& a, const State& o, const InjectList& inj_in,
+                              const ProbeList& probes_in, bool sh_only) {
   InjectList inj = inj_in;
   inj.it = it;
   if (d_.sh) {
@@ -585,6 +603,12 @@ void Sim::adjoint_forward(int isrc, int adj_interval) {
   const size_t fb = field_elems_ * sizeof(float);
   if (fwd_nsa_ != nsa) {
     cudaFree(fwd_store_);
+  cudaFree(ck_store_);
+  cudaFree(seg_store_);
+  cudaFree(adj_store_);
+  cudaFree(u_tab_);
+  for (float* g : {g_lam_, g_mu_, g_b_})
+    if (g) cudaFree(g - size_t(kHaloRows) * ld_ - kHaloCols);
     fwd_store_ = nullptr;
     fwd_bytes_ = size_t(nsa) * fb;
     SW_CUDA(cudaMalloc(&fwd_store_, fwd_bytes_));
@@ -694,6 +718,191 @@ void Sim::download_kmu(float* host) const {
   }
   copy_field_to_host(kmu_, host);
   SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+}  // namespace seiswg
+
+namespace seiswg {
+
+// ---------------------------------------------------------------------------
+// Exact discrete adjoint
+// ---------------------------------------------------------------------------
+Sim::State Sim::slot_state(float* slot) const {
+  State s;
+  float* p = slot;
+  auto next = [&]() {
+    float* f = field_ptr(p);
+    p += field_elems_;
+    return f;
+  };
+  if (d_.sh) { s.vy = next(); s.sxy = next(); s.szy = next(); }
+  if (d_.psv) { s.vx = next(); s.vz = next(); s.sxx = next(); s.szz = next(); s.sxz = next(); }
+  return s;
+}
+
+void Sim::copy_state(const State& dst, const State& src) {
+  const size_t fb = field_elems_ * sizeof(float);
+  const size_t off = size_t(kHaloRows) * ld_ + kHaloCols;
+  auto cp = [&](float* d, const float* s) {
+    if (d && s) SW_CUDA(cudaMemcpyAsync(d - off, s - off, fb, cudaMemcpyDeviceToDevice, stream_));
+  };
+  cp(dst.vy, src.vy); cp(dst.sxy, src.sxy); cp(dst.szy, src.szy);
+  cp(dst.vx, src.vx); cp(dst.vz, src.vz); cp(dst.sxx, src.sxx); cp(dst.szz, src.szz); cp(dst.sxz, src.sxz);
+}
+
+void Sim::gradient_clear() {
+  const size_t fb = field_elems_ * sizeof(float);
+  auto ensure = [&](float*& g) {
+    if (!g) {
+      float* a = nullptr;
+      SW_CUDA(cudaMalloc(&a, fb));
+      g = field_ptr(a);
+    }
+    SW_CUDA(cudaMemsetAsync(g - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
+  };
+  ensure(g_mu_);
+  ensure(g_b_);
+  if (d_.psv) ensure(g_lam_);
+}
+
+void Sim::forward_op(int isrc, int ckpt_every) {
+  if (d_.spin) throw std::invalid_argument("the exact adjoint is defined for SH or PSV without spin");
+  if (d_.sh && d_.psv) throw std::invalid_argument("the exact adjoint runs one of SH or PSV at a time");
+  const int nt = d_.nt;
+  int k = ckpt_every > 0 ? ckpt_every : int(std::ceil(std::sqrt(double(std::max(nt, 1)))));
+  k = std::max(1, std::min(k, std::max(nt, 1)));
+  const int ncp = (nt + k - 1) / k;
+  const size_t state_elems = size_t(nstate()) * field_elems_;
+  if (k != ck_k_ || ncp != ck_n_) {
+    cudaFree(ck_store_);
+    cudaFree(seg_store_);
+    ck_store_ = seg_store_ = nullptr;
+    SW_CUDA(cudaMalloc(&ck_store_, std::max(1, ncp) * state_elems * sizeof(float)));
+    SW_CUDA(cudaMalloc(&seg_store_, size_t(k) * state_elems * sizeof(float)));
+    // Halos of every stored state stay zero.
+    SW_CUDA(cudaMemsetAsync(ck_store_, 0, std::max(1, ncp) * state_elems * sizeof(float), stream_));
+    SW_CUDA(cudaMemsetAsync(seg_store_, 0, size_t(k) * state_elems * sizeof(float), stream_));
+    ck_k_ = k;
+    ck_n_ = ncp;
+    ck_bytes_ = (size_t(ncp) + size_t(k)) * state_elems * sizeof(float);
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+  }
+  if (!g_mu_) gradient_clear();
+  InjectList inj = source_injections(isrc);
+  ProbeList pl = probe_list();
+  zero_state();
+  if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
+  const std::string key = "fop/" + std::to_string(inj.n) + "/" + std::to_string(k);
+  run_loop(key, [&] {
+    for (int it = 0; it < nt; ++it) {
+      if (it % k == 0) copy_state(slot_state(ck_store_ + size_t(it / k) * state_elems), st_[it & 1]);
+      enqueue_step(it, it & 1, inj, pl, false);
+    }
+    enqueue_traces();
+  });
+  cur_buf_ = nt & 1;
+  ck_isrc_ = isrc;
+}
+
+void Sim::backward_op(const float* adj_host) {
+  if (ck_isrc_ == -2) throw std::logic_error("backward_op without a preceding forward_op");
+  const int nt = d_.nt;
+  const int ncomp = d_.psv ? 2 : 1;
+  const size_t nrt = size_t(nrec_) * nt;
+  // dt * U, U^n = sum_{m >= n} dJ/dd^m, summed in double.
+  std::vector<float> u(size_t(ncomp) * nrt);
+  for (int c = 0; c < ncomp; ++c)
+    for (int r = 0; r < nrec_; ++r) {
+      double acc = 0.0;
+      for (int n = nt - 1; n >= 0; --n) {
+        acc += double(adj_host[size_t(c) * nrt + size_t(r) * nt + n]);
+        u[size_t(c) * nrt + size_t(r) * nt + n] = float(double(d_.dt) * acc);
+      }
+    }
+  if (!u_tab_ && !u.empty()) SW_CUDA(cudaMalloc(&u_tab_, u.size() * sizeof(float)));
+  if (!u.empty())
+    SW_CUDA(cudaMemcpyAsync(u_tab_, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  std::vector<Inject> list;
+  for (int r = 0; r < nrec_; ++r) list.push_back(Inject{rec_i_[r], rec_j_[r], r, 0});
+  std::stable_sort(list.begin(), list.end(),
+                   [](const Inject& a, const Inject& b) { return a.i != b.i ? a.i < b.i : a.j < b.j; });
+  upload_inject(list, 1);
+  InjectList rec{};
+  rec.list = inj_dev_[1];
+  rec.n = inj_n_[1];
+  rec.nt = nt;
+  if (d_.psv) { rec.val_x = u_tab_; rec.val_z = u_tab_ + nrt; }
+  else rec.val_y = u_tab_;
+  InjectList src = source_injections(ck_isrc_);
+  ProbeList none{};
+
+  const size_t state_elems = size_t(nstate()) * field_elems_;
+  if (!adj_store_) SW_CUDA(cudaMalloc(&adj_store_, 2 * state_elems * sizeof(float)));
+  SW_CUDA(cudaMemsetAsync(adj_store_, 0, 2 * state_elems * sizeof(float), stream_));
+  const State adj[2] = {slot_state(adj_store_), slot_state(adj_store_ + state_elems)};
+  const int k = ck_k_;
+  SW_CUDA(cudaStreamSynchronize(stream_));  // host tables above are released after this call
+
+  const std::string key = "bop/" + std::to_string(src.n) + "/" + std::to_string(rec.n) + "/" + std::to_string(k);
+  run_loop(key, [&] {
+    int cur = 0;
+    for (int seg = ck_n_ - 1; seg >= 0; --seg) {
+      const int n0 = seg * k, n1 = std::min(nt, n0 + k);
+      copy_state(slot_state(seg_store_), slot_state(ck_store_ + size_t(seg) * state_elems));
+      for (int n = n0; n < n1 - 1; ++n)
+        enqueue_step_states(n, slot_state(seg_store_ + size_t(n - n0) * state_elems),
+                            slot_state(seg_store_ + size_t(n - n0 + 1) * state_elems), src, none, false);
+      for (int n = n1 - 1; n >= n0; --n) {
+        const State f = slot_state(seg_store_ + size_t(n - n0) * state_elems);
+        const State& a = adj[cur];
+        const State& o = adj[1 - cur];
+        InjectList s2 = src, r2 = rec;
+        s2.it = n;
+        r2.it = n;
+        if (d_.psv) {
+          PsvAdjoint p{};
+          p.g = geom_;
+          p.vx = f.vx; p.vz = f.vz; p.sxx = f.sxx; p.szz = f.szz; p.sxz = f.sxz;
+          p.wx0 = a.vx; p.wz0 = a.vz; p.bxx0 = a.sxx; p.bzz0 = a.szz; p.bxz0 = a.sxz;
+          p.wx1 = o.vx; p.wz1 = o.vz; p.bxx1 = o.sxx; p.bzz1 = o.szz; p.bxz1 = o.sxz;
+          p.rho = rho_; p.lam = lam_; p.mu = mu_;
+          p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+          p.g_b = g_b_; p.g_lam = g_lam_; p.g_mu = g_mu_;
+          p.src = s2;
+          p.rec = r2;
+          p.err = err_;
+          SW_CUDA(launch_psv_adjoint(p, stream_));
+        } else {
+          ShAdjoint p{};
+          p.g = geom_;
+          p.vy = f.vy; p.sxy = f.sxy; p.szy = f.szy;
+          p.w0 = a.vy; p.bxy0 = a.sxy; p.bzy0 = a.szy;
+          p.w1 = o.vy; p.bxy1 = o.sxy; p.bzy1 = o.szy;
+          p.rho = rho_; p.mu = mu_;
+          p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+          p.g_b = g_b_; p.g_mu = g_mu_;
+          p.src = s2;
+          p.rec = r2;
+          p.err = err_;
+          SW_CUDA(launch_sh_adjoint(p, stream_));
+        }
+        ++launches_;
+        cur ^= 1;
+      }
+    }
+  });
+}
+
+void Sim::download_gradient(int which, float* host) const {
+  const float* g = which == 0 ? g_lam_ : which == 1 ? g_mu_ : g_b_;
+  if (!g) {
+    std::fill(host, host + size_t(d_.nx) * d_.nz, 0.0f);
+    return;
+  }
+  copy_field_to_host(g, host);
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  check_device_error();
 }
 
 }  // namespace seiswg

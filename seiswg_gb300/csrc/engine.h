@@ -109,6 +109,21 @@ class Sim {
   void smooth_kmu(float sigma);
   void download_kmu(float* host) const;
 
+  // ---- exact discrete adjoint with checkpointing --------------------------
+  // forward_op: one forward run of source isrc (-1: all) that also stores the
+  // full wavefield state every `ckpt_every` steps (0: ceil(sqrt(nt))).
+  // backward_op: the reverse sweep for the adjoint source adj = dJ/dd of the
+  // recorded traces, [ncomp][nrec][nt] (SH: uy; PSV: ux, uz), rebuilding the
+  // forward states of each checkpoint interval by recomputation; gradients
+  // with respect to lambda, mu and the buoyancy 1/rho accumulate across calls.
+  void gradient_clear();
+  void forward_op(int isrc, int ckpt_every);
+  void backward_op(const float* adj_host);
+  // which: 0 lambda, 1 mu, 2 buoyancy
+  void download_gradient(int which, float* host) const;
+  int checkpoint_interval() const { return ck_k_; }
+  size_t checkpoint_bytes() const { return ck_bytes_; }
+
   // Graph capture of whole time loops (replayed on repeated runs).
   void set_use_graphs(bool on) { use_graphs_ = on; }
   void set_chunk_rows(int lx);
@@ -136,6 +151,11 @@ class Sim {
   float* alloc_field();
   void zero_state();
   void enqueue_step(int it, int src_buf, const InjectList& inj, const ProbeList& probes, bool sh_only);
+  void enqueue_step_states(int it, const struct State& a, const struct State& o, const InjectList& inj,
+                           const ProbeList& probes, bool sh_only);
+  State slot_state(float* slot) const;  // nstate consecutive fields starting at `slot`
+  int nstate() const { return (d_.sh ? 3 : 0) + (d_.psv ? 5 : 0); }
+  void copy_state(const State& dst, const State& src);
   InjectList source_injections(int isrc);
   ProbeList probe_list() const;
   void enqueue_traces();
@@ -184,6 +204,15 @@ class Sim {
   int fwd_nsa_ = 0;
 
   int* err_ = nullptr;            // device error word
+  // exact adjoint storage
+  int ck_k_ = 0, ck_n_ = 0, ck_isrc_ = -2;
+  size_t ck_bytes_ = 0;
+  float* ck_store_ = nullptr;   // ck_n_ states
+  float* seg_store_ = nullptr;  // ck_k_ states of one interval
+  float* adj_store_ = nullptr;  // 2 adjoint states
+  float *g_lam_ = nullptr, *g_mu_ = nullptr, *g_b_ = nullptr;
+  float* u_tab_ = nullptr;      // dt * U, [ncomp][nrec][nt]
+
   bool use_graphs_ = true;
   std::map<std::string, cudaGraphExec_t> graphs_;
   std::map<std::string, uint64_t> graph_nodes_;

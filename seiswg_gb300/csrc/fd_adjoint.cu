@@ -1,0 +1,546 @@
+// fd_adjoint.cu -- fused reverse step of the exact discrete adjoint.
+//
+// For the forward step n (fd_step.cu)
+//   v^{n+1} = b (v^n + dt B (D- sigma^n + f^n)),    B = 1/rho
+//   sigma^{n+1} = sigma^n + dt C(lambda, mu) D+ v^{n+1}
+//   u_r^{n+1} = u_r^n + dt v^{n+1}(r)               (receiver displacement, d^n = u^{n+1})
+// and J(d), reverse-mode differentiation gives, for n = nt-1 .. 0, with the
+// carried adjoint velocity w^{n+1} and adjoint stress s^{n+1}:
+//   Vbar = w^{n+1} + dt U^n (at receivers) + (D+)^T (dt C s^{n+1})
+//   w^n  = b Vbar
+//   s^n  = s^{n+1} + (D-)^T (dt B w^n)
+//   g_B += dt w^n . (D- sigma^n + f^n)
+//   g_lambda, g_mu += dt s^{n+1} . dC/d(lambda, mu) D+ v^{n+1}
+// where U^n = sum_{m >= n} dJ/dd^m.  The transposes of the masked staggered
+// differences are differences with the other tap pattern applied to the
+// masked input: (D-)^T g = -D+taps(M- g), (D+)^T g = -D-taps(M+ g), so the
+// reverse step has the same row and column reach as the forward step and
+// uses the same warp march: iteration k handles Vbar/w of row i = ib-1+k and
+// the adjoint stress of row i-2.  The forward v^{n+1} and D- sigma^n are
+// recomputed from the forward state S^n inside the same pass.
+//
+// Algorithmic bytes per cell-update (PSV): forward state 5 + adjoint state
+// 5 r+w + model 3 + gradients 3 r+w = 96 B (SH: 3 + 3 r+w + 2 + 2 r+w = 60 B).
+#include "fd_kernels.h"
+#include "fd_pipe.cuh"
+
+namespace seiswg {
+
+namespace {
+
+// -fd4(a, b, c, d): the transposed difference (taps already masked).
+__device__ __forceinline__ float nfd4(float a, float b, float c, float d, float r) {
+  return -((9.0f * (c - b) - (d - a)) * r);
+}
+
+__device__ __forceinline__ f4 masked(const f4& a, int bits) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = (bits & (1 << e)) ? a.v[e] : 0.0f;
+  return o;
+}
+
+__device__ __forceinline__ f4 scaled(const f4& a, bool keep) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = keep ? a.v[e] : 0.0f;
+  return o;
+}
+
+// Transposed x differences over a ring of masked rows (oldest first).
+__device__ __forceinline__ f4 dxT(const f4& r0, const f4& r1, const f4& r2, const f4& r3, float r) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = nfd4(r0.v[e], r1.v[e], r2.v[e], r3.v[e], r);
+  return o;
+}
+
+// Transposed z differences of a masked lane float4: back taps (c-2..c+1)
+// for (D+)^T, forward taps (c-1..c+2) for (D-)^T.
+__device__ __forceinline__ f4 dzT_back(const f4& m, float r) {
+  const float pz = __shfl_up_sync(kFull, m.v[2], 1);
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float nx = __shfl_down_sync(kFull, m.v[0], 1);
+  f4 o;
+  o.v[0] = nfd4(pz, pw, m.v[0], m.v[1], r);
+  o.v[1] = nfd4(pw, m.v[0], m.v[1], m.v[2], r);
+  o.v[2] = nfd4(m.v[0], m.v[1], m.v[2], m.v[3], r);
+  o.v[3] = nfd4(m.v[1], m.v[2], m.v[3], nx, r);
+  return o;
+}
+
+__device__ __forceinline__ f4 dzT_fwd(const f4& m, float r) {
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float n0 = __shfl_down_sync(kFull, m.v[0], 1);
+  const float n1 = __shfl_down_sync(kFull, m.v[1], 1);
+  f4 o;
+  o.v[0] = nfd4(pw, m.v[0], m.v[1], m.v[2], r);
+  o.v[1] = nfd4(m.v[0], m.v[1], m.v[2], m.v[3], r);
+  o.v[2] = nfd4(m.v[1], m.v[2], m.v[3], n0, r);
+  o.v[3] = nfd4(m.v[2], m.v[3], n0, n1, r);
+  return o;
+}
+
+__device__ __forceinline__ bool mask_back(int i, int n) { return i >= 2 && i < n - 2; }  // D-
+__device__ __forceinline__ bool mask_fwd(int i, int n) { return i >= 1 && i < n - 2; }   // D+
+
+struct AMarch {
+  int lane, warp, strip, chunk, ib, ie;
+  bool active;
+};
+
+__device__ __forceinline__ AMarch amarch(const Geom& g) {
+  AMarch m;
+  m.lane = threadIdx.x & 31;
+  m.warp = threadIdx.x >> 5;
+  const int gw = blockIdx.x * (blockDim.x >> 5) + m.warp;
+  m.strip = gw % g.nstrips;
+  m.chunk = gw / g.nstrips;
+  m.active = m.chunk < g.nchunks;
+  m.ib = m.chunk * g.lx;
+  m.ie = min(g.nx, m.ib + g.lx);
+  return m;
+}
+
+template <bool X, bool Y, bool Z>
+__device__ __forceinline__ void add_row(const InjectList& inj, int i, int c0, int& ci, f4& ax, f4& ay, f4& az) {
+  while (ci < inj.n && __ldg(&inj.list[ci].i) == i) {
+    const int e = __ldg(&inj.list[ci].j) - c0;
+    if (e >= 0 && e < 4) {
+      const size_t o = size_t(__ldg(&inj.list[ci].row)) * inj.nt + inj.it;
+      const float vx = X ? __ldg(&inj.val_x[o]) : 0.0f;
+      const float vy = Y ? __ldg(&inj.val_y[o]) : 0.0f;
+      const float vz = Z ? __ldg(&inj.val_z[o]) : 0.0f;
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q == e) {
+          if (X) ax.v[q] += vx;
+          if (Y) ay.v[q] += vy;
+          if (Z) az.v[q] += vz;
+        }
+    }
+    ++ci;
+  }
+}
+
+template <class Loader>
+__device__ __forceinline__ Loader make_aloader(const typename Loader::SegsT& segs, const Geom& g, const AMarch& m,
+                                               const LaneCols& L, unsigned char* smem) {
+  float* buf = nullptr;
+  uint64_t* bar = nullptr;
+  if (Loader::kStages > 0) {
+    const size_t per = size_t(Loader::kStages) * Loader::kStageBytes;
+    buf = reinterpret_cast<float*>(smem + per * m.warp);
+    bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
+  }
+  return Loader(segs, size_t(g.ld), L.c0, m.ib, m.lane, buf, bar, m.ie - m.ib + 3);
+}
+
+template <int NSEG>
+struct ADirect : DirectRows<NSEG> {
+  using SegsT = Segs<NSEG>;
+  static constexpr uint32_t kStageBytes = 0;
+  using DirectRows<NSEG>::DirectRows;
+};
+
+template <int NSEG>
+struct ABulk : BulkRows<NSEG, kAdjStages> {
+  using SegsT = Segs<NSEG>;
+  using BulkRows<NSEG, kAdjStages>::BulkRows;
+};
+
+__device__ __forceinline__ void flag(int* err) {
+  if ((threadIdx.x & 31) == 0 && err) atomicOr(err, kErrWaitTimeout);
+}
+
+}  // namespace
+
+// --------------------------------------------------------------------------
+// PSV
+// --------------------------------------------------------------------------
+enum PsvAdjSeg {
+  PA_SXX = 0, PA_SXZ, PA_SZZ, PA_VX, PA_VZ,      // forward state S^n
+  PA_BXX, PA_BZZ, PA_BXZ,                         // adjoint stress s^{n+1}, row i+1
+  PA_WX, PA_WZ,                                   // adjoint velocity w^{n+1}, row i
+  PA_OXX, PA_OZZ, PA_OXZ,                         // adjoint stress s^{n+1}, row i-2
+  PA_B, PA_LAM, PA_MU,                            // 1/rho (row i), lambda, mu (row i+1)
+  PA_GB, PA_GL, PA_GM,                            // gradients: g_B (row i), g_lambda, g_mu (row i-2)
+  PA_NSEG
+};
+
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32, 2) psv_adjoint_kernel(const PsvAdjoint p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const Geom& g = p.g;
+  const AMarch m = amarch(g);
+  if (!m.active) return;
+  const LaneCols L = lane_cols(g, m.strip, m.lane);
+  const size_t ld = size_t(g.ld);
+  const float dt = g.dt;
+  const int c0 = L.c0;
+  auto at = [&](auto* base, int i) { return base + ptrdiff_t(i) * ptrdiff_t(ld) + c0; };
+
+  typename Loader::SegsT segs;
+  segs.base[PA_SXX] = p.sxx; segs.roff[PA_SXX] = 1;
+  segs.base[PA_SXZ] = p.sxz; segs.roff[PA_SXZ] = 1;
+  segs.base[PA_SZZ] = p.szz; segs.roff[PA_SZZ] = 0;
+  segs.base[PA_VX] = p.vx; segs.roff[PA_VX] = 0;
+  segs.base[PA_VZ] = p.vz; segs.roff[PA_VZ] = 0;
+  segs.base[PA_BXX] = p.bxx0; segs.roff[PA_BXX] = 1;
+  segs.base[PA_BZZ] = p.bzz0; segs.roff[PA_BZZ] = 1;
+  segs.base[PA_BXZ] = p.bxz0; segs.roff[PA_BXZ] = 1;
+  segs.base[PA_WX] = p.wx0; segs.roff[PA_WX] = 0;
+  segs.base[PA_WZ] = p.wz0; segs.roff[PA_WZ] = 0;
+  segs.base[PA_OXX] = p.bxx0; segs.roff[PA_OXX] = -2;
+  segs.base[PA_OZZ] = p.bzz0; segs.roff[PA_OZZ] = -2;
+  segs.base[PA_OXZ] = p.bxz0; segs.roff[PA_OXZ] = -2;
+  segs.base[PA_B] = p.rho; segs.roff[PA_B] = 0;
+  segs.base[PA_LAM] = p.lam; segs.roff[PA_LAM] = 1;
+  segs.base[PA_MU] = p.mu; segs.roff[PA_MU] = 1;
+  segs.base[PA_GB] = p.g_b; segs.roff[PA_GB] = 0;
+  segs.base[PA_GL] = p.g_lam; segs.roff[PA_GL] = -2;
+  segs.base[PA_GM] = p.g_mu; segs.roff[PA_GM] = -2;
+  Loader rows = make_aloader<Loader>(segs, g, m, L, smem);
+  rows.start();
+
+  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  // Adjoint strains e = dt C s (unmasked) for rows of the ring.
+  auto strain_adj = [&](const f4& bxx, const f4& bzz, const f4& bxz, const f4& lam, const f4& mu, f4& exx,
+                        f4& ezz, f4& exz) {
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float l = lam.v[e], mm = mu.v[e];
+      exx.v[e] = dt * ((l + 2.0f * mm) * bxx.v[e] + l * bzz.v[e]);
+      ezz.v[e] = dt * (l * bxx.v[e] + (l + 2.0f * mm) * bzz.v[e]);
+      exz.v[e] = dt * mm * bxz.v[e];
+    }
+  };
+
+  // Prologue rings: forward sxx, sxz rows ib-3..ib-1; adjoint strains of rows ib-3..ib-1.
+  f4 xx0 = ld4(at(p.sxx, m.ib - 3)), xx1 = ld4(at(p.sxx, m.ib - 2)), xx2 = ld4(at(p.sxx, m.ib - 1)), xx3;
+  f4 xz0 = ld4(at(p.sxz, m.ib - 3)), xz1 = ld4(at(p.sxz, m.ib - 2)), xz2 = ld4(at(p.sxz, m.ib - 1)), xz3;
+  f4 ex0, ex1, ex2, ex3;   // e_xx rows i-2..i+1
+  f4 eq0, eq1, eq2, eq3;   // e_xz rows i-2..i+1
+  f4 ezc, ezn;             // e_zz rows i, i+1
+  {
+    f4 dummy;
+    strain_adj(ld4(at(p.bxx0, m.ib - 3)), ld4(at(p.bzz0, m.ib - 3)), ld4(at(p.bxz0, m.ib - 3)),
+               ld4(at(p.lam, m.ib - 3)), ld4(at(p.mu, m.ib - 3)), ex0, dummy, eq0);
+    strain_adj(ld4(at(p.bxx0, m.ib - 2)), ld4(at(p.bzz0, m.ib - 2)), ld4(at(p.bxz0, m.ib - 2)),
+               ld4(at(p.lam, m.ib - 2)), ld4(at(p.mu, m.ib - 2)), ex1, dummy, eq1);
+    strain_adj(ld4(at(p.bxx0, m.ib - 1)), ld4(at(p.bzz0, m.ib - 1)), ld4(at(p.bxz0, m.ib - 1)),
+               ld4(at(p.lam, m.ib - 1)), ld4(at(p.mu, m.ib - 1)), ex2, ezn, eq2);
+  }
+  f4 na, nb, nc, nd;   // recomputed forward vx^{n+1}, rows i-3..i
+  f4 za, zb, zc, zd;   // recomputed forward vz^{n+1}
+  f4 qxa, qxb, qxc, qxd;  // q = dt B w (x), rows i-3..i
+  f4 qza, qzb, qzc, qzd;  // q (z)
+  int ci = lower_row(p.src.list, p.src.n, m.ib - 1);
+  int ri = lower_row(p.rec.list, p.rec.n, m.ib - 1);
+  const int nk = m.ie - m.ib + 3;
+
+  for (int k = 0; k < nk; ++k) {
+    const int i = m.ib - 1 + k;
+    if (!rows.acquire(k)) {
+      flag(p.err);
+      rows.drain(k);
+      return;
+    }
+    xx3 = rows.seg(PA_SXX);
+    xz3 = rows.seg(PA_SXZ);
+    const f4 szz_i = rows.seg(PA_SZZ);
+    const f4 vx_i = rows.seg(PA_VX), vz_i = rows.seg(PA_VZ);
+    ezc = ezn;
+    {
+      f4 e1, e2, e3;
+      strain_adj(rows.seg(PA_BXX), rows.seg(PA_BZZ), rows.seg(PA_BXZ), rows.seg(PA_LAM), rows.seg(PA_MU), e1, e2,
+                 e3);
+      ex3 = e1;
+      ezn = e2;
+      eq3 = e3;
+    }
+    f4 wx = rows.seg(PA_WX), wz = rows.seg(PA_WZ);
+    const f4 oxx = rows.seg(PA_OXX), ozz = rows.seg(PA_OZZ), oxz = rows.seg(PA_OXZ);
+    const f4 buoy = rows.seg(PA_B);
+    f4 gb = rows.seg(PA_GB);
+    f4 gl = rows.seg(PA_GL), gm = rows.seg(PA_GM);
+    rows.release();
+    const float bxi = __ldg(p.taper_x + i);
+    const bool xb = mask_back(i, g.nx);
+
+    // Forward recompute: D- sigma^n + f^n and v^{n+1} of row i.
+    f4 dsx = dx4(xx0, xx1, xx2, xx3, g.rdx, xb);
+    f4 dsz = dx4(xz0, xz1, xz2, xz3, g.rdx, xb);
+    {
+      const f4 a = dz_back(xz2, g.rdz, L.zb);
+      const f4 b = dz_back(szz_i, g.rdz, L.zb);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
+    }
+    add_row<true, false, true>(p.src, i, c0, ci, dsx, dsx, dsz);
+    f4 bb;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      bb.v[e] = (bxi * tb.v[e]) * tt.v[e];
+      nd.v[e] = bb.v[e] * (vx_i.v[e] + dt * dsx.v[e] * buoy.v[e]);
+      zd.v[e] = bb.v[e] * (vz_i.v[e] + dt * dsz.v[e] * buoy.v[e]);
+    }
+
+    // Adjoint velocity of row i: Vbar = w + dt U (receivers) + (D+)^T e.
+    {
+      const bool m0 = mask_fwd(i - 2, g.nx), m1 = mask_fwd(i - 1, g.nx), m2 = mask_fwd(i, g.nx),
+                 m3 = mask_fwd(i + 1, g.nx);
+      const f4 tx = dxT(scaled(ex0, m0), scaled(ex1, m1), scaled(ex2, m2), scaled(ex3, m3), g.rdx);
+      const f4 tzx = dxT(scaled(eq0, m0), scaled(eq1, m1), scaled(eq2, m2), scaled(eq3, m3), g.rdx);
+      const f4 tq = dzT_back(masked(eq2, L.zf), g.rdz);
+      const f4 tz = dzT_back(masked(ezc, L.zf), g.rdz);
+      add_row<true, false, true>(p.rec, i, c0, ri, wx, wx, wz);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        wx.v[e] = bb.v[e] * (wx.v[e] + tx.v[e] + tq.v[e]);
+        wz.v[e] = bb.v[e] * (wz.v[e] + tz.v[e] + tzx.v[e]);
+        qxd.v[e] = dt * buoy.v[e] * wx.v[e];
+        qzd.v[e] = dt * buoy.v[e] * wz.v[e];
+      }
+    }
+    if (i >= m.ib && i < m.ie) {
+      st4_masked(at(p.wx1, i), wx, L.own);
+      st4_masked(at(p.wz1, i), wz, L.own);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) gb.v[e] = gb.v[e] + dt * (wx.v[e] * dsx.v[e] + wz.v[e] * dsz.v[e]);
+      st4_masked(at(p.g_b, i), gb, L.own);
+    }
+
+    // Adjoint stress of row r = i-2 and the lambda/mu gradients there.
+    if (i >= m.ib + 2) {
+      const int r = i - 2;
+      const bool xf = mask_fwd(r, g.nx);
+      const f4 exx = dx4(na, nb, nc, nd, g.rdx, xf);
+      const f4 ezx = dx4(za, zb, zc, zd, g.rdx, xf);
+      const f4 exz = dz_fwd(nb, g.rdz, L.zf);
+      const f4 ezz = dz_fwd(zb, g.rdz, L.zf);
+      const bool m0 = mask_back(r - 1, g.nx), m1 = mask_back(r, g.nx), m2 = mask_back(r + 1, g.nx),
+                 m3 = mask_back(r + 2, g.nx);
+      const f4 ax = dxT(scaled(qxa, m0), scaled(qxb, m1), scaled(qxc, m2), scaled(qxd, m3), g.rdx);
+      const f4 az = dxT(scaled(qza, m0), scaled(qzb, m1), scaled(qzc, m2),
+                        scaled(qzd, m3), g.rdx);
+      const f4 bx = dzT_fwd(masked(qxb, L.zb), g.rdz);
+      const f4 bz = dzT_fwd(masked(qzb, L.zb), g.rdz);
+      f4 sxx, szz, sxz;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        sxx.v[e] = oxx.v[e] + ax.v[e];
+        szz.v[e] = ozz.v[e] + bz.v[e];
+        sxz.v[e] = oxz.v[e] + (bx.v[e] + az.v[e]);
+        gl.v[e] = gl.v[e] + dt * (oxx.v[e] + ozz.v[e]) * (exx.v[e] + ezz.v[e]);
+        gm.v[e] = gm.v[e] + dt * (2.0f * oxx.v[e] * exx.v[e] + 2.0f * ozz.v[e] * ezz.v[e] +
+                                  oxz.v[e] * (exz.v[e] + ezx.v[e]));
+      }
+      st4_masked(at(p.bxx1, r), sxx, L.own);
+      st4_masked(at(p.bzz1, r), szz, L.own);
+      st4_masked(at(p.bxz1, r), sxz, L.own);
+      st4_masked(at(p.g_lam, r), gl, L.own);
+      st4_masked(at(p.g_mu, r), gm, L.own);
+    }
+
+    na = nb; nb = nc; nc = nd;
+    za = zb; zb = zc; zc = zd;
+    qxa = qxb; qxb = qxc; qxc = qxd;
+    qza = qzb; qzb = qzc; qzc = qzd;
+    xx0 = xx1; xx1 = xx2; xx2 = xx3;
+    xz0 = xz1; xz1 = xz2; xz2 = xz3;
+    ex0 = ex1; ex1 = ex2; ex2 = ex3;
+    eq0 = eq1; eq1 = eq2; eq2 = eq3;
+  }
+}
+
+// --------------------------------------------------------------------------
+// SH
+// --------------------------------------------------------------------------
+enum ShAdjSeg {
+  SA_SXY = 0, SA_SZY, SA_VY,   // forward state S^n: sxy (row i+1), szy (row i), vy (row i)
+  SA_BXY, SA_BZY,              // adjoint stress s^{n+1}, row i+1
+  SA_W,                        // adjoint velocity w^{n+1}, row i
+  SA_OXY, SA_OZY,              // adjoint stress s^{n+1}, row i-2
+  SA_B, SA_MU,                 // 1/rho (row i), mu (row i+1)
+  SA_GB, SA_GM,                // g_B (row i), g_mu (row i-2)
+  SA_NSEG
+};
+
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32, 2) sh_adjoint_kernel(const ShAdjoint p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const Geom& g = p.g;
+  const AMarch m = amarch(g);
+  if (!m.active) return;
+  const LaneCols L = lane_cols(g, m.strip, m.lane);
+  const size_t ld = size_t(g.ld);
+  const float dt = g.dt;
+  const int c0 = L.c0;
+  auto at = [&](auto* base, int i) { return base + ptrdiff_t(i) * ptrdiff_t(ld) + c0; };
+
+  typename Loader::SegsT segs;
+  segs.base[SA_SXY] = p.sxy; segs.roff[SA_SXY] = 1;
+  segs.base[SA_SZY] = p.szy; segs.roff[SA_SZY] = 0;
+  segs.base[SA_VY] = p.vy; segs.roff[SA_VY] = 0;
+  segs.base[SA_BXY] = p.bxy0; segs.roff[SA_BXY] = 1;
+  segs.base[SA_BZY] = p.bzy0; segs.roff[SA_BZY] = 1;
+  segs.base[SA_W] = p.w0; segs.roff[SA_W] = 0;
+  segs.base[SA_OXY] = p.bxy0; segs.roff[SA_OXY] = -2;
+  segs.base[SA_OZY] = p.bzy0; segs.roff[SA_OZY] = -2;
+  segs.base[SA_B] = p.rho; segs.roff[SA_B] = 0;
+  segs.base[SA_MU] = p.mu; segs.roff[SA_MU] = 1;
+  segs.base[SA_GB] = p.g_b; segs.roff[SA_GB] = 0;
+  segs.base[SA_GM] = p.g_mu; segs.roff[SA_GM] = -2;
+  Loader rows = make_aloader<Loader>(segs, g, m, L, smem);
+  rows.start();
+
+  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  auto times = [&](const f4& a, const f4& mu) {
+    f4 o;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) o.v[e] = mu.v[e] * dt * a.v[e];  // (mu*dt) as in add_sy_sh
+    return o;
+  };
+  f4 xy0 = ld4(at(p.sxy, m.ib - 3)), xy1 = ld4(at(p.sxy, m.ib - 2)), xy2 = ld4(at(p.sxy, m.ib - 1)), xy3;
+  f4 ex0 = times(ld4(at(p.bxy0, m.ib - 3)), ld4(at(p.mu, m.ib - 3)));
+  f4 ex1 = times(ld4(at(p.bxy0, m.ib - 2)), ld4(at(p.mu, m.ib - 2)));
+  f4 ex2 = times(ld4(at(p.bxy0, m.ib - 1)), ld4(at(p.mu, m.ib - 1)));
+  f4 ex3;
+  f4 ezc, ezn = times(ld4(at(p.bzy0, m.ib - 1)), ld4(at(p.mu, m.ib - 1)));
+  f4 na, nb, nc, nd;
+  f4 qa, qb, qc, qd;
+  int ci = lower_row(p.src.list, p.src.n, m.ib - 1);
+  int ri = lower_row(p.rec.list, p.rec.n, m.ib - 1);
+  const int nk = m.ie - m.ib + 3;
+
+  for (int k = 0; k < nk; ++k) {
+    const int i = m.ib - 1 + k;
+    if (!rows.acquire(k)) {
+      flag(p.err);
+      rows.drain(k);
+      return;
+    }
+    xy3 = rows.seg(SA_SXY);
+    const f4 szy_i = rows.seg(SA_SZY);
+    const f4 vy_i = rows.seg(SA_VY);
+    const f4 mu1 = rows.seg(SA_MU);
+    ex3 = times(rows.seg(SA_BXY), mu1);
+    ezc = ezn;
+    ezn = times(rows.seg(SA_BZY), mu1);
+    f4 w = rows.seg(SA_W);
+    const f4 oxy = rows.seg(SA_OXY), ozy = rows.seg(SA_OZY);
+    const f4 buoy = rows.seg(SA_B);
+    f4 gb = rows.seg(SA_GB), gm = rows.seg(SA_GM);
+    rows.release();
+    const float bxi = __ldg(p.taper_x + i);
+
+    f4 ds = dx4(xy0, xy1, xy2, xy3, g.rdx, mask_back(i, g.nx));
+    {
+      const f4 a = dz_back(szy_i, g.rdz, L.zb);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ds.v[e] = ds.v[e] + a.v[e];
+    }
+    add_row<false, true, false>(p.src, i, c0, ci, ds, ds, ds);
+    f4 bb;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      bb.v[e] = (bxi * tb.v[e]) * tt.v[e];
+      nd.v[e] = bb.v[e] * (vy_i.v[e] + dt * ds.v[e] * buoy.v[e]);
+    }
+    {
+      const f4 tx = dxT(scaled(ex0, mask_fwd(i - 2, g.nx)), scaled(ex1, mask_fwd(i - 1, g.nx)),
+                        scaled(ex2, mask_fwd(i, g.nx)), scaled(ex3, mask_fwd(i + 1, g.nx)), g.rdx);
+      const f4 tz = dzT_back(masked(ezc, L.zf), g.rdz);
+      add_row<false, true, false>(p.rec, i, c0, ri, w, w, w);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        w.v[e] = bb.v[e] * (w.v[e] + tx.v[e] + tz.v[e]);
+        qd.v[e] = dt * buoy.v[e] * w.v[e];
+      }
+    }
+    if (i >= m.ib && i < m.ie) {
+      st4_masked(at(p.w1, i), w, L.own);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) gb.v[e] = gb.v[e] + dt * w.v[e] * ds.v[e];
+      st4_masked(at(p.g_b, i), gb, L.own);
+    }
+    if (i >= m.ib + 2) {
+      const int r = i - 2;
+      const f4 ex = dx4(na, nb, nc, nd, g.rdx, mask_fwd(r, g.nx));
+      const f4 ez = dz_fwd(nb, g.rdz, L.zf);
+      const f4 ax = dxT(scaled(qa, mask_back(r - 1, g.nx)), scaled(qb, mask_back(r, g.nx)),
+                        scaled(qc, mask_back(r + 1, g.nx)), scaled(qd, mask_back(r + 2, g.nx)), g.rdx);
+      const f4 az = dzT_fwd(masked(qb, L.zb), g.rdz);
+      f4 sxy, szy;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        sxy.v[e] = oxy.v[e] + ax.v[e];
+        szy.v[e] = ozy.v[e] + az.v[e];
+        gm.v[e] = gm.v[e] + dt * (oxy.v[e] * ex.v[e] + ozy.v[e] * ez.v[e]);
+      }
+      st4_masked(at(p.bxy1, r), sxy, L.own);
+      st4_masked(at(p.bzy1, r), szy, L.own);
+      st4_masked(at(p.g_mu, r), gm, L.own);
+    }
+
+    na = nb; nb = nc; nc = nd;
+    qa = qb; qb = qc; qc = qd;
+    xy0 = xy1; xy1 = xy2; xy2 = xy3;
+    ex0 = ex1; ex1 = ex2; ex2 = ex3;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Launchers
+// --------------------------------------------------------------------------
+namespace {
+
+unsigned ablocks(const Geom& g) {
+  const long warps = long(g.nstrips) * g.nchunks;
+  return unsigned((warps + kStepWarps - 1) / kStepWarps);
+}
+
+template <class L>
+size_t asmem() {
+  return L::kStages ? size_t(kStepWarps) * L::smem_bytes_per_warp() : 0;
+}
+
+template <typename K>
+cudaError_t aprep(K kernel, size_t smem) {
+  if (smem > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  return cudaSuccess;
+}
+
+template <class L>
+cudaError_t launch_psv_adj(const PsvAdjoint& p, cudaStream_t s) {
+  const size_t smem = asmem<L>();
+  static const cudaError_t attr = aprep(psv_adjoint_kernel<L>, smem);
+  if (attr != cudaSuccess) return attr;
+  psv_adjoint_kernel<L><<<ablocks(p.g), kStepWarps * 32, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <class L>
+cudaError_t launch_sh_adj(const ShAdjoint& p, cudaStream_t s) {
+  const size_t smem = asmem<L>();
+  static const cudaError_t attr = aprep(sh_adjoint_kernel<L>, smem);
+  if (attr != cudaSuccess) return attr;
+  sh_adjoint_kernel<L><<<ablocks(p.g), kStepWarps * 32, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s) {
+  if (p.g.loader == kLoaderBulk) return launch_psv_adj<ABulk<PA_NSEG>>(p, s);
+  return launch_psv_adj<ADirect<PA_NSEG>>(p, s);
+}
+
+cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s) {
+  if (p.g.loader == kLoaderBulk) return launch_sh_adj<ABulk<SA_NSEG>>(p, s);
+  return launch_sh_adj<ADirect<SA_NSEG>>(p, s);
+}
+
+}  // namespace seiswg

@@ -60,6 +60,36 @@ int step_blocks_per_sm(bool psv, bool spin, int loader);
 cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s);
 cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s);
 
+// ---- exact discrete adjoint (fd_adjoint.cu) --------------------------------
+struct PsvAdjoint {
+  Geom g;
+  const float *vx, *vz, *sxx, *szz, *sxz;       // forward state S^n
+  const float *wx0, *wz0, *bxx0, *bzz0, *bxz0;  // adjoint state after step n
+  float *wx1, *wz1, *bxx1, *bzz1, *bxz1;        // adjoint state before step n
+  const float *rho, *lam, *mu;                  // 1/rho, lambda, mu
+  const float *taper_x, *taper_zb, *taper_zt;
+  float *g_b, *g_lam, *g_mu;                    // gradient accumulators (buoyancy, lambda, mu)
+  InjectList src;                               // forward sources of step n (val_x, val_z)
+  InjectList rec;                               // dt * U at the receivers (val_x, val_z)
+  int* err;
+};
+
+struct ShAdjoint {
+  Geom g;
+  const float *vy, *sxy, *szy;
+  const float *w0, *bxy0, *bzy0;
+  float *w1, *bxy1, *bzy1;
+  const float *rho, *mu;
+  const float *taper_x, *taper_zb, *taper_zt;
+  float *g_b, *g_mu;
+  InjectList src;  // val_y
+  InjectList rec;  // val_y
+  int* err;
+};
+
+cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s);
+cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s);
+
 // ---- auxiliary kernels (fd_aux.cu) ----------------------------------------
 
 // Pitched field helpers.  `f` points at element (0, 0).

@@ -56,7 +56,8 @@ struct Geom {
 
 // Row loaders of the step kernels (fd_pipe.cuh).
 enum { kLoaderDirect = 0, kLoaderBulk = 1 };
-constexpr int kPipeStages = 3;  // shared-memory stages per warp (2 rows in flight)
+constexpr int kPipeStages = 3;  // shared-memory stages per warp of the step kernels (2 rows in flight)
+constexpr int kAdjStages = 2;   // stages of the adjoint kernels (19 row segments per stage)
 
 // Bits of the device error word.
 enum { kErrWaitTimeout = 1 };

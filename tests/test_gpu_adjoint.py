@@ -1,0 +1,156 @@
+"""Exact discrete adjoint on the GPU (fd_adjoint.cu, checkpointed reverse
+sweep) against the FP64 oracle adjoint, finite differences of the FP32
+misfit, and invariance under the checkpoint interval."""
+import numpy as np
+import pytest
+
+from tests.examples import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+NX, NZ, NT, DX, DT = 70, 150, 260, 10.0, 1.5e-3
+
+
+def _problem(phys, seed=0):
+    rng = np.random.default_rng(seed)
+    vp = (3000 * (1 + 0.05 * np.tanh(rng.standard_normal((NX, NZ))))).astype(np.float32)
+    vs = (vp / np.sqrt(3)).astype(np.float32)
+    rho = (2500 * (1 + 0.03 * np.tanh(rng.standard_normal((NX, NZ))))).astype(np.float32)
+    flags = dict(sh=phys == "sh", psv=phys == "psv", abs_left=True, abs_right=True, abs_bottom=True, abs_width=12)
+    src = [(20, 40, 25.0, 0.04, 30.0), (50, 100, 20.0, 0.05, 60.0)]
+    rec = [(i, 20) for i in range(4, 67, 7)] + [(60, 140), (10, 130)]
+    return vp, vs, rho, flags, src, rec
+
+
+def _sim(vp, vs, rho, flags, src, rec):
+    import seiswg_gb300 as sw
+
+    sim = sw.Sim(NX, NZ, NT, DX, DX, DT, **flags)
+    sim.upload_model("vp", vp)
+    sim.upload_model("vs", vs)
+    sim.upload_model("rho", rho)
+    sim.prepare()
+    stf = np.stack([sw.ricker(NT, DT, s[2], s[3], s[4], 1.0e10) for s in src], axis=1)
+    sim.set_sources([s[0] for s in src], [s[1] for s in src], stf)
+    sim.set_receivers([r[0] for r in rec], [r[1] for r in rec])
+    return sim, stf
+
+
+def _comps(flags):
+    return [0, 2] if flags["psv"] else [1]
+
+
+def _observed(vp, vs, rho, flags, src, rec, isrc):
+    sim, _ = _sim(vp * 1.02, vs * 0.98, rho, flags, src, rec)
+    sim.forward(isrc)
+    obs = sim.traces()[_comps(flags)]
+    sim.close()
+    return obs
+
+
+def _gpu_gradient(sim, flags, obs, isrc, ckpt):
+    import seiswg_gb300 as sw
+
+    sim.gradient_clear()
+    sim.forward_op(isrc, ckpt)
+    syn = sim.traces()[_comps(flags)]
+    J, adj = sw.l2_misfit(syn, obs, DT)
+    sim.backward_op(adj)
+    return J, adj, {p: sim.gradient(p) for p in ("lambda", "mu", "buoyancy")}
+
+
+@pytest.mark.parametrize("phys", ["psv", "sh"])
+def test_gradient_matches_fp64_oracle(phys):
+    from oracle import oracle as O
+
+    vp, vs, rho, flags, src, rec = _problem(phys)
+    obs = _observed(vp, vs, rho, flags, src, rec, 0)
+    sim, stf = _sim(vp, vs, rho, flags, src, rec)
+    J, adj, g = _gpu_gradient(sim, flags, obs, 0, 0)
+    sim.close()
+    s = O.Setup(NX, NZ, NT, DX, DX, DT, **flags)
+    o = O.FD2DOracle(s, np.array([x[0] * NZ + x[1] for x in src]), stf.astype(np.float64),
+                     np.array([r[0] * NZ + r[1] for r in rec], np.int32), 64)
+    o.set_field("LAM", vp)
+    o.set_field("MU", vs)
+    o.set_field("RHO", rho)
+    o.init_model()
+    o.run_forward(0)
+    syn64 = np.stack([o.obs(c) for c in (("X", "Z") if flags["psv"] else ("Y",))])
+    J64, adj64 = O.l2_misfit(syn64, obs, DT)
+    gl, gm, gb = o.exact_gradient(adj64, 0)
+    assert abs(J - J64) <= 1e-4 * J64
+    assert rel_l2(g["mu"], gm) <= 1e-4
+    assert rel_l2(g["buoyancy"], gb) <= 1e-4
+    if flags["psv"]:
+        assert rel_l2(g["lambda"], gl) <= 1e-4
+
+
+@pytest.mark.parametrize("phys", ["psv", "sh"])
+def test_checkpoint_interval_does_not_change_the_gradient(phys):
+    vp, vs, rho, flags, src, rec = _problem(phys, 1)
+    obs = _observed(vp, vs, rho, flags, src, rec, -1)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    ref = _gpu_gradient(sim, flags, obs, -1, 1)[2]       # every state stored
+    for k in (7, 0, NT):                                # 7 steps, sqrt(nt), one interval
+        g = _gpu_gradient(sim, flags, obs, -1, k)[2]
+        for p in g:
+            assert np.array_equal(g[p], ref[p]), (k, p)
+    sim.close()
+
+
+def test_psv_gradient_matches_finite_differences_of_fp32_misfit():
+    import seiswg_gb300 as sw
+
+    vp, vs, rho, flags, src, rec = _problem("psv", 2)
+    obs = _observed(vp, vs, rho, flags, src, rec, 1)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    _, _, g = _gpu_gradient(sim, flags, obs, 1, 0)
+    sim.close()
+    gvp, gvs, grho = sw.velocity_gradients(g["lambda"], g["mu"], g["buoyancy"], vp, vs, rho)
+    grads = dict(vp=gvp, vs=gvs, rho=grho)
+    rng = np.random.default_rng(5)
+    # cells where the sensitivity is large (illuminated), seeded
+    mag = np.abs(gvs)
+    cand = np.argwhere(mag > 0.2 * mag.max())
+    picks = cand[rng.choice(len(cand), 16, replace=False)]
+    for q, (i, j) in enumerate(picks):
+        name = ("vp", "vs", "rho")[q % 3]
+        base = dict(vp=vp, vs=vs, rho=rho)
+        h = np.float32(2e-3) * base[name][i, j]
+
+        def J_of(sign):
+            m = {k: v.copy() for k, v in base.items()}
+            m[name][i, j] += sign * h
+            s, _ = _sim(m["vp"], m["vs"], m["rho"], flags, src, rec)
+            s.forward(1)
+            syn = s.traces()[[0, 2]]
+            s.close()
+            return sw.l2_misfit(syn, obs, DT)[0]
+
+        fd = (J_of(1) - J_of(-1)) / (2 * float(h))
+        assert abs(grads[name][i, j] - fd) <= 2e-2 * abs(fd), (name, i, j, grads[name][i, j], fd)
+
+
+def test_gradients_accumulate_over_shots_and_scale_linearly():
+    vp, vs, rho, flags, src, rec = _problem("psv", 3)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    rng = np.random.default_rng(4)
+    adj = [rng.standard_normal((2, len(rec), NT)).astype(np.float32) for _ in range(2)]
+    parts = []
+    for s in range(2):
+        sim.gradient_clear()
+        sim.forward_op(s, 0)
+        sim.backward_op(adj[s])
+        parts.append(sim.gradient("mu"))
+    sim.gradient_clear()
+    for s in range(2):
+        sim.forward_op(s, 0)
+        sim.backward_op(adj[s])
+    both = sim.gradient("mu")
+    assert rel_l2(both, parts[0] + parts[1]) <= 1e-6
+    sim.gradient_clear()
+    sim.forward_op(0, 0)
+    sim.backward_op(2.0 * adj[0])
+    assert rel_l2(sim.gradient("mu"), 2.0 * parts[0]) <= 1e-6
+    sim.close()
