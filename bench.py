@@ -344,6 +344,157 @@ def run_e2e(args, W, stf):
     return {"seconds": sec, "h2d": h2d, "d2h": d2h}
 
 
+def _timed(stream, fn, reps):
+    import torch
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def run_secondary(args):
+    """The other benchmark configurations, one JSON line each (not the headline)."""
+    import torch
+
+    import seiswg_gb300 as sw
+    from seiswg_gb300 import configs
+
+    peak, peak_kind = _peaks()
+    out = {"impl": "ours", "workload_key": args.workload, "warmup": args.warmup, "steps": args.steps,
+           "dtype": "f32", "data": "synthetic", "n_gpus": 1}
+    if args.workload in ("c1", "c3"):
+        W = configs.c1_sh_forward() if args.workload == "c1" else configs.c3_spin_forward(nt=args.nt or 3000)
+        sim = W.make_sim()
+        stream = torch.cuda.ExternalStream(sim.stream)
+        snap = W.extra.get("snap_every", 0)
+        run = (lambda: sim.forward(0, snap, ["vy"])) if snap else (lambda: sim.forward(0, sync=False))
+        for _ in range(args.warmup):
+            run()
+        sim.synchronize()
+        l0 = sim.launches
+        with Clocks(0) as clk:
+            ms = _timed(stream, run, args.steps)
+        sim.synchronize()
+        bpc = BYTES_PER_CELL["sh" if args.workload == "c1" else "spin"]
+        achieved = bpc * W.cells * W.nt / (ms / 1e3) / 1e9
+        out.update(metric=METRIC, value=W.cells * W.nt / (ms / 1e3) / 1e9, unit=METRIC, ms_per_step=ms,
+                   higher_is_better=True, config={"workload": W.name, **{k: v for k, v in W.extra.items()
+                                                                          if k != "true_model"}},
+                   roofline={"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "bytes_per_cell_update": bpc, "peak_source": peak_kind,
+                             "note": "L2-resident grid (3 state + 2 model fields x 160 KB)" if args.workload == "c1"
+                             else None},
+                   gpu_launches=int((sim.launches - l0) / args.steps), clocks=clk.summary(),
+                   traces_finite=bool(np.isfinite(sim.traces()).all()))
+        sim.close()
+    elif args.workload == "c4":
+        W = configs.c4_psv_adjoint(nt=args.nt or 3000)
+        sim_t = W.make_sim(model=W.extra["true_model"])
+        obs = []
+        for s in range(len(W.sources)):
+            sim_t.forward(s)
+            obs.append(sim_t.traces()[[0, 2]])
+        sim_t.close()
+        sim = W.make_sim()
+        stream = torch.cuda.ExternalStream(sim.stream)
+        Js = []
+
+        def gradient():
+            sim.gradient_clear()
+            Js.clear()
+            for s in range(len(W.sources)):
+                sim.forward_op(s, 0)
+                J, adj = sw.l2_misfit(sim.traces()[[0, 2]], obs[s], W.dt)
+                Js.append(J)
+                sim.backward_op(adj)
+
+        for _ in range(max(1, args.warmup)):
+            gradient()
+        sim.synchronize()
+        with Clocks(0) as clk:
+            t0 = time.perf_counter()
+            ms = _timed(stream, gradient, args.steps)
+            wall = (time.perf_counter() - t0) / args.steps
+        g = {p: sim.gradient(p) for p in ("lambda", "mu", "buoyancy")}
+        gvp, gvs, grho = sw.velocity_gradients(g["lambda"], g["mu"], g["buoyancy"], W.model["vp"], W.model["vs"],
+                                               W.model["rho"])
+        nshot = len(W.sources)
+        cell_updates = 2.0 * W.cells * W.nt * nshot   # forward + adjoint; recomputation not counted
+        out.update(metric="gradients/s", value=1000.0 / ms, unit="gradients/s", ms_per_step=ms,
+                   higher_is_better=True, wall_s_per_gradient=wall,
+                   gcell_updates_per_s=cell_updates / (ms / 1e3) / 1e9,
+                   config={"workload": W.name, "checkpoint_interval": int(math.ceil(math.sqrt(W.nt))),
+                           "misfit": "L2 waveform, ux+uz", "J_per_shot": list(Js),
+                           "receivers": int(W.rec_i.size), "shots": nshot},
+                   gradient_finite=bool(np.isfinite(gvp).all() and np.isfinite(gvs).all()),
+                   gradient_vs_peak_cell=[int(v) for v in np.unravel_index(np.argmax(np.abs(gvs)), gvs.shape)],
+                   clocks=clk.summary())
+        sim.close()
+    elif args.workload == "c5":
+        problems = configs.c5_batch()
+        comps = [[0, 2] if w.flags["psv"] else [1] for w in problems]
+        obs = []
+        for w, c in zip(problems, comps):   # observed data from the true models (untimed)
+            st = w.make_sim(model=w.extra["true_model"])
+            o = []
+            for s in range(len(w.sources)):
+                st.forward(s)
+                o.append(st.traces()[c])
+            st.close()
+            obs.append(np.array(o))
+        sims = [w.make_sim() for w in problems]
+        nshots = sum(len(w.sources) for w in problems)
+        # plain path: one problem and one shot at a time, host misfit
+        plain = []
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for w, sim, o, c in zip(problems, sims, obs, comps):
+            sim.gradient_clear()
+            for s in range(len(w.sources)):
+                sim.forward_op(s, 0)
+                _, adj = sw.l2_misfit(sim.traces()[c], o[s], w.dt)
+                sim.backward_op(adj)
+            sim.synchronize()
+            plain.append(sim.gradient("mu"))
+            sim.release_workspace()
+        plain_s = time.perf_counter() - t0
+        batch = sw.Batch(sims, obs)
+        stream = torch.cuda.ExternalStream(batch.stream)
+        t0 = time.perf_counter()
+        batch.run()                       # captures and instantiates the graph
+        first_s = time.perf_counter() - t0
+        for _ in range(max(0, args.warmup - 1)):
+            batch.run()
+        with Clocks(0) as clk:
+            t0 = time.perf_counter()
+            ms = _timed(stream, batch.run, args.steps)
+            wall = (time.perf_counter() - t0) / args.steps
+        errs = [rel_err for rel_err in (float(np.linalg.norm(batch.gradient(i, "mu") - plain[i]) /
+                                              max(np.linalg.norm(plain[i]), 1e-30)) for i in range(len(problems)))]
+        info = batch.info()
+        cells = sum(2.0 * w.cells * w.nt * len(w.sources) for w in problems)
+        out.update(metric="gradients/s", value=len(problems) / (wall), unit="problem-gradients/s",
+                   ms_per_step=wall * 1e3, higher_is_better=True,
+                   batched={"problem_gradients_per_s": len(problems) / wall, "shot_gradients_per_s": nshots / wall,
+                            "gcell_updates_per_s": cells / wall / 1e9, "seconds": wall, "event_ms": ms,
+                            "first_run_s_with_graph_capture": first_s},
+                   plain={"problem_gradients_per_s": len(problems) / plain_s, "shot_gradients_per_s": nshots / plain_s,
+                          "gcell_updates_per_s": cells / plain_s / 1e9, "seconds": plain_s},
+                   speedup=plain_s / wall, max_rel_l2_mu_vs_plain=max(errs),
+                   config={"workload": "c5: 48 problems, 256..1536 per axis, nt 1000..3000, SH/PSV, 1-4 shots",
+                           "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
+                           "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job"},
+                   clocks=clk.summary())
+        batch.close()
+        for s in sims:
+            s.close()
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -357,6 +508,8 @@ def main():
     ap.add_argument("--grid", type=int, default=4096, help="grid edge (4096 = the headline workload)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2 (default) is the headline; the others print their own line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -364,6 +517,11 @@ def main():
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload != "c2":
+        if args.nt == 4000:
+            args.nt = 0  # each configuration's own nt
+        run_secondary(args)
         return
     if world > 1:
         import torch.distributed as tdist

@@ -150,6 +150,9 @@ int seiswg_sim_forward_op(seiswg_sim* sim, int32_t isrc, int32_t ckpt_every);
 int seiswg_sim_backward_op(seiswg_sim* sim, const float* adj);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values. */
 int seiswg_sim_gradient(seiswg_sim* sim, const char* param, float* host);
+/* Frees the checkpoint, adjoint and snapshot buffers until their next use
+ * (gradients are kept). */
+int seiswg_sim_release_workspace(seiswg_sim* sim);
 /* Options: "graphs" (0/1), "chunk_rows" (rows per warp march), "loader"
  * (0: plain loads, 1: TMA bulk-copy row pipeline, the default). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
@@ -158,6 +161,29 @@ int seiswg_sim_synchronize(seiswg_sim* sim);
 uint64_t seiswg_sim_launches(const seiswg_sim* sim);
 void* seiswg_sim_stream(const seiswg_sim* sim);
 size_t seiswg_sim_device_bytes(const seiswg_sim* sim);
+
+/* ---- batched gradients of many problems ------------------------------------
+ * No counterpart in the reference (its shots run one after another,
+ * solver.rs:1372).  Each problem is a prepared seiswg_sim (SH or PSV, sources
+ * = its shots, receivers set) with observed traces obs[p] laid out
+ * [nshot][ncomp][nrec][nt].  seiswg_batch_run computes, for every shot of
+ * every problem at once, the recording forward pass with checkpoints every
+ * ckpt_every steps (0: ceil(sqrt(nt)) per shot), the L2 misfit and adjoint
+ * source on the device (as seiswg_l2_misfit), the reverse sweep, and the
+ * gradients summed per problem.  Problems must outlive the batch and must not
+ * run other work meanwhile.  The first run captures the schedule as a CUDA
+ * graph; later runs replay it. */
+typedef struct seiswg_batch seiswg_batch;
+int seiswg_batch_create(seiswg_sim* const* sims, const float* const* obs, int32_t nproblems, int32_t ckpt_every,
+                        void* stream, seiswg_batch** out);
+int seiswg_batch_run(seiswg_batch* batch);
+/* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */
+int seiswg_batch_gradient(seiswg_batch* batch, int32_t problem, const char* param, float* host);
+double seiswg_batch_misfit(const seiswg_batch* batch, int32_t problem);
+int seiswg_batch_info(const seiswg_batch* batch, int32_t* jobs, int32_t* slots, uint64_t* launches_per_run,
+                      size_t* device_bytes);
+void* seiswg_batch_stream(const seiswg_batch* batch);
+void seiswg_batch_free(seiswg_batch* batch);
 
 /* ---- smoothing without device allocation ----------------------------------
  * No counterpart in the reference.  Smooths an nx*nz float field

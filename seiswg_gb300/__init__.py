@@ -89,6 +89,7 @@ PROTOTYPES = [
     ("seiswg_sim_forward_op", _c_int, [_vp, _i32, _i32]),
     ("seiswg_sim_backward_op", _c_int, [_vp, _pf]),
     ("seiswg_sim_gradient", _c_int, [_vp, _cp, _pf]),
+    ("seiswg_sim_release_workspace", _c_int, [_vp]),
     ("seiswg_sim_set_option", _c_int, [_vp, _cp, ctypes.c_int64]),
     ("seiswg_sim_synchronize", _c_int, [_vp]),
     ("seiswg_sim_launches", ctypes.c_uint64, [_vp]),
@@ -99,6 +100,13 @@ PROTOTYPES = [
     ("seiswg_npy_encode", _c_int, [_pf, _sz, _sz, _vp, ctypes.POINTER(_sz)]),
     ("seiswg_infer_grid", _c_int, [_pf, _pf, _sz, _pi, _pi, _pf, _pf]),
     ("seiswg_smooth_noalloc", _c_int, [_vp, _vp, _i32, _i32, _f32, _vp]),
+    ("seiswg_batch_create", _c_int, [ctypes.POINTER(_vp), ctypes.POINTER(_pf), _i32, _i32, _vp, ctypes.POINTER(_vp)]),
+    ("seiswg_batch_run", _c_int, [_vp]),
+    ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
+    ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
+    ("seiswg_batch_info", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
+    ("seiswg_batch_stream", _vp, [_vp]),
+    ("seiswg_batch_free", None, [_vp]),
     ("seiswg_l2_misfit", _c_int, [_pf, _pf, _i32, _i32, _f32, _pf, ctypes.POINTER(ctypes.c_double)]),
     ("seiswg_velocity_gradients", _c_int, [_pf, _pf, _pf, _pf, _pf, _pf, _sz, _pf, _pf, _pf]),
 ]
@@ -359,6 +367,9 @@ class Sim:
         _check(lib().seiswg_sim_gradient(self._h, param.encode(), _fp(out)))
         return out
 
+    def release_workspace(self):
+        _check(lib().seiswg_sim_release_workspace(self._h))
+
     def set_option(self, key: str, value: int):
         _check(lib().seiswg_sim_set_option(self._h, key.encode(), int(value)))
 
@@ -387,6 +398,50 @@ class Sim:
 
     def __exit__(self, *a):
         self.close()
+
+    def __del__(self):
+        self.close()
+
+
+class Batch:
+    """Gradients of many independent problems in grouped launches under one
+    CUDA graph.  sims: prepared Sim objects (SH or PSV, sources = shots);
+    obs[p]: observed traces [nshot][ncomp][nrec][nt] of problem p."""
+
+    def __init__(self, sims, obs, ckpt_every: int = 0, stream=None):
+        self._sims = list(sims)   # the problems must outlive the batch
+        self._obs = [_f32(o).reshape(-1) for o in obs]
+        hs = (_vp * len(sims))(*[s._h for s in sims])
+        ps = (_pf * len(sims))(*[_fp(o) for o in self._obs])
+        h = _vp()
+        _check(lib().seiswg_batch_create(hs, ps, len(sims), ckpt_every, stream, ctypes.byref(h)))
+        self._h = h
+
+    def run(self):
+        _check(lib().seiswg_batch_run(self._h))
+
+    def gradient(self, problem: int, param: str):
+        s = self._sims[problem]
+        out = np.zeros((s.nx, s.nz), np.float32)
+        _check(lib().seiswg_batch_gradient(self._h, problem, param.encode(), _fp(out)))
+        return out
+
+    def misfit(self, problem: int) -> float:
+        return lib().seiswg_batch_misfit(self._h, problem)
+
+    def info(self):
+        j, s, l, b = _i32(), _i32(), ctypes.c_uint64(), _sz()
+        _check(lib().seiswg_batch_info(self._h, ctypes.byref(j), ctypes.byref(s), ctypes.byref(l), ctypes.byref(b)))
+        return dict(jobs=j.value, slots=s.value, launches_per_run=l.value, device_bytes=b.value)
+
+    @property
+    def stream(self) -> int:
+        return lib().seiswg_batch_stream(self._h) or 0
+
+    def close(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.seiswg_batch_free(self._h)
+            self._h = None
 
     def __del__(self):
         self.close()
@@ -459,5 +514,5 @@ def infer_grid(x, z):
     return nx.value, nz.value, dx.value, dz.value
 
 
-__all__ = ["SeiswgError", "Vfs", "Config", "Solver", "Sim", "SimDesc", "ricker", "waveform_misfit",
+__all__ = ["SeiswgError", "Vfs", "Config", "Solver", "Sim", "Batch", "SimDesc", "ricker", "waveform_misfit",
            "npy_encode", "infer_grid", "smooth_noalloc", "l2_misfit", "velocity_gradients", "lib", "LIB_PATH", "CLI_PATH", "PROTOTYPES"]

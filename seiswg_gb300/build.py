@@ -35,8 +35,8 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompile
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
              f"-I{os.path.join(ROOT, 'include')}"]
 
-CU_SOURCES = ["fd_step.cu", "fd_aux.cu", "fd_adjoint.cu", "noalloc.cu"]
-CXX_SOURCES = ["engine.cpp", "host.cpp", "capi.cpp"]
+CU_SOURCES = ["fd_step.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "noalloc.cu"]
+CXX_SOURCES = ["engine.cpp", "host.cpp", "batch.cpp", "capi.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 
 

@@ -1,0 +1,282 @@
+// batch.cpp -- see batch.h.
+#include "batch.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace seiswg {
+
+namespace {
+
+enum Kind { kFwdSh = 0, kFwdPsv, kAdjSh, kAdjPsv, kMisfit, kKinds };
+
+struct HostOp {
+  int kind, it, a, b, flags;
+};
+
+}  // namespace
+
+Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStream_t stream)
+    : problems_(problems), stream_(stream), ckpt_every_(ckpt_every) {
+  if (!stream_) {
+    SW_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    own_stream_ = true;
+  }
+  SW_CUDA(cudaMalloc(&err_, sizeof(int)));
+  SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
+  std::vector<JobDesc> descs;
+  for (size_t p = 0; p < problems_.size(); ++p) {
+    Sim* sim = problems_[p].sim;
+    const SimDesc& d = sim->desc();
+    if (d.spin || d.sh == d.psv) throw std::invalid_argument("batched gradients need SH or PSV (no spin)");
+    const Sim::View v = sim->view();
+    const int nt = d.nt, nrec = sim->nrec(), ncomp = d.psv ? 2 : 1;
+    const size_t fe = v.field_elems;
+    const size_t halo = size_t(kHaloRows) * v.ld + kHaloCols;
+    if (problems_[p].obs.size() != size_t(sim->nsrc()) * ncomp * nrec * nt)
+      throw std::invalid_argument("observed traces of problem " + std::to_string(p) + " have the wrong size");
+    float* sum = nullptr;
+    SW_CUDA(cudaMalloc(&sum, 3 * fe * sizeof(float)));
+    SW_CUDA(cudaMemsetAsync(sum, 0, 3 * fe * sizeof(float), stream_));
+    sums_.push_back(sum);
+    bytes_ += 3 * fe * sizeof(float);
+    std::vector<Inject> rec;
+    for (int r = 0; r < nrec; ++r) rec.push_back(Inject{v.rec_i[r], v.rec_j[r], r, 0});
+    std::stable_sort(rec.begin(), rec.end(),
+                     [](const Inject& a, const Inject& b) { return a.i != b.i ? a.i < b.i : a.j < b.j; });
+    for (int s = 0; s < sim->nsrc(); ++s) {
+      Job j;
+      j.problem = int(p);
+      j.shot = s;
+      j.nt = nt;
+      j.psv = d.psv;
+      j.nstate = d.psv ? 5 : 3;
+      j.ncomp = ncomp;
+      j.nrec = nrec;
+      j.k = ckpt_every > 0 ? std::min(ckpt_every, std::max(nt, 1))
+                           : int(std::ceil(std::sqrt(double(std::max(nt, 1)))));
+      j.ncp = (nt + j.k - 1) / j.k;
+      j.nslot = j.ncp + j.k + 1;
+      const size_t slot = size_t(j.nstate) * fe;
+      const size_t ntr = size_t(ncomp) * nrec;
+      SW_CUDA(cudaMalloc(&j.pool, size_t(j.nslot) * slot * sizeof(float)));
+      SW_CUDA(cudaMemsetAsync(j.pool, 0, size_t(j.nslot) * slot * sizeof(float), stream_));
+      SW_CUDA(cudaMalloc(&j.adj, 2 * slot * sizeof(float)));
+      SW_CUDA(cudaMemsetAsync(j.adj, 0, 2 * slot * sizeof(float), stream_));
+      SW_CUDA(cudaMalloc(&j.grads, 3 * fe * sizeof(float)));
+      SW_CUDA(cudaMemsetAsync(j.grads, 0, 3 * fe * sizeof(float), stream_));
+      SW_CUDA(cudaMalloc(&j.acc, std::max(1, v.nprobe) * sizeof(float)));
+      SW_CUDA(cudaMalloc(&j.hist, std::max<size_t>(1, size_t(v.nprobe) * nt) * sizeof(float)));
+      SW_CUDA(cudaMalloc(&j.obs, std::max<size_t>(1, ntr * nt) * sizeof(float)));
+      SW_CUDA(cudaMalloc(&j.u_tab, std::max<size_t>(1, ntr * nt) * sizeof(float)));
+      SW_CUDA(cudaMalloc(&j.J, std::max<size_t>(1, ntr) * sizeof(double)));
+      SW_CUDA(cudaMalloc(&j.src, sizeof(Inject)));
+      SW_CUDA(cudaMalloc(&j.rec, std::max(1, nrec) * sizeof(Inject)));
+      bytes_ += (size_t(j.nslot) + 2) * slot * sizeof(float) + 3 * fe * sizeof(float) +
+                (size_t(v.nprobe) * (nt + 1) + 2 * ntr * nt) * sizeof(float);
+      const Inject src{v.src_i[s], v.src_j[s], s, 0};
+      SW_CUDA(cudaMemcpyAsync(j.src, &src, sizeof(Inject), cudaMemcpyHostToDevice, stream_));
+      if (nrec) SW_CUDA(cudaMemcpyAsync(j.rec, rec.data(), nrec * sizeof(Inject), cudaMemcpyHostToDevice, stream_));
+      if (ntr)
+        SW_CUDA(cudaMemcpyAsync(j.obs, problems_[p].obs.data() + size_t(s) * ntr * nt, ntr * nt * sizeof(float),
+                                cudaMemcpyHostToDevice, stream_));
+      SW_CUDA(cudaStreamSynchronize(stream_));  // `src` and `rec` are host temporaries
+
+      JobDesc jd{};
+      jd.g = v.geom;
+      jd.psv = d.psv;
+      jd.nstate = j.nstate;
+      jd.field_elems = (long long)fe;
+      jd.slot_elems = (long long)slot;
+      jd.halo = (long long)halo;
+      jd.pool = j.pool;
+      jd.adj = j.adj;
+      jd.rho = v.rho; jd.lam = v.lam; jd.mu = v.mu;
+      jd.taper_x = v.taper_x; jd.taper_zb = v.taper_zb; jd.taper_zt = v.taper_zt;
+      jd.g_lam = j.grads + halo;
+      jd.g_mu = j.grads + fe + halo;
+      jd.g_b = j.grads + 2 * fe + halo;
+      const size_t nst = size_t(sim->nsrc()) * nt;
+      jd.src = InjectList{j.src, 1, nt, 0, v.stf, v.stf + nst, v.stf + 2 * nst};
+      jd.probes.list = v.probes + (d.psv ? v.probe_split : 0);
+      jd.probes.n = d.psv ? v.nprobe - v.probe_split : v.probe_split;
+      jd.probes.nt = nt;
+      jd.probes.acc = j.acc;
+      jd.probes.hist = j.hist;
+      jd.rec = InjectList{j.rec, nrec, nt, 0, nullptr, nullptr, nullptr};
+      if (d.psv) { jd.rec.val_x = j.u_tab; jd.rec.val_z = j.u_tab + size_t(nrec) * nt; }
+      else jd.rec.val_y = j.u_tab;
+      jd.tr_idx = v.tr_idx;
+      jd.obs = j.obs;
+      jd.u_tab = j.u_tab;
+      jd.J = j.J;
+      jd.nrec = nrec;
+      jd.nt = nt;
+      jd.dt = d.dt;
+      jd.err = err_;
+      descs.push_back(jd);
+      jobs_.push_back(j);
+    }
+  }
+  SW_CUDA(cudaMalloc(&d_jobs_, std::max<size_t>(1, descs.size()) * sizeof(JobDesc)));
+  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs.data(), descs.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  build_schedule();
+}
+
+Batch::~Batch() {
+  if (graph_) cudaGraphExecDestroy(graph_);
+  for (Job& j : jobs_) {
+    for (void* p : {(void*)j.pool, (void*)j.adj, (void*)j.grads, (void*)j.acc, (void*)j.hist, (void*)j.obs,
+                    (void*)j.u_tab, (void*)j.J, (void*)j.src, (void*)j.rec})
+      cudaFree(p);
+  }
+  for (float* s : sums_) cudaFree(s);
+  cudaFree(d_jobs_);
+  cudaFree(d_ops_);
+  cudaFree(err_);
+  if (own_stream_) cudaStreamDestroy(stream_);
+}
+
+// Operation list of each job (batch.h), then one launch per (slot, kind).
+void Batch::build_schedule() {
+  std::vector<std::vector<HostOp>> lists(jobs_.size());
+  for (size_t q = 0; q < jobs_.size(); ++q) {
+    const Job& j = jobs_[q];
+    const int k = j.k, ncp = j.ncp, nt = j.nt;
+    auto seg = [&](int m) { return ncp + m - 1; };  // interval buffer, m >= 1
+    auto pp = [&](int t) { return ncp + k - 1 + (t & 1); };
+    const int fwd = j.psv ? kFwdPsv : kFwdSh, adj = j.psv ? kAdjPsv : kAdjSh;
+    std::vector<HostOp>& L = lists[q];
+    for (int t = 0; t < nt; ++t) {
+      const int a = (t % k == 0) ? t / k : pp(t);
+      const int b = ((t + 1) % k == 0 && t + 1 < nt) ? (t + 1) / k : pp(t + 1);
+      L.push_back(HostOp{fwd, t, a, b, 1});
+    }
+    L.push_back(HostOp{kMisfit, 0, 0, 0, 0});
+    int parity = 0;
+    for (int c = ncp - 1; c >= 0; --c) {
+      const int n0 = c * k, n1 = std::min(nt, n0 + k);
+      for (int m = 1; m <= n1 - n0 - 1; ++m) L.push_back(HostOp{fwd, n0 + m - 1, m == 1 ? c : seg(m - 1), seg(m), 0});
+      for (int n = n1 - 1; n >= n0; --n) {
+        L.push_back(HostOp{adj, n, n == n0 ? c : seg(n - n0), parity, 0});
+        parity ^= 1;
+      }
+    }
+  }
+  size_t T = 0;
+  for (auto& L : lists) T = std::max(T, L.size());
+  nslots_ = int(T);
+  std::vector<GroupOp> all;
+  plan_.assign(T, {});
+  for (size_t t = 0; t < T; ++t) {
+    for (int kind = 0; kind < kKinds; ++kind) {
+      Launch l{kind, int(all.size()), 0, 0};
+      for (size_t q = 0; q < jobs_.size(); ++q) {
+        if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
+        const HostOp& h = lists[q][t];
+        const Sim::View v = problems_[jobs_[q].problem].sim->view();
+        all.push_back(GroupOp{int(q), h.it, h.a, h.b, h.flags, l.warps});
+        l.warps += (kind == kMisfit) ? 1 : v.geom.nstrips * v.geom.nchunks;
+        ++l.count;
+      }
+      if (l.count) plan_[t].push_back(l);
+    }
+  }
+  SW_CUDA(cudaMalloc(&d_ops_, std::max<size_t>(1, all.size()) * sizeof(GroupOp)));
+  SW_CUDA(cudaMemcpyAsync(d_ops_, all.data(), all.size() * sizeof(GroupOp), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  bytes_ += all.size() * sizeof(GroupOp);
+}
+
+void Batch::enqueue_run() {
+  launches_per_run_ = 0;
+  for (const Job& j : jobs_) {
+    const size_t fe = problems_[j.problem].sim->view().field_elems;
+    const size_t slot = size_t(j.nstate) * fe;
+    SW_CUDA(cudaMemsetAsync(j.adj, 0, 2 * slot * sizeof(float), stream_));
+    SW_CUDA(cudaMemsetAsync(j.grads, 0, 3 * fe * sizeof(float), stream_));
+    const Sim::View v = problems_[j.problem].sim->view();
+    SW_CUDA(cudaMemsetAsync(j.acc, 0, std::max(1, v.nprobe) * sizeof(float), stream_));
+  }
+  for (int t = 0; t < nslots_; ++t) {
+    for (const Launch& l : plan_[t]) {
+      const GroupOp* ops = d_ops_ + l.offset;
+      switch (l.kind) {
+        case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
+        case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
+        case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
+        case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
+        case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, stream_)); break;
+      }
+      ++launches_per_run_;
+    }
+  }
+  // Sum the shots of each problem.
+  for (size_t p = 0; p < problems_.size(); ++p) {
+    const Sim::View v = problems_[p].sim->view();
+    const size_t fe = v.field_elems, halo = size_t(kHaloRows) * v.ld + kHaloCols;
+    const SimDesc& d = problems_[p].sim->desc();
+    SW_CUDA(cudaMemsetAsync(sums_[p], 0, 3 * fe * sizeof(float), stream_));
+    for (const Job& j : jobs_) {
+      if (j.problem != int(p)) continue;
+      for (int f = 0; f < 3; ++f) {
+        float* s = sums_[p] + f * fe + halo;
+        SW_CUDA(launch_add_fields(s, s, j.grads + f * fe + halo, d.nx, d.nz, v.ld, stream_));
+        ++launches_per_run_;
+      }
+    }
+  }
+}
+
+void Batch::run() {
+  if (!graph_) {
+    cudaGraph_t g = nullptr;
+    SW_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    try {
+      enqueue_run();
+    } catch (...) {
+      cudaStreamEndCapture(stream_, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    SW_CUDA(cudaStreamEndCapture(stream_, &g));
+    cudaError_t e = cudaGraphInstantiate(&graph_, g, 0);
+    cudaGraphDestroy(g);
+    SW_CUDA(e);
+  }
+  SW_CUDA(cudaGraphLaunch(graph_, stream_));
+  // Per-trace misfits, summed per problem in a fixed order.
+  host_J_.assign(problems_.size(), 0.0);
+  std::vector<double> buf;
+  for (const Job& j : jobs_) {
+    buf.resize(size_t(j.ncomp) * j.nrec);
+    if (!buf.empty())
+      SW_CUDA(cudaMemcpyAsync(buf.data(), j.J, buf.size() * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    SW_CUDA(cudaStreamSynchronize(stream_));
+    for (double x : buf) host_J_[j.problem] += x;
+  }
+  int e = 0;
+  SW_CUDA(cudaMemcpy(&e, err_, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) throw CudaError("a batched kernel gave up waiting for its row pipeline (bounded wait expired)");
+}
+
+void Batch::download_gradient(int problem, int which, float* host) const {
+  if (problem < 0 || problem >= int(problems_.size())) throw std::invalid_argument("problem index out of range");
+  if (which < 0 || which > 2) throw std::invalid_argument("gradient index out of range");
+  const Sim::View v = problems_[problem].sim->view();
+  const SimDesc& d = problems_[problem].sim->desc();
+  const size_t halo = size_t(kHaloRows) * v.ld + kHaloCols;
+  SW_CUDA(cudaMemcpy2DAsync(host, size_t(d.nz) * sizeof(float), sums_[problem] + which * v.field_elems + halo,
+                            size_t(v.ld) * sizeof(float), size_t(d.nz) * sizeof(float), size_t(d.nx),
+                            cudaMemcpyDeviceToHost, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+double Batch::misfit(int problem) const {
+  if (problem < 0 || problem >= int(host_J_.size())) return 0.0;
+  return host_J_[problem];
+}
+
+}  // namespace seiswg

@@ -1,0 +1,81 @@
+// batch.h -- gradients of many independent problems (uneven grids, SH or
+// PSV, several shots each) advanced together.
+//
+// Every (problem, shot) is a job with its own wavefield storage.  The host
+// builds each job's operation list -- a recording forward pass writing a
+// checkpoint every k steps, the on-device misfit, then for each checkpoint
+// interval from the last one a forward recomputation followed by the reverse
+// steps -- and lays all lists side by side: global slot t holds operation t
+// of every job that has one.  Each slot is one grouped launch per kind
+// (forward SH, forward PSV, reverse SH, reverse PSV, misfit) whose warps
+// cover all jobs doing that kind of work, so that small problems share the
+// GPU.  The whole schedule is captured once as a CUDA graph and replayed.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "engine.h"
+
+namespace seiswg {
+
+struct BatchProblem {
+  Sim* sim;                  // model, sources and receivers set up; not owned
+  std::vector<float> obs;    // observed traces [nshot][ncomp][nrec][nt]
+};
+
+class Batch {
+ public:
+  // ckpt_every: checkpoint interval of every job (0: ceil(sqrt(nt)) per job).
+  // stream: nullptr for a stream of the batch's own.
+  Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStream_t stream);
+  ~Batch();
+  Batch(const Batch&) = delete;
+  Batch& operator=(const Batch&) = delete;
+
+  // All gradients: every shot of every problem, summed per problem.
+  void run();
+  // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
+  void download_gradient(int problem, int which, float* host) const;
+  double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
+  int jobs() const { return int(jobs_.size()); }
+  int slots() const { return nslots_; }
+  size_t device_bytes() const { return bytes_; }
+  uint64_t launches_per_run() const { return launches_per_run_; }
+  cudaStream_t stream() const { return stream_; }
+
+ private:
+  struct Job {
+    int problem, shot, k, ncp, nslot, nt, nstate, ncomp, nrec;
+    bool psv;
+    float *pool = nullptr, *adj = nullptr, *grads = nullptr, *acc = nullptr, *hist = nullptr, *obs = nullptr,
+          *u_tab = nullptr;
+    double* J = nullptr;
+    Inject* src = nullptr;
+    Inject* rec = nullptr;
+  };
+  void build_schedule();
+  void enqueue_run();
+
+  std::vector<BatchProblem> problems_;
+  std::vector<Job> jobs_;
+  cudaStream_t stream_;
+  bool own_stream_ = false;
+  int ckpt_every_;
+  JobDesc* d_jobs_ = nullptr;
+  GroupOp* d_ops_ = nullptr;
+  int* err_ = nullptr;
+  // per slot and kind: [offset, count, warps] into d_ops_
+  struct Launch {
+    int kind, offset, count, warps;
+  };
+  std::vector<std::vector<Launch>> plan_;
+  int nslots_ = 0;
+  std::vector<float*> sums_;   // per problem: 3 gradient fields
+  std::vector<double> host_J_;
+  size_t bytes_ = 0;
+  cudaGraphExec_t graph_ = nullptr;
+  uint64_t launches_per_run_ = 0;
+};
+
+}  // namespace seiswg

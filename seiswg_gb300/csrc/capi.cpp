@@ -6,6 +6,7 @@
 #include <new>
 #include <string>
 
+#include "batch.h"
 #include "host.h"
 
 struct seiswg_vfs {
@@ -19,6 +20,10 @@ struct seiswg_config {
 struct seiswg_sim {
   seiswg::Sim* sim = nullptr;
   bool owned = false;
+};
+
+struct seiswg_batch {
+  std::unique_ptr<seiswg::Batch> batch;
 };
 
 struct seiswg_solver {
@@ -407,6 +412,10 @@ int seiswg_sim_gradient(seiswg_sim* s, const char* param, float* host) {
   });
 }
 
+int seiswg_sim_release_workspace(seiswg_sim* s) {
+  return guarded([&] { sim_of(s).release_workspace(); });
+}
+
 int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
   return guarded([&] {
     seiswg::Sim& sim = sim_of(s);
@@ -425,6 +434,57 @@ int seiswg_sim_synchronize(seiswg_sim* s) {
 uint64_t seiswg_sim_launches(const seiswg_sim* s) { return (s && s->sim) ? s->sim->kernel_launches() : 0; }
 void* seiswg_sim_stream(const seiswg_sim* s) { return (s && s->sim) ? static_cast<void*>(s->sim->stream()) : nullptr; }
 size_t seiswg_sim_device_bytes(const seiswg_sim* s) { return (s && s->sim) ? s->sim->device_bytes() : 0; }
+
+// ---- batched gradients -----------------------------------------------------------
+int seiswg_batch_create(seiswg_sim* const* sims, const float* const* obs, int32_t n, int32_t ckpt_every,
+                        void* stream, seiswg_batch** out) {
+  if (!sims || !obs || n <= 0 || !out) return fail(SEISWG_EINVAL, "seiswg_batch_create: bad argument");
+  *out = nullptr;
+  return guarded([&] {
+    std::vector<seiswg::BatchProblem> ps;
+    for (int p = 0; p < n; ++p) {
+      seiswg::Sim& sim = sim_of(sims[p]);
+      const auto& d = sim.desc();
+      const size_t count = size_t(sim.nsrc()) * (d.psv ? 2 : 1) * sim.nrec() * d.nt;
+      if (!obs[p] && count) throw std::invalid_argument("null observed traces");
+      ps.push_back(seiswg::BatchProblem{&sim, std::vector<float>(obs[p], obs[p] + count)});
+    }
+    std::unique_ptr<seiswg_batch> b(new seiswg_batch());
+    b->batch.reset(new seiswg::Batch(ps, ckpt_every, static_cast<cudaStream_t>(stream)));
+    *out = b.release();
+  });
+}
+
+int seiswg_batch_run(seiswg_batch* b) {
+  if (!b) return fail(SEISWG_EINVAL, "null batch");
+  return guarded([&] { b->batch->run(); });
+}
+
+int seiswg_batch_gradient(seiswg_batch* b, int32_t problem, const char* param, float* host) {
+  if (!b || !param || !host) return fail(SEISWG_EINVAL, "seiswg_batch_gradient: null argument");
+  return guarded([&] {
+    std::string p = param;
+    int which = p == "lambda" ? 0 : p == "mu" ? 1 : p == "buoyancy" ? 2 : -1;
+    if (which < 0) throw std::invalid_argument("gradient parameter must be lambda, mu or buoyancy");
+    b->batch->download_gradient(problem, which, host);
+  });
+}
+
+double seiswg_batch_misfit(const seiswg_batch* b, int32_t problem) { return b ? b->batch->misfit(problem) : 0.0; }
+
+int seiswg_batch_info(const seiswg_batch* b, int32_t* jobs, int32_t* slots, uint64_t* launches, size_t* bytes) {
+  if (!b) return fail(SEISWG_EINVAL, "null batch");
+  if (jobs) *jobs = b->batch->jobs();
+  if (slots) *slots = b->batch->slots();
+  if (launches) *launches = b->batch->launches_per_run();
+  if (bytes) *bytes = b->batch->device_bytes();
+  g_last_error.clear();
+  return SEISWG_OK;
+}
+
+void* seiswg_batch_stream(const seiswg_batch* b) { return b ? static_cast<void*>(b->batch->stream()) : nullptr; }
+
+void seiswg_batch_free(seiswg_batch* b) { delete b; }
 
 // ---- host numerics ------------------------------------------------------------
 int seiswg_ricker(int32_t nt, float dt, float f0, float t0, float ang_deg, float amp, float* out) {

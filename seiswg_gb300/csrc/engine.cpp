@@ -894,6 +894,22 @@ void Sim::backward_op(const float* adj_host) {
   });
 }
 
+void Sim::release_workspace() {
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+  for (float** p : {&ck_store_, &seg_store_, &adj_store_, &fwd_store_, &snap_store_}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  ck_k_ = ck_n_ = 0;
+  ck_isrc_ = -2;
+  ck_bytes_ = 0;
+  fwd_nsa_ = 0;
+  fwd_bytes_ = 0;
+  snap_cap_ = 0;
+}
+
 void Sim::download_gradient(int which, float* host) const {
   const float* g = which == 0 ? g_lam_ : which == 1 ? g_mu_ : g_b_;
   if (!g) {
@@ -903,6 +919,27 @@ void Sim::download_gradient(int which, float* host) const {
   copy_field_to_host(g, host);
   SW_CUDA(cudaStreamSynchronize(stream_));
   check_device_error();
+}
+
+}  // namespace seiswg
+
+namespace seiswg {
+
+Sim::View Sim::view() const {
+  View v;
+  v.geom = geom_;
+  v.ld = ld_;
+  v.field_elems = field_elems_;
+  v.rho = rho_; v.lam = lam_; v.mu = mu_;
+  v.taper_x = taper_x_; v.taper_zb = taper_zb_; v.taper_zt = taper_zt_;
+  v.stf = stf_;
+  v.probes = probes_;
+  v.nprobe = nprobe_;
+  v.probe_split = probe_split_;
+  v.tr_idx = tr_idx_;
+  v.src_i = src_i_.data(); v.src_j = src_j_.data();
+  v.rec_i = rec_i_.data(); v.rec_j = rec_j_.data();
+  return v;
 }
 
 }  // namespace seiswg

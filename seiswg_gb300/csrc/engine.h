@@ -122,7 +122,25 @@ class Sim {
   // which: 0 lambda, 1 mu, 2 buoyancy
   void download_gradient(int which, float* host) const;
   int checkpoint_interval() const { return ck_k_; }
+  // Frees the checkpoint, interval, adjoint and snapshot buffers (they are
+  // allocated again on the next use); gradients are kept.
+  void release_workspace();
   size_t checkpoint_bytes() const { return ck_bytes_; }
+
+  // Device-side pieces of this simulation that a Batch shares between the
+  // jobs of one problem (read-only after set-up).
+  struct View {
+    Geom geom;
+    int ld;
+    size_t field_elems;
+    const float *rho, *lam, *mu, *taper_x, *taper_zb, *taper_zt;
+    const float* stf;       // [3][nsrc][nt]
+    const Probe* probes;    // SH segment, then PSV segment
+    int nprobe, probe_split;
+    const int* tr_idx;      // [nrec][12]
+    const int *src_i, *src_j, *rec_i, *rec_j;  // host arrays
+  };
+  View view() const;
 
   // Graph capture of whole time loops (replayed on repeated runs).
   void set_use_graphs(bool on) { use_graphs_ = on; }

@@ -89,11 +89,10 @@ struct AMarch {
   bool active;
 };
 
-__device__ __forceinline__ AMarch amarch(const Geom& g) {
+__device__ __forceinline__ AMarch amarch(const Geom& g, int gw) {
   AMarch m;
   m.lane = threadIdx.x & 31;
   m.warp = threadIdx.x >> 5;
-  const int gw = blockIdx.x * (blockDim.x >> 5) + m.warp;
   m.strip = gw % g.nstrips;
   m.chunk = gw / g.nstrips;
   m.active = m.chunk < g.nchunks;
@@ -169,10 +168,9 @@ enum PsvAdjSeg {
 };
 
 template <class Loader>
-__global__ void __launch_bounds__(kStepWarps * 32, 2) psv_adjoint_kernel(const PsvAdjoint p) {
-  extern __shared__ __align__(128) unsigned char smem[];
+__device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, unsigned char* smem) {
   const Geom& g = p.g;
-  const AMarch m = amarch(g);
+  const AMarch m = amarch(g, gw);
   if (!m.active) return;
   const LaneCols L = lane_cols(g, m.strip, m.lane);
   const size_t ld = size_t(g.ld);
@@ -368,10 +366,9 @@ enum ShAdjSeg {
 };
 
 template <class Loader>
-__global__ void __launch_bounds__(kStepWarps * 32, 2) sh_adjoint_kernel(const ShAdjoint p) {
-  extern __shared__ __align__(128) unsigned char smem[];
+__device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, unsigned char* smem) {
   const Geom& g = p.g;
-  const AMarch m = amarch(g);
+  const AMarch m = amarch(g, gw);
   if (!m.active) return;
   const LaneCols L = lane_cols(g, m.strip, m.lane);
   const size_t ld = size_t(g.ld);
@@ -491,6 +488,18 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) sh_adjoint_kernel(const Sh
   }
 }
 
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32, 2) psv_adjoint_kernel(const PsvAdjoint p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  psv_adjoint_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32, 2) sh_adjoint_kernel(const ShAdjoint p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  sh_adjoint_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
 // --------------------------------------------------------------------------
 // Launchers
 // --------------------------------------------------------------------------
@@ -532,6 +541,88 @@ cudaError_t launch_sh_adj(const ShAdjoint& p, cudaStream_t s) {
 }
 
 }  // namespace
+
+// ---- grouped reverse steps ------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ int find_aop(const GroupOp* __restrict__ ops, int nops, int gw) {
+  int lo = 0, hi = nops - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&ops[mid].warp_begin) <= gw) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ float* afield(float* base, const JobDesc& J, int slot, int f) {
+  return base + slot * J.slot_elems + f * J.field_elems + J.halo;
+}
+
+}  // namespace
+
+template <bool PSV>
+__global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_adjoint_kernel(const JobDesc* __restrict__ jobs,
+                                                                             const GroupOp* __restrict__ ops,
+                                                                             int nops) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const GroupOp op = ops[find_aop(ops, nops, gw)];
+  const JobDesc& J = jobs[op.job];
+  const int lw = gw - op.warp_begin;
+  if (lw >= J.g.nstrips * J.g.nchunks) return;
+  const int in = op.b & 1, out = 1 - in;
+  InjectList src = J.src, rec = J.rec;
+  src.it = op.it;
+  rec.it = op.it;
+  if constexpr (PSV) {
+    PsvAdjoint p{};
+    p.g = J.g;
+    p.vx = afield(J.pool, J, op.a, 0); p.vz = afield(J.pool, J, op.a, 1); p.sxx = afield(J.pool, J, op.a, 2);
+    p.szz = afield(J.pool, J, op.a, 3); p.sxz = afield(J.pool, J, op.a, 4);
+    p.wx0 = afield(J.adj, J, in, 0); p.wz0 = afield(J.adj, J, in, 1); p.bxx0 = afield(J.adj, J, in, 2);
+    p.bzz0 = afield(J.adj, J, in, 3); p.bxz0 = afield(J.adj, J, in, 4);
+    p.wx1 = afield(J.adj, J, out, 0); p.wz1 = afield(J.adj, J, out, 1); p.bxx1 = afield(J.adj, J, out, 2);
+    p.bzz1 = afield(J.adj, J, out, 3); p.bxz1 = afield(J.adj, J, out, 4);
+    p.rho = J.rho; p.lam = J.lam; p.mu = J.mu;
+    p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
+    p.g_b = J.g_b; p.g_lam = J.g_lam; p.g_mu = J.g_mu;
+    p.src = src;
+    p.rec = rec;
+    p.err = J.err;
+    psv_adjoint_march<ABulk<PA_NSEG>>(p, lw, smem);
+  } else {
+    ShAdjoint p{};
+    p.g = J.g;
+    p.vy = afield(J.pool, J, op.a, 0); p.sxy = afield(J.pool, J, op.a, 1); p.szy = afield(J.pool, J, op.a, 2);
+    p.w0 = afield(J.adj, J, in, 0); p.bxy0 = afield(J.adj, J, in, 1); p.bzy0 = afield(J.adj, J, in, 2);
+    p.w1 = afield(J.adj, J, out, 0); p.bxy1 = afield(J.adj, J, out, 1); p.bzy1 = afield(J.adj, J, out, 2);
+    p.rho = J.rho; p.mu = J.mu;
+    p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
+    p.g_b = J.g_b; p.g_mu = J.g_mu;
+    p.src = src;
+    p.rec = rec;
+    p.err = J.err;
+    sh_adjoint_march<ABulk<SA_NSEG>>(p, lw, smem);
+  }
+}
+
+cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
+                                   cudaStream_t s) {
+  if (nops <= 0 || warps <= 0) return cudaSuccess;
+  const unsigned blocks = unsigned((warps + kStepWarps - 1) / kStepWarps);
+  if (psv) {
+    const size_t smem = asmem<ABulk<PA_NSEG>>();
+    static const cudaError_t attr = aprep(grouped_adjoint_kernel<true>, smem);
+    if (attr != cudaSuccess) return attr;
+    grouped_adjoint_kernel<true><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+  } else {
+    const size_t smem = asmem<ABulk<SA_NSEG>>();
+    static const cudaError_t attr = aprep(grouped_adjoint_kernel<false>, smem);
+    if (attr != cudaSuccess) return attr;
+    grouped_adjoint_kernel<false><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+  }
+  return cudaGetLastError();
+}
 
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s) {
   if (p.g.loader == kLoaderBulk) return launch_psv_adj<ABulk<PA_NSEG>>(p, s);

@@ -90,6 +90,50 @@ struct ShAdjoint {
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s);
 cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s);
 
+// ---- grouped launches over many independent jobs (fd_step.cu, fd_adjoint.cu,
+// fd_batch.cu) ---------------------------------------------------------------
+// A job is one shot of one problem, with its own wavefield storage: a pool of
+// state slots (checkpoints, interval buffer, forward ping-pong), two adjoint
+// slots, gradient accumulators, probe histories and adjoint-source tables.
+// Field f of slot s starts at pool + s*slot_elems + f*field_elems + halo;
+// fields in a slot: SH vy, sxy, szy; PSV vx, vz, sxx, szz, sxz.
+struct JobDesc {
+  Geom g;
+  int psv;                 // 1 PSV, 0 SH
+  int nstate;
+  long long field_elems, slot_elems, halo;
+  float* pool;
+  float* adj;              // 2 adjoint slots
+  const float *rho, *lam, *mu;
+  const float *taper_x, *taper_zb, *taper_zt;
+  float *g_b, *g_lam, *g_mu;
+  InjectList src;          // the shot's source
+  ProbeList probes;        // receiver probes of this physics, with the job's acc/hist
+  InjectList rec;          // receivers, val = u_tab components
+  const int* tr_idx;       // [nrec][12] probe indices per receiver
+  const float* obs;        // observed traces [ncomp][nrec][nt]
+  float* u_tab;            // dt * U, [ncomp][nrec][nt]
+  double* J;               // per-trace misfit [ncomp][nrec]
+  int nrec, nt;
+  float dt;
+  int* err;
+};
+
+// One operation of one job in a grouped launch.  Forward: step `it` from slot
+// a to slot b (flags & 1: record the probes).  Adjoint: reverse step `it` with
+// the forward state in slot a and the adjoint state in slot (b & 1), writing
+// slot 1 - (b & 1).  Misfit: traces -> adjoint-source tables and J.  Warps
+// [warp_begin, warp_begin + nstrips*nchunks) of the launch belong to the op.
+struct GroupOp {
+  int job, it, a, b, flags, warp_begin;
+};
+
+cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
+                                   cudaStream_t s);
+cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
+                                   cudaStream_t s);
+cudaError_t launch_grouped_misfit(const JobDesc* jobs, const GroupOp* ops, int nops, cudaStream_t s);
+
 // ---- auxiliary kernels (fd_aux.cu) ----------------------------------------
 
 // Pitched field helpers.  `f` points at element (0, 0).

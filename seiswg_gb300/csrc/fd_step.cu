@@ -35,11 +35,10 @@ struct March {
   bool active;
 };
 
-__device__ __forceinline__ March march_of(const Geom& g) {
+__device__ __forceinline__ March march_of(const Geom& g, int gw) {
   March m;
   m.lane = threadIdx.x & 31;
   m.warp = threadIdx.x >> 5;
-  int gw = blockIdx.x * (blockDim.x >> 5) + m.warp;
   m.strip = gw % g.nstrips;
   m.chunk = gw / g.nstrips;
   m.active = m.chunk < g.nchunks;
@@ -139,11 +138,12 @@ __device__ __forceinline__ Loader make_loader(const typename Loader::SegsT& segs
 // --------------------------------------------------------------------------
 enum ShSeg { SH_SXY = 0, SH_SZY, SH_VY, SH_RHO, SH_MU, SH_NSEG };
 
+// One warp's march over its (strip, chunk); gw is the warp's index within
+// the problem.  Shared by the single-problem and the grouped kernels.
 template <class Loader>
-__global__ void __launch_bounds__(kStepWarps * 32) sh_step_kernel(const ShStep p) {
-  extern __shared__ __align__(128) unsigned char smem[];
+__device__ __forceinline__ void sh_march(const ShStep& p, int gw, unsigned char* smem) {
   const Geom& g = p.g;
-  const March m = march_of(g);
+  const March m = march_of(g, gw);
   if (!m.active) return;
   const LaneCols L = lane_cols(g, m.strip, m.lane);
   const size_t ld = size_t(g.ld);
@@ -238,10 +238,9 @@ enum PsvSeg {
 };
 
 template <bool SPIN, class Loader>
-__global__ void __launch_bounds__(kStepWarps * 32) psv_step_kernel(const PsvStep p) {
-  extern __shared__ __align__(128) unsigned char smem[];
+__device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned char* smem) {
   const Geom& g = p.g;
-  const March m = march_of(g);
+  const March m = march_of(g, gw);
   if (!m.active) return;
   const LaneCols L = lane_cols(g, m.strip, m.lane);
   const size_t ld = size_t(g.ld);
@@ -421,6 +420,18 @@ __global__ void __launch_bounds__(kStepWarps * 32) psv_step_kernel(const PsvStep
   }
 }
 
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32) sh_step_kernel(const ShStep p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  sh_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
+template <bool SPIN, class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32) psv_step_kernel(const PsvStep p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  psv_march<SPIN, Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
 // --------------------------------------------------------------------------
 // Launchers
 // --------------------------------------------------------------------------
@@ -463,6 +474,83 @@ cudaError_t launch_psv(const PsvStep& p, cudaStream_t s) {
 }
 
 }  // namespace
+
+// ---- grouped forward steps ----------------------------------------------------
+namespace {
+
+__device__ __forceinline__ int find_op(const GroupOp* __restrict__ ops, int nops, int gw) {
+  int lo = 0, hi = nops - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&ops[mid].warp_begin) <= gw) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ float* slot_field(const JobDesc& J, int slot, int f) {
+  return J.pool + slot * J.slot_elems + f * J.field_elems + J.halo;
+}
+
+}  // namespace
+
+template <bool PSV>
+__global__ void __launch_bounds__(kStepWarps * 32) grouped_forward_kernel(const JobDesc* __restrict__ jobs,
+                                                                          const GroupOp* __restrict__ ops, int nops) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const GroupOp op = ops[find_op(ops, nops, gw)];
+  const JobDesc& J = jobs[op.job];
+  const int lw = gw - op.warp_begin;
+  if (lw >= J.g.nstrips * J.g.nchunks) return;
+  ProbeList pl = J.probes;
+  if (!(op.flags & 1)) pl.n = 0;
+  pl.it = op.it;
+  InjectList inj = J.src;
+  inj.it = op.it;
+  if constexpr (PSV) {
+    PsvStep p{};
+    p.g = J.g;
+    p.vx0 = slot_field(J, op.a, 0); p.vz0 = slot_field(J, op.a, 1); p.sxx0 = slot_field(J, op.a, 2);
+    p.szz0 = slot_field(J, op.a, 3); p.sxz0 = slot_field(J, op.a, 4);
+    p.vx1 = slot_field(J, op.b, 0); p.vz1 = slot_field(J, op.b, 1); p.sxx1 = slot_field(J, op.b, 2);
+    p.szz1 = slot_field(J, op.b, 3); p.sxz1 = slot_field(J, op.b, 4);
+    p.rho = J.rho; p.lam = J.lam; p.mu = J.mu;
+    p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
+    p.inj = inj;
+    p.probes = pl;
+    p.err = J.err;
+    psv_march<false, BulkL<PV_NSEG>>(p, lw, smem);
+  } else {
+    ShStep p{};
+    p.g = J.g;
+    p.vy0 = slot_field(J, op.a, 0); p.sxy0 = slot_field(J, op.a, 1); p.szy0 = slot_field(J, op.a, 2);
+    p.vy1 = slot_field(J, op.b, 0); p.sxy1 = slot_field(J, op.b, 1); p.szy1 = slot_field(J, op.b, 2);
+    p.rho = J.rho; p.mu = J.mu;
+    p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
+    p.inj = inj;
+    p.probes = pl;
+    p.err = J.err;
+    sh_march<BulkL<SH_NSEG>>(p, lw, smem);
+  }
+}
+
+cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
+                                   cudaStream_t s) {
+  if (nops <= 0 || warps <= 0) return cudaSuccess;
+  const unsigned blocks = unsigned((warps + kStepWarps - 1) / kStepWarps);
+  if (psv) {
+    const size_t smem = smem_for<BulkL<PV_NSEG>>();
+    static const cudaError_t attr = prepare_kernel(grouped_forward_kernel<true>, smem);
+    if (attr != cudaSuccess) return attr;
+    grouped_forward_kernel<true><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+  } else {
+    const size_t smem = smem_for<BulkL<SH_NSEG>>();
+    static const cudaError_t attr = prepare_kernel(grouped_forward_kernel<false>, smem);
+    if (attr != cudaSuccess) return attr;
+    grouped_forward_kernel<false><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+  }
+  return cudaGetLastError();
+}
 
 size_t step_smem_bytes(bool psv, bool spin, int loader) {
   if (loader != kLoaderBulk) return 0;

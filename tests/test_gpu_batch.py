@@ -1,0 +1,84 @@
+"""Batched gradients of uneven problems (grouped launches under one CUDA
+graph, on-device misfit) against the plain per-shot path, problem by
+problem.  The tolerance is the benchmark spec's gradient accuracy, relative L2
+1e-4; the two paths share their kernels, so they agree far closer."""
+import numpy as np
+import pytest
+
+from tests.examples import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+# (nx, nz, nt, physics, shots)
+PROBLEMS = [(130, 160, 300, "psv", 2), (200, 140, 250, "sh", 1), (96, 300, 220, "psv", 3), (150, 150, 280, "sh", 2)]
+
+
+def _problems():
+    import seiswg_gb300 as sw
+    from seiswg_gb300.configs import Workload
+
+    out = []
+    rng = np.random.default_rng(7)
+    for (nx, nz, nt, phys, shots) in PROBLEMS:
+        vp = (3000 * (1 + 0.04 * np.tanh(rng.standard_normal((nx, nz))))).astype(np.float32)
+        vs = (vp / np.sqrt(3)).astype(np.float32)
+        rho = np.full((nx, nz), 2500.0, np.float32)
+        flags = dict(sh=phys == "sh", psv=phys == "psv", abs_left=True, abs_right=True, abs_bottom=True,
+                     abs_width=10)
+        src = [(int(i), 12, 25.0, 0.04, 20.0 * s, 1.0e10)
+               for s, i in enumerate(np.linspace(15, nx - 16, shots).astype(int))]
+        rec_i = np.arange(5, nx - 5, 9, dtype=np.int32)
+        w = Workload("t", nx, nz, nt, 10.0, 10.0, 1.5e-3, flags, dict(vp=vp, vs=vs, rho=rho), src, rec_i,
+                     np.full(rec_i.size, 20, np.int32))
+        true = dict(vp=vp * 1.03, vs=vs * 0.97, rho=rho)
+        st = w.make_sim(model=true)
+        comps = [0, 2] if phys == "psv" else [1]
+        obs = []
+        for s in range(shots):
+            st.forward(s)
+            obs.append(st.traces()[comps])
+        st.close()
+        out.append((w, np.array(obs), comps))
+    return out
+
+
+def _plain(w, obs, comps):
+    import seiswg_gb300 as sw
+
+    sim = w.make_sim()
+    sim.gradient_clear()
+    J = 0.0
+    for s in range(len(w.sources)):
+        sim.forward_op(s, 0)
+        j, adj = sw.l2_misfit(sim.traces()[comps], obs[s], w.dt)
+        J += j
+        sim.backward_op(adj)
+    g = {p: sim.gradient(p) for p in ("lambda", "mu", "buoyancy")}
+    sim.close()
+    return J, g
+
+
+def test_batch_matches_plain_path_and_replays():
+    import seiswg_gb300 as sw
+
+    probs = _problems()
+    plain = [_plain(w, obs, comps) for (w, obs, comps) in probs]
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    info = batch.info()
+    assert info["jobs"] == sum(p[4] for p in PROBLEMS)
+    results = []
+    for _ in range(2):   # first run captures the graph, second replays it
+        batch.run()
+        results.append([{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))])
+        for i, (J, _) in enumerate(plain):
+            assert abs(batch.misfit(i) - J) <= 1e-6 * J
+    for i, (J, g) in enumerate(plain):
+        params = ("lambda", "mu", "buoyancy") if probs[i][0].flags["psv"] else ("mu", "buoyancy")
+        for p in params:
+            assert np.abs(g[p]).max() > 0
+            assert rel_l2(results[0][i][p], g[p]) <= 1e-4, (i, p)
+            assert np.array_equal(results[0][i][p], results[1][i][p])
+    batch.close()
+    for s in sims:
+        s.close()
