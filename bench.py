@@ -369,6 +369,8 @@ def run_secondary(args):
     if args.workload in ("c1", "c3"):
         W = configs.c1_sh_forward() if args.workload == "c1" else configs.c3_spin_forward(nt=args.nt or 3000)
         sim = W.make_sim()
+        if args.autotune:
+            sim.set_option("autotune", 50)
         stream = torch.cuda.ExternalStream(sim.stream)
         snap = W.extra.get("snap_every", 0)
         run = (lambda: sim.forward(0, snap, ["vy"])) if snap else (lambda: sim.forward(0, sync=False))
@@ -508,6 +510,7 @@ def main():
     ap.add_argument("--grid", type=int, default=4096, help="grid edge (4096 = the headline workload)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="empirical loader/chunk tuning before timing")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default) is the headline; the others print their own line")
     args = ap.parse_args()

@@ -153,8 +153,10 @@ int seiswg_sim_gradient(seiswg_sim* sim, const char* param, float* host);
 /* Frees the checkpoint, adjoint and snapshot buffers until their next use
  * (gradients are kept). */
 int seiswg_sim_release_workspace(seiswg_sim* sim);
-/* Options: "graphs" (0/1), "chunk_rows" (rows per warp march), "loader"
- * (0: plain loads, 1: TMA bulk-copy row pipeline, the default). */
+/* Options: "graphs" (0/1), "chunk_rows" (rows per warp march; 0: the
+ * occupancy model), "loader" (0: plain loads, 1: TMA bulk-copy row pipeline,
+ * the default), "autotune" (value = steps timed per candidate: picks the
+ * fastest loader and chunk rows for this problem). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */

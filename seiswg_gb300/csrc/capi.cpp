@@ -423,6 +423,7 @@ int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
     if (k == "graphs") sim.set_use_graphs(value != 0);
     else if (k == "chunk_rows") sim.set_chunk_rows(value > 0 ? int(value) : sim.model_chunk_rows());
     else if (k == "loader") sim.set_loader(int(value));
+    else if (k == "autotune") sim.autotune(int(value));
     else throw std::invalid_argument("unknown option " + k);
   });
 }

@@ -155,6 +155,47 @@ int Sim::model_chunk_rows() const {
   return best;
 }
 
+double Sim::autotune(int steps) {
+  if (steps < 1) steps = 1;
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  const bool graphs = use_graphs_;
+  use_graphs_ = false;
+  InjectList inj = source_injections(-1);
+  ProbeList none{};
+  cudaEvent_t e0, e1;
+  SW_CUDA(cudaEventCreate(&e0));
+  SW_CUDA(cudaEventCreate(&e1));
+  std::vector<int> rows = {1, 2, 4, 8, 16, 32, 64, 128};
+  const int model = model_chunk_rows();
+  if (std::find(rows.begin(), rows.end(), model) == rows.end()) rows.push_back(model);
+  float best = 1e30f;
+  int best_loader = geom_.loader, best_lx = geom_.lx;
+  for (int loader : {kLoaderDirect, kLoaderBulk}) {
+    geom_.loader = loader;
+    for (int lx : rows) {
+      if (lx > std::max(d_.nx, 1) && lx != rows.front()) continue;
+      geom_.lx = lx;
+      geom_.nchunks = (d_.nx + lx - 1) / lx;
+      for (int it = 0; it < 2; ++it) enqueue_step(it, it & 1, inj, none, false);  // warm-up
+      SW_CUDA(cudaEventRecord(e0, stream_));
+      for (int it = 0; it < steps; ++it) enqueue_step(it % std::max(d_.nt, 1), it & 1, inj, none, false);
+      SW_CUDA(cudaEventRecord(e1, stream_));
+      SW_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.0f;
+      SW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) { best = ms; best_loader = loader; best_lx = lx; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  zero_state();
+  use_graphs_ = graphs;
+  geom_.loader = best_loader;
+  set_chunk_rows(best_lx);
+  check_device_error();
+  return 1e3 * double(best) / steps;
+}
+
 void Sim::set_loader(int loader) {
   if (loader != kLoaderDirect && loader != kLoaderBulk) throw std::invalid_argument("unknown loader");
   geom_.loader = loader;

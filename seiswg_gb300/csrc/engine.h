@@ -149,6 +149,12 @@ class Sim {
   // from the occupancy of the step kernel; the cost of a choice is
   // ceil(warps / resident) waves x (lx + 5) rows per warp.
   int model_chunk_rows() const;
+  // Empirical tuning: times `steps` forward steps for each candidate
+  // (row loader x rows per chunk) on this problem and keeps the fastest.
+  // Runs on the current state buffers, which every run resets, so it must
+  // not be called between a forward_op and its backward_op.  Returns the
+  // best time per step in microseconds.
+  double autotune(int steps);
   void set_loader(int loader);  // kLoaderDirect or kLoaderBulk
   int loader() const { return geom_.loader; }
   // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
