@@ -28,10 +28,12 @@ CLI = os.path.join(OUT, "seiswg")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# -fmad=false: the stencil keeps the reference's separate multiply and add
-# (fd2d.wgsl); the kernels are bandwidth-bound, so this costs nothing.
-NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xptxas", "-warn-spills"]
+NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
+# -fmad=false: the forward stencil keeps the reference's separate multiply and
+# add (fd2d.wgsl); those kernels are bandwidth-bound, so this costs nothing.
+# The reverse step has no counterpart in the reference and is issue-bound, so
+# it contracts multiply-add pairs.
+FMAD = {"fd_adjoint.cu": "true"}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
              f"-I{os.path.join(ROOT, 'include')}"]
 
@@ -70,7 +72,7 @@ def build(verbose=False, force=False):
     for s in CU_SOURCES:
         src, obj = os.path.join(CSRC, s), os.path.join(OBJ, s + ".o")
         if force or _stale(src, obj, hdr):
-            jobs.append([NVCC] + NVCC_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([NVCC] + NVCC_FLAGS + [f"-fmad={FMAD.get(s, 'false')}", "-c", src, "-o", obj])
     for s in CXX_SOURCES + CLI_SOURCES:
         src, obj = os.path.join(CSRC, s), os.path.join(OBJ, s + ".o")
         if force or _stale(src, obj, hdr):

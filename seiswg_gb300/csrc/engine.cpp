@@ -136,11 +136,10 @@ void Sim::set_chunk_rows(int lx) {
   graphs_.clear();
 }
 
-int Sim::model_chunk_rows() const {
+int Sim::chunk_rows_for(int per_sm) const {
   int dev = 0, nsm = 0;
   SW_CUDA(cudaGetDevice(&dev));
   SW_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  int per_sm = step_blocks_per_sm(d_.psv, d_.psv && d_.spin, geom_.loader);
   if (per_sm < 1) per_sm = 1;
   const long resident = long(per_sm) * nsm * kStepWarps;
   const int nstrips = (d_.nz + kStripCols - 1) / kStripCols;
@@ -153,6 +152,18 @@ int Sim::model_chunk_rows() const {
     if (cost < best_cost - 1e-9) { best_cost = cost; best = lx; }
   }
   return best;
+}
+
+int Sim::model_chunk_rows() const {
+  return chunk_rows_for(step_blocks_per_sm(d_.psv, d_.psv && d_.spin, geom_.loader));
+}
+
+Geom Sim::adjoint_geom() {
+  if (adj_lx_[geom_.loader] == 0) adj_lx_[geom_.loader] = chunk_rows_for(adjoint_blocks_per_sm(d_.psv, geom_.loader));
+  Geom g = geom_;
+  g.lx = adj_lx_[geom_.loader];
+  g.nchunks = (d_.nx + g.lx - 1) / g.lx;
+  return g;
 }
 
 double Sim::autotune(int steps) {
@@ -883,6 +894,7 @@ void Sim::backward_op(const float* adj_host) {
   SW_CUDA(cudaMemsetAsync(adj_store_, 0, 2 * state_elems * sizeof(float), stream_));
   const State adj[2] = {slot_state(adj_store_), slot_state(adj_store_ + state_elems)};
   const int k = ck_k_;
+  const Geom ga = adjoint_geom();
   SW_CUDA(cudaStreamSynchronize(stream_));  // host tables above are released after this call
 
   const std::string key = "bop/" + std::to_string(src.n) + "/" + std::to_string(rec.n) + "/" + std::to_string(k);
@@ -903,7 +915,7 @@ void Sim::backward_op(const float* adj_host) {
         r2.it = n;
         if (d_.psv) {
           PsvAdjoint p{};
-          p.g = geom_;
+          p.g = ga;
           p.vx = f.vx; p.vz = f.vz; p.sxx = f.sxx; p.szz = f.szz; p.sxz = f.sxz;
           p.wx0 = a.vx; p.wz0 = a.vz; p.bxx0 = a.sxx; p.bzz0 = a.szz; p.bxz0 = a.sxz;
           p.wx1 = o.vx; p.wz1 = o.vz; p.bxx1 = o.sxx; p.bzz1 = o.szz; p.bxz1 = o.sxz;
@@ -916,7 +928,7 @@ void Sim::backward_op(const float* adj_host) {
           SW_CUDA(launch_psv_adjoint(p, stream_));
         } else {
           ShAdjoint p{};
-          p.g = geom_;
+          p.g = ga;
           p.vy = f.vy; p.sxy = f.sxy; p.szy = f.szy;
           p.w0 = a.vy; p.bxy0 = a.sxy; p.bzy0 = a.szy;
           p.w1 = o.vy; p.bxy1 = o.sxy; p.bzy1 = o.szy;

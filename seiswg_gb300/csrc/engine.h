@@ -149,6 +149,8 @@ class Sim {
   // from the occupancy of the step kernel; the cost of a choice is
   // ceil(warps / resident) waves x (lx + 5) rows per warp.
   int model_chunk_rows() const;
+  // The same model for the reverse-step kernel, whose occupancy differs.
+  Geom adjoint_geom();
   // Empirical tuning: times `steps` forward steps for each candidate
   // (row loader x rows per chunk) on this problem and keeps the fastest.
   // Runs on the current state buffers, which every run resets, so it must
@@ -188,6 +190,7 @@ class Sim {
   void upload_inject(const std::vector<Inject>& list, int which);
   void run_loop(const std::string& key, const std::function<void()>& body);
   void copy_field_to_host(const float* dev, float* host) const;
+  int chunk_rows_for(int blocks_per_sm) const;
 
   SimDesc d_;
   cudaStream_t stream_;
@@ -195,6 +198,7 @@ class Sim {
   int ld_ = 0;
   size_t field_elems_ = 0;  // rows_alloc * ld
   Geom geom_{};
+  int adj_lx_[2] = {0, 0};  // reverse-step rows per chunk, per loader (0: not yet modelled)
   Arena arena_;
   State st_[2];
   float *rho_ = nullptr, *lam_ = nullptr, *mu_ = nullptr;

@@ -624,6 +624,32 @@ cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int 
   return cudaGetLastError();
 }
 
+int adjoint_blocks_per_sm(bool psv, int loader) {
+  int n = 0;
+  const int threads = kStepWarps * 32;
+  cudaError_t e;
+  if (psv) {
+    if (loader == kLoaderBulk) {
+      const size_t smem = asmem<ABulk<PA_NSEG>>();
+      e = aprep(psv_adjoint_kernel<ABulk<PA_NSEG>>, smem);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_adjoint_kernel<ABulk<PA_NSEG>>, threads, smem);
+    } else {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_adjoint_kernel<ADirect<PA_NSEG>>, threads, 0);
+    }
+  } else {
+    if (loader == kLoaderBulk) {
+      const size_t smem = asmem<ABulk<SA_NSEG>>();
+      e = aprep(sh_adjoint_kernel<ABulk<SA_NSEG>>, smem);
+      if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_adjoint_kernel<ABulk<SA_NSEG>>, threads, smem);
+    } else {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_adjoint_kernel<ADirect<SA_NSEG>>, threads, 0);
+    }
+  }
+  return e == cudaSuccess ? n : 0;
+}
+
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s) {
   if (p.g.loader == kLoaderBulk) return launch_psv_adj<ABulk<PA_NSEG>>(p, s);
   return launch_psv_adj<ADirect<PA_NSEG>>(p, s);

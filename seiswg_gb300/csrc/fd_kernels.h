@@ -87,6 +87,8 @@ struct ShAdjoint {
   int* err;
 };
 
+// Resident CTAs per SM of the reverse-step kernel for a loader (occupancy query).
+int adjoint_blocks_per_sm(bool psv, int loader);
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s);
 cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s);
 

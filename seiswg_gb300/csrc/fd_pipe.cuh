@@ -7,8 +7,8 @@
 //   DirectRows  plain 16-byte __ldg loads issued at the top of the iteration.
 //   BulkRows    a ring of S stages in shared memory filled by the TMA engine's
 //               bulk copy (cp.async.bulk ... mbarrier::complete_tx::bytes),
-//               lane 0 issuing S-1 iterations ahead; completion is tracked by
-//               one mbarrier per stage.  Waits are bounded: after kWaitLimit
+//               issued S-1 iterations ahead, lane q copying segment q;
+//               completion is tracked by one mbarrier per stage.  Waits are bounded: after kWaitLimit
 //               polls the warp records an error in *err, drains the copies it
 //               issued (again bounded) and leaves its march.
 #pragma once
@@ -101,26 +101,38 @@ struct DirectRows {
 
 template <int NSEG, int S>
 struct BulkRows {
+  static_assert(NSEG <= 32, "one lane issues each segment's copy");
   static constexpr int kStages = S;
   static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
   static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
-  Segs<NSEG> s;
+  const float* src;  // lane q < NSEG: segment q's field at row 0, the warp's first column
+  int roff;          // lane q < NSEG: segment q's row offset
   size_t ld;
-  int c0, ib, lane, nk, cur;
+  int ib, lane, nk, cur;
   float* buf;      // [S][NSEG][128]
   uint64_t* bar;   // [S]
   __device__ BulkRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int lane_, float* buf_,
                       uint64_t* bar_, int nk_)
-      : s(segs), ld(ld_), c0(c0_), ib(ib_), lane(lane_), nk(nk_), cur(0), buf(buf_), bar(bar_) {}
+      : src(nullptr), roff(0), ld(ld_), ib(ib_), lane(lane_), nk(nk_), cur(0), buf(buf_), bar(bar_) {
+    const int col0 = c0_ - 4 * lane_;  // the warp's first column (16-byte aligned)
+#pragma unroll
+    for (int q = 0; q < NSEG; ++q)
+      if (lane_ == q) {
+        src = segs.base[q] + col0;
+        roff = segs.roff[q];
+      }
+  }
 
+  // Lane 0 arms the stage's barrier with the stage's bytes; lanes 0..NSEG-1
+  // then copy one 512-byte segment each.  (A copy completing before the
+  // arrive would only take the transaction count below zero transiently,
+  // which the barrier allows; the warp issues the arrive first anyway.)
   __device__ __forceinline__ void issue(int k) {
     const int st = k % S;
     const int i = ib - 1 + k;
-    const int col0 = c0 - 4 * lane;  // the warp's first column (16-byte aligned)
-    mbar_expect_tx(&bar[st], kStageBytes);
-#pragma unroll
-    for (int q = 0; q < NSEG; ++q)
-      bulk_g2s(buf + (st * NSEG + q) * kSegFloats, s.base[q] + ptrdiff_t(i + s.roff[q]) * ptrdiff_t(ld) + col0,
+    if (lane == 0) mbar_expect_tx(&bar[st], kStageBytes);
+    if (lane < NSEG)
+      bulk_g2s(buf + (st * NSEG + lane) * kSegFloats, src + ptrdiff_t(i + roff) * ptrdiff_t(ld),
                kSegFloats * sizeof(float), &bar[st]);
   }
 
@@ -129,15 +141,16 @@ struct BulkRows {
     if (lane == 0) {
       for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
       fence_mbar_init();
-      for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
     }
+    __syncwarp();
+    for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
     __syncwarp();
   }
 
   // Refills the stage consumed in iteration k-1 with iteration k+S-1, then
   // waits for iteration k and reads the lane's float4 of every segment.
   __device__ __forceinline__ bool acquire(int k) {
-    if (lane == 0 && k + S - 1 < nk) {
+    if (k + S - 1 < nk) {
       fence_proxy_async();  // order the warp's reads of the old stage before the copy
       issue(k + S - 1);
     }
