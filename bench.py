@@ -173,6 +173,56 @@ def cpu_oracle_rate(W, nt_sample):
     return W["nx"] * W["nz"] * nt_sample / dtm / 1e9, dtm, O.num_threads()
 
 
+_ORACLE_SLOT = {"vp": "LAM", "vs": "MU", "rho": "RHO", "lambda": "LAM", "mu": "MU", "nu": "NU", "j": "J",
+                "lambda_c": "LAM_C", "mu_c": "MU_C", "nu_c": "NU_C"}
+
+
+def workload_oracle(W, nt, model=None, precision=32):
+    """The oracle set up with a configs.Workload's grid, flags, model, sources
+    and receivers, for `nt` steps."""
+    from oracle import oracle as O
+
+    f = W.flags
+    s = O.Setup(W.nx, W.nz, nt, W.dx, W.dz, W.dt, sh=f.get("sh", False), psv=f.get("psv", True),
+                spin=f.get("spin", False), abs_left=f.get("abs_left", False), abs_right=f.get("abs_right", False),
+                abs_bottom=f.get("abs_bottom", False), abs_top=f.get("abs_top", False),
+                abs_width=f.get("abs_width", 20), abs_alpha=f.get("abs_alpha", 0.015))
+    stf = O.stf_table([(0, 0, f0, t0, ang, amp) for (_, _, f0, t0, ang, amp) in W.sources], nt, W.dt, precision)
+    o = O.FD2DOracle(s, [i * W.nz + j for (i, j, *_) in W.sources], stf,
+                     np.asarray(W.rec_i, np.int64) * W.nz + np.asarray(W.rec_j, np.int64), precision)
+    for k, v in (model or W.model).items():
+        o.set_field(_ORACLE_SLOT[k], v)
+    o.init_model()
+    return o
+
+
+def cpu_forward_rate(W, nt_sample):
+    """FP32 oracle forward of shot 0 for nt_sample steps on the full grid:
+    (Gcell/s, seconds, threads)."""
+    from oracle import oracle as O
+
+    o = workload_oracle(W, nt_sample)
+    t0 = time.perf_counter()
+    o.run_forward(0)
+    dtm = time.perf_counter() - t0
+    return W.cells * nt_sample / dtm / 1e9, dtm, O.num_threads()
+
+
+def cpu_gradient_rate(W, nt_sample):
+    """FP32 oracle exact gradient (forward with every step's strains kept, then
+    the reverse sweep) of shot 0 for nt_sample steps on the full grid: counted
+    cell-updates (2 per cell and step) per second, seconds, threads."""
+    from oracle import oracle as O
+
+    o = workload_oracle(W, nt_sample)
+    ncomp = 2 if W.flags.get("psv", True) else 1
+    adj = np.random.default_rng(0).standard_normal((ncomp, W.rec_i.size, nt_sample)) * 1e-12
+    t0 = time.perf_counter()
+    o.exact_gradient(adj, 0)
+    dtm = time.perf_counter() - t0
+    return 2.0 * W.cells * nt_sample / dtm / 1e9, dtm, O.num_threads()
+
+
 def run_reference(args, rank):
     if rank != 0:
         return
@@ -393,6 +443,11 @@ def run_secondary(args):
                    gpu_launches=int((sim.launches - l0) / args.steps), clocks=clk.summary(),
                    traces_finite=bool(np.isfinite(sim.traces()).all()))
         sim.close()
+        if not args.no_cpu:
+            ns = W.nt if args.workload == "c1" else min(W.nt, 300)
+            r, dtm, thr = cpu_forward_rate(W, ns)
+            out["cpu_baseline"] = {"value": r, "unit": METRIC, "cores": thr, "kind": "port",
+                                   "sample": f"full grid, {ns} of {W.nt} steps (FP32 oracle, OpenMP), {dtm:.1f} s"}
     elif args.workload == "c4":
         W = configs.c4_psv_adjoint(nt=args.nt or 3000)
         sim_t = W.make_sim(model=W.extra["true_model"])
@@ -436,8 +491,16 @@ def run_secondary(args):
                    gradient_vs_peak_cell=[int(v) for v in np.unravel_index(np.argmax(np.abs(gvs)), gvs.shape)],
                    clocks=clk.summary())
         sim.close()
+        if not args.no_cpu:
+            ns = 24
+            r, dtm, thr = cpu_gradient_rate(W, ns)
+            out["cpu_baseline"] = {"value": r * 1e9 / cell_updates, "unit": "gradients/s", "cores": thr,
+                                   "kind": "port", "gcell_updates_per_s": r,
+                                   "sample": f"full grid, one shot, {ns} of {W.nt} steps (FP32 oracle exact "
+                                             f"gradient, every step's strains kept, OpenMP), {dtm:.1f} s; "
+                                             f"extrapolated to {nshot} shots x {W.nt} steps by cell-updates"}
     elif args.workload == "c5":
-        problems = configs.c5_batch()
+        problems = configs.c5_batch(count=args.count)
         comps = [[0, 2] if w.flags["psv"] else [1] for w in problems]
         obs = []
         for w, c in zip(problems, comps):   # observed data from the true models (untimed)
@@ -450,21 +513,33 @@ def run_secondary(args):
             obs.append(np.array(o))
         sims = [w.make_sim() for w in problems]
         nshots = sum(len(w.sources) for w in problems)
-        # plain path: one problem and one shot at a time, host misfit
+        # plain path: one problem and one shot at a time, host misfit (as the
+        # reference's solver.rs:432-467); each problem once untimed (graph
+        # capture, buffers), then timed.
         plain = []
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
+        plain_s = 0.0
         for w, sim, o, c in zip(problems, sims, obs, comps):
-            sim.gradient_clear()
-            for s in range(len(w.sources)):
-                sim.forward_op(s, 0)
-                _, adj = sw.l2_misfit(sim.traces()[c], o[s], w.dt)
-                sim.backward_op(adj)
-            sim.synchronize()
+            for rep in range(2):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                sim.gradient_clear()
+                for s in range(len(w.sources)):
+                    sim.forward_op(s, 0)
+                    _, adj = sw.l2_misfit(sim.traces()[c], o[s], w.dt)
+                    sim.backward_op(adj)
+                sim.synchronize()
+                if rep == 1:
+                    plain_s += time.perf_counter() - t0
             plain.append(sim.gradient("mu"))
             sim.release_workspace()
-        plain_s = time.perf_counter() - t0
         batch = sw.Batch(sims, obs)
+        tune_ms = None
+        if args.autotune:
+            t0 = time.perf_counter()
+            batch.set_option("autotune", 48)
+            tune_ms = (time.perf_counter() - t0) * 1e3
+        elif args.chunk_rows:
+            batch.set_option("chunk_rows", args.chunk_rows)
         stream = torch.cuda.ExternalStream(batch.stream)
         t0 = time.perf_counter()
         batch.run()                       # captures and instantiates the graph
@@ -487,10 +562,22 @@ def run_secondary(args):
                    plain={"problem_gradients_per_s": len(problems) / plain_s, "shot_gradients_per_s": nshots / plain_s,
                           "gcell_updates_per_s": cells / plain_s / 1e9, "seconds": plain_s},
                    speedup=plain_s / wall, max_rel_l2_mu_vs_plain=max(errs),
-                   config={"workload": "c5: 48 problems, 256..1536 per axis, nt 1000..3000, SH/PSV, 1-4 shots",
+                   config={"workload": f"c5: {len(problems)} problems, 256..1536 per axis, nt 1000..3000, SH/PSV, "
+                                       "1-4 shots",
                            "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
-                           "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job"},
+                           "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
+                           "chunk_rows": info.get("chunk_rows"), "autotune_ms": tune_ms},
                    clocks=clk.summary())
+        if not args.no_cpu:
+            small = min(range(len(problems)), key=lambda q: problems[q].cells)
+            ns = min(problems[small].nt, 300)
+            r, dtm, thr = cpu_gradient_rate(problems[small], ns)
+            out["cpu_baseline"] = {"value": r * 1e9 / cells * len(problems), "unit": "problem-gradients/s",
+                                   "cores": thr, "kind": "port", "gcell_updates_per_s": r,
+                                   "sample": f"smallest problem ({problems[small].nx}x{problems[small].nz}), one "
+                                             f"shot, {ns} of {problems[small].nt} steps (FP32 oracle exact "
+                                             f"gradient, OpenMP), {dtm:.1f} s; extrapolated to all {len(problems)} problems "
+                                             f"by cell-updates"}
         batch.close()
         for s in sims:
             s.close()
@@ -511,6 +598,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="empirical loader/chunk tuning before timing")
+    ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default) is the headline; the others print their own line")
     args = ap.parse_args()

@@ -148,6 +148,16 @@ int seiswg_sim_kernel(seiswg_sim* sim, float* host);
 int seiswg_sim_gradient_clear(seiswg_sim* sim);
 int seiswg_sim_forward_op(seiswg_sim* sim, int32_t isrc, int32_t ckpt_every);
 int seiswg_sim_backward_op(seiswg_sim* sim, const float* adj);
+/* The misfit and adjoint source on the device (the host misfit of
+ * solver.rs:432-467 without the trace download and the adjoint-source
+ * upload).  set_observed copies the observed traces, [ncomp][nrec][nt] in the
+ * components of backward_op; misfit_op, after forward_op, returns the L2
+ * waveform misfit J (seiswg_l2_misfit's taper and formula) and keeps its
+ * adjoint source on the device; backward_op_device runs the reverse sweep
+ * with it. */
+int seiswg_sim_set_observed(seiswg_sim* sim, const float* obs);
+int seiswg_sim_misfit_op(seiswg_sim* sim, double* J);
+int seiswg_sim_backward_op_device(seiswg_sim* sim);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values. */
 int seiswg_sim_gradient(seiswg_sim* sim, const char* param, float* host);
 /* Frees the checkpoint, adjoint and snapshot buffers until their next use
@@ -179,6 +189,13 @@ typedef struct seiswg_batch seiswg_batch;
 int seiswg_batch_create(seiswg_sim* const* sims, const float* const* obs, int32_t nproblems, int32_t ckpt_every,
                         void* stream, seiswg_batch** out);
 int seiswg_batch_run(seiswg_batch* batch);
+/* key "chunk_rows": rows per warp chunk of every job (0: each problem's own
+ * chunk model); "autotune": tries chunk rows 0, 16, 32, 48, 64, 96 and 128,
+ * timing `value` slots of the recording pass and of the reverse sweep each,
+ * and keeps the fastest.  Either drops the captured graph. */
+int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
+/* The chunk rows in use (0: each problem's own chunk model). */
+int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */
 int seiswg_batch_gradient(seiswg_batch* batch, int32_t problem, const char* param, float* host);
 double seiswg_batch_misfit(const seiswg_batch* batch, int32_t problem);
@@ -224,7 +241,10 @@ int seiswg_l2_misfit(const float* syn, const float* obs, int32_t ntr, int32_t nt
  * lambda = rho (vp^2 - 2 vs^2) (0 where vp <= vs), mu = rho vs^2. */
 int seiswg_velocity_gradients(const float* g_lam, const float* g_mu, const float* g_b, const float* vp,
                               const float* vs, const float* rho, size_t n, float* g_vp, float* g_vs, float* g_rho);
-/* nx, nz, dx, dz from coordinate arrays (solver.rs:646-656). */
+/* nx, nz, dx, dz from coordinate arrays: the reference's aspect-ratio rule
+ * (solver.rs:646-656) where it yields a grid consistent with the coordinate
+ * layout (square cells); otherwise, for rectangular cells (dx != dz), the grid
+ * read from the layout k = i*nz + j (nz = the first run of equal x). */
 int seiswg_infer_grid(const float* x, const float* z, size_t npt, int32_t* nx, int32_t* nz, float* dx, float* dz);
 
 #ifdef __cplusplus

@@ -88,6 +88,9 @@ PROTOTYPES = [
     ("seiswg_sim_gradient_clear", _c_int, [_vp]),
     ("seiswg_sim_forward_op", _c_int, [_vp, _i32, _i32]),
     ("seiswg_sim_backward_op", _c_int, [_vp, _pf]),
+    ("seiswg_sim_set_observed", _c_int, [_vp, _pf]),
+    ("seiswg_sim_misfit_op", _c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    ("seiswg_sim_backward_op_device", _c_int, [_vp]),
     ("seiswg_sim_gradient", _c_int, [_vp, _cp, _pf]),
     ("seiswg_sim_release_workspace", _c_int, [_vp]),
     ("seiswg_sim_set_option", _c_int, [_vp, _cp, ctypes.c_int64]),
@@ -102,6 +105,8 @@ PROTOTYPES = [
     ("seiswg_smooth_noalloc", _c_int, [_vp, _vp, _i32, _i32, _f32, _vp]),
     ("seiswg_batch_create", _c_int, [ctypes.POINTER(_vp), ctypes.POINTER(_pf), _i32, _i32, _vp, ctypes.POINTER(_vp)]),
     ("seiswg_batch_run", _c_int, [_vp]),
+    ("seiswg_batch_set_option", _c_int, [_vp, _cp, ctypes.c_int64]),
+    ("seiswg_batch_chunk_rows", _i32, [_vp]),
     ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
     ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
     ("seiswg_batch_info", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
@@ -362,6 +367,22 @@ class Sim:
         a = _f32(adj).reshape(-1)
         _check(lib().seiswg_sim_backward_op(self._h, _fp(a)))
 
+    def set_observed(self, obs):
+        """Observed traces [ncomp][nrec][nt] for misfit_op (kept on the device)."""
+        a = _f32(obs).reshape(-1)
+        _check(lib().seiswg_sim_set_observed(self._h, _fp(a)))
+
+    def misfit_op(self) -> float:
+        """L2 waveform misfit of the last forward_op on the device; keeps its
+        adjoint source there for backward_op_device()."""
+        J = ctypes.c_double(0.0)
+        _check(lib().seiswg_sim_misfit_op(self._h, ctypes.byref(J)))
+        return J.value
+
+    def backward_op_device(self):
+        """Reverse sweep with the adjoint source left by misfit_op()."""
+        _check(lib().seiswg_sim_backward_op_device(self._h))
+
     def gradient(self, param: str):
         out = np.zeros((self.nx, self.nz), np.float32)
         _check(lib().seiswg_sim_gradient(self._h, param.encode(), _fp(out)))
@@ -420,6 +441,10 @@ class Batch:
     def run(self):
         _check(lib().seiswg_batch_run(self._h))
 
+    def set_option(self, key: str, value: int):
+        """"chunk_rows" (0: per-problem model) or "autotune" (slots per timing window)."""
+        _check(lib().seiswg_batch_set_option(self._h, key.encode(), int(value)))
+
     def gradient(self, problem: int, param: str):
         s = self._sims[problem]
         out = np.zeros((s.nx, s.nz), np.float32)
@@ -432,7 +457,8 @@ class Batch:
     def info(self):
         j, s, l, b = _i32(), _i32(), ctypes.c_uint64(), _sz()
         _check(lib().seiswg_batch_info(self._h, ctypes.byref(j), ctypes.byref(s), ctypes.byref(l), ctypes.byref(b)))
-        return dict(jobs=j.value, slots=s.value, launches_per_run=l.value, device_bytes=b.value)
+        return dict(jobs=j.value, slots=s.value, launches_per_run=l.value, device_bytes=b.value,
+                    chunk_rows=int(lib().seiswg_batch_chunk_rows(self._h)))
 
     @property
     def stream(self) -> int:

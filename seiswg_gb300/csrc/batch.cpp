@@ -25,7 +25,6 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
   }
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
-  std::vector<JobDesc> descs;
   for (size_t p = 0; p < problems_.size(); ++p) {
     Sim* sim = problems_[p].sim;
     const SimDesc& d = sim->desc();
@@ -115,14 +114,65 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       jd.nt = nt;
       jd.dt = d.dt;
       jd.err = err_;
-      descs.push_back(jd);
+      descs_.push_back(jd);
+      model_geom_.push_back(jd.g);
       jobs_.push_back(j);
     }
   }
-  SW_CUDA(cudaMalloc(&d_jobs_, std::max<size_t>(1, descs.size()) * sizeof(JobDesc)));
-  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs.data(), descs.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaMalloc(&d_jobs_, std::max<size_t>(1, descs_.size()) * sizeof(JobDesc)));
+  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
   build_schedule();
+}
+
+void Batch::set_chunk_rows(int lx) {
+  if (lx != 0 && lx < 4) throw std::invalid_argument("chunk_rows must be 0 or >= 4");
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  for (size_t q = 0; q < descs_.size(); ++q) {
+    Geom g = model_geom_[q];
+    if (lx > 0) {
+      g.lx = lx;
+      g.nchunks = (g.nx + lx - 1) / lx;
+    }
+    descs_[q].g = g;
+  }
+  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
+  cudaFree(d_ops_);
+  d_ops_ = nullptr;
+  chunk_rows_ = lx;
+  build_schedule();
+}
+
+double Batch::autotune(int slots) {
+  if (slots < 1) slots = 1;
+  const int w = std::min(slots, nslots_);
+  const int mid = std::min(std::max(0, nslots_ - w), nslots_ * 3 / 5);
+  std::vector<int> cand = {0, 16, 32, 48, 64, 96, 128};
+  cudaEvent_t e0, e1;
+  SW_CUDA(cudaEventCreate(&e0));
+  SW_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int best_lx = chunk_rows_;
+  for (int lx : cand) {
+    set_chunk_rows(lx);
+    enqueue_slots(0, std::min(2, nslots_));  // warm-up
+    SW_CUDA(cudaEventRecord(e0, stream_));
+    enqueue_slots(0, w);
+    enqueue_slots(mid, mid + w);
+    SW_CUDA(cudaEventRecord(e1, stream_));
+    SW_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    SW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) { best = ms; best_lx = lx; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
+  set_chunk_rows(best_lx);
+  return double(best);
 }
 
 Batch::~Batch() {
@@ -176,9 +226,9 @@ void Batch::build_schedule() {
       for (size_t q = 0; q < jobs_.size(); ++q) {
         if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
         const HostOp& h = lists[q][t];
-        const Sim::View v = problems_[jobs_[q].problem].sim->view();
+        const Geom& g = descs_[q].g;
         all.push_back(GroupOp{int(q), h.it, h.a, h.b, h.flags, l.warps});
-        l.warps += (kind == kMisfit) ? 1 : v.geom.nstrips * v.geom.nchunks;
+        l.warps += (kind == kMisfit) ? 1 : g.nstrips * g.nchunks;
         ++l.count;
       }
       if (l.count) plan_[t].push_back(l);
@@ -187,7 +237,8 @@ void Batch::build_schedule() {
   SW_CUDA(cudaMalloc(&d_ops_, std::max<size_t>(1, all.size()) * sizeof(GroupOp)));
   SW_CUDA(cudaMemcpyAsync(d_ops_, all.data(), all.size() * sizeof(GroupOp), cudaMemcpyHostToDevice, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
-  bytes_ += all.size() * sizeof(GroupOp);
+  bytes_ += all.size() * sizeof(GroupOp) - ops_bytes_;
+  ops_bytes_ = all.size() * sizeof(GroupOp);
 }
 
 void Batch::enqueue_run() {
@@ -200,19 +251,7 @@ void Batch::enqueue_run() {
     const Sim::View v = problems_[j.problem].sim->view();
     SW_CUDA(cudaMemsetAsync(j.acc, 0, std::max(1, v.nprobe) * sizeof(float), stream_));
   }
-  for (int t = 0; t < nslots_; ++t) {
-    for (const Launch& l : plan_[t]) {
-      const GroupOp* ops = d_ops_ + l.offset;
-      switch (l.kind) {
-        case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
-        case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
-        case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
-        case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
-        case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, stream_)); break;
-      }
-      ++launches_per_run_;
-    }
-  }
+  enqueue_slots(0, nslots_);
   // Sum the shots of each problem.
   for (size_t p = 0; p < problems_.size(); ++p) {
     const Sim::View v = problems_[p].sim->view();
@@ -226,6 +265,22 @@ void Batch::enqueue_run() {
         SW_CUDA(launch_add_fields(s, s, j.grads + f * fe + halo, d.nx, d.nz, v.ld, stream_));
         ++launches_per_run_;
       }
+    }
+  }
+}
+
+void Batch::enqueue_slots(int t0, int t1) {
+  for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
+    for (const Launch& l : plan_[t]) {
+      const GroupOp* ops = d_ops_ + l.offset;
+      switch (l.kind) {
+        case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
+        case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
+        case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
+        case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
+        case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, stream_)); break;
+      }
+      ++launches_per_run_;
     }
   }
 }

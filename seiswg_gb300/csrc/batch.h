@@ -35,6 +35,15 @@ class Batch {
 
   // All gradients: every shot of every problem, summed per problem.
   void run();
+  // Rows per warp chunk of every job (0: each problem's own chunk model).
+  // Rebuilds the schedule; the captured graph is dropped.
+  void set_chunk_rows(int lx);
+  // Empirical tuning of the chunk rows: times two windows of `slots` slots of
+  // the schedule (the recording forward pass, and the reverse sweep) for each
+  // candidate and keeps the fastest.  Returns its time in milliseconds.  The
+  // timed launches leave results that the next run() overwrites.
+  double autotune(int slots);
+  int chunk_rows() const { return chunk_rows_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -56,6 +65,11 @@ class Batch {
   };
   void build_schedule();
   void enqueue_run();
+  void enqueue_slots(int t0, int t1);
+  std::vector<JobDesc> descs_;   // host copy of d_jobs_
+  std::vector<Geom> model_geom_; // each job's geometry from its problem's chunk model
+  int chunk_rows_ = 0;
+  size_t ops_bytes_ = 0;
 
   std::vector<BatchProblem> problems_;
   std::vector<Job> jobs_;

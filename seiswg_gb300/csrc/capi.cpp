@@ -402,6 +402,24 @@ int seiswg_sim_backward_op(seiswg_sim* s, const float* adj) {
   });
 }
 
+int seiswg_sim_set_observed(seiswg_sim* s, const float* obs) {
+  return guarded([&] {
+    if (!obs) throw std::invalid_argument("null observed traces");
+    sim_of(s).set_observed(obs);
+  });
+}
+
+int seiswg_sim_misfit_op(seiswg_sim* s, double* J) {
+  return guarded([&] {
+    if (!J) throw std::invalid_argument("null J");
+    *J = sim_of(s).misfit_op();
+  });
+}
+
+int seiswg_sim_backward_op_device(seiswg_sim* s) {
+  return guarded([&] { sim_of(s).backward_op_device(); });
+}
+
 int seiswg_sim_gradient(seiswg_sim* s, const char* param, float* host) {
   return guarded([&] {
     if (!param || !host) throw std::invalid_argument("null argument");
@@ -460,6 +478,18 @@ int seiswg_batch_run(seiswg_batch* b) {
   if (!b) return fail(SEISWG_EINVAL, "null batch");
   return guarded([&] { b->batch->run(); });
 }
+
+int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
+  if (!b || !key) return fail(SEISWG_EINVAL, "seiswg_batch_set_option: null argument");
+  return guarded([&] {
+    const std::string k(key);
+    if (k == "chunk_rows") b->batch->set_chunk_rows(int(value));
+    else if (k == "autotune") b->batch->autotune(int(value));
+    else throw std::invalid_argument("unknown batch option: " + k);
+  });
+}
+
+int32_t seiswg_batch_chunk_rows(const seiswg_batch* b) { return b ? b->batch->chunk_rows() : 0; }
 
 int seiswg_batch_gradient(seiswg_batch* b, int32_t problem, const char* param, float* host) {
   if (!b || !param || !host) return fail(SEISWG_EINVAL, "seiswg_batch_gradient: null argument");

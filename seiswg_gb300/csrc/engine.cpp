@@ -121,6 +121,8 @@ Sim::~Sim() {
   cudaFree(seg_store_);
   cudaFree(adj_store_);
   cudaFree(u_tab_);
+  cudaFree(obs_in_);
+  cudaFree(j_tr_);
   for (float* g : {g_lam_, g_mu_, g_b_})
     if (g) cudaFree(g - size_t(kHaloRows) * ld_ - kHaloCols);
   if (kmu_) cudaFree(kmu_ - size_t(kHaloRows) * ld_ - kHaloCols);
@@ -818,6 +820,7 @@ void Sim::gradient_clear() {
 }
 
 void Sim::forward_op(int isrc, int ckpt_every) {
+  u_ready_ = false;
   if (d_.spin) throw std::invalid_argument("the exact adjoint is defined for SH or PSV without spin");
   if (d_.sh && d_.psv) throw std::invalid_argument("the exact adjoint runs one of SH or PSV at a time");
   const int nt = d_.nt;
@@ -872,9 +875,54 @@ void Sim::backward_op(const float* adj_host) {
         u[size_t(c) * nrt + size_t(r) * nt + n] = float(double(d_.dt) * acc);
       }
     }
-  if (!u_tab_ && !u.empty()) SW_CUDA(cudaMalloc(&u_tab_, u.size() * sizeof(float)));
+  ensure_u_tab();
   if (!u.empty())
     SW_CUDA(cudaMemcpyAsync(u_tab_, u.data(), u.size() * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  run_backward();
+}
+
+void Sim::ensure_u_tab() {
+  const size_t n = size_t(d_.psv ? 2 : 1) * nrec_ * d_.nt;
+  if (!u_tab_ && n) SW_CUDA(cudaMalloc(&u_tab_, n * sizeof(float)));
+}
+
+void Sim::set_observed(const float* obs_host) {
+  const size_t n = size_t(d_.psv ? 2 : 1) * nrec_ * d_.nt;
+  if (!n) throw std::invalid_argument("set_observed needs receivers");
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  cudaFree(obs_in_);
+  obs_in_ = nullptr;
+  SW_CUDA(cudaMalloc(&obs_in_, n * sizeof(float)));
+  SW_CUDA(cudaMemcpyAsync(obs_in_, obs_host, n * sizeof(float), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+double Sim::misfit_op() {
+  if (ck_isrc_ == -2) throw std::logic_error("misfit_op without a preceding forward_op");
+  if (!obs_in_) throw std::logic_error("misfit_op without observed traces (set_observed)");
+  const int ntr = (d_.psv ? 2 : 1) * nrec_;
+  ensure_u_tab();
+  if (!j_tr_) SW_CUDA(cudaMalloc(&j_tr_, size_t(ntr) * sizeof(double)));
+  SW_CUDA(launch_sim_misfit(obs_, obs_in_, u_tab_, j_tr_, nrec_, d_.nt, d_.psv, d_.dt, stream_));
+  ++launches_;
+  std::vector<double> jt(ntr);
+  SW_CUDA(cudaMemcpyAsync(jt.data(), j_tr_, size_t(ntr) * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  double J = 0.0;
+  for (double v : jt) J += v;
+  u_ready_ = true;
+  return J;
+}
+
+void Sim::backward_op_device() {
+  if (ck_isrc_ == -2) throw std::logic_error("backward_op without a preceding forward_op");
+  if (!u_ready_) throw std::logic_error("backward_op_device without a misfit_op after the forward_op");
+  run_backward();
+}
+
+void Sim::run_backward() {
+  const int nt = d_.nt;
+  const size_t nrt = size_t(nrec_) * nt;
   std::vector<Inject> list;
   for (int r = 0; r < nrec_; ++r) list.push_back(Inject{rec_i_[r], rec_j_[r], r, 0});
   std::stable_sort(list.begin(), list.end(),

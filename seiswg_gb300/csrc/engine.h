@@ -119,6 +119,14 @@ class Sim {
   void gradient_clear();
   void forward_op(int isrc, int ckpt_every);
   void backward_op(const float* adj_host);
+  // On-device misfit: the host pair (l2 misfit of downloaded traces, upload of
+  // the adjoint source) without the round trip.  set_observed uploads the
+  // observed traces [ncomp][nrec][nt] (same components as backward_op);
+  // misfit_op, after a forward_op, returns J and leaves dt * U on the device;
+  // backward_op_device then runs the reverse sweep with it.
+  void set_observed(const float* obs_host);
+  double misfit_op();
+  void backward_op_device();
   // which: 0 lambda, 1 mu, 2 buoyancy
   void download_gradient(int which, float* host) const;
   int checkpoint_interval() const { return ck_k_; }
@@ -240,6 +248,11 @@ class Sim {
   float* adj_store_ = nullptr;  // 2 adjoint states
   float *g_lam_ = nullptr, *g_mu_ = nullptr, *g_b_ = nullptr;
   float* u_tab_ = nullptr;      // dt * U, [ncomp][nrec][nt]
+  float* obs_in_ = nullptr;     // observed traces for misfit_op, [ncomp][nrec][nt]
+  double* j_tr_ = nullptr;      // misfit per trace
+  bool u_ready_ = false;        // u_tab_ holds the adjoint source of the last forward_op
+  void run_backward();
+  void ensure_u_tab();
 
   bool use_graphs_ = true;
   std::map<std::string, cudaGraphExec_t> graphs_;

@@ -142,10 +142,12 @@ struct ADirect : DirectRows<NSEG> {
   using DirectRows<NSEG>::DirectRows;
 };
 
+// The reverse step reads 12 (SH) or 19 (PSV) segments per row: their copies
+// are issued one per lane.
 template <int NSEG>
-struct ABulk : BulkRows<NSEG, kAdjStages> {
+struct ABulk : BulkRows<NSEG, kAdjStages, true> {
   using SegsT = Segs<NSEG>;
-  using BulkRows<NSEG, kAdjStages>::BulkRows;
+  using BulkRows<NSEG, kAdjStages, true>::BulkRows;
 };
 
 __device__ __forceinline__ void flag(int* err) {
@@ -545,15 +547,6 @@ cudaError_t launch_sh_adj(const ShAdjoint& p, cudaStream_t s) {
 // ---- grouped reverse steps ------------------------------------------------------
 namespace {
 
-__device__ __forceinline__ int find_aop(const GroupOp* __restrict__ ops, int nops, int gw) {
-  int lo = 0, hi = nops - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&ops[mid].warp_begin) <= gw) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ float* afield(float* base, const JobDesc& J, int slot, int f) {
   return base + slot * J.slot_elems + f * J.field_elems + J.halo;
 }
@@ -566,7 +559,7 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_adjoint_kernel(con
                                                                              int nops) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const GroupOp op = ops[find_aop(ops, nops, gw)];
+  const GroupOp op = ops[group_op_of(ops, nops, gw)];
   const JobDesc& J = jobs[op.job];
   const int lw = gw - op.warp_begin;
   if (lw >= J.g.nstrips * J.g.nchunks) return;

@@ -130,10 +130,41 @@ struct GroupOp {
   int job, it, a, b, flags, warp_begin;
 };
 
+#ifdef __CUDACC__
+// The op of warp gw in a grouped launch: the last op with warp_begin <= gw
+// (ops sorted by warp_begin, ops[0].warp_begin == 0).  The warp reads the
+// begins of 32 ops per step, up to four steps' loads in flight together, and
+// votes, instead of a binary search's chain of dependent loads.  gw is
+// uniform over the warp and all lanes are active.
+__device__ __forceinline__ int group_op_of(const GroupOp* __restrict__ ops, int nops, int gw) {
+  const int lane = threadIdx.x & 31;
+  int found = 0;
+  for (int base = 0; base < nops; base += 128) {
+    bool le[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int q = base + 32 * u + lane;
+      le[u] = q < nops && __ldg(&ops[q].warp_begin) <= gw;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned m = __ballot_sync(0xffffffffu, le[u]);
+      if (m == 0u) return found;
+      found = base + 32 * u + 31 - __clz(int(m));
+    }
+  }
+  return found;
+}
+#endif
+
 cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
                                    cudaStream_t s);
 cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
                                    cudaStream_t s);
+// Misfit of one problem's assembled traces against obs [ncomp][nrec][nt];
+// writes J per trace and the adjoint-source table dt * U.
+cudaError_t launch_sim_misfit(const float* syn, const float* obs, float* u_tab, double* J, int nrec, int nt,
+                              bool psv, float dt, cudaStream_t s);
 cudaError_t launch_grouped_misfit(const JobDesc* jobs, const GroupOp* ops, int nops, cudaStream_t s);
 
 // ---- auxiliary kernels (fd_aux.cu) ----------------------------------------

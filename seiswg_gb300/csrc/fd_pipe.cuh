@@ -7,8 +7,9 @@
 //   DirectRows  plain 16-byte __ldg loads issued at the top of the iteration.
 //   BulkRows    a ring of S stages in shared memory filled by the TMA engine's
 //               bulk copy (cp.async.bulk ... mbarrier::complete_tx::bytes),
-//               issued S-1 iterations ahead, lane q copying segment q;
-//               completion is tracked by one mbarrier per stage.  Waits are bounded: after kWaitLimit
+//               issued S-1 iterations ahead by lane 0 or, for many
+//               segments, lane q copying segment q; completion is tracked by
+//               one mbarrier per stage.  Waits are bounded: after kWaitLimit
 //               polls the warp records an error in *err, drains the copies it
 //               issued (again bounded) and leaves its march.
 #pragma once
@@ -99,42 +100,54 @@ struct DirectRows {
   __device__ __forceinline__ void drain(int) {}
 };
 
-template <int NSEG, int S>
+template <int NSEG, int S, bool kLaneIssue = false>
 struct BulkRows {
-  static_assert(NSEG <= 32, "one lane issues each segment's copy");
+  static_assert(!kLaneIssue || NSEG <= 32, "one lane issues each segment's copy");
   static constexpr int kStages = S;
   static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
   static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
-  const float* src;  // lane q < NSEG: segment q's field at row 0, the warp's first column
-  int roff;          // lane q < NSEG: segment q's row offset
+  Segs<NSEG> s;      // serial issue: every segment's field
+  const float* src;  // lane issue, lane q < NSEG: segment q's field at row 0, the warp's first column
+  int roff;          // lane issue, lane q < NSEG: segment q's row offset
   size_t ld;
-  int ib, lane, nk, cur;
+  int col0, ib, lane, nk, cur;
   float* buf;      // [S][NSEG][128]
   uint64_t* bar;   // [S]
   __device__ BulkRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int lane_, float* buf_,
                       uint64_t* bar_, int nk_)
-      : src(nullptr), roff(0), ld(ld_), ib(ib_), lane(lane_), nk(nk_), cur(0), buf(buf_), bar(bar_) {
-    const int col0 = c0_ - 4 * lane_;  // the warp's first column (16-byte aligned)
+      : s(segs), src(nullptr), roff(0), ld(ld_), col0(c0_ - 4 * lane_), ib(ib_), lane(lane_), nk(nk_), cur(0),
+        buf(buf_), bar(bar_) {
+    if constexpr (kLaneIssue) {
 #pragma unroll
-    for (int q = 0; q < NSEG; ++q)
-      if (lane_ == q) {
-        src = segs.base[q] + col0;
-        roff = segs.roff[q];
-      }
+      for (int q = 0; q < NSEG; ++q)
+        if (lane_ == q) {
+          src = segs.base[q] + col0;
+          roff = segs.roff[q];
+        }
+    }
   }
 
-  // Lane 0 arms the stage's barrier with the stage's bytes; lanes 0..NSEG-1
-  // then copy one 512-byte segment each.  (A copy completing before the
-  // arrive would only take the transaction count below zero transiently,
-  // which the barrier allows; the warp issues the arrive first anyway.)
+  // Arms the stage's barrier with the stage's bytes and copies its NSEG
+  // 512-byte segments: all by lane 0 (serial issue), or segment q by lane q
+  // (lane issue; a copy completing before lane 0's arrive only takes the
+  // transaction count below zero transiently, which the barrier allows).
+  // Called by the issuing lanes only.
   __device__ __forceinline__ void issue(int k) {
     const int st = k % S;
     const int i = ib - 1 + k;
-    if (lane == 0) mbar_expect_tx(&bar[st], kStageBytes);
-    if (lane < NSEG)
+    if constexpr (kLaneIssue) {
+      if (lane == 0) mbar_expect_tx(&bar[st], kStageBytes);
       bulk_g2s(buf + (st * NSEG + lane) * kSegFloats, src + ptrdiff_t(i + roff) * ptrdiff_t(ld),
                kSegFloats * sizeof(float), &bar[st]);
+    } else {
+      mbar_expect_tx(&bar[st], kStageBytes);
+#pragma unroll
+      for (int q = 0; q < NSEG; ++q)
+        bulk_g2s(buf + (st * NSEG + q) * kSegFloats, s.base[q] + ptrdiff_t(i + s.roff[q]) * ptrdiff_t(ld) + col0,
+                 kSegFloats * sizeof(float), &bar[st]);
+    }
   }
+  __device__ __forceinline__ bool issuer() const { return kLaneIssue ? lane < NSEG : lane == 0; }
 
   // Barrier set-up and the first S-1 stages.
   __device__ __forceinline__ void start() {
@@ -143,14 +156,15 @@ struct BulkRows {
       fence_mbar_init();
     }
     __syncwarp();
-    for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
+    if (issuer())
+      for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
     __syncwarp();
   }
 
   // Refills the stage consumed in iteration k-1 with iteration k+S-1, then
   // waits for iteration k and reads the lane's float4 of every segment.
   __device__ __forceinline__ bool acquire(int k) {
-    if (k + S - 1 < nk) {
+    if (k + S - 1 < nk && issuer()) {
       fence_proxy_async();  // order the warp's reads of the old stage before the copy
       issue(k + S - 1);
     }

@@ -478,15 +478,6 @@ cudaError_t launch_psv(const PsvStep& p, cudaStream_t s) {
 // ---- grouped forward steps ----------------------------------------------------
 namespace {
 
-__device__ __forceinline__ int find_op(const GroupOp* __restrict__ ops, int nops, int gw) {
-  int lo = 0, hi = nops - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&ops[mid].warp_begin) <= gw) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
-
 __device__ __forceinline__ float* slot_field(const JobDesc& J, int slot, int f) {
   return J.pool + slot * J.slot_elems + f * J.field_elems + J.halo;
 }
@@ -498,7 +489,7 @@ __global__ void __launch_bounds__(kStepWarps * 32) grouped_forward_kernel(const 
                                                                           const GroupOp* __restrict__ ops, int nops) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const GroupOp op = ops[find_op(ops, nops, gw)];
+  const GroupOp op = ops[group_op_of(ops, nops, gw)];
   const JobDesc& J = jobs[op.job];
   const int lw = gw - op.warp_begin;
   if (lw >= J.g.nstrips * J.g.nchunks) return;

@@ -343,6 +343,35 @@ double waveform_misfit(const float* syn, const float* obs, int nrec, int nt, flo
   return std::sqrt(misfit);
 }
 
+namespace {
+
+// The grid read from the layout itself (k = i*nz + j, z fastest): nz is the
+// length of the first run of equal x, nx = npt / nz, and every run must
+// repeat the first run's z values at one x.  Returns false when the
+// coordinates do not form such a grid.
+bool grid_from_layout(const std::vector<float>& x, const std::vector<float>& z, GridInfo& g) {
+  const size_t npt = x.size();
+  size_t nz = 1;
+  while (nz < npt && x[nz] == x[0]) ++nz;
+  if (nz < 2 || npt % nz != 0 || npt / nz < 2) return false;
+  const size_t nx = npt / nz;
+  for (size_t i = 0; i < nx; ++i) {
+    const float xi = x[i * nz];
+    if (i > 0 && !(xi > x[(i - 1) * nz])) return false;
+    for (size_t j = 0; j < nz; ++j)
+      if (x[i * nz + j] != xi || z[i * nz + j] != z[j]) return false;
+  }
+  for (size_t j = 1; j < nz; ++j)
+    if (!(z[j] > z[j - 1])) return false;
+  g.nx = int(nx);
+  g.nz = int(nz);
+  g.dx = (x[(nx - 1) * nz] - x[0]) / float(nx - 1);
+  g.dz = (z[nz - 1] - z[0]) / float(nz - 1);
+  return true;
+}
+
+}  // namespace
+
 GridInfo infer_grid(const std::vector<float>& x, const std::vector<float>& z) {
   if (x.empty() || z.empty() || x.size() != z.size()) throw Error("coordinate files are empty or differ in size");
   auto extent = [](const std::vector<float>& v) {
@@ -352,16 +381,24 @@ GridInfo infer_grid(const std::vector<float>& x, const std::vector<float>& z) {
   };
   const float lx = extent(x), lz = extent(z);
   if (!(lx > 0.0f) || !(lz > 0.0f)) throw Error("coordinate extents must be positive");
+  // The reference's rule (solver.rs:646-656): nx, nz from npt and the extents'
+  // aspect ratio, which holds for square cells (dx == dz).
   const double npt = double(x.size());
   GridInfo g;
   g.nx = int(std::round(std::sqrt(npt * double(lx) / double(lz))));
   g.nz = int(std::round(std::sqrt(npt * double(lz) / double(lx))));
-  if (g.nx < 2 || g.nz < 2 || size_t(g.nx) * size_t(g.nz) != x.size())
-    throw Error("cannot infer a rectangular grid from the coordinates (nx=" + std::to_string(g.nx) +
-                ", nz=" + std::to_string(g.nz) + ", npt=" + std::to_string(x.size()) + ")");
-  g.dx = lx / float(g.nx - 1);
-  g.dz = lz / float(g.nz - 1);
-  return g;
+  GridInfo lay{};
+  const bool have_layout = grid_from_layout(x, z, lay);
+  if (g.nx >= 2 && g.nz >= 2 && size_t(g.nx) * size_t(g.nz) == x.size() && (!have_layout || lay.nz == g.nz)) {
+    g.dx = lx / float(g.nx - 1);
+    g.dz = lz / float(g.nz - 1);
+    return g;
+  }
+  // Rectangular cells (dx != dz), where the aspect-ratio rule cannot work:
+  // the grid read from the coordinate layout.
+  if (have_layout) return lay;
+  throw Error("cannot infer a rectangular grid from the coordinates (nx=" + std::to_string(g.nx) +
+              ", nz=" + std::to_string(g.nz) + ", npt=" + std::to_string(x.size()) + ")");
 }
 
 uint32_t grid_index(float coord, float step) {

@@ -154,3 +154,28 @@ def test_gradients_accumulate_over_shots_and_scale_linearly():
     sim.backward_op(2.0 * adj[0])
     assert rel_l2(sim.gradient("mu"), 2.0 * parts[0]) <= 1e-6
     sim.close()
+
+
+@pytest.mark.parametrize("phys", ["psv", "sh"])
+def test_device_misfit_matches_host_misfit(phys):
+    """misfit_op + backward_op_device (traces and adjoint source stay on the
+    GPU) against l2_misfit on downloaded traces + backward_op."""
+    vp, vs, rho, flags, src, rec = _problem(phys, seed=5)
+    obs = _observed(vp, vs, rho, flags, src, rec, 1)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    try:
+        J_host, _, g_host = _gpu_gradient(sim, flags, obs, 1, 0)
+        sim.set_observed(obs)
+        sim.gradient_clear()
+        sim.forward_op(1, 0)
+        J_dev = sim.misfit_op()
+        sim.backward_op_device()
+        g_dev = {p: sim.gradient(p) for p in ("lambda", "mu", "buoyancy")}
+        with pytest.raises(Exception):
+            sim.forward_op(1, 0)
+            sim.backward_op_device()   # no misfit_op since the last forward_op
+    finally:
+        sim.close()
+    assert abs(J_dev - J_host) <= 1e-12 * abs(J_host)
+    for p in ("lambda", "mu") if phys == "psv" else ("mu", "buoyancy"):
+        assert rel_l2(g_dev[p], g_host[p]) <= 1e-6, p

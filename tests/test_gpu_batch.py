@@ -82,3 +82,33 @@ def test_batch_matches_plain_path_and_replays():
     batch.close()
     for s in sims:
         s.close()
+
+
+def test_chunk_rows_and_autotune_leave_gradients_unchanged():
+    """The chunk rows only re-partition the same cell updates among warps:
+    gradients are bitwise equal for every setting, including after autotune."""
+    import seiswg_gb300 as sw
+
+    probs = _problems()[:3]
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    try:
+        batch.run()
+        ref = [batch.gradient(i, "mu") for i in range(len(probs))]
+        for lx in (16, 128, 0):
+            batch.set_option("chunk_rows", lx)
+            assert batch.info()["chunk_rows"] == lx
+            batch.run()
+            for i in range(len(probs)):
+                assert np.array_equal(batch.gradient(i, "mu"), ref[i]), (lx, i)
+        batch.set_option("autotune", 8)
+        assert batch.info()["chunk_rows"] in (0, 16, 32, 48, 64, 96, 128)
+        batch.run()
+        for i in range(len(probs)):
+            assert np.array_equal(batch.gradient(i, "mu"), ref[i]), ("autotune", i)
+        with pytest.raises(sw.SeiswgError):
+            batch.set_option("chunk_rows", 2)
+    finally:
+        batch.close()
+        for s in sims:
+            s.close()

@@ -86,3 +86,50 @@ def test_adjoint_example(tmp_path):
     assert int.from_bytes(hdr[:4], "little") == 201 * 201
     assert np.array_equal(np.frombuffer(hdr[4:], "<f4"), kmu)
     assert misfit > 0
+
+
+def test_rectangular_cells_through_the_host_api(tmp_path):
+    """dx != dz: the grid comes from the coordinate layout (the reference's
+    aspect-ratio rule needs square cells); traces match the oracle set up with
+    the same dx, dz and station rounding."""
+    import seiswg_gb300 as sw
+    from oracle import oracle as O
+    from tests.examples import write_bin
+
+    nx, nz, dx, dz, nt, dt = 90, 140, 10.0, 6.0, 500, 6.0e-4
+    rng = np.random.default_rng(7)
+    vp = (3000 * (1 + 0.03 * rng.standard_normal((nx, nz)))).astype(np.float32)
+    vs = (vp / np.sqrt(3)).astype(np.float32)
+    rho = np.full((nx, nz), 2400, np.float32)
+    d = tmp_path / "rect"
+    (d / "model").mkdir(parents=True)
+    x = np.repeat(np.arange(nx, dtype=np.float32) * np.float32(dx), nz)
+    z = np.tile(np.arange(nz, dtype=np.float32) * np.float32(dz), nx)
+    for n, a in (("x", x), ("z", z), ("vp", vp), ("vs", vs), ("rho", rho)):
+        write_bin(str(d / "model" / f"proc000000_{n}.bin"), a)
+    (d / "sources.dat").write_text("450.0 420.0 0 18.0 0.06 30.0 1e10\n")
+    st = [(100.0 + 70.0 * q, 30.0 + 5.0 * (q % 3)) for q in range(10)]
+    (d / "stations.dat").write_text("".join(f"{a} {b}\n" for a, b in st))
+    (d / "config.ini").write_text(
+        f"[workflow]\nmode = forward\n[solver]\nsh = yes\npsv = yes\nnt = {nt}\ndt = {dt}\nabs_left = yes\n"
+        "abs_right = yes\nabs_bottom = yes\nabs_top = yes\nabs_width = 12\n[path]\noutput = output\n"
+        "model_init = model\nsources = sources.dat\nstations = stations.dat\n")
+    with _solver(str(d / "config.ini")) as s:
+        assert (s.info()["nx"], s.info()["nz"]) == (nx, nz)
+        s.run_forward()
+    setup = O.Setup(nx, nz, nt, dx, dz, float(np.float32(dt)), sh=True, psv=True, abs_left=True, abs_right=True,
+                    abs_bottom=True, abs_top=True, abs_width=12)
+    src = O.source_params(O.parse_table((d / "sources.dat").read_text()))
+    sk = O.locate([r[0] for r in src], [r[1] for r in src], dx, dz, nz)
+    rk = O.locate([a for a, _ in st], [b for _, b in st], dx, dz, nz)
+    o = O.FD2DOracle(setup, sk, O.stf_table(src, nt, setup.dt, 32), rk, 32)
+    o.set_field("LAM", vp)
+    o.set_field("MU", vs)
+    o.set_field("RHO", rho)
+    o.init_model()
+    o.run_forward(-1)
+    for comp in ("x", "y", "z"):
+        ours = np.load(d / "output" / "traces" / f"u{comp}_000000.npy")
+        ref = o.obs(comp.upper())
+        assert rel_l2(ours, ref) <= L2_TOL, comp
+        assert max_rel(ours, ref) <= REL_TOL, comp

@@ -161,11 +161,20 @@ def test_infer_grid_matches_oracle():
     z = np.tile(np.arange(50, dtype=np.float32) * 7.0, 30)
     assert sw.infer_grid(x, z) == (30, 50, 7.0, 7.0)
     # The reference infers nx from the extents' aspect ratio, which assumes
-    # dx == dz; with dx != dz it gets nx*nz != npt.  That is an error here.
+    # dx == dz; with dx != dz it gets nx*nz != npt.  Rectangular cells are
+    # read from the coordinate layout instead.
     z3 = np.tile(np.arange(50, dtype=np.float32) * 3.0, 30)
     assert O.infer_grid(x, z3)[:2] == (46, 33)
+    assert sw.infer_grid(x, z3) == (30, 50, 7.0, 3.0)
+    # a coincidental nx*nz == npt under the aspect-ratio rule still defers to the layout
+    xs = np.repeat(np.arange(40, dtype=np.float32) * 10.0, 90)
+    zs = np.tile(np.arange(90, dtype=np.float32) * 1.0, 40)
+    nx_ref, nz_ref = O.infer_grid(xs, zs)[:2]
+    assert nx_ref * nz_ref != 3600 or (nx_ref, nz_ref) != (40, 90)
+    assert sw.infer_grid(xs, zs) == (40, 90, 10.0, 1.0)
+    # coordinates that form no grid: errors
     with pytest.raises(sw.SeiswgError) as e:
-        sw.infer_grid(x, z3)
+        sw.infer_grid(x, np.random.default_rng(0).random(x.size).astype(np.float32) * 100)
     assert "rectangular grid" in str(e.value)
     with pytest.raises(sw.SeiswgError):
         sw.infer_grid(np.zeros(10, np.float32), np.zeros(10, np.float32))
