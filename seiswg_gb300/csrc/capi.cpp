@@ -60,7 +60,7 @@ int guarded(F&& f) {
               m.rfind("Cannot create", 0) == 0 || m.rfind("Cannot write", 0) == 0 ||
               m.rfind("Cannot load", 0) == 0;
     return fail(io ? SEISWG_EIO : SEISWG_EINVAL, m);
-  } catch (const std::invalid_argument& e) {
+  } catch (const std::logic_error& e) {  // invalid arguments and out-of-order calls
     return fail(SEISWG_EINVAL, e.what());
   } catch (const std::bad_alloc&) {
     return fail(SEISWG_EINTERNAL, "host out of memory");
