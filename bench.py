@@ -268,6 +268,11 @@ def run_ours(args, rank, world):
                  abs_bottom=True, abs_top=True, abs_width=W["w"], abs_alpha=W["alpha"])
     if args.chunk_rows:
         sim.set_option("chunk_rows", args.chunk_rows)
+    if args.two_step >= 0:
+        sim.set_option("two_step", args.two_step)
+    if args.two_step_rows:
+        sim.set_option("two_step_rows", args.two_step_rows)
+    two_step = args.two_step != 0   # the engine's default for PSV alone is on
     sim.upload_model("vp", W["vp"])
     sim.upload_model("vs", W["vs"])
     sim.upload_model("rho", W["rho"])
@@ -305,13 +310,19 @@ def run_ours(args, rank, world):
     cells = float(nx) * nz * nt
     ms_per_step = ms / args.steps
     value = world * cells * args.steps / (ms / 1e3) / 1e9
-    # Dominant kernel: one psv step launch per time step; its average duration
-    # is the timed region over nt launches (memsets and the trace kernel are
-    # < 0.1 % of it; see the launch list under profiles/).
-    launch_s = ms_per_step / 1e3 / nt
-    achieved = BYTES_PER_CELL["psv"] * nx * nz / launch_s / 1e9
+    # Dominant kernel: one launch per time step (one-step kernel) or per two
+    # steps (two-step kernel, nt even and no snapshots here); its average
+    # duration is the timed region over its launches (memsets and the trace
+    # kernel are < 0.1 % of it; see the launch lists under profiles/).
+    # Algorithmic bytes: 52 B per cell-update, the one-step scheme's minimum;
+    # the two-step kernel moves about half of that (traffic), so its fraction
+    # can exceed 1.
+    kernel = "psv_step2_kernel" if two_step else "psv_step_kernel"
+    per_launch = 2 if two_step else 1
+    launch_s = ms_per_step / 1e3 / (nt / per_launch)
+    achieved = BYTES_PER_CELL["psv"] * per_launch * nx * nz / launch_s / 1e9
     peak, peak_kind = _peaks()
-    traffic = _traffic("psv_step_kernel", nx, nz)
+    traffic = _traffic(kernel, nx, nz)
 
     # ---- end to end through the reference-facing C ABI ---------------------
     e2e = None
@@ -336,8 +347,8 @@ def run_ours(args, rank, world):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(W, nt),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "psv_step_kernel", "bytes_per_cell_update": BYTES_PER_CELL["psv"],
-                         "peak_source": peak_kind},
+                         "kernel": kernel, "bytes_per_cell_update": BYTES_PER_CELL["psv"],
+                         "cell_updates_per_launch": per_launch * nx * nz, "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "traces_finite": finite,
@@ -598,6 +609,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="empirical loader/chunk tuning before timing")
+    ap.add_argument("--two-step", type=int, default=-1,
+                    help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
+    ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default) is the headline; the others print their own line")

@@ -166,7 +166,11 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
 /* Options: "graphs" (0/1), "chunk_rows" (rows per warp march; 0: the
  * occupancy model), "loader" (0: plain loads, 1: TMA bulk-copy row pipeline,
  * the default), "autotune" (value = steps timed per candidate: picks the
- * fastest loader and chunk rows for this problem). */
+ * fastest loader and chunk rows for this problem), "two_step" (0/1: forward
+ * runs advance two time steps per launch; PSV without SH or spin only, and
+ * on by default there;
+ * multiply-add contraction, so results match the one-step kernel to rounding), "two_step_rows" (rows
+ * per march of the two-step kernel; 0: its occupancy model). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */

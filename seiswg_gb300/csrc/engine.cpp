@@ -40,9 +40,6 @@ void* Arena::take(size_t bytes) {
 // ---------------------------------------------------------------------------
 // Sim
 // ---------------------------------------------------------------------------
-namespace {
-int round_up(int x, int m) { return (x + m - 1) / m * m; }
-}  // namespace
 
 Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   if (d.nx < 5 || d.nz < 5) throw std::invalid_argument("grid must be at least 5 x 5");
@@ -54,7 +51,7 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
     own_stream_ = true;
   }
   // A warp strip reads columns [j0-4, j0+124) with j0 <= nz-117 (fd_common.cuh).
-  ld_ = round_up(std::max(128, d.nz + 12), 32);
+  ld_ = field_pitch(d.nz);
   const size_t rows_alloc = size_t(d.nx) + 2 * kHaloRows;
   field_elems_ = rows_alloc * size_t(ld_);
   const size_t fb = field_elems_ * sizeof(float);
@@ -99,6 +96,8 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   den_z_ = 8.0f * d.dz;
   geom_.loader = kLoaderBulk;
   set_chunk_rows(model_chunk_rows());
+  // PSV alone runs its forward passes two steps per launch by default.
+  if (d.psv && !d.sh && !d.spin) set_two_step(true);
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
   use_graphs_ = (size_t(d.nx) * d.nz <= (size_t(1) << 20));
@@ -138,30 +137,82 @@ void Sim::set_chunk_rows(int lx) {
   graphs_.clear();
 }
 
-int Sim::chunk_rows_for(int per_sm) const {
+int Sim::chunk_rows_for(int per_sm, int strip_cols, int extra_rows) const {
   int dev = 0, nsm = 0;
   SW_CUDA(cudaGetDevice(&dev));
   SW_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   if (per_sm < 1) per_sm = 1;
   const long resident = long(per_sm) * nsm * kStepWarps;
-  const int nstrips = (d_.nz + kStripCols - 1) / kStripCols;
+  const int nstrips = (d_.nz + strip_cols - 1) / strip_cols;
   int best = 64;
   double best_cost = 1e300;
   for (int lx = 8; lx <= 256; ++lx) {
     const long warps = long(nstrips) * ((d_.nx + lx - 1) / lx);
     const long waves = (warps + resident - 1) / resident;
-    const double cost = double(waves) * double(std::min(lx, d_.nx) + 5);
+    const double cost = double(waves) * double(std::min(lx, d_.nx) + extra_rows);
     if (cost < best_cost - 1e-9) { best_cost = cost; best = lx; }
   }
   return best;
 }
 
+void Sim::set_two_step(bool on) {
+  if (on && !(d_.psv && !d_.sh && !d_.spin)) throw std::invalid_argument("the two-step kernel is PSV only (no SH, no spin)");
+  if (on && geom2_.lx == 0) set_two_step_rows(0);
+  two_step_ = on;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+void Sim::set_two_step_rows(int lx) {
+  geom2_ = geom_;
+  geom2_.nstrips = (d_.nz + kStripCols2 - 1) / kStripCols2;
+  geom2_.lx = lx > 0 ? std::max(lx, 4) : chunk_rows_for(step2_blocks_per_sm(), kStripCols2, 11);
+  geom2_.nchunks = (d_.nx + geom2_.lx - 1) / geom2_.lx;
+  geom2_.loader = kLoaderBulk;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+int Sim::final_buffer(int every) const {
+  int b = 0;
+  for (int it = 0; it < d_.nt;) {
+    const bool snap_between = every > 0 && it > 0 && it % every == 0;
+    const int n = (two_step_ && it + 1 < d_.nt && !snap_between) ? 2 : 1;
+    b ^= 1;
+    it += n;
+  }
+  return b;
+}
+
+void Sim::enqueue_step2(int it, int b, const InjectList& inj_in, const ProbeList& probes_in) {
+  const State& a = st_[b];
+  const State& o = st_[1 - b];
+  PsvStep p{};
+  p.g = geom2_;
+  p.vx0 = a.vx; p.vz0 = a.vz; p.sxx0 = a.sxx; p.szz0 = a.szz; p.sxz0 = a.sxz;
+  p.vx1 = o.vx; p.vz1 = o.vz; p.sxx1 = o.sxx; p.szz1 = o.szz; p.sxz1 = o.sxz;
+  p.rho = rho_; p.lam = lam_; p.mu = mu_;
+  p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+  p.inj = inj_in;
+  p.inj.it = it;
+  p.probes = probes_in;
+  p.probes.it = it;
+  p.err = err_;
+  if (probes_in.n) {
+    p.probes.list = probes_ + probe_split_;
+    p.probes.n = nprobe_ - probe_split_;
+  }
+  SW_CUDA(launch_psv_step2(p, stream_));
+  ++launches_;
+}
+
 int Sim::model_chunk_rows() const {
-  return chunk_rows_for(step_blocks_per_sm(d_.psv, d_.psv && d_.spin, geom_.loader));
+  return chunk_rows_for(step_blocks_per_sm(d_.psv, d_.psv && d_.spin, geom_.loader), kStripCols, 5);
 }
 
 Geom Sim::adjoint_geom() {
-  if (adj_lx_[geom_.loader] == 0) adj_lx_[geom_.loader] = chunk_rows_for(adjoint_blocks_per_sm(d_.psv, geom_.loader));
+  if (adj_lx_[geom_.loader] == 0)
+    adj_lx_[geom_.loader] = chunk_rows_for(adjoint_blocks_per_sm(d_.psv, geom_.loader), kStripCols, 5);
   Geom g = geom_;
   g.lx = adj_lx_[geom_.loader];
   g.nchunks = (d_.nx + g.lx - 1) / g.lx;
@@ -591,21 +642,35 @@ void Sim::run_forward(int isrc, Snapshots* snaps) {
   std::string key = "fwd/" + std::to_string(inj.n) + "/" + std::to_string(every);
   for (StateField f : (snaps ? snaps->fields : std::vector<StateField>{})) key += "/" + std::to_string(int(f));
   const size_t fbytes = field_elems_ * sizeof(float);
+  if (two_step_) key += "/2";
   run_loop(key, [&] {
     size_t q = 0;
-    for (int it = 0; it < d_.nt; ++it) {
-      enqueue_step(it, it & 1, inj, pl, false);
-      if (every > 0 && it > 0 && it % every == 0) {
-        for (StateField f : snaps->fields) {
-          const float* src = state_ptr(f, (it + 1) & 1) - size_t(kHaloRows) * ld_ - kHaloCols;
-          SW_CUDA(cudaMemcpyAsync(snap_store_ + q * field_elems_, src, fbytes, cudaMemcpyDeviceToDevice, stream_));
-          ++q;
-        }
+    int b = 0;  // buffer holding the state before step it
+    auto snap = [&](int it) {  // the state after step it, if a snapshot is due
+      if (!(every > 0 && it > 0 && it % every == 0)) return;
+      for (StateField f : snaps->fields) {
+        const float* src = state_ptr(f, b) - size_t(kHaloRows) * ld_ - kHaloCols;
+        SW_CUDA(cudaMemcpyAsync(snap_store_ + q * field_elems_, src, fbytes, cudaMemcpyDeviceToDevice, stream_));
+        ++q;
+      }
+    };
+    for (int it = 0; it < d_.nt;) {
+      const bool snap_between = every > 0 && it > 0 && it % every == 0;
+      if (two_step_ && it + 1 < d_.nt && !snap_between) {
+        enqueue_step2(it, b, inj, pl);
+        b ^= 1;
+        snap(it + 1);
+        it += 2;
+      } else {
+        enqueue_step(it, b, inj, pl, false);
+        b ^= 1;
+        snap(it);
+        ++it;
       }
     }
     enqueue_traces();
   });
-  cur_buf_ = d_.nt & 1;
+  cur_buf_ = final_buffer(every);
   if (snaps) {
     snaps->steps = snap_steps;
     snaps->frames.assign(need, std::vector<float>());

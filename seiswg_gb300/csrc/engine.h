@@ -166,6 +166,13 @@ class Sim {
   // best time per step in microseconds.
   double autotune(int steps);
   void set_loader(int loader);  // kLoaderDirect or kLoaderBulk
+  // Forward runs advance two steps per launch (PSV without SH or spin, the
+  // default there; steps before a snapshot and an odd last step run the
+  // one-step kernel).  Rows per chunk of that kernel: 0 = its own
+  // wave-quantisation model.
+  void set_two_step(bool on);
+  void set_two_step_rows(int lx);
+  bool two_step() const { return two_step_; }
   int loader() const { return geom_.loader; }
   // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
   void check_device_error() const;
@@ -198,7 +205,9 @@ class Sim {
   void upload_inject(const std::vector<Inject>& list, int which);
   void run_loop(const std::string& key, const std::function<void()>& body);
   void copy_field_to_host(const float* dev, float* host) const;
-  int chunk_rows_for(int blocks_per_sm) const;
+  int chunk_rows_for(int blocks_per_sm, int strip_cols, int extra_rows) const;
+  void enqueue_step2(int it, int b, const InjectList& inj, const ProbeList& probes);
+  int final_buffer(int snap_every) const;  // buffer holding the state after run_forward
 
   SimDesc d_;
   cudaStream_t stream_;
@@ -206,6 +215,8 @@ class Sim {
   int ld_ = 0;
   size_t field_elems_ = 0;  // rows_alloc * ld
   Geom geom_{};
+  Geom geom2_{};            // decomposition of the two-step kernel (lx 0: not yet modelled)
+  bool two_step_ = false;
   int adj_lx_[2] = {0, 0};  // reverse-step rows per chunk, per loader (0: not yet modelled)
   Arena arena_;
   State st_[2];

@@ -59,6 +59,12 @@ size_t step_smem_bytes(bool psv, bool spin, int loader);
 int step_blocks_per_sm(bool psv, bool spin, int loader);
 cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s);
 cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s);
+// Two PSV steps (inj.it and inj.it + 1; no spin) from the *0 state to the *1
+// state.  p.g describes the two-step decomposition: nstrips over
+// kStripCols2-column strips, lx / nchunks its own chunk rows.
+cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s);
+size_t step2_smem_bytes();
+int step2_blocks_per_sm();
 
 // ---- exact discrete adjoint (fd_adjoint.cu) --------------------------------
 struct PsvAdjoint {

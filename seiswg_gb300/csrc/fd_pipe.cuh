@@ -100,9 +100,14 @@ struct DirectRows {
   __device__ __forceinline__ void drain(int) {}
 };
 
-template <int NSEG, int S, bool kLaneIssue = false>
+// KEEP: the stages of the last KEEP iterations stay readable (seg_back), so a
+// stage is refilled KEEP iterations later and S-1-KEEP iterations are in
+// flight.
+template <int NSEG, int S, bool kLaneIssue = false, int KEEP = 0>
 struct BulkRows {
   static_assert(!kLaneIssue || NSEG <= 32, "one lane issues each segment's copy");
+  static_assert(S - 1 - KEEP >= 1, "at least one stage in flight");
+  static constexpr int kAhead = S - 1 - KEEP;
   static constexpr int kStages = S;
   static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
   static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
@@ -157,19 +162,29 @@ struct BulkRows {
     }
     __syncwarp();
     if (issuer())
-      for (int k = 0; k < S - 1 && k < nk; ++k) issue(k);
+      for (int k = 0; k < kAhead && k < nk; ++k) issue(k);
     __syncwarp();
   }
 
-  // Refills the stage consumed in iteration k-1 with iteration k+S-1, then
-  // waits for iteration k and reads the lane's float4 of every segment.
+  // Refills the stage consumed in iteration k-1-KEEP with iteration
+  // k+kAhead, then waits for iteration k and reads the lane's float4 of every
+  // segment.
   __device__ __forceinline__ bool acquire(int k) {
-    if (k + S - 1 < nk && issuer()) {
+    if (KEEP > 0) __syncwarp();  // the previous iteration's seg_back reads are done
+    if (k + kAhead < nk && issuer()) {
       fence_proxy_async();  // order the warp's reads of the old stage before the copy
-      issue(k + S - 1);
+      issue(k + kAhead);
     }
     cur = k % S;
     return __all_sync(kFull, mbar_wait(&bar[cur], uint32_t(k / S) & 1u));
+  }
+  // Segment q of the stage of iteration (current - d), 1 <= d <= KEEP.
+  __device__ __forceinline__ f4 seg_back(int q, int d) const {
+    const int st = (cur + S - d) % S;
+    const float4 t = *reinterpret_cast<const float4*>(buf + (st * NSEG + q) * kSegFloats + 4 * lane);
+    f4 r;
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    return r;
   }
   // The lane's float4 of segment q of the acquired stage.
   __device__ __forceinline__ f4 seg(int q) const {
@@ -183,7 +198,7 @@ struct BulkRows {
   // After a failed wait at iteration k: wait (bounded) for the copies still
   // in flight so that none lands after the warp has left.
   __device__ __forceinline__ void drain(int k) {
-    for (int kk = k; kk < k + S && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
+    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
     __syncwarp();
   }
 };

@@ -23,115 +23,11 @@
 // (built with -fmad=false), except that divisions by 8*dx, rho and J are
 // multiplies by precomputed reciprocals; results track the FP32 reference to
 // rounding (relative L2 ~1e-7 over thousands of steps).
-#include "fd_kernels.h"
-#include "fd_pipe.cuh"
+#include "fd_march.cuh"
 
 namespace seiswg {
 
-namespace {
 
-struct March {
-  int lane, warp, strip, chunk, ib, ie;
-  bool active;
-};
-
-__device__ __forceinline__ March march_of(const Geom& g, int gw) {
-  March m;
-  m.lane = threadIdx.x & 31;
-  m.warp = threadIdx.x >> 5;
-  m.strip = gw % g.nstrips;
-  m.chunk = gw / g.nstrips;
-  m.active = m.chunk < g.nchunks;
-  m.ib = m.chunk * g.lx;
-  m.ie = min(g.nx, m.ib + g.lx);
-  return m;
-}
-
-// Adds the injections of row i (sources, or adjoint sources at receivers) to
-// the lane's divergence values.  `ci` is the list cursor, advanced past row i.
-// Element e of an f4 is selected with unrolled compares: a runtime index
-// into a register array would move the whole array to local memory.
-template <bool X, bool Y, bool Z>
-__device__ __forceinline__ void inject_row(const InjectList& inj, int i, int c0, int& ci, f4& ds_x, f4& ds_y,
-                                           f4& ds_z) {
-  while (ci < inj.n && __ldg(&inj.list[ci].i) == i) {
-    const int e = __ldg(&inj.list[ci].j) - c0;
-    if (e >= 0 && e < 4) {
-      const size_t o = size_t(__ldg(&inj.list[ci].row)) * inj.nt + inj.it;
-      const float ax = X ? __ldg(&inj.val_x[o]) : 0.0f;
-      const float ay = Y ? __ldg(&inj.val_y[o]) : 0.0f;
-      const float az = Z ? __ldg(&inj.val_z[o]) : 0.0f;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        if (q == e) {
-          if (X) ds_x.v[q] += ax;
-          if (Y) ds_y.v[q] += ay;
-          if (Z) ds_z.v[q] += az;
-        }
-      }
-    }
-    ++ci;
-  }
-}
-
-__device__ __forceinline__ float pick4(const f4& a, int e) {
-  float r = a.v[0];
-#pragma unroll
-  for (int q = 1; q < 4; ++q) r = (q == e) ? a.v[q] : r;
-  return r;
-}
-
-// Integrates the displacement of the owned probes of row i and records it.
-template <typename Pick>
-__device__ __forceinline__ void probe_row(const ProbeList& pr, int i, const LaneCols& L, int& pi, float dt,
-                                          Pick pick) {
-  while (pi < pr.n && __ldg(&pr.list[pi].i) == i) {
-    int j = __ldg(&pr.list[pi].j);
-    int e = j - L.c0;
-    if (e >= 0 && e < 4 && (L.own & (1 << e))) {
-      int idx = __ldg(&pr.list[pi].idx);
-      float v = pick(__ldg(&pr.list[pi].comp), e);
-      float u = pr.acc[idx] + v * dt;  // af(F_U*, k, v * dt), fd2d.wgsl:270
-      pr.acc[idx] = u;
-      pr.hist[size_t(idx) * pr.nt + pr.it] = u;
-    }
-    ++pi;
-  }
-}
-
-__device__ __forceinline__ void flag_timeout(int* err) {
-  if ((threadIdx.x & 31) == 0 && err) atomicOr(err, kErrWaitTimeout);
-}
-
-template <int NSEG>
-struct DirectL : DirectRows<NSEG> {
-  using SegsT = Segs<NSEG>;
-  static constexpr uint32_t kStageBytes = 0;
-  using DirectRows<NSEG>::DirectRows;
-};
-
-template <int NSEG>
-struct BulkL : BulkRows<NSEG, kPipeStages> {
-  using SegsT = Segs<NSEG>;
-  using BulkRows<NSEG, kPipeStages>::BulkRows;
-};
-
-// Per-warp slices of the CTA's dynamic shared memory: [warps][S][NSEG][128]
-// floats, then [warps][S] mbarriers.
-template <class Loader>
-__device__ __forceinline__ Loader make_loader(const typename Loader::SegsT& segs, const Geom& g, const March& m,
-                                              const LaneCols& L, unsigned char* smem) {
-  float* buf = nullptr;
-  uint64_t* bar = nullptr;
-  if (Loader::kStages > 0) {
-    const size_t per = size_t(Loader::kStages) * Loader::kStageBytes;
-    buf = reinterpret_cast<float*>(smem + per * m.warp);
-    bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
-  }
-  return Loader(segs, size_t(g.ld), L.c0, m.ib, m.lane, buf, bar, m.ie - m.ib + 3);
-}
-
-}  // namespace
 
 // --------------------------------------------------------------------------
 // SH: state vy, sxy, szy; material 1/rho, mu.  fd2d.wgsl:242-301.
@@ -165,8 +61,8 @@ __device__ __forceinline__ void sh_march(const ShStep& p, int gw, unsigned char*
   f4 xy0 = ld4(at(p.sxy0, m.ib - 3)), xy1 = ld4(at(p.sxy0, m.ib - 2)), xy2 = ld4(at(p.sxy0, m.ib - 1)), xy3;
   f4 zy0 = ld4(at(p.szy0, m.ib - 3)), zy1 = ld4(at(p.szy0, m.ib - 2)), zy2 = ld4(at(p.szy0, m.ib - 1)), zy3;
   f4 va, vb, vc, vd;
-  int ci = lower_row(p.inj.list, p.inj.n, m.ib - 1);
-  int pi = lower_row(p.probes.list, p.probes.n, m.ib);
+  Cursor ci = cursor_at(p.inj.list, p.inj.n, m.ib - 1);
+  Cursor pi = cursor_at(p.probes.list, p.probes.n, m.ib);
   const int nk = m.ie - m.ib + 3;
 
   for (int k = 0; k < nk; ++k) {
@@ -190,7 +86,7 @@ __device__ __forceinline__ void sh_march(const ShStep& p, int gw, unsigned char*
     const f4 dz = dz_back(zy2, g.rdz, L.zb);
 #pragma unroll
     for (int e = 0; e < 4; ++e) ds.v[e] = ds.v[e] + dz.v[e];
-    inject_row<false, true, false>(p.inj, i, c0, ci, ds, ds, ds);  // stf_dsy / adj_dsy
+    inject_at<false, true, false>(p.inj, i, c0, ci, ds, ds, ds);  // stf_dsy / adj_dsy
 
     // add_vy (fd2d.wgsl:268): vy = b * (vy + dt * DSY / rho), with the
     // buoyancy 1/rho stored in place of rho.
@@ -201,7 +97,7 @@ __device__ __forceinline__ void sh_march(const ShStep& p, int gw, unsigned char*
     }
     if (i >= m.ib && i < m.ie) {
       st4_masked(at(p.vy1, i), vd, L.own);
-      if (p.probes.n) probe_row(p.probes, i, L, pi, dt, [&](int, int e) { return pick4(vd, e); });
+      probe_at(p.probes, i, L, pi, dt, [&](int, int e) { return pick4(vd, e); });
     }
 
     // Stress of row r = i-2 from new vy rows r-1..r+2 = (va, vb, vc, vd).
@@ -282,8 +178,8 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
   f4 xa, xb_, xc, xd;   // new vx rows i-3..i
   f4 za, zb_, zc, zd;   // new vz rows i-3..i
   f4 ya, yb, yc, yd;    // new vy_c rows i-3..i
-  int ci = lower_row(p.inj.list, p.inj.n, m.ib - 1);
-  int pi = lower_row(p.probes.list, p.probes.n, m.ib);
+  Cursor ci = cursor_at(p.inj.list, p.inj.n, m.ib - 1);
+  Cursor pi = cursor_at(p.probes.list, p.probes.n, m.ib);
   const int nk = m.ie - m.ib + 3;
 
   for (int k = 0; k < nk; ++k) {
@@ -339,7 +235,7 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
         dsy.v[e] += 2.0f * yy2.v[e];
       }
     }
-    inject_row<true, false, true>(p.inj, i, c0, ci, dsx, dsx, dsz);  // stf_dsxz, fd2d.wgsl:350-351
+    inject_at<true, false, true>(p.inj, i, c0, ci, dsx, dsx, dsz);  // stf_dsxz, fd2d.wgsl:350-351
 
     // add_vxz (fd2d.wgsl:362-363), rho holding 1/rho
 #pragma unroll
@@ -360,12 +256,11 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
       st4_masked(at(p.vx1, i), xd, L.own);
       st4_masked(at(p.vz1, i), zd, L.own);
       if constexpr (SPIN) st4_masked(at(p.vyc1, i), yd, L.own);
-      if (p.probes.n)
-        probe_row(p.probes, i, L, pi, dt, [&](int comp, int e) {
-          if constexpr (SPIN)
-            return comp == kProbeVX ? pick4(xd, e) : comp == kProbeVZ ? pick4(zd, e) : pick4(yd, e);
-          return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e);
-        });
+      probe_at(p.probes, i, L, pi, dt, [&](int comp, int e) {
+        if constexpr (SPIN)
+          return comp == kProbeVX ? pick4(xd, e) : comp == kProbeVZ ? pick4(zd, e) : pick4(yd, e);
+        return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e);
+      });
     }
 
     // Stress of row r = i-2.
@@ -432,29 +327,11 @@ __global__ void __launch_bounds__(kStepWarps * 32) psv_step_kernel(const PsvStep
   psv_march<SPIN, Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
 }
 
+
 // --------------------------------------------------------------------------
 // Launchers
 // --------------------------------------------------------------------------
 namespace {
-
-unsigned blocks_for(const Geom& g) {
-  long warps = long(g.nstrips) * g.nchunks;
-  return unsigned((warps + kStepWarps - 1) / kStepWarps);
-}
-
-template <class L>
-size_t smem_for() {
-  return L::kStages ? size_t(kStepWarps) * L::smem_bytes_per_warp() : 0;
-}
-
-template <typename K>
-cudaError_t prepare_kernel(K kernel, size_t smem) {
-  // Opt in to more than 48 KB of dynamic shared memory.
-  if (smem > 48 * 1024)
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  return cudaSuccess;
-}
-
 template <class L>
 cudaError_t launch_sh(const ShStep& p, cudaStream_t s) {
   const size_t smem = smem_for<L>();

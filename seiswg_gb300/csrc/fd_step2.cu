@@ -1,0 +1,336 @@
+// fd_step2.cu -- two PSV time steps per launch (temporal blocking).
+//
+// Built with multiply-add contraction (the one-step kernels keep the
+// reference's separate multiply and add): the two-step march is bound by
+// instruction issue, not by HBM.
+#include "fd_march.cuh"
+
+namespace seiswg {
+
+namespace {
+
+// --------------------------------------------------------------------------
+// PSV, two time steps per pass (temporal blocking).
+//
+// Level 1 is the one-step march above (velocity of row i, stress of row i-2,
+// step `it`); its new rows stay in registers and feed level 2, which runs the
+// same update for step it+1 three rows behind (velocity of row i-3, stress of
+// row i-5).  Only level-2 rows are written: per two steps each state field is
+// read and written once and each material field read twice (once per level,
+// the second time from L2), 26 B of HBM traffic per cell-update instead of 52.
+//
+// Reach: two steps need level-1 values 3 columns and 4 rows beyond the
+// level-2 outputs, so a strip owns 112 columns (lanes 2..29) and a chunk of
+// rows [ib, ie) marches i over [ib-4, ie+4].  Level-1 values outside the grid
+// are forced to zero, as a one-step launch leaves the halo of its output.
+// Each arithmetic expression is the one-step kernel's; with multiply-add
+// contraction the results differ from two one-step launches by rounding only.
+// --------------------------------------------------------------------------
+enum Psv2Seg {
+  P2_SXX = 0, P2_SXZ, P2_SZZ,  // sigma^n, row i+1
+  P2_VX, P2_VZ,                // v^n, row i
+  P2_RHO, P2_LAM, P2_MU,       // 1/rho row i, lambda/mu row i-2
+  P2_NSEG
+};
+
+// Six stages per warp: two rows in flight and the stages of the last three
+// iterations kept, whose 1/rho (row i-3) and lambda/mu (row i-5) are the
+// material of level 2.
+struct Bulk2 : BulkRows<P2_NSEG, 6, false, 3> {
+  using SegsT = Segs<P2_NSEG>;
+  using BulkRows<P2_NSEG, 6, false, 3>::BulkRows;
+};
+
+__device__ __forceinline__ LaneCols lane_cols2(const Geom& g, int strip, int lane, int& valid) {
+  LaneCols L;
+  const int own_lo = strip * kStripCols2;
+  int j0 = own_lo;
+  if (j0 + kStripCols2 > g.nz) j0 = g.nz > kStripCols2 ? ((g.nz - kStripCols2 + 3) & ~3) : 0;
+  const int own_hi = min(g.nz, own_lo + kStripCols2);
+  L.c0 = j0 - 8 + 4 * lane;
+  L.own_lo = own_lo;
+  L.own_hi = own_hi;
+  L.zb = L.zf = L.own = 0;
+  valid = 0;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int c = L.c0 + e;
+    if (c >= 2 && c < g.nz - 2) L.zb |= 1 << e;
+    if (c >= 1 && c < g.nz - 2) L.zf |= 1 << e;
+    if (c >= 0 && c < g.nz) valid |= 1 << e;
+    if (lane >= 2 && lane <= 29 && c >= own_lo && c < own_hi) L.own |= 1 << e;
+  }
+  return L;
+}
+
+// Masked differences with the mask folded into the reciprocal: r = 0 where
+// the edge rule zeroes the derivative (fd4 of finite samples times 0).
+__device__ __forceinline__ f4 dx4r(const f4& r0, const f4& r1, const f4& r2, const f4& r3, float r) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = fd4(r0.v[e], r1.v[e], r2.v[e], r3.v[e], r);
+  return o;
+}
+
+__device__ __forceinline__ f4 dz_back_r(const f4& m, const f4& r) {
+  const float pz = __shfl_up_sync(kFull, m.v[2], 1);
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float nx = __shfl_down_sync(kFull, m.v[0], 1);
+  f4 o;
+  o.v[0] = fd4(pz, pw, m.v[0], m.v[1], r.v[0]);
+  o.v[1] = fd4(pw, m.v[0], m.v[1], m.v[2], r.v[1]);
+  o.v[2] = fd4(m.v[0], m.v[1], m.v[2], m.v[3], r.v[2]);
+  o.v[3] = fd4(m.v[1], m.v[2], m.v[3], nx, r.v[3]);
+  return o;
+}
+
+__device__ __forceinline__ f4 dz_fwd_r(const f4& m, const f4& r) {
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float n0 = __shfl_down_sync(kFull, m.v[0], 1);
+  const float n1 = __shfl_down_sync(kFull, m.v[1], 1);
+  f4 o;
+  o.v[0] = fd4(pw, m.v[0], m.v[1], m.v[2], r.v[0]);
+  o.v[1] = fd4(m.v[0], m.v[1], m.v[2], m.v[3], r.v[1]);
+  o.v[2] = fd4(m.v[1], m.v[2], m.v[3], n0, r.v[2]);
+  o.v[3] = fd4(m.v[2], m.v[3], n0, n1, r.v[3]);
+  return o;
+}
+
+// Zero outside the grid: the whole row when it is not a grid row, else the
+// lane's columns outside [0, nz).
+__device__ __forceinline__ f4 in_grid(const f4& a, bool row_ok, int valid) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = (row_ok && (valid & (1 << e))) ? a.v[e] : 0.0f;
+  return o;
+}
+
+// EDGE: derivatives masked by index and level-1 values outside the grid
+// zeroed.  (A second, test-free instantiation for interior warps executed 17 %
+// fewer instructions but ran 8 % slower: two bodies of this size no longer
+// fit the instruction cache.)
+template <class Loader, bool EDGE>
+__device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, const LaneCols& L, int valid,
+                                          unsigned char* smem) {
+  const Geom& g = p.g;
+  const size_t ld = size_t(g.ld);
+  const float dt = g.dt;
+  const int c0 = L.c0;
+  const int nx = g.nx;
+  auto at = [&](auto* base, int i) { return base + ptrdiff_t(i) * ptrdiff_t(ld) + c0; };
+
+  typename Loader::SegsT segs;
+  segs.base[P2_SXX] = p.sxx0; segs.roff[P2_SXX] = 1;
+  segs.base[P2_SXZ] = p.sxz0; segs.roff[P2_SXZ] = 1;
+  segs.base[P2_SZZ] = p.szz0; segs.roff[P2_SZZ] = 1;
+  segs.base[P2_VX] = p.vx0; segs.roff[P2_VX] = 0;
+  segs.base[P2_VZ] = p.vz0; segs.roff[P2_VZ] = 0;
+  segs.base[P2_RHO] = p.rho; segs.roff[P2_RHO] = 0;
+  segs.base[P2_LAM] = p.lam; segs.roff[P2_LAM] = -2;
+  segs.base[P2_MU] = p.mu; segs.roff[P2_MU] = -2;
+  const int i0 = m.ib - 4;                 // first level-1 row
+  const int nk = (m.ie - m.ib) + 9;        // level-1 rows [ib-4, ie+4]
+  float* buf = nullptr;
+  uint64_t* bar = nullptr;
+  if (Loader::kStages > 0) {
+    const size_t per = size_t(Loader::kStages) * Loader::kStageBytes;
+    buf = reinterpret_cast<float*>(smem + per * m.warp);
+    bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
+  }
+  Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
+  rows.start();
+
+  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  // sigma^n rings, rows i-2..i+1
+  f4 xx0 = ld4(at(p.sxx0, i0 - 2)), xx1 = ld4(at(p.sxx0, i0 - 1)), xx2 = ld4(at(p.sxx0, i0)), xx3;
+  f4 xz0 = ld4(at(p.sxz0, i0 - 2)), xz1 = ld4(at(p.sxz0, i0 - 1)), xz2 = ld4(at(p.sxz0, i0)), xz3;
+  f4 zz0 = ld4(at(p.szz0, i0 - 2)), zz1 = ld4(at(p.szz0, i0 - 1)), zz2 = ld4(at(p.szz0, i0)), zz3;
+  const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
+  f4 xa = z4, xb_ = z4, xc = z4, xd = z4, za = z4, zb_ = z4, zc = z4, zd = z4;  // level-1 v rows i-3..i
+  f4 sx0 = z4, sx1 = z4, sx2 = z4, sx3 = z4;    // level-1 sxx rows i-5..i-2
+  f4 sq0 = z4, sq1 = z4, sq2 = z4, sq3 = z4;    // level-1 sxz rows i-5..i-2
+  f4 sz0 = z4, sz1 = z4, sz2 = z4, sz3 = z4;    // level-1 szz rows i-5..i-2
+  f4 ua = z4, ub = z4, uc = z4, ud = z4, wa = z4, wb = z4, wc = z4, wd = z4;  // level-2 v rows i-6..i-3
+  InjectList inj2 = p.inj;
+  inj2.it = p.inj.it + 1;
+  ProbeList pr2 = p.probes;
+  pr2.it = p.probes.it + 1;
+  Cursor ci1 = cursor_at(p.inj.list, p.inj.n, i0);
+  Cursor ci2 = cursor_at(p.inj.list, p.inj.n, m.ib - 1);
+  Cursor pi1 = cursor_at(p.probes.list, p.probes.n, m.ib);
+  Cursor pi2 = pi1;
+  f4 rzb, rzf;  // 1/(8 dz) where the z-derivative is allowed, else 0
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    rzb.v[e] = (!EDGE || (L.zb & (1 << e))) ? g.rdz : 0.0f;
+    rzf.v[e] = (!EDGE || (L.zf & (1 << e))) ? g.rdz : 0.0f;
+  }
+  // Some lane holds columns outside the grid: level-1 values there are zeroed.
+  const bool cols_out = EDGE && !__all_sync(kFull, valid == 0xF);
+
+  for (int k = 0; k < nk; ++k) {
+    const int i = i0 + k;
+    if (!rows.acquire(k)) {
+      flag_timeout(p.err);
+      rows.drain(k);
+      return;
+    }
+    xx3 = rows.seg(P2_SXX);
+    xz3 = rows.seg(P2_SXZ);
+    zz3 = rows.seg(P2_SZZ);
+    const f4 vxo = rows.seg(P2_VX);
+    const f4 vzo = rows.seg(P2_VZ);
+    const f4 rho = rows.seg(P2_RHO);
+    const f4 lam = rows.seg(P2_LAM);
+    const f4 mu = rows.seg(P2_MU);
+    rows.release();
+
+    // ---- level 1, velocity of row i (step it)
+    {
+      const float bxi = __ldg(p.taper_x + i);
+      const float rx = (!EDGE || (i >= 2 && i < nx - 2)) ? g.rdx : 0.0f;
+      f4 dsx = dx4r(xx0, xx1, xx2, xx3, rx);
+      f4 dsz = dx4r(xz0, xz1, xz2, xz3, rx);
+      const f4 a = dz_back_r(xz2, rzb);
+      const f4 b = dz_back_r(zz2, rzb);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
+      inject_at<true, false, true>(p.inj, i, c0, ci1, dsx, dsx, dsz);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float bb = (bxi * tb.v[e]) * tt.v[e];
+        xd.v[e] = bb * (vxo.v[e] + dt * dsx.v[e] * rho.v[e]);
+        zd.v[e] = bb * (vzo.v[e] + dt * dsz.v[e] * rho.v[e]);
+      }
+      const bool row_ok = (i >= 0 && i < nx);
+      if (EDGE && (!row_ok || cols_out)) {
+        xd = in_grid(xd, row_ok, valid);
+        zd = in_grid(zd, row_ok, valid);
+      }
+      if (i >= m.ib && i < m.ie)
+        probe_at(p.probes, i, L, pi1, dt,
+                 [&](int comp, int e) { return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e); });
+    }
+
+    // ---- level 1, stress of row i-2 (step it)
+    if (k >= 3) {
+      const int r = i - 2;
+      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? g.rdx : 0.0f;
+      const f4 dvxdx = dx4r(xa, xb_, xc, xd, rx);
+      const f4 dvzdx = dx4r(za, zb_, zc, zd, rx);
+      const f4 dvxdz = dz_fwd_r(xb_, rzf);
+      const f4 dvzdz = dz_fwd_r(zb_, rzf);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float l = lam.v[e], mm = mu.v[e];
+        sx3.v[e] = xx0.v[e] + dt * ((l + 2.0f * mm) * dvxdx.v[e] + l * dvzdz.v[e]);
+        sz3.v[e] = zz0.v[e] + dt * ((l + 2.0f * mm) * dvzdz.v[e] + l * dvxdx.v[e]);
+        sq3.v[e] = xz0.v[e] + dt * mm * (dvxdz.v[e] + dvzdx.v[e]);
+      }
+      const bool row_ok = (r >= 0 && r < nx);
+      if (EDGE && (!row_ok || cols_out)) {
+        sx3 = in_grid(sx3, row_ok, valid);
+        sz3 = in_grid(sz3, row_ok, valid);
+        sq3 = in_grid(sq3, row_ok, valid);
+      }
+    }
+
+    // ---- level 2, velocity of row i-3 (step it+1)
+    if (k >= 6) {
+      const int r = i - 3;
+      const f4 rho2 = rows.seg_back(P2_RHO, 3);
+      const float bxr = __ldg(p.taper_x + r);
+      const float rx = (!EDGE || (r >= 2 && r < nx - 2)) ? g.rdx : 0.0f;
+      f4 dsx = dx4r(sx0, sx1, sx2, sx3, rx);
+      f4 dsz = dx4r(sq0, sq1, sq2, sq3, rx);
+      const f4 a = dz_back_r(sq2, rzb);
+      const f4 b = dz_back_r(sz2, rzb);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
+      inject_at<true, false, true>(inj2, r, c0, ci2, dsx, dsx, dsz);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float bb = (bxr * tb.v[e]) * tt.v[e];
+        ud.v[e] = bb * (xa.v[e] + dt * dsx.v[e] * rho2.v[e]);
+        wd.v[e] = bb * (za.v[e] + dt * dsz.v[e] * rho2.v[e]);
+      }
+      if (r >= m.ib && r < m.ie) {
+        st4_masked(at(p.vx1, r), ud, L.own);
+        st4_masked(at(p.vz1, r), wd, L.own);
+        probe_at(pr2, r, L, pi2, dt,
+                 [&](int comp, int e) { return comp == kProbeVX ? pick4(ud, e) : pick4(wd, e); });
+      }
+    }
+
+    // ---- level 2, stress of row i-5 (step it+1)
+    if (k >= 9) {
+      const int r = i - 5;
+      const f4 lam2 = rows.seg_back(P2_LAM, 3), mu2 = rows.seg_back(P2_MU, 3);
+      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? g.rdx : 0.0f;
+      const f4 dvxdx = dx4r(ua, ub, uc, ud, rx);
+      const f4 dvzdx = dx4r(wa, wb, wc, wd, rx);
+      const f4 dvxdz = dz_fwd_r(ub, rzf);
+      const f4 dvzdz = dz_fwd_r(wb, rzf);
+      f4 sxx, szz, sxz;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float l = lam2.v[e], mm = mu2.v[e];
+        sxx.v[e] = sx0.v[e] + dt * ((l + 2.0f * mm) * dvxdx.v[e] + l * dvzdz.v[e]);
+        szz.v[e] = sz0.v[e] + dt * ((l + 2.0f * mm) * dvzdz.v[e] + l * dvxdx.v[e]);
+        sxz.v[e] = sq0.v[e] + dt * mm * (dvxdz.v[e] + dvzdx.v[e]);
+      }
+      st4_masked(at(p.sxx1, r), sxx, L.own);
+      st4_masked(at(p.szz1, r), szz, L.own);
+      st4_masked(at(p.sxz1, r), sxz, L.own);
+    }
+
+    ua = ub; ub = uc; uc = ud;
+    wa = wb; wb = wc; wc = wd;
+    sx0 = sx1; sx1 = sx2; sx2 = sx3;
+    sq0 = sq1; sq1 = sq2; sq2 = sq3;
+    sz0 = sz1; sz1 = sz2; sz2 = sz3;
+    xa = xb_; xb_ = xc; xc = xd;
+    za = zb_; zb_ = zc; zc = zd;
+    xx0 = xx1; xx1 = xx2; xx2 = xx3;
+    xz0 = xz1; xz1 = xz2; xz2 = xz3;
+    zz0 = zz1; zz1 = zz2; zz2 = zz3;
+  }
+}
+
+template <class Loader>
+__device__ __forceinline__ void psv2_march(const PsvStep& p, int gw, unsigned char* smem) {
+  const March m = march_of(p.g, gw);
+  if (!m.active) return;
+  int valid;
+  const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
+  psv2_body<Loader, true>(p, m, L, valid, smem);
+}
+
+}  // namespace
+
+template <class Loader>
+__global__ void __launch_bounds__(kStepWarps * 32, 2) psv_step2_kernel(const PsvStep p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  psv2_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
+size_t step2_smem_bytes() { return smem_for<Bulk2>(); }
+
+int step2_blocks_per_sm() {
+  int n = 0;
+  const size_t smem = smem_for<Bulk2>();
+  cudaError_t e = prepare_kernel(psv_step2_kernel<Bulk2>, smem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step2_kernel<Bulk2>, kStepWarps * 32, smem);
+  return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s) {
+  const size_t smem = smem_for<Bulk2>();
+  static const cudaError_t attr = prepare_kernel(psv_step2_kernel<Bulk2>, smem);
+  if (attr != cudaSuccess) return attr;
+  psv_step2_kernel<Bulk2><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
+  return cudaGetLastError();
+}
+
+}  // namespace seiswg

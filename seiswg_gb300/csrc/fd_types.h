@@ -3,9 +3,9 @@
 //
 // Grid layout in HBM (one allocation per field):
 //   rows i in [-kHaloRows, nx + kHaloRows), row pitch `ld` floats (a multiple
-//   of 32, so every row starts on a 128-byte boundary); column j of row i is
-//   at base[i * ld + j] and the element (0, 0) sits kHaloCols floats into a
-//   row, i.e. 16-byte aligned.  z (j) is the contiguous direction, as in the
+//   of 32, so every row starts on a 128-byte boundary; field_pitch below);
+//   column j of row i is at base[i * ld + j] and the element (0, 0) sits
+//   kHaloCols floats into a row, i.e. 32-byte aligned.  z (j) is the contiguous direction, as in the
 //   reference (fd2d.wgsl:140-145, k = i*nz + j).  Halo rows and columns are
 //   zero and never written; the reference's edge rules (derivatives forced to
 //   zero near the edges, fd2d.wgsl:151-180) are applied by index, so halo
@@ -16,16 +16,24 @@
 // holds the float4 of columns [j0 - 4 + 4L, j0 + 4L); lanes 0 and 31 are the
 // strip's halo, lanes 1..30 own the 120 output columns.  z-derivatives take
 // their neighbours from adjacent lanes with warp shuffles; x-derivatives read
-// register rings of the previous rows.
+// register rings of the previous rows.  The two-step kernel advances two time
+// steps per pass: its strips own kStripCols2 columns (lanes 2..29; the two
+// steps reach 6 columns to each side) and its marches read rows from 9 above
+// to 5 below their chunk, hence the halo sizes.
 #pragma once
 
 #include <cstdint>
 
 namespace seiswg {
 
-constexpr int kHaloRows = 4;
-constexpr int kHaloCols = 4;
+constexpr int kHaloRows = 12;
+constexpr int kHaloCols = 8;
 constexpr int kStripCols = 120;
+constexpr int kStripCols2 = 112;
+
+// Row pitch of every field: room for the strips' reach past nz on the right
+// (up to 11 columns) and for kHaloCols on the left, rounded to 128 bytes.
+constexpr int field_pitch(int nz) { return ((nz > 128 ? nz : 128) + 24 + 31) / 32 * 32; }
 constexpr unsigned kFull = 0xffffffffu;
 
 // An injection (source or adjoint source) at cell (i, j).  `row` indexes the

@@ -210,6 +210,7 @@ Config parse_config(const Ini& ini, const std::string& base) {
   uint32_t u;
   if (ini_get(ini, "cuda", "chunk_rows", &v) && parse_u32(v, &u)) c.chunk_rows = int(u);
   if (ini_get(ini, "cuda", "graphs", &v)) c.graphs = lower(trim(v)) == "yes" ? 1 : 0;
+  if (ini_get(ini, "cuda", "two_step", &v)) c.two_step = lower(trim(v)) == "yes" ? 1 : 0;
   return c;
 }
 
@@ -537,6 +538,7 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
   sim_.reset(new Sim(d));
   if (cfg.chunk_rows > 0) sim_->set_chunk_rows(cfg.chunk_rows);
   if (cfg.graphs >= 0) sim_->set_use_graphs(cfg.graphs == 1);
+  if (cfg.two_step >= 0) sim_->set_two_step(cfg.two_step == 1);
   for (const auto& f : fields) {
     const bool spin_only = f.first == ModelField::NU || f.first == ModelField::J || f.first == ModelField::MU_C ||
                            f.first == ModelField::NU_C;

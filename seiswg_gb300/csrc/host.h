@@ -42,6 +42,7 @@ struct Config {
   // [cuda] -- keys the reference ignores
   int chunk_rows = 0;   // 0: engine default
   int graphs = -1;      // -1: engine default, 0 off, 1 on
+  int two_step = -1;    // [cuda] two_step: -1 engine default (on for PSV alone), 0 off, 1 on
 };
 
 // config::load (config.rs:118) and config::load_from_str (config.rs:132).
