@@ -495,7 +495,7 @@ def run_secondary(args):
         out.update(metric="gradients/s", value=1000.0 / ms, unit="gradients/s", ms_per_step=ms,
                    higher_is_better=True, wall_s_per_gradient=wall,
                    gcell_updates_per_s=cell_updates / (ms / 1e3) / 1e9,
-                   config={"workload": W.name, "checkpoint_interval": int(math.ceil(math.sqrt(W.nt))),
+                   config={"workload": W.name, "checkpoint_interval": sim.checkpoint_interval,
                            "misfit": "L2 waveform, ux+uz", "J_per_shot": list(Js),
                            "receivers": int(W.rec_i.size), "shots": nshot},
                    gradient_finite=bool(np.isfinite(gvp).all() and np.isfinite(gvs).all()),

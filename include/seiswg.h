@@ -148,6 +148,8 @@ int seiswg_sim_kernel(seiswg_sim* sim, float* host);
 int seiswg_sim_gradient_clear(seiswg_sim* sim);
 int seiswg_sim_forward_op(seiswg_sim* sim, int32_t isrc, int32_t ckpt_every);
 int seiswg_sim_backward_op(seiswg_sim* sim, const float* adj);
+/* The checkpoint interval of the last forward_op (0 before the first). */
+int32_t seiswg_sim_checkpoint_interval(const seiswg_sim* sim);
 /* The misfit and adjoint source on the device (the host misfit of
  * solver.rs:432-467 without the trace download and the adjoint-source
  * upload).  set_observed copies the observed traces, [ncomp][nrec][nt] in the

@@ -88,6 +88,7 @@ PROTOTYPES = [
     ("seiswg_sim_gradient_clear", _c_int, [_vp]),
     ("seiswg_sim_forward_op", _c_int, [_vp, _i32, _i32]),
     ("seiswg_sim_backward_op", _c_int, [_vp, _pf]),
+    ("seiswg_sim_checkpoint_interval", _i32, [_vp]),
     ("seiswg_sim_set_observed", _c_int, [_vp, _pf]),
     ("seiswg_sim_misfit_op", _c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     ("seiswg_sim_backward_op_device", _c_int, [_vp]),
@@ -366,6 +367,11 @@ class Sim:
         """Reverse sweep for dJ/dd, [ncomp][nrec][nt] (SH: uy; PSV: ux, uz)."""
         a = _f32(adj).reshape(-1)
         _check(lib().seiswg_sim_backward_op(self._h, _fp(a)))
+
+    @property
+    def checkpoint_interval(self) -> int:
+        """Checkpoint interval of the last forward_op."""
+        return int(lib().seiswg_sim_checkpoint_interval(self._h))
 
     def set_observed(self, obs):
         """Observed traces [ncomp][nrec][nt] for misfit_op (kept on the device)."""

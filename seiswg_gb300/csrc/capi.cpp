@@ -402,6 +402,10 @@ int seiswg_sim_backward_op(seiswg_sim* s, const float* adj) {
   });
 }
 
+int32_t seiswg_sim_checkpoint_interval(const seiswg_sim* s) {
+  return s && s->sim ? s->sim->checkpoint_interval() : 0;
+}
+
 int seiswg_sim_set_observed(seiswg_sim* s, const float* obs) {
   return guarded([&] {
     if (!obs) throw std::invalid_argument("null observed traces");

@@ -184,9 +184,8 @@ int Sim::final_buffer(int every) const {
   return b;
 }
 
-void Sim::enqueue_step2(int it, int b, const InjectList& inj_in, const ProbeList& probes_in) {
-  const State& a = st_[b];
-  const State& o = st_[1 - b];
+void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList& inj_in,
+                        const ProbeList& probes_in) {
   PsvStep p{};
   p.g = geom2_;
   p.vx0 = a.vx; p.vz0 = a.vz; p.sxx0 = a.sxx; p.szz0 = a.szz; p.sxz0 = a.sxz;
@@ -657,7 +656,7 @@ void Sim::run_forward(int isrc, Snapshots* snaps) {
     for (int it = 0; it < d_.nt;) {
       const bool snap_between = every > 0 && it > 0 && it % every == 0;
       if (two_step_ && it + 1 < d_.nt && !snap_between) {
-        enqueue_step2(it, b, inj, pl);
+        enqueue_step2(it, st_[b], st_[1 - b], inj, pl);
         b ^= 1;
         snap(it + 1);
         it += 2;
@@ -884,12 +883,28 @@ void Sim::gradient_clear() {
   if (d_.psv) ensure(g_lam_);
 }
 
+int Sim::default_checkpoint_interval() const {
+  const int nt = std::max(d_.nt, 1);
+  const int k_sqrt = std::max(1, int(std::ceil(std::sqrt(double(nt)))));
+  // Where HBM allows, checkpoint every second step: with the forward pass
+  // running two steps per launch this recomputes half a forward pass per
+  // gradient instead of a whole one.  Budget: half of the free memory plus
+  // what the current checkpoints hold.
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return k_sqrt;
+  const double state_b = double(nstate()) * double(field_elems_) * sizeof(float);
+  const double budget = 0.5 * double(free_b) + double(ck_bytes_);
+  const int k2 = std::min(2, nt);
+  if ((double((nt + k2 - 1) / k2) + k2) * state_b <= budget) return k2;
+  return k_sqrt;
+}
+
 void Sim::forward_op(int isrc, int ckpt_every) {
   u_ready_ = false;
   if (d_.spin) throw std::invalid_argument("the exact adjoint is defined for SH or PSV without spin");
   if (d_.sh && d_.psv) throw std::invalid_argument("the exact adjoint runs one of SH or PSV at a time");
   const int nt = d_.nt;
-  int k = ckpt_every > 0 ? ckpt_every : int(std::ceil(std::sqrt(double(std::max(nt, 1)))));
+  int k = ckpt_every > 0 ? ckpt_every : default_checkpoint_interval();
   k = std::max(1, std::min(k, std::max(nt, 1)));
   const int ncp = (nt + k - 1) / k;
   const size_t state_elems = size_t(nstate()) * field_elems_;
@@ -897,9 +912,11 @@ void Sim::forward_op(int isrc, int ckpt_every) {
     cudaFree(ck_store_);
     cudaFree(seg_store_);
     ck_store_ = seg_store_ = nullptr;
+    ck_bytes_ = 0;
     SW_CUDA(cudaMalloc(&ck_store_, std::max(1, ncp) * state_elems * sizeof(float)));
     SW_CUDA(cudaMalloc(&seg_store_, size_t(k) * state_elems * sizeof(float)));
-    // Halos of every stored state stay zero.
+    // Halos of every stored state stay zero; so does checkpoint 0 (the zero
+    // initial state), which no step writes.
     SW_CUDA(cudaMemsetAsync(ck_store_, 0, std::max(1, ncp) * state_elems * sizeof(float), stream_));
     SW_CUDA(cudaMemsetAsync(seg_store_, 0, size_t(k) * state_elems * sizeof(float), stream_));
     ck_k_ = k;
@@ -913,15 +930,41 @@ void Sim::forward_op(int isrc, int ckpt_every) {
   ProbeList pl = probe_list();
   zero_state();
   if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
-  const std::string key = "fop/" + std::to_string(inj.n) + "/" + std::to_string(k);
-  run_loop(key, [&] {
-    for (int it = 0; it < nt; ++it) {
-      if (it % k == 0) copy_state(slot_state(ck_store_ + size_t(it / k) * state_elems), st_[it & 1]);
-      enqueue_step(it, it & 1, inj, pl, false);
+  // Steps write straight into the checkpoint they end on; the others
+  // alternate between the two state buffers.  Two steps per launch wherever
+  // no checkpoint falls between them.
+  auto ckpt = [&](int c) { return slot_state(ck_store_ + size_t(c) * state_elems); };
+  int last = -1;
+  auto plan = [&](const std::function<void(int, int, const State&, const State&)>& step) {
+    State cur = ckpt(0);
+    int pp = 0;
+    last = -1;
+    for (int it = 0; it < nt;) {
+      const int n = (two_step_ && it + 1 < nt && (it + 1) % k != 0) ? 2 : 1;
+      const int e = it + n;
+      State dst;
+      if (e % k == 0 && e < nt) {
+        dst = ckpt(e / k);
+      } else {
+        dst = st_[pp];
+        last = pp;
+        pp ^= 1;
+      }
+      step(it, n, cur, dst);
+      cur = dst;
+      it = e;
     }
+  };
+  const std::string key = "fop/" + std::to_string(inj.n) + "/" + std::to_string(k) + (two_step_ ? "/2" : "");
+  run_loop(key, [&] {
+    plan([&](int it, int n, const State& a, const State& o) {
+      if (n == 2) enqueue_step2(it, a, o, inj, pl);
+      else enqueue_step_states(it, a, o, inj, pl, false);
+    });
     enqueue_traces();
   });
-  cur_buf_ = nt & 1;
+  plan([](int, int, const State&, const State&) {});  // the buffer of the final state (graph replays skip the body)
+  cur_buf_ = last < 0 ? 0 : last;
   ck_isrc_ = isrc;
 }
 
@@ -1015,12 +1058,15 @@ void Sim::run_backward() {
     int cur = 0;
     for (int seg = ck_n_ - 1; seg >= 0; --seg) {
       const int n0 = seg * k, n1 = std::min(nt, n0 + k);
-      copy_state(slot_state(seg_store_), slot_state(ck_store_ + size_t(seg) * state_elems));
-      for (int n = n0; n < n1 - 1; ++n)
-        enqueue_step_states(n, slot_state(seg_store_ + size_t(n - n0) * state_elems),
-                            slot_state(seg_store_ + size_t(n - n0 + 1) * state_elems), src, none, false);
+      // S^n0 is the checkpoint itself; S^(n0+1..n1-1) are recomputed into
+      // the interval buffer.
+      auto fstate = [&](int n) {
+        return n == n0 ? slot_state(ck_store_ + size_t(seg) * state_elems)
+                       : slot_state(seg_store_ + size_t(n - n0) * state_elems);
+      };
+      for (int n = n0; n < n1 - 1; ++n) enqueue_step_states(n, fstate(n), fstate(n + 1), src, none, false);
       for (int n = n1 - 1; n >= n0; --n) {
-        const State f = slot_state(seg_store_ + size_t(n - n0) * state_elems);
+        const State f = fstate(n);
         const State& a = adj[cur];
         const State& o = adj[1 - cur];
         InjectList s2 = src, r2 = rec;

@@ -111,7 +111,8 @@ class Sim {
 
   // ---- exact discrete adjoint with checkpointing --------------------------
   // forward_op: one forward run of source isrc (-1: all) that also stores the
-  // full wavefield state every `ckpt_every` steps (0: ceil(sqrt(nt))).
+  // full wavefield state every `ckpt_every` steps (0: every second step when
+  // half of the free HBM holds those states, else ceil(sqrt(nt))).
   // backward_op: the reverse sweep for the adjoint source adj = dJ/dd of the
   // recorded traces, [ncomp][nrec][nt] (SH: uy; PSV: ux, uz), rebuilding the
   // forward states of each checkpoint interval by recomputation; gradients
@@ -206,7 +207,8 @@ class Sim {
   void run_loop(const std::string& key, const std::function<void()>& body);
   void copy_field_to_host(const float* dev, float* host) const;
   int chunk_rows_for(int blocks_per_sm, int strip_cols, int extra_rows) const;
-  void enqueue_step2(int it, int b, const InjectList& inj, const ProbeList& probes);
+  void enqueue_step2(int it, const State& a, const State& o, const InjectList& inj, const ProbeList& probes);
+  int default_checkpoint_interval() const;
   int final_buffer(int snap_every) const;  // buffer holding the state after run_forward
 
   SimDesc d_;

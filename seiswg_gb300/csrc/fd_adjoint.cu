@@ -204,6 +204,7 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  const f4 rzb = masked_recip(g.rdz, L.zb), rzf = masked_recip(g.rdz, L.zf);
   // Adjoint strains e = dt C s (unmasked) for rows of the ring.
   auto strain_adj = [&](const f4& bxx, const f4& bzz, const f4& bxz, const f4& lam, const f4& mu, f4& exx,
                         f4& ezz, f4& exz) {
@@ -266,14 +267,14 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
     f4 gl = rows.seg(PA_GL), gm = rows.seg(PA_GM);
     rows.release();
     const float bxi = __ldg(p.taper_x + i);
-    const bool xb = mask_back(i, g.nx);
+    const float rxb = mask_back(i, g.nx) ? g.rdx : 0.0f;
 
     // Forward recompute: D- sigma^n + f^n and v^{n+1} of row i.
-    f4 dsx = dx4(xx0, xx1, xx2, xx3, g.rdx, xb);
-    f4 dsz = dx4(xz0, xz1, xz2, xz3, g.rdx, xb);
+    f4 dsx = dx4r(xx0, xx1, xx2, xx3, rxb);
+    f4 dsz = dx4r(xz0, xz1, xz2, xz3, rxb);
     {
-      const f4 a = dz_back(xz2, g.rdz, L.zb);
-      const f4 b = dz_back(szz_i, g.rdz, L.zb);
+      const f4 a = dz_back_r(xz2, rzb);
+      const f4 b = dz_back_r(szz_i, rzb);
 #pragma unroll
       for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
     }
@@ -290,8 +291,14 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
     {
       const bool m0 = mask_fwd(i - 2, g.nx), m1 = mask_fwd(i - 1, g.nx), m2 = mask_fwd(i, g.nx),
                  m3 = mask_fwd(i + 1, g.nx);
-      const f4 tx = dxT(scaled(ex0, m0), scaled(ex1, m1), scaled(ex2, m2), scaled(ex3, m3), g.rdx);
-      const f4 tzx = dxT(scaled(eq0, m0), scaled(eq1, m1), scaled(eq2, m2), scaled(eq3, m3), g.rdx);
+      f4 tx, tzx;
+      if (m0 && m1 && m2 && m3) {  // interior rows (uniform over the warp): no row masks
+        tx = dxT(ex0, ex1, ex2, ex3, g.rdx);
+        tzx = dxT(eq0, eq1, eq2, eq3, g.rdx);
+      } else {
+        tx = dxT(scaled(ex0, m0), scaled(ex1, m1), scaled(ex2, m2), scaled(ex3, m3), g.rdx);
+        tzx = dxT(scaled(eq0, m0), scaled(eq1, m1), scaled(eq2, m2), scaled(eq3, m3), g.rdx);
+      }
       const f4 tq = dzT_back(masked(eq2, L.zf), g.rdz);
       const f4 tz = dzT_back(masked(ezc, L.zf), g.rdz);
       add_row<true, false, true>(p.rec, i, c0, ri, wx, wx, wz);
@@ -314,16 +321,21 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
     // Adjoint stress of row r = i-2 and the lambda/mu gradients there.
     if (i >= m.ib + 2) {
       const int r = i - 2;
-      const bool xf = mask_fwd(r, g.nx);
-      const f4 exx = dx4(na, nb, nc, nd, g.rdx, xf);
-      const f4 ezx = dx4(za, zb, zc, zd, g.rdx, xf);
-      const f4 exz = dz_fwd(nb, g.rdz, L.zf);
-      const f4 ezz = dz_fwd(zb, g.rdz, L.zf);
+      const float rxf = mask_fwd(r, g.nx) ? g.rdx : 0.0f;
+      const f4 exx = dx4r(na, nb, nc, nd, rxf);
+      const f4 ezx = dx4r(za, zb, zc, zd, rxf);
+      const f4 exz = dz_fwd_r(nb, rzf);
+      const f4 ezz = dz_fwd_r(zb, rzf);
       const bool m0 = mask_back(r - 1, g.nx), m1 = mask_back(r, g.nx), m2 = mask_back(r + 1, g.nx),
                  m3 = mask_back(r + 2, g.nx);
-      const f4 ax = dxT(scaled(qxa, m0), scaled(qxb, m1), scaled(qxc, m2), scaled(qxd, m3), g.rdx);
-      const f4 az = dxT(scaled(qza, m0), scaled(qzb, m1), scaled(qzc, m2),
-                        scaled(qzd, m3), g.rdx);
+      f4 ax, az;
+      if (m0 && m1 && m2 && m3) {
+        ax = dxT(qxa, qxb, qxc, qxd, g.rdx);
+        az = dxT(qza, qzb, qzc, qzd, g.rdx);
+      } else {
+        ax = dxT(scaled(qxa, m0), scaled(qxb, m1), scaled(qxc, m2), scaled(qxd, m3), g.rdx);
+        az = dxT(scaled(qza, m0), scaled(qzb, m1), scaled(qzc, m2), scaled(qzd, m3), g.rdx);
+      }
       const f4 bx = dzT_fwd(masked(qxb, L.zb), g.rdz);
       const f4 bz = dzT_fwd(masked(qzb, L.zb), g.rdz);
       f4 sxx, szz, sxz;
@@ -395,6 +407,7 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  const f4 rzb = masked_recip(g.rdz, L.zb), rzf = masked_recip(g.rdz, L.zf);
   auto times = [&](const f4& a, const f4& mu) {
     f4 o;
 #pragma unroll
@@ -434,9 +447,9 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
     rows.release();
     const float bxi = __ldg(p.taper_x + i);
 
-    f4 ds = dx4(xy0, xy1, xy2, xy3, g.rdx, mask_back(i, g.nx));
+    f4 ds = dx4r(xy0, xy1, xy2, xy3, mask_back(i, g.nx) ? g.rdx : 0.0f);
     {
-      const f4 a = dz_back(szy_i, g.rdz, L.zb);
+      const f4 a = dz_back_r(szy_i, rzb);
 #pragma unroll
       for (int e = 0; e < 4; ++e) ds.v[e] = ds.v[e] + a.v[e];
     }
@@ -448,8 +461,11 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
       nd.v[e] = bb.v[e] * (vy_i.v[e] + dt * ds.v[e] * buoy.v[e]);
     }
     {
-      const f4 tx = dxT(scaled(ex0, mask_fwd(i - 2, g.nx)), scaled(ex1, mask_fwd(i - 1, g.nx)),
-                        scaled(ex2, mask_fwd(i, g.nx)), scaled(ex3, mask_fwd(i + 1, g.nx)), g.rdx);
+      const bool m0 = mask_fwd(i - 2, g.nx), m1 = mask_fwd(i - 1, g.nx), m2 = mask_fwd(i, g.nx),
+                 m3 = mask_fwd(i + 1, g.nx);
+      const f4 tx = (m0 && m1 && m2 && m3)
+                        ? dxT(ex0, ex1, ex2, ex3, g.rdx)
+                        : dxT(scaled(ex0, m0), scaled(ex1, m1), scaled(ex2, m2), scaled(ex3, m3), g.rdx);
       const f4 tz = dzT_back(masked(ezc, L.zf), g.rdz);
       add_row<false, true, false>(p.rec, i, c0, ri, w, w, w);
 #pragma unroll
@@ -466,10 +482,13 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
     }
     if (i >= m.ib + 2) {
       const int r = i - 2;
-      const f4 ex = dx4(na, nb, nc, nd, g.rdx, mask_fwd(r, g.nx));
-      const f4 ez = dz_fwd(nb, g.rdz, L.zf);
-      const f4 ax = dxT(scaled(qa, mask_back(r - 1, g.nx)), scaled(qb, mask_back(r, g.nx)),
-                        scaled(qc, mask_back(r + 1, g.nx)), scaled(qd, mask_back(r + 2, g.nx)), g.rdx);
+      const f4 ex = dx4r(na, nb, nc, nd, mask_fwd(r, g.nx) ? g.rdx : 0.0f);
+      const f4 ez = dz_fwd_r(nb, rzf);
+      const bool m0 = mask_back(r - 1, g.nx), m1 = mask_back(r, g.nx), m2 = mask_back(r + 1, g.nx),
+                 m3 = mask_back(r + 2, g.nx);
+      const f4 ax = (m0 && m1 && m2 && m3)
+                        ? dxT(qa, qb, qc, qd, g.rdx)
+                        : dxT(scaled(qa, m0), scaled(qb, m1), scaled(qc, m2), scaled(qd, m3), g.rdx);
       const f4 az = dzT_fwd(masked(qb, L.zb), g.rdz);
       f4 sxy, szy;
 #pragma unroll

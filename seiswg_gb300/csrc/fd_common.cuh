@@ -82,6 +82,40 @@ __device__ __forceinline__ f4 dx4(const f4& r0, const f4& r1, const f4& r2, cons
   return r;
 }
 
+// Masked differences with the mask folded into the reciprocal: r = 0 where
+// the edge rule zeroes the derivative (fd4 of finite samples times 0 is a
+// zero, possibly -0, which no later sum or product tells apart from +0).
+__device__ __forceinline__ f4 dx4r(const f4& r0, const f4& r1, const f4& r2, const f4& r3, float r) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = fd4(r0.v[e], r1.v[e], r2.v[e], r3.v[e], r);
+  return o;
+}
+
+__device__ __forceinline__ f4 dz_back_r(const f4& m, const f4& r) {
+  const float pz = __shfl_up_sync(kFull, m.v[2], 1);
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float nx = __shfl_down_sync(kFull, m.v[0], 1);
+  f4 o;
+  o.v[0] = fd4(pz, pw, m.v[0], m.v[1], r.v[0]);
+  o.v[1] = fd4(pw, m.v[0], m.v[1], m.v[2], r.v[1]);
+  o.v[2] = fd4(m.v[0], m.v[1], m.v[2], m.v[3], r.v[2]);
+  o.v[3] = fd4(m.v[1], m.v[2], m.v[3], nx, r.v[3]);
+  return o;
+}
+
+__device__ __forceinline__ f4 dz_fwd_r(const f4& m, const f4& r) {
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float n0 = __shfl_down_sync(kFull, m.v[0], 1);
+  const float n1 = __shfl_down_sync(kFull, m.v[1], 1);
+  f4 o;
+  o.v[0] = fd4(pw, m.v[0], m.v[1], m.v[2], r.v[0]);
+  o.v[1] = fd4(m.v[0], m.v[1], m.v[2], m.v[3], r.v[1]);
+  o.v[2] = fd4(m.v[1], m.v[2], m.v[3], n0, r.v[2]);
+  o.v[3] = fd4(m.v[2], m.v[3], n0, n1, r.v[3]);
+  return o;
+}
+
 // Per-lane column facts, fixed for the whole march.
 struct LaneCols {
   int c0;        // first column of the lane
@@ -112,6 +146,14 @@ __device__ __forceinline__ LaneCols lane_cols(const Geom& g, int strip, int lane
     if (lane >= 1 && lane <= 30 && c >= own_lo && c < own_hi) L.own |= 1 << e;
   }
   return L;
+}
+
+// r at the lane's columns whose bit is set in `mask`, 0 elsewhere.
+__device__ __forceinline__ f4 masked_recip(float r, int mask) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = (mask & (1 << e)) ? r : 0.0f;
+  return o;
 }
 
 // Bounded-size cursor over a (i, j)-sorted list: the first entry with row >= i0.

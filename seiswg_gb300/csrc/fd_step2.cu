@@ -63,39 +63,6 @@ __device__ __forceinline__ LaneCols lane_cols2(const Geom& g, int strip, int lan
   return L;
 }
 
-// Masked differences with the mask folded into the reciprocal: r = 0 where
-// the edge rule zeroes the derivative (fd4 of finite samples times 0).
-__device__ __forceinline__ f4 dx4r(const f4& r0, const f4& r1, const f4& r2, const f4& r3, float r) {
-  f4 o;
-#pragma unroll
-  for (int e = 0; e < 4; ++e) o.v[e] = fd4(r0.v[e], r1.v[e], r2.v[e], r3.v[e], r);
-  return o;
-}
-
-__device__ __forceinline__ f4 dz_back_r(const f4& m, const f4& r) {
-  const float pz = __shfl_up_sync(kFull, m.v[2], 1);
-  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
-  const float nx = __shfl_down_sync(kFull, m.v[0], 1);
-  f4 o;
-  o.v[0] = fd4(pz, pw, m.v[0], m.v[1], r.v[0]);
-  o.v[1] = fd4(pw, m.v[0], m.v[1], m.v[2], r.v[1]);
-  o.v[2] = fd4(m.v[0], m.v[1], m.v[2], m.v[3], r.v[2]);
-  o.v[3] = fd4(m.v[1], m.v[2], m.v[3], nx, r.v[3]);
-  return o;
-}
-
-__device__ __forceinline__ f4 dz_fwd_r(const f4& m, const f4& r) {
-  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
-  const float n0 = __shfl_down_sync(kFull, m.v[0], 1);
-  const float n1 = __shfl_down_sync(kFull, m.v[1], 1);
-  f4 o;
-  o.v[0] = fd4(pw, m.v[0], m.v[1], m.v[2], r.v[0]);
-  o.v[1] = fd4(m.v[0], m.v[1], m.v[2], m.v[3], r.v[1]);
-  o.v[2] = fd4(m.v[1], m.v[2], m.v[3], n0, r.v[2]);
-  o.v[3] = fd4(m.v[2], m.v[3], n0, n1, r.v[3]);
-  return o;
-}
-
 // Zero outside the grid: the whole row when it is not a grid row, else the
 // lane's columns outside [0, nz).
 __device__ __forceinline__ f4 in_grid(const f4& a, bool row_ok, int valid) {
