@@ -170,9 +170,12 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * the default), "autotune" (value = steps timed per candidate: picks the
  * fastest loader and chunk rows for this problem), "two_step" (0/1: forward
  * runs advance two time steps per launch; PSV without SH or spin only, and
- * on by default there;
- * multiply-add contraction, so results match the one-step kernel to rounding), "two_step_rows" (rows
- * per march of the two-step kernel; 0: its occupancy model). */
+ * on by default there; multiply-add contraction, so results match the
+ * one-step kernel to rounding), "two_step_rows" (rows per march of the
+ * two-step kernel; 0: its occupancy model), "cluster" (0/1: SH grids whose
+ * state and material fit one thread-block cluster's shared memory run each
+ * forward pass in one launch with the wavefield on chip; default on; results
+ * are the one-step kernel's bits). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */

@@ -37,7 +37,7 @@ FMAD = {"fd_adjoint.cu": "true", "fd_step2.cu": "true"}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
              f"-I{os.path.join(ROOT, 'include')}"]
 
-CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "noalloc.cu"]
+CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_cluster.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "noalloc.cu"]
 CXX_SOURCES = ["engine.cpp", "host.cpp", "batch.cpp", "capi.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 

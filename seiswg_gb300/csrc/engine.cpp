@@ -641,6 +641,47 @@ void Sim::run_forward(int isrc, Snapshots* snaps) {
   std::string key = "fwd/" + std::to_string(inj.n) + "/" + std::to_string(every);
   for (StateField f : (snaps ? snaps->fields : std::vector<StateField>{})) key += "/" + std::to_string(int(f));
   const size_t fbytes = field_elems_ * sizeof(float);
+  // Small SH grids: the whole run on chip in one thread-block cluster.
+  bool only_vy = true;
+  for (StateField f : (snaps ? snaps->fields : std::vector<StateField>{})) only_vy = only_vy && f == StateField::VY;
+  if (use_cluster_ && d_.sh && !d_.psv && only_vy && inj.n <= 64 && d_.nt > 0) {
+    if (cluster_ctas_ < 0) cluster_ctas_ = sh_cluster_ctas(d_.nx, d_.nz);
+    if (cluster_ctas_ > 0) {
+      ShCluster p{};
+      p.nx = d_.nx; p.nz = d_.nz; p.ld = ld_;
+      p.rows = (d_.nx + cluster_ctas_ - 1) / cluster_ctas_;
+      p.it0 = 0; p.it1 = d_.nt;
+      p.dt = geom_.dt; p.rdx = geom_.rdx; p.rdz = geom_.rdz;
+      p.vy0 = p.vy1 = st_[0].vy; p.sxy0 = p.sxy1 = st_[0].sxy; p.szy0 = p.szy1 = st_[0].szy;
+      p.rho = rho_; p.mu = mu_;
+      p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+      p.inj = inj;
+      p.probes = pl;
+      p.probes.n = probe_split_;
+      p.probes.it = 0;
+      p.snap = (every > 0 && nf > 0) ? snap_store_ + size_t(kHaloRows) * ld_ + kHaloCols : nullptr;
+      p.snap_every = every > 0 ? every : 1;
+      p.snap_first = 0;
+      p.snap_stride = (long long)field_elems_;
+      run_loop(key + "/cluster", [&] {
+        SW_CUDA(launch_sh_cluster(p, cluster_ctas_, stream_));
+        ++launches_;
+        enqueue_traces();
+      });
+      cur_buf_ = 0;
+      if (snaps) {
+        snaps->steps = snap_steps;
+        snaps->frames.assign(need, std::vector<float>());
+        for (size_t q = 0; q < need; ++q) {
+          snaps->frames[q].resize(size_t(d_.nx) * d_.nz);
+          copy_field_to_host(snap_store_ + q * field_elems_ + size_t(kHaloRows) * ld_ + kHaloCols,
+                             snaps->frames[q].data());
+        }
+        SW_CUDA(cudaStreamSynchronize(stream_));
+      }
+      return;
+    }
+  }
   if (two_step_) key += "/2";
   run_loop(key, [&] {
     size_t q = 0;

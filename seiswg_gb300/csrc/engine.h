@@ -174,6 +174,9 @@ class Sim {
   void set_two_step(bool on);
   void set_two_step_rows(int lx);
   bool two_step() const { return two_step_; }
+  // Small SH grids run whole forward passes in one thread-block cluster when
+  // state and material fit its shared memory (default on).
+  void set_use_cluster(bool on) { use_cluster_ = on; }
   int loader() const { return geom_.loader; }
   // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
   void check_device_error() const;
@@ -219,6 +222,8 @@ class Sim {
   Geom geom_{};
   Geom geom2_{};            // decomposition of the two-step kernel (lx 0: not yet modelled)
   bool two_step_ = false;
+  bool use_cluster_ = true;
+  int cluster_ctas_ = -1;   // CTAs of the cluster path (0: grid too large; -1: not yet queried)
   int adj_lx_[2] = {0, 0};  // reverse-step rows per chunk, per loader (0: not yet modelled)
   Arena arena_;
   State st_[2];

@@ -59,6 +59,29 @@ size_t step_smem_bytes(bool psv, bool spin, int loader);
 int step_blocks_per_sm(bool psv, bool spin, int loader);
 cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s);
 cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s);
+// Whole forward runs of small SH grids in one thread-block cluster
+// (fd_cluster.cu).  State *0 is read at the start and *1 written at the end
+// (they may alias); vy snapshots go to snap + q * snap_stride (padded fields)
+// for q = snap_first, ... at every step it > 0 with it % snap_every == 0.
+constexpr int kClusterThreads = 1024;
+struct ShCluster {
+  int nx, nz, ld, rows;  // rows per CTA
+  int it0, it1;          // steps [it0, it1)
+  float dt, rdx, rdz;
+  const float *vy0, *sxy0, *szy0;
+  float *vy1, *sxy1, *szy1;
+  const float *rho, *mu, *taper_x, *taper_zb, *taper_zt;
+  InjectList inj;
+  ProbeList probes;
+  float* snap;
+  int snap_every, snap_first;
+  long long snap_stride;
+};
+// CTAs of the cluster that holds an nx x nz SH grid (8 or 16), 0 when none fits.
+int sh_cluster_ctas(int nx, int nz);
+size_t sh_cluster_smem_bytes(int nx, int nz, int ctas);
+cudaError_t launch_sh_cluster(const ShCluster& p, int ctas, cudaStream_t s);
+
 // Two PSV steps (inj.it and inj.it + 1; no spin) from the *0 state to the *1
 // state.  p.g describes the two-step decomposition: nstrips over
 // kStripCols2-column strips, lx / nchunks its own chunk rows.
