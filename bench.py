@@ -577,7 +577,8 @@ def run_secondary(args):
                                        "1-4 shots",
                            "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
                            "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
-                           "chunk_rows": info.get("chunk_rows"), "autotune_ms": tune_ms},
+                           "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
+                           "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
             small = min(range(len(problems)), key=lambda q: problems[q].cells)

@@ -199,12 +199,16 @@ int seiswg_batch_create(seiswg_sim* const* sims, const float* const* obs, int32_
                         void* stream, seiswg_batch** out);
 int seiswg_batch_run(seiswg_batch* batch);
 /* key "chunk_rows": rows per warp chunk of every job (0: each problem's own
- * chunk model); "autotune": tries chunk rows 0, 16, 32, 48, 64, 96 and 128,
- * timing `value` slots of the recording pass and of the reverse sweep each,
- * and keeps the fastest.  Either drops the captured graph. */
+ * chunk model); "two_step" (0/1): PSV jobs whose problem runs two steps per
+ * launch record their forward pass that way (default 1); "autotune": tries
+ * chunk rows 0, 16, 32, 48, 64, 96 and 128 with and without two-step
+ * recording, timing `value` slots of the recording pass and of the reverse
+ * sweep each, and keeps the fastest.  Each drops the captured graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
-/* The chunk rows in use (0: each problem's own chunk model). */
+/* The chunk rows in use (0: each problem's own chunk model), and whether PSV
+ * jobs record two steps per launch. */
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);
+int32_t seiswg_batch_two_step(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */
 int seiswg_batch_gradient(seiswg_batch* batch, int32_t problem, const char* param, float* host);
 double seiswg_batch_misfit(const seiswg_batch* batch, int32_t problem);

@@ -108,6 +108,7 @@ PROTOTYPES = [
     ("seiswg_batch_run", _c_int, [_vp]),
     ("seiswg_batch_set_option", _c_int, [_vp, _cp, ctypes.c_int64]),
     ("seiswg_batch_chunk_rows", _i32, [_vp]),
+    ("seiswg_batch_two_step", _i32, [_vp]),
     ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
     ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
     ("seiswg_batch_info", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
@@ -448,7 +449,7 @@ class Batch:
         _check(lib().seiswg_batch_run(self._h))
 
     def set_option(self, key: str, value: int):
-        """"chunk_rows" (0: per-problem model) or "autotune" (slots per timing window)."""
+        """"chunk_rows" (0: per-problem model), "two_step" (0/1) or "autotune" (slots per timing window)."""
         _check(lib().seiswg_batch_set_option(self._h, key.encode(), int(value)))
 
     def gradient(self, problem: int, param: str):
@@ -464,7 +465,8 @@ class Batch:
         j, s, l, b = _i32(), _i32(), ctypes.c_uint64(), _sz()
         _check(lib().seiswg_batch_info(self._h, ctypes.byref(j), ctypes.byref(s), ctypes.byref(l), ctypes.byref(b)))
         return dict(jobs=j.value, slots=s.value, launches_per_run=l.value, device_bytes=b.value,
-                    chunk_rows=int(lib().seiswg_batch_chunk_rows(self._h)))
+                    chunk_rows=int(lib().seiswg_batch_chunk_rows(self._h)),
+                    two_step=bool(lib().seiswg_batch_two_step(self._h)))
 
     @property
     def stream(self) -> int:

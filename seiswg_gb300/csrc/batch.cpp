@@ -9,7 +9,7 @@ namespace seiswg {
 
 namespace {
 
-enum Kind { kFwdSh = 0, kFwdPsv, kAdjSh, kAdjPsv, kMisfit, kKinds };
+enum Kind { kFwdSh = 0, kFwdPsv, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
 
 struct HostOp {
   int kind, it, a, b, flags;
@@ -84,6 +84,7 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
 
       JobDesc jd{};
       jd.g = v.geom;
+      jd.g2 = v.geom2;  // lx 0 unless the problem runs two steps per launch
       jd.psv = d.psv;
       jd.nstate = j.nstate;
       jd.field_elems = (long long)fe;
@@ -146,18 +147,28 @@ void Batch::set_chunk_rows(int lx) {
   build_schedule();
 }
 
+void Batch::set_two_step(bool on) {
+  two_step_ = on;
+  set_chunk_rows(chunk_rows_);  // rebuilds the schedule
+}
+
 double Batch::autotune(int slots) {
   if (slots < 1) slots = 1;
-  const int w = std::min(slots, nslots_);
-  const int mid = std::min(std::max(0, nslots_ - w), nslots_ * 3 / 5);
   std::vector<int> cand = {0, 16, 32, 48, 64, 96, 128};
   cudaEvent_t e0, e1;
   SW_CUDA(cudaEventCreate(&e0));
   SW_CUDA(cudaEventCreate(&e1));
   float best = 1e30f;
   int best_lx = chunk_rows_;
-  for (int lx : cand) {
+  bool best_two = two_step_;
+  for (int c = 0; c < 2 * int(cand.size()); ++c) {
+    const int lx = cand[c % cand.size()];
+    two_step_ = c < int(cand.size());
     set_chunk_rows(lx);
+    // The same schedule positions for every candidate: the recording pass
+    // and a window of the reverse sweep.
+    const int w = std::min(slots, nslots_);
+    const int mid = std::min(std::max(0, nslots_ - w), nslots_ * 3 / 5);
     enqueue_slots(0, std::min(2, nslots_));  // warm-up
     SW_CUDA(cudaEventRecord(e0, stream_));
     enqueue_slots(0, w);
@@ -166,11 +177,12 @@ double Batch::autotune(int slots) {
     SW_CUDA(cudaEventSynchronize(e1));
     float ms = 0.0f;
     SW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-    if (ms < best) { best = ms; best_lx = lx; }
+    if (ms < best) { best = ms; best_lx = lx; best_two = two_step_; }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
+  two_step_ = best_two;
   set_chunk_rows(best_lx);
   return double(best);
 }
@@ -198,11 +210,25 @@ void Batch::build_schedule() {
     auto seg = [&](int m) { return ncp + m - 1; };  // interval buffer, m >= 1
     auto pp = [&](int t) { return ncp + k - 1 + (t & 1); };
     const int fwd = j.psv ? kFwdPsv : kFwdSh, adj = j.psv ? kAdjPsv : kAdjSh;
+    const bool two = two_step_ && j.psv && descs_[q].g2.lx > 0;
     std::vector<HostOp>& L = lists[q];
-    for (int t = 0; t < nt; ++t) {
-      const int a = (t % k == 0) ? t / k : pp(t);
-      const int b = ((t + 1) % k == 0 && t + 1 < nt) ? (t + 1) / k : pp(t + 1);
-      L.push_back(HostOp{fwd, t, a, b, 1});
+    // Recording pass: a step that ends on a checkpoint writes the checkpoint's
+    // slot, the others alternate between the two ping-pong slots; two steps
+    // per op where no checkpoint falls between them.
+    int cur = 0, ppi = 0;
+    for (int t = 0; t < nt;) {
+      const int n = (two && t + 1 < nt && (t + 1) % k != 0) ? 2 : 1;
+      const int e = t + n;
+      int dst;
+      if (e % k == 0 && e < nt) {
+        dst = e / k;
+      } else {
+        dst = pp(ppi);
+        ppi ^= 1;
+      }
+      L.push_back(HostOp{n == 2 ? int(kFwd2Psv) : fwd, t, cur, dst, 1});
+      cur = dst;
+      t = e;
     }
     L.push_back(HostOp{kMisfit, 0, 0, 0, 0});
     int parity = 0;
@@ -226,7 +252,7 @@ void Batch::build_schedule() {
       for (size_t q = 0; q < jobs_.size(); ++q) {
         if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
         const HostOp& h = lists[q][t];
-        const Geom& g = descs_[q].g;
+        const Geom& g = kind == kFwd2Psv ? descs_[q].g2 : descs_[q].g;
         all.push_back(GroupOp{int(q), h.it, h.a, h.b, h.flags, l.warps});
         l.warps += (kind == kMisfit) ? 1 : g.nstrips * g.nchunks;
         ++l.count;
@@ -276,6 +302,7 @@ void Batch::enqueue_slots(int t0, int t1) {
       switch (l.kind) {
         case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
         case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
+        case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, stream_)); break;
         case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
         case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
         case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, stream_)); break;

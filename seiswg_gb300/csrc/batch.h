@@ -44,6 +44,10 @@ class Batch {
   // timed launches leave results that the next run() overwrites.
   double autotune(int slots);
   int chunk_rows() const { return chunk_rows_; }
+  // PSV jobs record two steps per launch between checkpoints (default on);
+  // rebuilds the schedule.  The autotuner also tries both.
+  void set_two_step(bool on);
+  bool two_step() const { return two_step_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -69,6 +73,7 @@ class Batch {
   std::vector<JobDesc> descs_;   // host copy of d_jobs_
   std::vector<Geom> model_geom_; // each job's geometry from its problem's chunk model
   int chunk_rows_ = 0;
+  bool two_step_ = true;
   size_t ops_bytes_ = 0;
 
   std::vector<BatchProblem> problems_;

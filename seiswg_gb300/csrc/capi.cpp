@@ -492,11 +492,14 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     const std::string k(key);
     if (k == "chunk_rows") b->batch->set_chunk_rows(int(value));
     else if (k == "autotune") b->batch->autotune(int(value));
+    else if (k == "two_step") b->batch->set_two_step(value != 0);
     else throw std::invalid_argument("unknown batch option: " + k);
   });
 }
 
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* b) { return b ? b->batch->chunk_rows() : 0; }
+
+int32_t seiswg_batch_two_step(const seiswg_batch* b) { return b && b->batch->two_step() ? 1 : 0; }
 
 int seiswg_batch_gradient(seiswg_batch* b, int32_t problem, const char* param, float* host) {
   if (!b || !param || !host) return fail(SEISWG_EINVAL, "seiswg_batch_gradient: null argument");

@@ -1181,6 +1181,8 @@ namespace seiswg {
 Sim::View Sim::view() const {
   View v;
   v.geom = geom_;
+  v.geom2 = geom2_;
+  if (!two_step_) v.geom2.lx = 0;
   v.ld = ld_;
   v.field_elems = field_elems_;
   v.rho = rho_; v.lam = lam_; v.mu = mu_;

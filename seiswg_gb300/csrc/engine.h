@@ -140,6 +140,7 @@ class Sim {
   // jobs of one problem (read-only after set-up).
   struct View {
     Geom geom;
+    Geom geom2;             // two-step decomposition (lx 0 when the two-step kernel is off)
     int ld;
     size_t field_elems;
     const float *rho, *lam, *mu, *taper_x, *taper_zb, *taper_zt;

@@ -130,6 +130,7 @@ cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s);
 // fields in a slot: SH vy, sxy, szy; PSV vx, vz, sxx, szz, sxz.
 struct JobDesc {
   Geom g;
+  Geom g2;                 // two-step decomposition (PSV; lx 0: one step per launch)
   int psv;                 // 1 PSV, 0 SH
   int nstate;
   long long field_elems, slot_elems, halo;
@@ -190,6 +191,8 @@ cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int 
                                    cudaStream_t s);
 cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
                                    cudaStream_t s);
+// Two PSV steps (op.it, op.it + 1) of every op's job, with the jobs' g2.
+cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, cudaStream_t s);
 // Misfit of one problem's assembled traces against obs [ncomp][nrec][nt];
 // writes J per trace and the adjoint-source table dt * U.
 cudaError_t launch_sim_misfit(const float* syn, const float* obs, float* u_tab, double* J, int nrec, int nt,

@@ -281,6 +281,45 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) psv_step2_kernel(const Psv
   psv2_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
 }
 
+// Grouped two-step launch (batched gradients): the warp's job and op as in
+// grouped_forward_kernel (fd_step.cu), then the two-step march.
+__global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(const JobDesc* __restrict__ jobs,
+                                                                              const GroupOp* __restrict__ ops,
+                                                                              int nops) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const GroupOp op = ops[group_op_of(ops, nops, gw)];
+  const JobDesc& J = jobs[op.job];
+  const int lw = gw - op.warp_begin;
+  if (lw >= J.g2.nstrips * J.g2.nchunks) return;
+  auto slot = [&](int s, int f) { return J.pool + s * J.slot_elems + f * J.field_elems + J.halo; };
+  PsvStep p{};
+  p.g = J.g2;
+  p.vx0 = slot(op.a, 0); p.vz0 = slot(op.a, 1); p.sxx0 = slot(op.a, 2); p.szz0 = slot(op.a, 3);
+  p.sxz0 = slot(op.a, 4);
+  p.vx1 = slot(op.b, 0); p.vz1 = slot(op.b, 1); p.sxx1 = slot(op.b, 2); p.szz1 = slot(op.b, 3);
+  p.sxz1 = slot(op.b, 4);
+  p.rho = J.rho; p.lam = J.lam; p.mu = J.mu;
+  p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
+  p.inj = J.src;
+  p.inj.it = op.it;
+  p.probes = J.probes;
+  if (!(op.flags & 1)) p.probes.n = 0;
+  p.probes.it = op.it;
+  p.err = J.err;
+  psv2_march<Bulk2>(p, lw, smem);
+}
+
+cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, cudaStream_t s) {
+  if (nops <= 0 || warps <= 0) return cudaSuccess;
+  const size_t smem = smem_for<Bulk2>();
+  static const cudaError_t attr = prepare_kernel(grouped_forward2_kernel, smem);
+  if (attr != cudaSuccess) return attr;
+  grouped_forward2_kernel<<<unsigned((warps + kStepWarps - 1) / kStepWarps), kStepWarps * 32, smem, s>>>(jobs, ops,
+                                                                                                         nops);
+  return cudaGetLastError();
+}
+
 size_t step2_smem_bytes() { return smem_for<Bulk2>(); }
 
 int step2_blocks_per_sm() {

@@ -101,11 +101,19 @@ def test_chunk_rows_and_autotune_leave_gradients_unchanged():
             batch.run()
             for i in range(len(probs)):
                 assert np.array_equal(batch.gradient(i, "mu"), ref[i]), (lx, i)
+        # two-step recording (the default) or not: the same gradient to rounding
+        batch.set_option("two_step", 0)
+        assert not batch.info()["two_step"]
+        batch.run()
+        one = [batch.gradient(i, "mu") for i in range(len(probs))]
+        for i in range(len(probs)):
+            assert rel_l2(one[i], ref[i]) <= 1e-5, ("one-step recording", i)
         batch.set_option("autotune", 8)
-        assert batch.info()["chunk_rows"] in (0, 16, 32, 48, 64, 96, 128)
+        info = batch.info()
+        assert info["chunk_rows"] in (0, 16, 32, 48, 64, 96, 128)
         batch.run()
         for i in range(len(probs)):
-            assert np.array_equal(batch.gradient(i, "mu"), ref[i]), ("autotune", i)
+            assert np.array_equal(batch.gradient(i, "mu"), ref[i] if info["two_step"] else one[i]), ("autotune", i)
         with pytest.raises(sw.SeiswgError):
             batch.set_option("chunk_rows", 2)
     finally:
