@@ -34,7 +34,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
 # The reverse step (no counterpart in the reference) and the two-step forward
 # kernel are issue-bound, so they contract multiply-add pairs.
 FMAD = {"fd_adjoint.cu": "true", "fd_step2.cu": "true"}
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fno-strict-aliasing", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
              f"-I{os.path.join(ROOT, 'include')}"]
 
 CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_cluster.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "noalloc.cu"]

@@ -597,7 +597,7 @@ int seiswg_velocity_gradients(const float* g_lam, const float* g_mu, const float
 int seiswg_infer_grid(const float* x, const float* z, size_t npt, int32_t* nx, int32_t* nz, float* dx, float* dz) {
   if (!x || !z || !nx || !nz || !dx || !dz) return fail(SEISWG_EINVAL, "seiswg_infer_grid: null argument");
   return guarded([&] {
-    seiswg::GridInfo g = seiswg::infer_grid(std::vector<float>(x, x + npt), std::vector<float>(z, z + npt));
+    seiswg::GridInfo g = seiswg::infer_grid(seiswg::ModelData{x, npt}, seiswg::ModelData{z, npt});
     *nx = g.nx;
     *nz = g.nz;
     *dx = g.dx;

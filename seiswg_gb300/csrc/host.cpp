@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <list>
 #include <sstream>
 
 namespace seiswg {
@@ -252,6 +253,19 @@ std::vector<float> parse_model_bin(const Bytes& b, const std::string& what) {
   return out;
 }
 
+ModelData view_model_bin(const Bytes& b, const std::string& what) {
+  if (b.size() < 4) throw Error("Model file too small: " + what);
+  int32_t n;
+  std::memcpy(&n, b.data(), 4);
+  if (n < 0) throw Error("Model file " + what + " has a negative point count");
+  const size_t expected = 4 + size_t(n) * 4;
+  if (b.size() < expected)
+    throw Error("Model file " + what + " too short (expected " + std::to_string(expected) + " bytes, got " +
+                std::to_string(b.size()) + ")");
+  // The payload follows the 4-byte header: 4-byte aligned floats, read in place.
+  return ModelData{reinterpret_cast<const float*>(b.data() + 4), size_t(n)};
+}
+
 Bytes make_model_bin(const std::vector<float>& d) {
   Bytes out(4 + d.size() * 4);
   int32_t n = int32_t(d.size());
@@ -350,7 +364,7 @@ namespace {
 // length of the first run of equal x, nx = npt / nz, and every run must
 // repeat the first run's z values at one x.  Returns false when the
 // coordinates do not form such a grid.
-bool grid_from_layout(const std::vector<float>& x, const std::vector<float>& z, GridInfo& g) {
+bool grid_from_layout(const ModelData& x, const ModelData& z, GridInfo& g) {
   const size_t npt = x.size();
   size_t nz = 1;
   while (nz < npt && x[nz] == x[0]) ++nz;
@@ -374,11 +388,27 @@ bool grid_from_layout(const std::vector<float>& x, const std::vector<float>& z, 
 }  // namespace
 
 GridInfo infer_grid(const std::vector<float>& x, const std::vector<float>& z) {
-  if (x.empty() || z.empty() || x.size() != z.size()) throw Error("coordinate files are empty or differ in size");
-  auto extent = [](const std::vector<float>& v) {
-    float lo = v[0], hi = v[0];
-    for (float a : v) { lo = std::min(lo, a); hi = std::max(hi, a); }
-    return hi - lo;
+  if (x.size() != z.size()) throw Error("coordinate files are empty or differ in size");
+  return infer_grid(ModelData{x.data(), x.size()}, ModelData{z.data(), z.size()});
+}
+
+GridInfo infer_grid(const ModelData& x, const ModelData& z) {
+  if (x.size() == 0 || z.size() == 0 || x.size() != z.size()) throw Error("coordinate files are empty or differ in size");
+  auto extent = [](const ModelData& v) {
+    // Four independent min/max chains (the compiler vectorises them).
+    float lo[4] = {v[0], v[0], v[0], v[0]}, hi[4] = {v[0], v[0], v[0], v[0]};
+    const size_t n = v.size(), n4 = n / 4 * 4;
+    for (size_t k = 0; k < n4; k += 4)
+      for (int q = 0; q < 4; ++q) {
+        lo[q] = std::min(lo[q], v[k + q]);
+        hi[q] = std::max(hi[q], v[k + q]);
+      }
+    for (size_t k = n4; k < n; ++k) {
+      lo[0] = std::min(lo[0], v[k]);
+      hi[0] = std::max(hi[0], v[k]);
+    }
+    return std::max(std::max(hi[0], hi[1]), std::max(hi[2], hi[3])) -
+           std::min(std::min(lo[0], lo[1]), std::min(lo[2], lo[3]));
   };
   const float lx = extent(x), lz = extent(z);
   if (!(lx > 0.0f) || !(lz > 0.0f)) throw Error("coordinate extents must be positive");
@@ -388,13 +418,16 @@ GridInfo infer_grid(const std::vector<float>& x, const std::vector<float>& z) {
   GridInfo g;
   g.nx = int(std::round(std::sqrt(npt * double(lx) / double(lz))));
   g.nz = int(std::round(std::sqrt(npt * double(lz) / double(lx))));
-  GridInfo lay{};
-  const bool have_layout = grid_from_layout(x, z, lay);
-  if (g.nx >= 2 && g.nz >= 2 && size_t(g.nx) * size_t(g.nz) == x.size() && (!have_layout || lay.nz == g.nz)) {
+  // Accepted when it tiles npt and agrees with the layout's first run of
+  // equal x (nz values, then a new x): O(1), without scanning the layout.
+  if (g.nx >= 2 && g.nz >= 2 && size_t(g.nx) * size_t(g.nz) == x.size() && x[size_t(g.nz) - 1] == x[0] &&
+      x[size_t(g.nz)] != x[0]) {
     g.dx = lx / float(g.nx - 1);
     g.dz = lz / float(g.nz - 1);
     return g;
   }
+  GridInfo lay{};
+  const bool have_layout = grid_from_layout(x, z, lay);
   // Rectangular cells (dx != dz), where the aspect-ratio rule cannot work:
   // the grid read from the coordinate layout.
   if (have_layout) return lay;
@@ -417,10 +450,17 @@ void log_info(const std::string& msg) {
 
 // ---- Solver ----------------------------------------------------------------
 Bytes Solver::lookup(const Vfs& vfs, const std::string& path) const {
+  Bytes hold;
+  const Bytes& b = lookup_ref(vfs, path, hold);
+  return &b == &hold ? std::move(hold) : b;
+}
+
+const Bytes& Solver::lookup_ref(const Vfs& vfs, const std::string& path, Bytes& hold) const {
   auto it = vfs.find(path);
   if (it == vfs.end() && path.rfind("./", 0) == 0) it = vfs.find(path.substr(2));
   if (it != vfs.end()) return it->second;
-  return read_file(path);
+  hold = read_file(path);
+  return hold;
 }
 
 void Solver::write_file(const std::string& path, const Bytes& b) const {
@@ -434,13 +474,22 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
   const std::string model_dir = cfg.has_model_init ? cfg.model_init : cfg.has_model_true ? cfg.model_true : "";
   if (!cfg.has_model_init && !cfg.has_model_true) throw Error("No model path in config");
   const bool spin = cfg.spin;
+  // Model files are read in place from the VFS (files not in the VFS are
+  // read from disk into `held`): no copies of the fields on the host.
+  std::list<Bytes> held;
   auto load = [&](const std::string& name) {
     std::string p = path_join(model_dir, "proc000000_" + name + ".bin");
-    return parse_model_bin(lookup(vfs, p), p);
+    Bytes hold;
+    const Bytes& b = lookup_ref(vfs, p, hold);
+    if (&b == &hold) {
+      held.push_back(std::move(hold));
+      return view_model_bin(held.back(), p);
+    }
+    return view_model_bin(b, p);
   };
-  std::vector<float> rho = load("rho");
+  ModelData rho = load("rho");
   const size_t npt = rho.size();
-  std::vector<float> x = load("x"), z = load("z");
+  ModelData x = load("x"), z = load("z");
   if (x.size() != npt || z.size() != npt) throw Error("coordinate files do not match the model size");
   grid_ = infer_grid(x, z);
   {
@@ -501,8 +550,8 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
   }
   // Remaining model fields (solver.rs:626-638, 661-675): spin models carry
   // lambda/mu directly, the others vp/vs.
-  std::vector<std::pair<ModelField, std::vector<float>>> fields;
-  fields.emplace_back(ModelField::RHO, std::move(rho));
+  std::vector<std::pair<ModelField, ModelData>> fields;
+  fields.emplace_back(ModelField::RHO, rho);
   if (spin) {
     fields.emplace_back(ModelField::LAMBDA, load("lambda"));
     fields.emplace_back(ModelField::MU, load("mu"));
@@ -543,7 +592,7 @@ Solver::Solver(const Config& cfg, const Vfs& vfs) : cfg_(cfg) {
     const bool spin_only = f.first == ModelField::NU || f.first == ModelField::J || f.first == ModelField::MU_C ||
                            f.first == ModelField::NU_C;
     if (spin_only && !cfg.psv) continue;  // the SH system has no micropolar fields
-    sim_->upload_model(f.first, f.second.data());
+    sim_->upload_model(f.first, f.second.data);
   }
   sim_->prepare_model();
 

@@ -73,7 +73,17 @@ struct GridInfo {
   int nx, nz;
   float dx, dz;
 };
+// Float payload of a model file, read in place (the bytes stay owned by the
+// VFS entry or file buffer they come from).
+struct ModelData {
+  const float* data;
+  size_t n;
+  size_t size() const { return n; }
+  float operator[](size_t k) const { return data[k]; }
+};
+ModelData view_model_bin(const Bytes& b, const std::string& what);
 GridInfo infer_grid(const std::vector<float>& x, const std::vector<float>& z);
+GridInfo infer_grid(const ModelData& x, const ModelData& z);
 // round(x / dx) as the reference's saturating `as u32` of f32::round.
 uint32_t grid_index(float coord, float step);
 
@@ -110,6 +120,8 @@ class Solver {
 
  private:
   Bytes lookup(const Vfs& vfs, const std::string& path) const;
+  // The VFS entry itself, or the file read into `hold` when the VFS lacks it.
+  const Bytes& lookup_ref(const Vfs& vfs, const std::string& path, Bytes& hold) const;
   void write_file(const std::string& path, const Bytes& b) const;
 
   Config cfg_;
