@@ -69,3 +69,16 @@ def test_cluster_per_shot_without_graphs():
         one = _run(nx, nz, nt, src, rec, False, isrc=isrc, graphs=0)
         clu = _run(nx, nz, nt, src, rec, True, isrc=isrc, graphs=0)
         assert np.array_equal(one["traces"], clu["traces"]) and np.array_equal(one["vy"], clu["vy"])
+
+
+@pytest.mark.parametrize("nt,snap", [(1, 0), (2, 1), (5, 2)])
+def test_cluster_short_runs(nt, snap):
+    src = [(20, 20, 40.0, 0.0, 0.0)]
+    rec = [(20, 20), (20, 21), (21, 20)]
+    one = _run(40, 44, nt, src, rec, False, snap=snap)
+    clu = _run(40, 44, nt, src, rec, True, snap=snap)
+    assert np.array_equal(one["traces"], clu["traces"])
+    for f in FIELDS:
+        assert np.array_equal(one[f], clu[f]), f
+    if snap:
+        assert np.array_equal(one["snaps"], clu["snaps"])

@@ -108,3 +108,20 @@ def test_two_step_is_refused_where_it_does_not_apply():
     with sw.Sim(40, 40, 10, 10.0, 10.0, 1e-3, sh=True, psv=True) as sim:
         with pytest.raises(sw.SeiswgError):
             sim.set_option("two_step", 1)
+
+
+@pytest.mark.parametrize("nt,snap", [(1, 0), (2, 0), (3, 0), (6, 1), (7, 2)])
+def test_two_step_short_runs_and_dense_snapshots(nt, snap):
+    """Runs shorter than a pair, odd lengths, and snapshots after every step
+    (no pairs at all) or every second step."""
+    src = [(20, 20, 40.0, 0.0, 30.0)]
+    rec = [(20, 20), (20, 21), (21, 20), (19, 19)]
+    one = _run(40, 44, nt, src, rec, False, snap=snap)
+    two = _run(40, 44, nt, src, rec, True, snap=snap)
+    assert np.abs(one["traces"]).max() > 0
+    assert rel_l2(two["traces"], one["traces"]) <= TOL
+    for f in FIELDS:
+        assert rel_l2(two[f], one[f]) <= TOL or np.abs(one[f]).max() == 0, f
+    if snap:
+        assert two["snaps"].shape == one["snaps"].shape
+        assert rel_l2(two["snaps"], one["snaps"]) <= TOL
