@@ -191,3 +191,43 @@ def test_device_misfit_matches_host_misfit(phys):
     assert abs(J_dev - J_host) <= 1e-12 * abs(J_host)
     for p in ("lambda", "mu") if phys == "psv" else ("mu", "buoyancy"):
         assert rel_l2(g_dev[p], g_host[p]) <= 1e-6, p
+
+
+def test_exact_gradient_agrees_with_the_reference_imaging_kernel(tmp_path):
+    """The reference's adjoint example (SH, 12 shots; its K_MU fixture is the
+    WGSL imaging-condition kernel, smoothed with sigma 5) against our exact
+    gradient of the same tapered L2 misfit with respect to mu, smoothed the
+    same way.  The two are different discretisations of the same sensitivity
+    (the reference correlates velocity derivatives every adj_interval steps),
+    so the test asks for the same spatial pattern, not equal values."""
+    import torch
+
+    import seiswg_gb300 as sw
+    from tests.examples import golden, write_example
+
+    d = tmp_path / "adjoint"
+    write_example("adjoint", str(d))
+    g = golden("adjoint")
+    with sw.Solver(sw.Config.load(str(d / "config_true.ini"))) as s:
+        s.run_forward()
+    with sw.Solver(sw.Config.load(str(d / "config.ini"))) as s:
+        sim = s.sim
+        nshot, dt = s.info()["nsrc"], float(np.float32(0.06))
+        sim.gradient_clear()
+        for shot in range(nshot):
+            sim.forward_op(shot, 0)
+            syn = sim.traces()[[1]]
+            obs = np.load(d / "obs_traces" / f"uy_{shot:06d}.npy")[None]
+            _, adj = sw.l2_misfit(syn, obs, dt)
+            sim.backward_op(adj)
+        g_mu = sim.gradient("mu")
+    nx, nz = g_mu.shape
+    src = torch.from_numpy(np.ascontiguousarray(g_mu)).cuda()
+    dst = torch.empty_like(src)
+    sw.smooth_noalloc(src.data_ptr(), dst.data_ptr(), nx, nz, 5.0, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    ours = dst.cpu().numpy().astype(np.float64).ravel()
+    ref = g["fix_proc000000_kmu"].astype(np.float64).ravel()
+    corr = abs(float(ours @ ref / (np.linalg.norm(ours) * np.linalg.norm(ref))))
+    print(f"corr(exact g_mu, reference K_MU) = {corr:.3f}")
+    assert corr > 0.9, corr  # measured 0.948
