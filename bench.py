@@ -501,6 +501,73 @@ def run_secondary(args):
                    gradient_finite=bool(np.isfinite(gvp).all() and np.isfinite(gvs).all()),
                    gradient_vs_peak_cell=[int(v) for v in np.unravel_index(np.argmax(np.abs(gvs)), gvs.shape)],
                    clocks=clk.summary())
+        # Outputs: the vp, vs, rho kernels smoothed with sigma = 5 cells on the device (after the timed region).
+        sig = float(W.extra.get("smooth_sigma", 5.0))
+        smoothed = {}
+        for name, a in (("vp", gvp), ("vs", gvs), ("rho", grho)):
+            src_t = torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+            dst_t = torch.empty_like(src_t)
+            sw.smooth_noalloc(src_t.data_ptr(), dst_t.data_ptr(), W.nx, W.nz, sig,
+                              torch.cuda.current_stream().cuda_stream)
+            smoothed[name] = dst_t.cpu().numpy()
+        out["smoothed_kernels"] = {"sigma_cells": sig, "finite": bool(all(np.isfinite(v).all()
+                                                                             for v in smoothed.values()))}
+        if args.fd_check:
+            # Central finite differences of the misfit on seeded cells among the
+            # strongest vp sensitivities of the illuminated zone: away (40
+            # cells) from the source and receiver lines, whose near field
+            # makes the misfit strongly nonlinear in a single cell, and from
+            # the absorbing edges.
+            rng = np.random.default_rng(1)
+            w = int(W.flags["abs_width"])
+            zone = np.abs(gvp).copy()
+            zone[:, : int(W.sources[0][1]) + 40] = 0.0
+            zone[:, W.nz // 2:] = 0.0
+            zone[: w + 40, :] = 0.0
+            zone[W.nx - w - 40:, :] = 0.0
+            strong = np.argsort(zone.ravel())[-2000:]
+            cells = [int(c) for c in rng.choice(strong, args.fd_check, replace=False)]
+
+            def misfit(vp):
+                sim.upload_model("vp", vp)
+                sim.upload_model("vs", W.model["vs"])
+                sim.upload_model("rho", W.model["rho"])
+                sim.prepare()
+                J = 0.0
+                for s_ in range(len(W.sources)):
+                    sim.forward(s_)
+                    J += sw.l2_misfit(sim.traces()[[0, 2]], obs[s_], W.dt)[0]
+                return J
+
+            errs = []
+            for c in cells:
+                i, j = divmod(c, W.nz)
+                h = args.fd_h * float(W.model["vp"][i, j])
+                vp_p = W.model["vp"].copy()
+                vp_p[i, j] += h
+                vp_m = W.model["vp"].copy()
+                vp_m[i, j] -= h
+                fd = (misfit(vp_p) - misfit(vp_m)) / (2 * h)
+                errs.append(abs(float(gvp[i, j]) - fd) / max(abs(fd), 1e-300))
+            # Directional derivative along the true anomaly's vp shape (many
+            # cells at once).  FP32 rounding of the traces makes the misfit
+            # noisy in the model at small steps (single-cell differences at
+            # this size are limited by it); the directional difference
+            # converges as eps grows (at 512^2: 22 %, 3.5 %, 1.6 %, 0.5 % off
+            # for eps 1e-3, 3e-3, 1e-2, 3e-2, against a gradient that matches
+            # the FP64 oracle's exact gradient to 2e-4).
+            dm = (W.extra["true_model"]["vp"].astype(np.float64) - W.model["vp"]).astype(np.float64)
+            eps = 3e-2
+            jp = misfit((W.model["vp"] + eps * dm).astype(np.float32))
+            jm = misfit((W.model["vp"] - eps * dm).astype(np.float32))
+            fd_dir = (jp - jm) / (2 * eps)
+            g_dir = float((gvp.astype(np.float64) * dm).sum())
+            out["fd_check"] = {"cells": len(cells), "h": f"{100 * args.fd_h:g} % of vp", "max_rel_err": float(max(errs)),
+                               "median_rel_err": float(np.median(errs)),
+                               "zone": "top |g_vp| cells 40+ cells from sources, receivers and absorbing edges",
+                               "directional": {"direction": "true vp anomaly", "eps": eps, "fd": fd_dir,
+                                               "gradient": g_dir,
+                                               "rel_err": abs(g_dir - fd_dir) / max(abs(fd_dir), 1e-300)}}
         sim.close()
         if not args.no_cpu:
             ns = 24
@@ -614,6 +681,8 @@ def main():
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
+    ap.add_argument("--fd-check", type=int, default=0, help="c4: finite-difference check on this many cells")
+    ap.add_argument("--fd-h", type=float, default=1e-3, help="c4: relative vp step of the finite differences")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2 (default) is the headline; the others print their own line")
     args = ap.parse_args()

@@ -231,3 +231,45 @@ def test_exact_gradient_agrees_with_the_reference_imaging_kernel(tmp_path):
     corr = abs(float(ours @ ref / (np.linalg.norm(ours) * np.linalg.norm(ref))))
     print(f"corr(exact g_mu, reference K_MU) = {corr:.3f}")
     assert corr > 0.9, corr  # measured 0.948
+
+
+def test_gradient_matches_fp64_oracle_in_the_c4_geometry():
+    """The C4 set-up (PSV, absorbing on all edges, sources and receivers near
+    the top, Gaussian anomaly in the true model) at 320^2, 600 steps, 2
+    shots: GPU exact gradient against the FP64 oracle's exact gradient, cell
+    by cell and along the anomaly's direction."""
+    import seiswg_gb300 as sw
+    from oracle import oracle as O
+    from seiswg_gb300 import configs
+    import bench
+
+    W = configs.c4_psv_adjoint(n=320, nt=600, shots=2)
+    st = W.make_sim(model=W.extra["true_model"])
+    obs = []
+    for s in range(len(W.sources)):
+        st.forward(s)
+        obs.append(st.traces()[[0, 2]])
+    st.close()
+    sim = W.make_sim()
+    sim.gradient_clear()
+    for s in range(len(W.sources)):
+        sim.forward_op(s, 0)
+        _, adj = sw.l2_misfit(sim.traces()[[0, 2]], obs[s], W.dt)
+        sim.backward_op(adj)
+    g = {p: sim.gradient(p) for p in ("lambda", "mu", "buoyancy")}
+    sim.close()
+    ours = sw.velocity_gradients(g["lambda"], g["mu"], g["buoyancy"], W.model["vp"], W.model["vs"], W.model["rho"])
+    gl = gm = gb = 0.0
+    for s in range(len(W.sources)):
+        o = bench.workload_oracle(W, W.nt, precision=64)
+        o.run_forward(s)
+        syn = np.stack([o.obs("X"), o.obs("Z")])
+        _, adj = O.l2_misfit(syn, obs[s].astype(np.float64), W.dt)
+        a, b, c = o.exact_gradient(adj, s)
+        gl, gm, gb = gl + a, gm + b, gb + c
+    ref = O.lame_to_velocity_gradients(gl, gm, gb, W.model["vp"], W.model["vs"], W.model["rho"])
+    for k, name in enumerate(("vp", "vs", "rho")):
+        assert rel_l2(ours[k], ref[k]) <= 1e-3, name
+    dm = W.extra["true_model"]["vp"].astype(np.float64) - W.model["vp"]
+    d_ours, d_ref = float((ours[0] * dm).sum()), float((ref[0] * dm).sum())
+    assert abs(d_ours - d_ref) <= 1e-3 * abs(d_ref)
