@@ -115,12 +115,15 @@ struct BulkRows {
   const float* src;  // lane issue, lane q < NSEG: segment q's field at row 0, the warp's first column
   int roff;          // lane issue, lane q < NSEG: segment q's row offset
   size_t ld;
-  int col0, ib, lane, nk, cur;
+  int col0, ib, lane, nk;
+  int cur;         // stage of the acquired iteration
+  int nxt;         // stage of the next iteration to acquire
+  uint32_t par;    // barrier phase parity of the next iteration to acquire
   float* buf;      // [S][NSEG][128]
   uint64_t* bar;   // [S]
   __device__ BulkRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int lane_, float* buf_,
                       uint64_t* bar_, int nk_)
-      : s(segs), src(nullptr), roff(0), ld(ld_), col0(c0_ - 4 * lane_), ib(ib_), lane(lane_), nk(nk_), cur(0),
+      : s(segs), src(nullptr), roff(0), ld(ld_), col0(c0_ - 4 * lane_), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0),
         buf(buf_), bar(bar_) {
     if constexpr (kLaneIssue) {
 #pragma unroll
@@ -137,8 +140,9 @@ struct BulkRows {
   // (lane issue; a copy completing before lane 0's arrive only takes the
   // transaction count below zero transiently, which the barrier allows).
   // Called by the issuing lanes only.
-  __device__ __forceinline__ void issue(int k) {
-    const int st = k % S;
+  __device__ __forceinline__ void issue(int k) { issue_at(k, k % S); }
+  // As issue(k), with the stage st = k % S supplied by the caller.
+  __device__ __forceinline__ void issue_at(int k, int st) {
     const int i = ib - 1 + k;
     if constexpr (kLaneIssue) {
       if (lane == 0) mbar_expect_tx(&bar[st], kStageBytes);
@@ -171,16 +175,23 @@ struct BulkRows {
   // segment.
   __device__ __forceinline__ bool acquire(int k) {
     if (KEEP > 0) __syncwarp();  // the previous iteration's seg_back reads are done
+    // Stages advance by one per iteration: cur = k % S, par = (k / S) & 1,
+    // and iteration k + kAhead fills stage (k + kAhead) % S.
+    cur = nxt;
+    const uint32_t ph = par;
+    if (++nxt == S) {
+      nxt = 0;
+      par ^= 1u;
+    }
     if (k + kAhead < nk && issuer()) {
       fence_proxy_async();  // order the warp's reads of the old stage before the copy
-      issue(k + kAhead);
+      issue_at(k + kAhead, cur + kAhead < S ? cur + kAhead : cur + kAhead - S);
     }
-    cur = k % S;
-    return __all_sync(kFull, mbar_wait(&bar[cur], uint32_t(k / S) & 1u));
+    return __all_sync(kFull, mbar_wait(&bar[cur], ph));
   }
   // Segment q of the stage of iteration (current - d), 1 <= d <= KEEP.
   __device__ __forceinline__ f4 seg_back(int q, int d) const {
-    const int st = (cur + S - d) % S;
+    const int st = cur >= d ? cur - d : cur + S - d;
     const float4 t = *reinterpret_cast<const float4*>(buf + (st * NSEG + q) * kSegFloats + 4 * lane);
     f4 r;
     r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;

@@ -72,6 +72,92 @@ __device__ __forceinline__ f4 in_grid(const f4& a, bool row_ok, int valid) {
   return o;
 }
 
+// The fourth-order difference 9 (c - b) - (d - a) before its factor; the
+// two-step march multiplies it by dt/(8 h), folding the time step into the
+// derivative (one multiply fewer per update than dt * (...)).
+__device__ __forceinline__ float d4(float a, float b, float c, float d) { return fmaf(9.0f, c - b, a - d); }
+
+// Differences along the rows (four row registers) and along the columns
+// (neighbour lanes' elements by shuffles), backward- and forward-staggered.
+__device__ __forceinline__ f4 d4_rows(const f4& r0, const f4& r1, const f4& r2, const f4& r3) {
+  f4 o;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) o.v[e] = d4(r0.v[e], r1.v[e], r2.v[e], r3.v[e]);
+  return o;
+}
+__device__ __forceinline__ f4 d4_cols_back(const f4& m) {
+  const float pz = __shfl_up_sync(kFull, m.v[2], 1);
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float nx = __shfl_down_sync(kFull, m.v[0], 1);
+  f4 o;
+  o.v[0] = d4(pz, pw, m.v[0], m.v[1]);
+  o.v[1] = d4(pw, m.v[0], m.v[1], m.v[2]);
+  o.v[2] = d4(m.v[0], m.v[1], m.v[2], m.v[3]);
+  o.v[3] = d4(m.v[1], m.v[2], m.v[3], nx);
+  return o;
+}
+__device__ __forceinline__ f4 d4_cols_fwd(const f4& m) {
+  const float pw = __shfl_up_sync(kFull, m.v[3], 1);
+  const float n0 = __shfl_down_sync(kFull, m.v[0], 1);
+  const float n1 = __shfl_down_sync(kFull, m.v[1], 1);
+  f4 o;
+  o.v[0] = d4(pw, m.v[0], m.v[1], m.v[2]);
+  o.v[1] = d4(m.v[0], m.v[1], m.v[2], m.v[3]);
+  o.v[2] = d4(m.v[1], m.v[2], m.v[3], n0);
+  o.v[3] = d4(m.v[2], m.v[3], n0, n1);
+  return o;
+}
+
+// dt times the stress divergence at a velocity row (div_sxz, fd2d.wgsl:315-316):
+// x from the sigma_xx / sigma_xz rows a0..a3 / b0..b3, z from the current
+// sigma_xz / sigma_zz rows cz / zz.  rx = dt/(8 dx) or 0, rz = dt/(8 dz) or 0.
+__device__ __forceinline__ void vel_div(const f4& a0, const f4& a1, const f4& a2, const f4& a3, const f4& b0,
+                                        const f4& b1, const f4& b2, const f4& b3, const f4& cz, const f4& zz,
+                                        float rx, const f4& rz, f4& dsx, f4& dsz) {
+  const f4 ax = d4_rows(a0, a1, a2, a3), bx = d4_rows(b0, b1, b2, b3);
+  const f4 cb = d4_cols_back(cz), zb = d4_cols_back(zz);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    dsx.v[e] = fmaf(cb.v[e], rz.v[e], ax.v[e] * rx);
+    dsz.v[e] = fmaf(zb.v[e], rz.v[e], bx.v[e] * rx);
+  }
+}
+
+// Stress update of one row from the velocity rows u0..u3 (vx) and w0..w3 (vz)
+// (div_vxz and add_sxz, fd2d.wgsl:378-381, 396-398): sxx += (l+2m) dvx/dx +
+// l dvz/dz, szz += (l+2m) dvz/dz + l dvx/dx, sxz += m (dvx/dz + dvz/dx), the
+// derivatives carrying dt.
+__device__ __forceinline__ void stress(const f4& u0, const f4& u1, const f4& u2, const f4& u3, const f4& w0,
+                                       const f4& w1, const f4& w2, const f4& w3, float rx, const f4& rz,
+                                       const f4& lam, const f4& mu, const f4& xx, const f4& zz, const f4& xz,
+                                       f4& oxx, f4& ozz, f4& oxz) {
+  const f4 ux = d4_rows(u0, u1, u2, u3), wx = d4_rows(w0, w1, w2, w3);
+  const f4 uz = d4_cols_fwd(u1), wz = d4_cols_fwd(w1);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const float l = lam.v[e], m = mu.v[e];
+    const float dvxdx = ux.v[e] * rx, dvzdz = wz.v[e] * rz.v[e];
+    const float l2m = fmaf(2.0f, m, l);
+    oxx.v[e] = fmaf(l2m, dvxdx, fmaf(l, dvzdz, xx.v[e]));
+    ozz.v[e] = fmaf(l2m, dvzdz, fmaf(l, dvxdx, zz.v[e]));
+    oxz.v[e] = fmaf(m, fmaf(uz.v[e], rz.v[e], wx.v[e] * rx), xz.v[e]);
+  }
+}
+
+// Sources of row i (stf_dsxz, fd2d.wgsl:350-351) added to dt times the
+// divergence: dt * f.
+__device__ __forceinline__ void inject_dt(const InjectList& inj, int i, int c0, Cursor& cur, float dt, f4& dsx,
+                                          f4& dsz) {
+  const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
+  f4 fx = z4, fz = z4;
+  inject_at<true, false, true>(inj, i, c0, cur, fx, fx, fz);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    dsx.v[e] = fmaf(dt, fx.v[e], dsx.v[e]);
+    dsz.v[e] = fmaf(dt, fz.v[e], dsz.v[e]);
+  }
+}
+
 // EDGE: derivatives masked by index and level-1 values outside the grid
 // zeroed.  (A second, test-free instantiation for interior warps executed 17 %
 // fewer instructions but ran 8 % slower: two bodies of this size no longer
@@ -107,7 +193,16 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
   rows.start();
 
-  const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+  // Column taper product, and dt folded into the difference factors:
+  // dt/(8 dx) per row (0 where the row derivative is zeroed), dt/(8 dz) per
+  // column (0 where the column derivative is zeroed).
+  f4 tbt;
+  {
+    const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) tbt.v[e] = tb.v[e] * tt.v[e];
+  }
+  const float sx_dt = dt * g.rdx, sz_dt = dt * g.rdz;
   // sigma^n rings, rows i-2..i+1
   f4 xx0 = ld4(at(p.sxx0, i0 - 2)), xx1 = ld4(at(p.sxx0, i0 - 1)), xx2 = ld4(at(p.sxx0, i0)), xx3;
   f4 xz0 = ld4(at(p.sxz0, i0 - 2)), xz1 = ld4(at(p.sxz0, i0 - 1)), xz2 = ld4(at(p.sxz0, i0)), xz3;
@@ -126,17 +221,24 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
   Cursor ci2 = cursor_at(p.inj.list, p.inj.n, m.ib - 1);
   Cursor pi1 = cursor_at(p.probes.list, p.probes.n, m.ib);
   Cursor pi2 = pi1;
-  f4 rzb, rzf;  // 1/(8 dz) where the z-derivative is allowed, else 0
+  f4 rzb, rzf;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
-    rzb.v[e] = (!EDGE || (L.zb & (1 << e))) ? g.rdz : 0.0f;
-    rzf.v[e] = (!EDGE || (L.zf & (1 << e))) ? g.rdz : 0.0f;
+    rzb.v[e] = (!EDGE || (L.zb & (1 << e))) ? sz_dt : 0.0f;
+    rzf.v[e] = (!EDGE || (L.zf & (1 << e))) ? sz_dt : 0.0f;
   }
   // Some lane holds columns outside the grid: level-1 values there are zeroed.
   const bool cols_out = EDGE && !__all_sync(kFull, valid == 0xF);
+  // Row taper of the two velocity rows of the next iteration (i + 1 and
+  // i - 2), loaded one iteration ahead; rows down to -7 and up to nx + 5 lie
+  // in the taper's halo.
+  float bx1_next = __ldg(p.taper_x + i0), bx2_next = __ldg(p.taper_x + i0 - 3);
 
   for (int k = 0; k < nk; ++k) {
     const int i = i0 + k;
+    const float bx1 = bx1_next, bx2 = bx2_next;
+    bx1_next = __ldg(p.taper_x + i + 1);
+    bx2_next = __ldg(p.taper_x + i - 2);
     if (!rows.acquire(k)) {
       flag_timeout(p.err);
       rows.drain(k);
@@ -154,20 +256,15 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
 
     // ---- level 1, velocity of row i (step it)
     {
-      const float bxi = __ldg(p.taper_x + i);
-      const float rx = (!EDGE || (i >= 2 && i < nx - 2)) ? g.rdx : 0.0f;
-      f4 dsx = dx4r(xx0, xx1, xx2, xx3, rx);
-      f4 dsz = dx4r(xz0, xz1, xz2, xz3, rx);
-      const f4 a = dz_back_r(xz2, rzb);
-      const f4 b = dz_back_r(zz2, rzb);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
-      inject_at<true, false, true>(p.inj, i, c0, ci1, dsx, dsx, dsz);
+      const float rx = (!EDGE || (i >= 2 && i < nx - 2)) ? sx_dt : 0.0f;
+      f4 dsx, dsz;
+      vel_div(xx0, xx1, xx2, xx3, xz0, xz1, xz2, xz3, xz2, zz2, rx, rzb, dsx, dsz);
+      if (ci1.row == i) inject_dt(p.inj, i, c0, ci1, dt, dsx, dsz);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const float bb = (bxi * tb.v[e]) * tt.v[e];
-        xd.v[e] = bb * (vxo.v[e] + dt * dsx.v[e] * rho.v[e]);
-        zd.v[e] = bb * (vzo.v[e] + dt * dsz.v[e] * rho.v[e]);
+        const float bb = bx1 * tbt.v[e];
+        xd.v[e] = bb * fmaf(dsx.v[e], rho.v[e], vxo.v[e]);
+        zd.v[e] = bb * fmaf(dsz.v[e], rho.v[e], vzo.v[e]);
       }
       const bool row_ok = (i >= 0 && i < nx);
       if (EDGE && (!row_ok || cols_out)) {
@@ -182,18 +279,8 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     // ---- level 1, stress of row i-2 (step it)
     if (k >= 3) {
       const int r = i - 2;
-      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? g.rdx : 0.0f;
-      const f4 dvxdx = dx4r(xa, xb_, xc, xd, rx);
-      const f4 dvzdx = dx4r(za, zb_, zc, zd, rx);
-      const f4 dvxdz = dz_fwd_r(xb_, rzf);
-      const f4 dvzdz = dz_fwd_r(zb_, rzf);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float l = lam.v[e], mm = mu.v[e];
-        sx3.v[e] = xx0.v[e] + dt * ((l + 2.0f * mm) * dvxdx.v[e] + l * dvzdz.v[e]);
-        sz3.v[e] = zz0.v[e] + dt * ((l + 2.0f * mm) * dvzdz.v[e] + l * dvxdx.v[e]);
-        sq3.v[e] = xz0.v[e] + dt * mm * (dvxdz.v[e] + dvzdx.v[e]);
-      }
+      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sx_dt : 0.0f;
+      stress(xa, xb_, xc, xd, za, zb_, zc, zd, rx, rzf, lam, mu, xx0, zz0, xz0, sx3, sz3, sq3);
       const bool row_ok = (r >= 0 && r < nx);
       if (EDGE && (!row_ok || cols_out)) {
         sx3 = in_grid(sx3, row_ok, valid);
@@ -206,20 +293,15 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     if (k >= 6) {
       const int r = i - 3;
       const f4 rho2 = rows.seg_back(P2_RHO, 3);
-      const float bxr = __ldg(p.taper_x + r);
-      const float rx = (!EDGE || (r >= 2 && r < nx - 2)) ? g.rdx : 0.0f;
-      f4 dsx = dx4r(sx0, sx1, sx2, sx3, rx);
-      f4 dsz = dx4r(sq0, sq1, sq2, sq3, rx);
-      const f4 a = dz_back_r(sq2, rzb);
-      const f4 b = dz_back_r(sz2, rzb);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
-      inject_at<true, false, true>(inj2, r, c0, ci2, dsx, dsx, dsz);
+      const float rx = (!EDGE || (r >= 2 && r < nx - 2)) ? sx_dt : 0.0f;
+      f4 dsx, dsz;
+      vel_div(sx0, sx1, sx2, sx3, sq0, sq1, sq2, sq3, sq2, sz2, rx, rzb, dsx, dsz);
+      if (ci2.row == r) inject_dt(inj2, r, c0, ci2, dt, dsx, dsz);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const float bb = (bxr * tb.v[e]) * tt.v[e];
-        ud.v[e] = bb * (xa.v[e] + dt * dsx.v[e] * rho2.v[e]);
-        wd.v[e] = bb * (za.v[e] + dt * dsz.v[e] * rho2.v[e]);
+        const float bb = bx2 * tbt.v[e];
+        ud.v[e] = bb * fmaf(dsx.v[e], rho2.v[e], xa.v[e]);
+        wd.v[e] = bb * fmaf(dsz.v[e], rho2.v[e], za.v[e]);
       }
       if (r >= m.ib && r < m.ie) {
         st4_masked(at(p.vx1, r), ud, L.own);
@@ -233,19 +315,9 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     if (k >= 9) {
       const int r = i - 5;
       const f4 lam2 = rows.seg_back(P2_LAM, 3), mu2 = rows.seg_back(P2_MU, 3);
-      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? g.rdx : 0.0f;
-      const f4 dvxdx = dx4r(ua, ub, uc, ud, rx);
-      const f4 dvzdx = dx4r(wa, wb, wc, wd, rx);
-      const f4 dvxdz = dz_fwd_r(ub, rzf);
-      const f4 dvzdz = dz_fwd_r(wb, rzf);
+      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sx_dt : 0.0f;
       f4 sxx, szz, sxz;
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float l = lam2.v[e], mm = mu2.v[e];
-        sxx.v[e] = sx0.v[e] + dt * ((l + 2.0f * mm) * dvxdx.v[e] + l * dvzdz.v[e]);
-        szz.v[e] = sz0.v[e] + dt * ((l + 2.0f * mm) * dvzdz.v[e] + l * dvxdx.v[e]);
-        sxz.v[e] = sq0.v[e] + dt * mm * (dvxdz.v[e] + dvzdx.v[e]);
-      }
+      stress(ua, ub, uc, ud, wa, wb, wc, wd, rx, rzf, lam2, mu2, sx0, sz0, sq0, sxx, szz, sxz);
       st4_masked(at(p.sxx1, r), sxx, L.own);
       st4_masked(at(p.szz1, r), szz, L.own);
       st4_masked(at(p.sxz1, r), sxz, L.own);
