@@ -31,13 +31,14 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-warn-spills"]
 # -fmad=false: the forward stencil keeps the reference's separate multiply and
 # add (fd2d.wgsl); those kernels are bandwidth-bound, so this costs nothing.
-# The reverse step (no counterpart in the reference) and the two-step forward
-# kernel are issue-bound, so they contract multiply-add pairs.
-FMAD = {"fd_adjoint.cu": "true", "fd_step2.cu": "true"}
+# The reverse step (no counterpart in the reference), the two-step forward
+# kernel and the spin kernel are issue-bound, so they contract multiply-add
+# pairs.
+FMAD = {"fd_adjoint.cu": "true", "fd_step2.cu": "true", "fd_spin.cu": "true"}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fno-strict-aliasing", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
              f"-I{os.path.join(ROOT, 'include')}"]
 
-CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_cluster.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "noalloc.cu"]
+CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_spin.cu", "fd_cluster.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "noalloc.cu"]
 CXX_SOURCES = ["engine.cpp", "host.cpp", "batch.cpp", "capi.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 

@@ -59,6 +59,10 @@ size_t step_smem_bytes(bool psv, bool spin, int loader);
 int step_blocks_per_sm(bool psv, bool spin, int loader);
 cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s);
 cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s);
+// PSV + spin one-step kernel (fd_spin.cu), reached through the three above.
+size_t spin_step_smem_bytes(int loader);
+int spin_step_blocks_per_sm(int loader);
+cudaError_t launch_psv_spin_step(const PsvStep& p, cudaStream_t s);
 // Whole forward runs of small SH grids in one thread-block cluster
 // (fd_cluster.cu).  State *0 is read at the start and *1 written at the end
 // (they may alias); vy snapshots go to snap + q * snap_stride (padded fields)

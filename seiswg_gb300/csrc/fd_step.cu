@@ -1,4 +1,5 @@
-// fd_step.cu -- fused one-step kernels for the SH, PSV and PSV+spin systems.
+// fd_step.cu -- fused one-step kernels for the SH and PSV systems (PSV +
+// spin: fd_spin.cu).
 //
 // One launch advances the wavefield by one time step: the velocity update
 // (divergence of stress, source injection, Gaussian taper, displacement at
@@ -124,16 +125,12 @@ __device__ __forceinline__ void sh_march(const ShStep& p, int gw, unsigned char*
 }
 
 // --------------------------------------------------------------------------
-// PSV (+ micropolar spin): state vx, vz, sxx, szz, sxz (+ vy_c, syx_c, syy_c,
-// syz_c); material 1/rho, lambda, mu (+ nu, 1/J, mu_c+nu_c).
-// fd2d.wgsl:308-399 and 319-339, 405-445.
+// PSV: state vx, vz, sxx, szz, sxz; material 1/rho, lambda, mu.
+// fd2d.wgsl:308-399.  (PSV + spin: fd_spin.cu.)
 // --------------------------------------------------------------------------
-enum PsvSeg {
-  PV_SXX = 0, PV_SXZ, PV_SZZ, PV_VX, PV_VZ, PV_RHO, PV_LAM, PV_MU, PV_NSEG,
-  PV_SYX = PV_NSEG, PV_SYY, PV_SYZ, PV_VYC, PV_J, PV_NU, PV_MC, PV_NSEG_SPIN
-};
+enum PsvSeg { PV_SXX = 0, PV_SXZ, PV_SZZ, PV_VX, PV_VZ, PV_RHO, PV_LAM, PV_MU, PV_NSEG };
 
-template <bool SPIN, class Loader>
+template <class Loader>
 __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned char* smem) {
   const Geom& g = p.g;
   const March m = march_of(g, gw);
@@ -153,47 +150,17 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
   segs.base[PV_RHO] = p.rho; segs.roff[PV_RHO] = 0;
   segs.base[PV_LAM] = p.lam; segs.roff[PV_LAM] = -2;
   segs.base[PV_MU] = p.mu; segs.roff[PV_MU] = -2;
-  if constexpr (SPIN) {
-    segs.base[PV_SYX] = p.syx0; segs.roff[PV_SYX] = 1;
-    segs.base[PV_SYY] = p.syy0; segs.roff[PV_SYY] = 1;
-    segs.base[PV_SYZ] = p.syz0; segs.roff[PV_SYZ] = 1;
-    segs.base[PV_VYC] = p.vyc0; segs.roff[PV_VYC] = 0;
-    segs.base[PV_J] = p.jm; segs.roff[PV_J] = 0;
-    segs.base[PV_NU] = p.nu; segs.roff[PV_NU] = -2;
-    segs.base[PV_MC] = p.mc; segs.roff[PV_MC] = -2;
-  }
   Loader rows = make_loader<Loader>(segs, g, m, L, smem);
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
-  // Edge rule: the spin kernel folds the masks into the reciprocals (fewer
-  // instructions: it is issue-bound); the plain PSV kernel keeps the selects
-  // (measured 10 % faster that way).
-  const f4 rzb = masked_recip(g.rdz, L.zb), rzf = masked_recip(g.rdz, L.zf);
-  auto DX = [&](const f4& a, const f4& b, const f4& c, const f4& d, float r) {
-    if constexpr (SPIN) return dx4r(a, b, c, d, r);
-    return dx4(a, b, c, d, g.rdx, r != 0.0f);
-  };
-  auto DZB = [&](const f4& a) {
-    if constexpr (SPIN) return dz_back_r(a, rzb);
-    return dz_back(a, g.rdz, L.zb);
-  };
-  auto DZF = [&](const f4& a) {
-    if constexpr (SPIN) return dz_fwd_r(a, rzf);
-    return dz_fwd(a, g.rdz, L.zf);
-  };
+  // Edge rule by selects (dx4 / dz_back / dz_fwd): measured 10 % faster here
+  // than masks folded into the reciprocals.
   f4 xx0 = ld4(at(p.sxx0, m.ib - 3)), xx1 = ld4(at(p.sxx0, m.ib - 2)), xx2 = ld4(at(p.sxx0, m.ib - 1)), xx3;
   f4 xz0 = ld4(at(p.sxz0, m.ib - 3)), xz1 = ld4(at(p.sxz0, m.ib - 2)), xz2 = ld4(at(p.sxz0, m.ib - 1)), xz3;
   f4 zz0 = ld4(at(p.szz0, m.ib - 3)), zz1 = ld4(at(p.szz0, m.ib - 2)), zz2 = ld4(at(p.szz0, m.ib - 1)), zz3;
-  f4 yx0, yx1, yx2, yx3, yy0, yy1, yy2, yy3, yz0, yz1, yz2, yz3;
-  if constexpr (SPIN) {
-    yx0 = ld4(at(p.syx0, m.ib - 3)); yx1 = ld4(at(p.syx0, m.ib - 2)); yx2 = ld4(at(p.syx0, m.ib - 1));
-    yy0 = ld4(at(p.syy0, m.ib - 3)); yy1 = ld4(at(p.syy0, m.ib - 2)); yy2 = ld4(at(p.syy0, m.ib - 1));
-    yz0 = ld4(at(p.syz0, m.ib - 3)); yz1 = ld4(at(p.syz0, m.ib - 2)); yz2 = ld4(at(p.syz0, m.ib - 1));
-  }
   f4 xa, xb_, xc, xd;   // new vx rows i-3..i
   f4 za, zb_, zc, zd;   // new vz rows i-3..i
-  f4 ya, yb, yc, yd;    // new vy_c rows i-3..i
   Cursor ci = cursor_at(p.inj.list, p.inj.n, m.ib - 1);
   Cursor pi = cursor_at(p.probes.list, p.probes.n, m.ib);
   const int nk = m.ie - m.ib + 3;
@@ -213,43 +180,18 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
     const f4 rho = rows.seg(PV_RHO);
     const f4 lam = rows.seg(PV_LAM);
     const f4 mu = rows.seg(PV_MU);
-    f4 vyo, jj, nu, mc;
-    if constexpr (SPIN) {
-      yx3 = rows.seg(PV_SYX);
-      yy3 = rows.seg(PV_SYY);
-      yz3 = rows.seg(PV_SYZ);
-      vyo = rows.seg(PV_VYC);
-      jj = rows.seg(PV_J);
-      nu = rows.seg(PV_NU);
-      mc = rows.seg(PV_MC);
-    }
     rows.release();
     const float bxi = __ldg(p.taper_x + i);
-    const float rxb = (i >= 2 && i < g.nx - 2) ? g.rdx : 0.0f;  // edge rule folded into 1/(8 dx)
+    const bool xok = (i >= 2 && i < g.nx - 2);
 
     // div_sxz (fd2d.wgsl:315-316)
-    f4 dsx = DX(xx0, xx1, xx2, xx3, rxb);
-    f4 dsz = DX(xz0, xz1, xz2, xz3, rxb);
+    f4 dsx = dx4(xx0, xx1, xx2, xx3, g.rdx, xok);
+    f4 dsz = dx4(xz0, xz1, xz2, xz3, g.rdx, xok);
     {
-      const f4 a = DZB(xz2);
-      const f4 b = DZB(zz2);
+      const f4 a = dz_back(xz2, g.rdz, L.zb);
+      const f4 b = dz_back(zz2, g.rdz, L.zb);
 #pragma unroll
       for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
-    }
-    f4 dsy;
-    if constexpr (SPIN) {
-      // div_sy_c (fd2d.wgsl:338), then div_sxyz_c (fd2d.wgsl:326-329)
-      dsy = DX(yx0, yx1, yx2, yx3, rxb);
-      const f4 a = DZB(yz2);
-      const f4 zy = DZB(yy2);
-      const f4 xy = DX(yy0, yy1, yy2, yy3, rxb);
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        dsy.v[e] = dsy.v[e] + a.v[e];
-        dsx.v[e] += zy.v[e];
-        dsz.v[e] += -xy.v[e];
-        dsy.v[e] += 2.0f * yy2.v[e];
-      }
     }
     inject_at<true, false, true>(p.inj, i, c0, ci, dsx, dsx, dsz);  // stf_dsxz, fd2d.wgsl:350-351
 
@@ -260,34 +202,22 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
       xd.v[e] = b * (vxo.v[e] + dt * dsx.v[e] * rho.v[e]);
       zd.v[e] = b * (vzo.v[e] + dt * dsz.v[e] * rho.v[e]);
     }
-    if constexpr (SPIN) {
-      // add_vy_c (fd2d.wgsl:412), jm holding 1/J
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float b = (bxi * tb.v[e]) * tt.v[e];
-        yd.v[e] = b * (vyo.v[e] + dt * dsy.v[e] * jj.v[e]);
-      }
-    }
     if (i >= m.ib && i < m.ie) {
       st4_masked(at(p.vx1, i), xd, L.own);
       st4_masked(at(p.vz1, i), zd, L.own);
-      if constexpr (SPIN) st4_masked(at(p.vyc1, i), yd, L.own);
-      probe_at(p.probes, i, L, pi, dt, [&](int comp, int e) {
-        if constexpr (SPIN)
-          return comp == kProbeVX ? pick4(xd, e) : comp == kProbeVZ ? pick4(zd, e) : pick4(yd, e);
-        return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e);
-      });
+      probe_at(p.probes, i, L, pi, dt,
+               [&](int comp, int e) { return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e); });
     }
 
     // Stress of row r = i-2.
     if (i >= m.ib + 2) {
       const int r = i - 2;
-      const float rxf = (r >= 1 && r < g.nx - 2) ? g.rdx : 0.0f;
+      const bool rok = (r >= 1 && r < g.nx - 2);
       // div_vxz (fd2d.wgsl:378-381)
-      const f4 dvxdx = DX(xa, xb_, xc, xd, rxf);
-      const f4 dvzdx = DX(za, zb_, zc, zd, rxf);
-      const f4 dvxdz = DZF(xb_);
-      const f4 dvzdz = DZF(zb_);
+      const f4 dvxdx = dx4(xa, xb_, xc, xd, g.rdx, rok);
+      const f4 dvzdx = dx4(za, zb_, zc, zd, g.rdx, rok);
+      const f4 dvxdz = dz_fwd(xb_, g.rdz, L.zf);
+      const f4 dvzdz = dz_fwd(zb_, g.rdz, L.zf);
       f4 sxx, szz, sxz;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -300,21 +230,6 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
       st4_masked(at(p.sxx1, r), sxx, L.own);
       st4_masked(at(p.szz1, r), szz, L.own);
       st4_masked(at(p.sxz1, r), sxz, L.own);
-      if constexpr (SPIN) {
-        // div_vy_c (fd2d.wgsl:423-424), add_sy_c (fd2d.wgsl:442-444)
-        const f4 gx = DX(ya, yb, yc, yd, rxf);
-        const f4 gz = DZF(yb);
-        f4 syy, syx, syz;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          syy.v[e] = yy0.v[e] + 2.0f * dt * nu.v[e] * (-yb.v[e] - 0.5f * (dvzdx.v[e] - dvxdz.v[e]));
-          syx.v[e] = yx0.v[e] + dt * mc.v[e] * gx.v[e];
-          syz.v[e] = yz0.v[e] + dt * mc.v[e] * gz.v[e];
-        }
-        st4_masked(at(p.syy1, r), syy, L.own);
-        st4_masked(at(p.syx1, r), syx, L.own);
-        st4_masked(at(p.syz1, r), syz, L.own);
-      }
     }
 
     xa = xb_; xb_ = xc; xc = xd;
@@ -322,12 +237,6 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
     xx0 = xx1; xx1 = xx2; xx2 = xx3;
     xz0 = xz1; xz1 = xz2; xz2 = xz3;
     zz0 = zz1; zz1 = zz2; zz2 = zz3;
-    if constexpr (SPIN) {
-      ya = yb; yb = yc; yc = yd;
-      yx0 = yx1; yx1 = yx2; yx2 = yx3;
-      yy0 = yy1; yy1 = yy2; yy2 = yy3;
-      yz0 = yz1; yz1 = yz2; yz2 = yz3;
-    }
   }
 }
 
@@ -337,10 +246,10 @@ __global__ void __launch_bounds__(kStepWarps * 32) sh_step_kernel(const ShStep p
   sh_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
 }
 
-template <bool SPIN, class Loader>
+template <class Loader>
 __global__ void __launch_bounds__(kStepWarps * 32) psv_step_kernel(const PsvStep p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  psv_march<SPIN, Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+  psv_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
 }
 
 
@@ -357,12 +266,12 @@ cudaError_t launch_sh(const ShStep& p, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-template <bool SPIN, class L>
+template <class L>
 cudaError_t launch_psv(const PsvStep& p, cudaStream_t s) {
   const size_t smem = smem_for<L>();
-  static const cudaError_t attr = prepare_kernel(psv_step_kernel<SPIN, L>, smem);
+  static const cudaError_t attr = prepare_kernel(psv_step_kernel<L>, smem);
   if (attr != cudaSuccess) return attr;
-  psv_step_kernel<SPIN, L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
+  psv_step_kernel<L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
   return cudaGetLastError();
 }
 
@@ -403,7 +312,7 @@ __global__ void __launch_bounds__(kStepWarps * 32) grouped_forward_kernel(const 
     p.inj = inj;
     p.probes = pl;
     p.err = J.err;
-    psv_march<false, BulkL<PV_NSEG>>(p, lw, smem);
+    psv_march<BulkL<PV_NSEG>>(p, lw, smem);
   } else {
     ShStep p{};
     p.g = J.g;
@@ -439,7 +348,7 @@ cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int 
 size_t step_smem_bytes(bool psv, bool spin, int loader) {
   if (loader != kLoaderBulk) return 0;
   if (!psv) return smem_for<BulkL<SH_NSEG>>();
-  return spin ? smem_for<BulkL<PV_NSEG_SPIN>>() : smem_for<BulkL<PV_NSEG>>();
+  return spin ? spin_step_smem_bytes(loader) : smem_for<BulkL<PV_NSEG>>();
 }
 
 int step_blocks_per_sm(bool psv, bool spin, int loader) {
@@ -453,19 +362,12 @@ int step_blocks_per_sm(bool psv, bool spin, int loader) {
                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step_kernel<BulkL<SH_NSEG>>, threads, smem))
             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step_kernel<DirectL<SH_NSEG>>, threads, smem);
   } else if (spin) {
-    e = loader == kLoaderBulk
-            ? (prepare_kernel(psv_step_kernel<true, BulkL<PV_NSEG_SPIN>>, smem),
-               cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<true, BulkL<PV_NSEG_SPIN>>,
-                                                             threads, smem))
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<true, DirectL<PV_NSEG_SPIN>>,
-                                                            threads, smem);
+    return spin_step_blocks_per_sm(loader);
   } else {
     e = loader == kLoaderBulk
-            ? (prepare_kernel(psv_step_kernel<false, BulkL<PV_NSEG>>, smem),
-               cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<false, BulkL<PV_NSEG>>, threads,
-                                                             smem))
-            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<false, DirectL<PV_NSEG>>, threads,
-                                                            smem);
+            ? (prepare_kernel(psv_step_kernel<BulkL<PV_NSEG>>, smem),
+               cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<BulkL<PV_NSEG>>, threads, smem))
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, psv_step_kernel<DirectL<PV_NSEG>>, threads, smem);
   }
   return e == cudaSuccess ? n : 0;
 }
@@ -477,12 +379,9 @@ cudaError_t launch_sh_step(const ShStep& p, cudaStream_t s) {
 }
 
 cudaError_t launch_psv_step(const PsvStep& p, bool spin, cudaStream_t s) {
-  if (spin) {
-    if (p.g.loader == kLoaderBulk) return launch_psv<true, BulkL<PV_NSEG_SPIN>>(p, s);
-    return launch_psv<true, DirectL<PV_NSEG_SPIN>>(p, s);
-  }
-  if (p.g.loader == kLoaderBulk) return launch_psv<false, BulkL<PV_NSEG>>(p, s);
-  return launch_psv<false, DirectL<PV_NSEG>>(p, s);
+  if (spin) return launch_psv_spin_step(p, s);
+  if (p.g.loader == kLoaderBulk) return launch_psv<BulkL<PV_NSEG>>(p, s);
+  return launch_psv<DirectL<PV_NSEG>>(p, s);
 }
 
 }  // namespace seiswg
