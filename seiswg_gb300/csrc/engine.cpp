@@ -644,7 +644,8 @@ void Sim::run_forward(int isrc, Snapshots* snaps) {
   // Small SH grids: the whole run on chip in one thread-block cluster.
   bool only_vy = true;
   for (StateField f : (snaps ? snaps->fields : std::vector<StateField>{})) only_vy = only_vy && f == StateField::VY;
-  if (use_cluster_ && d_.sh && !d_.psv && only_vy && inj.n <= 64 && d_.nt > 0) {
+  if (use_cluster_ && d_.sh && !d_.psv && only_vy && inj.n <= kClusterSources && probe_split_ <= kClusterProbes &&
+      d_.nt > 0) {
     if (cluster_ctas_ < 0) cluster_ctas_ = sh_cluster_ctas(d_.nx, d_.nz);
     if (cluster_ctas_ > 0) {
       ShCluster p{};

@@ -68,6 +68,8 @@ cudaError_t launch_psv_spin_step(const PsvStep& p, cudaStream_t s);
 // (they may alias); vy snapshots go to snap + q * snap_stride (padded fields)
 // for q = snap_first, ... at every step it > 0 with it % snap_every == 0.
 constexpr int kClusterThreads = 1024;
+constexpr int kClusterSources = 64;    // injections per run the cluster kernel takes
+constexpr int kClusterProbes = 4096;   // probes per run the cluster kernel takes
 struct ShCluster {
   int nx, nz, ld, rows;  // rows per CTA
   int it0, it1;          // steps [it0, it1)
