@@ -21,8 +21,7 @@
 //
 // Algorithmic bytes per cell-update (PSV): forward state 5 + adjoint state
 // 5 r+w + model 3 + gradients 3 r+w = 96 B (SH: 3 + 3 r+w + 2 + 2 r+w = 60 B).
-#include "fd_kernels.h"
-#include "fd_pipe.cuh"
+#include "fd_march.cuh"
 
 namespace seiswg {
 
@@ -99,27 +98,6 @@ __device__ __forceinline__ AMarch amarch(const Geom& g, int gw) {
   m.ib = m.chunk * g.lx;
   m.ie = min(g.nx, m.ib + g.lx);
   return m;
-}
-
-template <bool X, bool Y, bool Z>
-__device__ __forceinline__ void add_row(const InjectList& inj, int i, int c0, int& ci, f4& ax, f4& ay, f4& az) {
-  while (ci < inj.n && __ldg(&inj.list[ci].i) == i) {
-    const int e = __ldg(&inj.list[ci].j) - c0;
-    if (e >= 0 && e < 4) {
-      const size_t o = size_t(__ldg(&inj.list[ci].row)) * inj.nt + inj.it;
-      const float vx = X ? __ldg(&inj.val_x[o]) : 0.0f;
-      const float vy = Y ? __ldg(&inj.val_y[o]) : 0.0f;
-      const float vz = Z ? __ldg(&inj.val_z[o]) : 0.0f;
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (q == e) {
-          if (X) ax.v[q] += vx;
-          if (Y) ay.v[q] += vy;
-          if (Z) az.v[q] += vz;
-        }
-    }
-    ++ci;
-  }
 }
 
 template <class Loader>
@@ -236,12 +214,17 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
   f4 za, zb, zc, zd;   // recomputed forward vz^{n+1}
   f4 qxa, qxb, qxc, qxd;  // q = dt B w (x), rows i-3..i
   f4 qza, qzb, qzc, qzd;  // q (z)
-  int ci = lower_row(p.src.list, p.src.n, m.ib - 1);
-  int ri = lower_row(p.rec.list, p.rec.n, m.ib - 1);
+  // Source and receiver list cursors; the row taper one iteration ahead
+  // (rows up to ie + 2 lie in the taper's halo).
+  Cursor cs = cursor_at(p.src.list, p.src.n, m.ib - 1);
+  Cursor cr = cursor_at(p.rec.list, p.rec.n, m.ib - 1);
   const int nk = m.ie - m.ib + 3;
+  float bx_next = __ldg(p.taper_x + m.ib - 1);
 
   for (int k = 0; k < nk; ++k) {
     const int i = m.ib - 1 + k;
+    const float bxi = bx_next;
+    bx_next = __ldg(p.taper_x + i + 1);
     if (!rows.acquire(k)) {
       flag(p.err);
       rows.drain(k);
@@ -266,7 +249,6 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
     f4 gb = rows.seg(PA_GB);
     f4 gl = rows.seg(PA_GL), gm = rows.seg(PA_GM);
     rows.release();
-    const float bxi = __ldg(p.taper_x + i);
     const float rxb = mask_back(i, g.nx) ? g.rdx : 0.0f;
 
     // Forward recompute: D- sigma^n + f^n and v^{n+1} of row i.
@@ -278,7 +260,7 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
 #pragma unroll
       for (int e = 0; e < 4; ++e) { dsx.v[e] = dsx.v[e] + a.v[e]; dsz.v[e] = dsz.v[e] + b.v[e]; }
     }
-    add_row<true, false, true>(p.src, i, c0, ci, dsx, dsx, dsz);
+    inject_at<true, false, true>(p.src, i, c0, cs, dsx, dsx, dsz);
     f4 bb;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -301,7 +283,7 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
       }
       const f4 tq = dzT_back(masked(eq2, L.zf), g.rdz);
       const f4 tz = dzT_back(masked(ezc, L.zf), g.rdz);
-      add_row<true, false, true>(p.rec, i, c0, ri, wx, wx, wz);
+      inject_at<true, false, true>(p.rec, i, c0, cr, wx, wx, wz);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         wx.v[e] = bb.v[e] * (wx.v[e] + tx.v[e] + tq.v[e]);
@@ -422,12 +404,15 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
   f4 ezc, ezn = times(ld4(at(p.bzy0, m.ib - 1)), ld4(at(p.mu, m.ib - 1)));
   f4 na, nb, nc, nd;
   f4 qa, qb, qc, qd;
-  int ci = lower_row(p.src.list, p.src.n, m.ib - 1);
-  int ri = lower_row(p.rec.list, p.rec.n, m.ib - 1);
+  Cursor cs = cursor_at(p.src.list, p.src.n, m.ib - 1);
+  Cursor cr = cursor_at(p.rec.list, p.rec.n, m.ib - 1);
   const int nk = m.ie - m.ib + 3;
+  float bx_next = __ldg(p.taper_x + m.ib - 1);
 
   for (int k = 0; k < nk; ++k) {
     const int i = m.ib - 1 + k;
+    const float bxi = bx_next;
+    bx_next = __ldg(p.taper_x + i + 1);
     if (!rows.acquire(k)) {
       flag(p.err);
       rows.drain(k);
@@ -445,7 +430,6 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
     const f4 buoy = rows.seg(SA_B);
     f4 gb = rows.seg(SA_GB), gm = rows.seg(SA_GM);
     rows.release();
-    const float bxi = __ldg(p.taper_x + i);
 
     f4 ds = dx4r(xy0, xy1, xy2, xy3, mask_back(i, g.nx) ? g.rdx : 0.0f);
     {
@@ -453,7 +437,7 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
 #pragma unroll
       for (int e = 0; e < 4; ++e) ds.v[e] = ds.v[e] + a.v[e];
     }
-    add_row<false, true, false>(p.src, i, c0, ci, ds, ds, ds);
+    inject_at<false, true, false>(p.src, i, c0, cs, ds, ds, ds);
     f4 bb;
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
@@ -467,7 +451,7 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
                         ? dxT(ex0, ex1, ex2, ex3, g.rdx)
                         : dxT(scaled(ex0, m0), scaled(ex1, m1), scaled(ex2, m2), scaled(ex3, m3), g.rdx);
       const f4 tz = dzT_back(masked(ezc, L.zf), g.rdz);
-      add_row<false, true, false>(p.rec, i, c0, ri, w, w, w);
+      inject_at<false, true, false>(p.rec, i, c0, cr, w, w, w);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         w.v[e] = bb.v[e] * (w.v[e] + tx.v[e] + tz.v[e]);
