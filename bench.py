@@ -60,10 +60,10 @@ def make_workload(nx=4096, nz=4096, nt=4000, seed=0):
                 rec_i=rec_i, rec_j=rec_j)
 
 
-def workload_config(W, nt):
-    return {"workload": f"PSV forward, heterogeneous {W['nx']}x{W['nz']}, nt={nt}",
+def workload_config(W, nt, physics="psv"):
+    return {"workload": f"{physics.upper()} forward, heterogeneous {W['nx']}x{W['nz']}, nt={nt}",
             "grid": [W["nx"], W["nz"]], "nt": nt, "dx_m": W["dx"], "dt_s": W["dt"],
-            "physics": "psv", "abs_width": W["w"], "receivers": int(W["rec_i"].size),
+            "physics": physics, "abs_width": W["w"], "receivers": int(W["rec_i"].size),
             "source": "Ricker f0=15 Hz t0=0.1 s angle 90 at (nx/2, w+10)",
             "model": "vp=2000+600*depth_km, Gaussian-filtered (sigma 20) +-5% perturbation, seed 0; "
                      "vs=vp/sqrt(3); rho=310*vp^0.25",
@@ -152,12 +152,12 @@ def _traffic(kernel, nx, nz):
     return None
 
 
-def cpu_oracle_rate(W, nt_sample):
+def cpu_oracle_rate(W, nt_sample, physics="psv"):
     """FP32 oracle (reference operation order, OpenMP) on the full grid for
     nt_sample steps; returns (Gcell/s, seconds, threads)."""
     from oracle import oracle as O
 
-    s = O.Setup(W["nx"], W["nz"], nt_sample, W["dx"], W["dz"], W["dt"], sh=False, psv=True,
+    s = O.Setup(W["nx"], W["nz"], nt_sample, W["dx"], W["dz"], W["dt"], sh=physics == "sh", psv=physics == "psv",
                 abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=W["w"],
                 abs_alpha=W["alpha"])
     sr = W["src"]
@@ -231,7 +231,7 @@ def run_reference(args, rank):
     for _ in range(args.warmup):
         cpu_oracle_rate(W, 2)
     for _ in range(args.steps):
-        r, dtm, thr = cpu_oracle_rate(W, args.ref_sample)
+        r, dtm, thr = cpu_oracle_rate(W, args.ref_sample, phys)
         rates.append(r)
     val = float(np.median(rates))
     line = {
@@ -264,15 +264,16 @@ def run_ours(args, rank, world):
     stf = sw.ricker(nt, W["dt"], sr["f0"], sr["t0"], sr["ang"], sr["amp"])[:, None, :]
 
     # ---- device-resident throughput --------------------------------------
-    sim = sw.Sim(nx, nz, nt, W["dx"], W["dz"], W["dt"], sh=False, psv=True, abs_left=True, abs_right=True,
-                 abs_bottom=True, abs_top=True, abs_width=W["w"], abs_alpha=W["alpha"])
+    phys = args.physics
+    sim = sw.Sim(nx, nz, nt, W["dx"], W["dz"], W["dt"], sh=phys == "sh", psv=phys == "psv", abs_left=True,
+                 abs_right=True, abs_bottom=True, abs_top=True, abs_width=W["w"], abs_alpha=W["alpha"])
     if args.chunk_rows:
         sim.set_option("chunk_rows", args.chunk_rows)
-    if args.two_step >= 0:
+    if args.two_step >= 0 and phys == "psv":
         sim.set_option("two_step", args.two_step)
     if args.two_step_rows:
         sim.set_option("two_step_rows", args.two_step_rows)
-    two_step = args.two_step != 0   # the engine's default for PSV alone is on
+    two_step = args.two_step != 0 and phys == "psv"   # the engine's default for PSV alone is on
     sim.upload_model("vp", W["vp"])
     sim.upload_model("vs", W["vs"])
     sim.upload_model("rho", W["rho"])
@@ -317,10 +318,10 @@ def run_ours(args, rank, world):
     # Algorithmic bytes: 52 B per cell-update, the one-step scheme's minimum;
     # the two-step kernel moves about half of that (traffic), so its fraction
     # can exceed 1.
-    kernel = "psv_step2_kernel" if two_step else "psv_step_kernel"
+    kernel = "psv_step2_kernel" if two_step else f"{phys}_step_kernel"
     per_launch = 2 if two_step else 1
     launch_s = ms_per_step / 1e3 / (nt / per_launch)
-    achieved = BYTES_PER_CELL["psv"] * per_launch * nx * nz / launch_s / 1e9
+    achieved = BYTES_PER_CELL[phys] * per_launch * nx * nz / launch_s / 1e9
     peak, peak_kind = _peaks()
     traffic = _traffic(kernel, nx, nz)
 
@@ -335,7 +336,7 @@ def run_ours(args, rank, world):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        r, dtm, thr = cpu_oracle_rate(W, args.ref_sample)
+        r, dtm, thr = cpu_oracle_rate(W, args.ref_sample, phys)
         cpu = {"value": r, "unit": METRIC, "cores": thr, "kind": "port",
                "sample": f"full {nx}x{nz} grid, {args.ref_sample} of {nt} steps (FP32 oracle restating "
                          f"fd2d.wgsl, OpenMP), {dtm:.1f} s"}
@@ -344,10 +345,10 @@ def run_ours(args, rank, world):
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(W, nt),
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(W, nt, phys),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": kernel, "bytes_per_cell_update": BYTES_PER_CELL["psv"],
+                         "kernel": kernel, "bytes_per_cell_update": BYTES_PER_CELL[phys],
                          "cell_updates_per_launch": per_launch * nx * nz, "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
@@ -382,13 +383,15 @@ def run_e2e(args, W, stf):
                           f"{sr['amp']}\n").encode()
     vfs["stations.dat"] = "".join(f"{i * W['dx']} {j * W['dz']}\n" for i, j in
                                   zip(W["rec_i"], W["rec_j"])).encode()
-    ini = (f"[workflow]\nmode = forward\n[solver]\nsh = no\npsv = yes\nnt = {nt}\ndt = {W['dt']!r}\n"
+    sh = args.physics == "sh"
+    ini = (f"[workflow]\nmode = forward\n[solver]\nsh = {'yes' if sh else 'no'}\npsv = {'no' if sh else 'yes'}\n"
+           f"nt = {nt}\ndt = {W['dt']!r}\n"
            f"abs_top = yes\nabs_bottom = yes\nabs_left = yes\nabs_right = yes\nabs_width = {W['w']}\n"
            f"abs_alpha = {W['alpha']}\ncombine_sources = yes\n[path]\noutput = out\nmodel_init = m\n"
            f"sources = sources.dat\nstations = stations.dat\n")
     cfg = sw.Config.from_str(ini, "")
     h2d = 3 * nx * nz * 4 + 3 * nt * 4 + 2 * 256 * 4
-    d2h = 5 * 256 * nt * 4
+    d2h = 5 * 256 * nt * 4  # the five trace components of the recorded receivers
 
     def one():
         s = sw.Solver(cfg, vfs, write_files=False)
@@ -401,7 +404,7 @@ def run_e2e(args, W, stf):
     for _ in range(args.e2e_steps):
         out = one()
     sec = time.perf_counter() - t0
-    assert any(k.endswith("ux_000000.npy") for k in out)
+    assert any(k.endswith(("uy_000000.npy" if sh else "ux_000000.npy")) for k in out)
     return {"seconds": sec, "h2d": h2d, "d2h": d2h}
 
 
@@ -674,6 +677,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=600, help="oracle steps in the CPU sample (~10 s)")
     ap.add_argument("--chunk-rows", type=int, default=0)
     ap.add_argument("--grid", type=int, default=4096, help="grid edge (4096 = the headline workload)")
+    ap.add_argument("--physics", default="psv", choices=["psv", "sh"],
+                    help="c2 grid and model with the SH system instead (the SH step kernel at scale)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--autotune", action="store_true", help="empirical loader/chunk tuning before timing")
