@@ -269,11 +269,11 @@ def run_ours(args, rank, world):
                  abs_right=True, abs_bottom=True, abs_top=True, abs_width=W["w"], abs_alpha=W["alpha"])
     if args.chunk_rows:
         sim.set_option("chunk_rows", args.chunk_rows)
-    if args.two_step >= 0 and phys == "psv":
+    if args.two_step >= 0:
         sim.set_option("two_step", args.two_step)
     if args.two_step_rows:
         sim.set_option("two_step_rows", args.two_step_rows)
-    two_step = args.two_step != 0 and phys == "psv"   # the engine's default for PSV alone is on
+    two_step = args.two_step != 0   # the engine's default for PSV alone and SH alone is on
     sim.upload_model("vp", W["vp"])
     sim.upload_model("vs", W["vs"])
     sim.upload_model("rho", W["rho"])
@@ -315,10 +315,10 @@ def run_ours(args, rank, world):
     # steps (two-step kernel, nt even and no snapshots here); its average
     # duration is the timed region over its launches (memsets and the trace
     # kernel are < 0.1 % of it; see the launch lists under profiles/).
-    # Algorithmic bytes: 52 B per cell-update, the one-step scheme's minimum;
-    # the two-step kernel moves about half of that (traffic), so its fraction
-    # can exceed 1.
-    kernel = "psv_step2_kernel" if two_step else f"{phys}_step_kernel"
+    # Algorithmic bytes: 52 B (PSV) or 32 B (SH) per cell-update, the one-step
+    # scheme's minimum; the two-step kernels move about half of that
+    # (traffic), so their fraction can exceed 1.
+    kernel = f"{phys}_step2_kernel" if two_step else f"{phys}_step_kernel"
     per_launch = 2 if two_step else 1
     launch_s = ms_per_step / 1e3 / (nt / per_launch)
     achieved = BYTES_PER_CELL[phys] * per_launch * nx * nz / launch_s / 1e9

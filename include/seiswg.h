@@ -169,13 +169,13 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * occupancy model), "loader" (0: plain loads, 1: TMA bulk-copy row pipeline,
  * the default), "autotune" (value = steps timed per candidate: picks the
  * fastest loader and chunk rows for this problem), "two_step" (0/1: forward
- * runs advance two time steps per launch; PSV without SH or spin only, and
- * on by default there; multiply-add contraction, so results match the
- * one-step kernel to rounding), "two_step_rows" (rows per march of the
- * two-step kernel; 0: its occupancy model), "cluster" (0/1: SH grids whose
- * state and material fit one thread-block cluster's shared memory run each
- * forward pass in one launch with the wavefield on chip; default on; results
- * are the one-step kernel's bits). */
+ * runs advance two time steps per launch; PSV alone (no SH, no spin) or SH
+ * alone, and on by default there; multiply-add contraction, so results
+ * match the one-step kernel to rounding), "two_step_rows" (rows per march of
+ * the two-step kernel; 0: its occupancy model), "cluster" (0/1: SH grids
+ * whose state and material fit one thread-block cluster's shared memory run
+ * each forward pass in one launch with the wavefield on chip; default on;
+ * results are the one-step kernel's bits). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */
@@ -199,13 +199,14 @@ int seiswg_batch_create(seiswg_sim* const* sims, const float* const* obs, int32_
                         void* stream, seiswg_batch** out);
 int seiswg_batch_run(seiswg_batch* batch);
 /* key "chunk_rows": rows per warp chunk of every job (0: each problem's own
- * chunk model); "two_step" (0/1): PSV jobs whose problem runs two steps per
- * launch record their forward pass that way (default 1); "autotune": tries
+ * chunk model); "two_step" (0/1): jobs whose problem runs two steps per
+ * launch (PSV alone, SH alone) record their forward pass that way (default
+ * 1); "autotune": tries
  * chunk rows 0, 16, 32, 48, 64, 96 and 128 with and without two-step
  * recording, timing `value` slots of the recording pass and of the reverse
  * sweep each, and keeps the fastest.  Each drops the captured graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
-/* The chunk rows in use (0: each problem's own chunk model), and whether PSV
+/* The chunk rows in use (0: each problem's own chunk model), and whether
  * jobs record two steps per launch. */
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);
 int32_t seiswg_batch_two_step(const seiswg_batch* batch);

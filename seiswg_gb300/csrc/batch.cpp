@@ -9,7 +9,7 @@ namespace seiswg {
 
 namespace {
 
-enum Kind { kFwdSh = 0, kFwdPsv, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
+enum Kind { kFwdSh = 0, kFwdPsv, kFwd2Sh, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
 
 struct HostOp {
   int kind, it, a, b, flags;
@@ -210,7 +210,8 @@ void Batch::build_schedule() {
     auto seg = [&](int m) { return ncp + m - 1; };  // interval buffer, m >= 1
     auto pp = [&](int t) { return ncp + k - 1 + (t & 1); };
     const int fwd = j.psv ? kFwdPsv : kFwdSh, adj = j.psv ? kAdjPsv : kAdjSh;
-    const bool two = two_step_ && j.psv && descs_[q].g2.lx > 0;
+    const bool two = two_step_ && descs_[q].g2.lx > 0;
+    const int fwd2 = j.psv ? kFwd2Psv : kFwd2Sh;
     std::vector<HostOp>& L = lists[q];
     // Recording pass: a step that ends on a checkpoint writes the checkpoint's
     // slot, the others alternate between the two ping-pong slots; two steps
@@ -226,7 +227,7 @@ void Batch::build_schedule() {
         dst = pp(ppi);
         ppi ^= 1;
       }
-      L.push_back(HostOp{n == 2 ? int(kFwd2Psv) : fwd, t, cur, dst, 1});
+      L.push_back(HostOp{n == 2 ? fwd2 : fwd, t, cur, dst, 1});
       cur = dst;
       t = e;
     }
@@ -252,7 +253,7 @@ void Batch::build_schedule() {
       for (size_t q = 0; q < jobs_.size(); ++q) {
         if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
         const HostOp& h = lists[q][t];
-        const Geom& g = kind == kFwd2Psv ? descs_[q].g2 : descs_[q].g;
+        const Geom& g = (kind == kFwd2Psv || kind == kFwd2Sh) ? descs_[q].g2 : descs_[q].g;
         all.push_back(GroupOp{int(q), h.it, h.a, h.b, h.flags, l.warps});
         l.warps += (kind == kMisfit) ? 1 : g.nstrips * g.nchunks;
         ++l.count;
@@ -302,7 +303,8 @@ void Batch::enqueue_slots(int t0, int t1) {
       switch (l.kind) {
         case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
         case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
-        case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, stream_)); break;
+        case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
+        case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
         case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
         case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
         case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, stream_)); break;

@@ -97,7 +97,7 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   geom_.loader = kLoaderBulk;
   set_chunk_rows(model_chunk_rows());
   // PSV alone runs its forward passes two steps per launch by default.
-  if (d.psv && !d.sh && !d.spin) set_two_step(true);
+  if ((d.psv && !d.sh && !d.spin) || (d.sh && !d.psv)) set_two_step(true);
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
   use_graphs_ = (size_t(d.nx) * d.nz <= (size_t(1) << 20));
@@ -156,7 +156,8 @@ int Sim::chunk_rows_for(int per_sm, int strip_cols, int extra_rows) const {
 }
 
 void Sim::set_two_step(bool on) {
-  if (on && !(d_.psv && !d_.sh && !d_.spin)) throw std::invalid_argument("the two-step kernel is PSV only (no SH, no spin)");
+  if (on && !((d_.psv && !d_.sh && !d_.spin) || (d_.sh && !d_.psv)))
+    throw std::invalid_argument("the two-step kernels are for PSV alone or SH alone (no spin, not both)");
   if (on && geom2_.lx == 0) set_two_step_rows(0);
   two_step_ = on;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
@@ -166,7 +167,8 @@ void Sim::set_two_step(bool on) {
 void Sim::set_two_step_rows(int lx) {
   geom2_ = geom_;
   geom2_.nstrips = (d_.nz + kStripCols2 - 1) / kStripCols2;
-  geom2_.lx = lx > 0 ? std::max(lx, 4) : chunk_rows_for(step2_blocks_per_sm(), kStripCols2, 11);
+  geom2_.lx = lx > 0 ? std::max(lx, 4)
+                     : chunk_rows_for(d_.sh ? sh_step2_blocks_per_sm() : step2_blocks_per_sm(), kStripCols2, 11);
   geom2_.nchunks = (d_.nx + geom2_.lx - 1) / geom2_.lx;
   geom2_.loader = kLoaderBulk;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
@@ -186,6 +188,23 @@ int Sim::final_buffer(int every) const {
 
 void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList& inj_in,
                         const ProbeList& probes_in) {
+  if (d_.sh) {
+    ShStep p{};
+    p.g = geom2_;
+    p.vy0 = a.vy; p.sxy0 = a.sxy; p.szy0 = a.szy;
+    p.vy1 = o.vy; p.sxy1 = o.sxy; p.szy1 = o.szy;
+    p.rho = rho_; p.mu = mu_;
+    p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+    p.inj = inj_in;
+    p.inj.it = it;
+    p.probes = probes_in;
+    p.probes.it = it;
+    p.err = err_;
+    if (probes_in.n) p.probes.n = probe_split_;
+    SW_CUDA(launch_sh_step2(p, stream_));
+    ++launches_;
+    return;
+  }
   PsvStep p{};
   p.g = geom2_;
   p.vx0 = a.vx; p.vz0 = a.vz; p.sxx0 = a.sxx; p.szz0 = a.szz; p.sxz0 = a.sxz;

@@ -94,6 +94,9 @@ cudaError_t launch_sh_cluster(const ShCluster& p, int ctas, cudaStream_t s);
 cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s);
 size_t step2_smem_bytes();
 int step2_blocks_per_sm();
+// Two SH time steps per launch (fd_step2.cu), same decomposition as the PSV one.
+cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s);
+int sh_step2_blocks_per_sm();
 
 // ---- exact discrete adjoint (fd_adjoint.cu) --------------------------------
 struct PsvAdjoint {
@@ -197,8 +200,10 @@ cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int 
                                    cudaStream_t s);
 cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
                                    cudaStream_t s);
-// Two PSV steps (op.it, op.it + 1) of every op's job, with the jobs' g2.
-cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, cudaStream_t s);
+// Two PSV (psv) or SH steps (op.it, op.it + 1) of every op's job, with the
+// jobs' g2.
+cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
+                                    cudaStream_t s);
 // Misfit of one problem's assembled traces against obs [ncomp][nrec][nt];
 // writes J per trace and the adjoint-source table dt * U.
 cudaError_t launch_sim_misfit(const float* syn, const float* obs, float* u_tab, double* J, int nrec, int nt,

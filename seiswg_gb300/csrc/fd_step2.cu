@@ -1,4 +1,4 @@
-// fd_step2.cu -- two PSV time steps per launch (temporal blocking).
+// fd_step2.cu -- two PSV or SH time steps per launch (temporal blocking).
 //
 // Built with multiply-add contraction (the one-step kernels keep the
 // reference's separate multiply and add): the two-step march is bound by
@@ -295,6 +295,197 @@ __device__ __forceinline__ void psv2_march(const PsvStep& p, int gw, unsigned ch
   psv2_body<Loader, true>(p, m, L, valid, smem);
 }
 
+// --------------------------------------------------------------------------
+// SH, two time steps per pass: the PSV scheme above with the SH update
+// (fd2d.wgsl:242-301): level 1 velocity of row i and stress of row i-2,
+// level 2 velocity of row i-3 and stress of row i-5; 16 B of HBM traffic per
+// cell-update instead of 32.
+// --------------------------------------------------------------------------
+enum Sh2Seg {
+  S2_SXY = 0, S2_SZY,  // sigma^n, row i+1
+  S2_VY,               // v^n, row i
+  S2_RHO, S2_MU,       // 1/rho row i, mu row i-2
+  S2_NSEG
+};
+
+// Six stages: two rows in flight, the last three iterations kept (level 2
+// reads 1/rho of row i-3 and mu of row i-5 from them).
+struct ShBulk2 : BulkRows<S2_NSEG, 6, false, 3> {
+  using SegsT = Segs<S2_NSEG>;
+  using BulkRows<S2_NSEG, 6, false, 3>::BulkRows;
+};
+
+// Sources of row i (stf_dsy, fd2d.wgsl:248-266) added to dt times the
+// divergence.
+__device__ __forceinline__ void inject_dt_y(const InjectList& inj, int i, int c0, Cursor& cur, float dt, f4& ds) {
+  const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
+  f4 fy = z4;
+  inject_at<false, true, false>(inj, i, c0, cur, fy, fy, fy);
+#pragma unroll
+  for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(dt, fy.v[e], ds.v[e]);
+}
+
+template <class Loader>
+__device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const LaneCols& L, int valid,
+                                         unsigned char* smem) {
+  const Geom& g = p.g;
+  const size_t ld = size_t(g.ld);
+  const float dt = g.dt;
+  const int c0 = L.c0;
+  const int nx = g.nx;
+  auto at = [&](auto* base, int i) { return base + ptrdiff_t(i) * ptrdiff_t(ld) + c0; };
+
+  typename Loader::SegsT segs;
+  segs.base[S2_SXY] = p.sxy0; segs.roff[S2_SXY] = 1;
+  segs.base[S2_SZY] = p.szy0; segs.roff[S2_SZY] = 1;
+  segs.base[S2_VY] = p.vy0; segs.roff[S2_VY] = 0;
+  segs.base[S2_RHO] = p.rho; segs.roff[S2_RHO] = 0;
+  segs.base[S2_MU] = p.mu; segs.roff[S2_MU] = -2;
+  const int i0 = m.ib - 4;                 // first level-1 row
+  const int nk = (m.ie - m.ib) + 9;        // level-1 rows [ib-4, ie+4]
+  float* buf = nullptr;
+  uint64_t* bar = nullptr;
+  if (Loader::kStages > 0) {
+    const size_t per = size_t(Loader::kStages) * Loader::kStageBytes;
+    buf = reinterpret_cast<float*>(smem + per * m.warp);
+    bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
+  }
+  Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
+  rows.start();
+
+  f4 tbt;
+  {
+    const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) tbt.v[e] = tb.v[e] * tt.v[e];
+  }
+  const float sx_dt = dt * g.rdx, sz_dt = dt * g.rdz;
+  // sigma^n rings, rows i-2..i+1
+  f4 xy0 = ld4(at(p.sxy0, i0 - 2)), xy1 = ld4(at(p.sxy0, i0 - 1)), xy2 = ld4(at(p.sxy0, i0)), xy3;
+  f4 zy0 = ld4(at(p.szy0, i0 - 2)), zy1 = ld4(at(p.szy0, i0 - 1)), zy2 = ld4(at(p.szy0, i0)), zy3;
+  const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
+  f4 va = z4, vb = z4, vc = z4, vd = z4;        // level-1 vy rows i-3..i
+  f4 sx0 = z4, sx1 = z4, sx2 = z4, sx3 = z4;    // level-1 sxy rows i-5..i-2
+  f4 sz0 = z4, sz1 = z4, sz2 = z4, sz3 = z4;    // level-1 szy rows i-5..i-2
+  f4 ua = z4, ub = z4, uc = z4, ud = z4;        // level-2 vy rows i-6..i-3
+  InjectList inj2 = p.inj;
+  inj2.it = p.inj.it + 1;
+  ProbeList pr2 = p.probes;
+  pr2.it = p.probes.it + 1;
+  Cursor ci1 = cursor_at(p.inj.list, p.inj.n, i0);
+  Cursor ci2 = cursor_at(p.inj.list, p.inj.n, m.ib - 1);
+  Cursor pi1 = cursor_at(p.probes.list, p.probes.n, m.ib);
+  Cursor pi2 = pi1;
+  f4 rzb, rzf;
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    rzb.v[e] = (L.zb & (1 << e)) ? sz_dt : 0.0f;
+    rzf.v[e] = (L.zf & (1 << e)) ? sz_dt : 0.0f;
+  }
+  const bool cols_out = !__all_sync(kFull, valid == 0xF);
+  float bx1_next = __ldg(p.taper_x + i0), bx2_next = __ldg(p.taper_x + i0 - 3);
+
+  for (int k = 0; k < nk; ++k) {
+    const int i = i0 + k;
+    const float bx1 = bx1_next, bx2 = bx2_next;
+    bx1_next = __ldg(p.taper_x + i + 1);
+    bx2_next = __ldg(p.taper_x + i - 2);
+    if (!rows.acquire(k)) {
+      flag_timeout(p.err);
+      rows.drain(k);
+      return;
+    }
+    xy3 = rows.seg(S2_SXY);
+    zy3 = rows.seg(S2_SZY);
+    const f4 vo = rows.seg(S2_VY);
+    const f4 rho = rows.seg(S2_RHO);
+    const f4 mu = rows.seg(S2_MU);
+    rows.release();
+
+    // ---- level 1, velocity of row i (step it): div_sy, source, add_vy
+    {
+      const float rx = (i >= 2 && i < nx - 2) ? sx_dt : 0.0f;
+      const f4 ax = d4_rows(xy0, xy1, xy2, xy3), az = d4_cols_back(zy2);
+      f4 ds;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(az.v[e], rzb.v[e], ax.v[e] * rx);
+      if (ci1.row == i) inject_dt_y(p.inj, i, c0, ci1, dt, ds);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) vd.v[e] = (bx1 * tbt.v[e]) * fmaf(ds.v[e], rho.v[e], vo.v[e]);
+      const bool row_ok = (i >= 0 && i < nx);
+      if (!row_ok || cols_out) vd = in_grid(vd, row_ok, valid);
+      if (i >= m.ib && i < m.ie) probe_at(p.probes, i, L, pi1, dt, [&](int, int e) { return pick4(vd, e); });
+    }
+
+    // ---- level 1, stress of row i-2 (step it): div_vy, add_sy_sh
+    if (k >= 3) {
+      const int r = i - 2;
+      const float rx = (r >= 1 && r < nx - 2) ? sx_dt : 0.0f;
+      const f4 gx = d4_rows(va, vb, vc, vd), gz = d4_cols_fwd(vb);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        sx3.v[e] = fmaf(mu.v[e], gx.v[e] * rx, xy0.v[e]);
+        sz3.v[e] = fmaf(mu.v[e], gz.v[e] * rzf.v[e], zy0.v[e]);
+      }
+      const bool row_ok = (r >= 0 && r < nx);
+      if (!row_ok || cols_out) {
+        sx3 = in_grid(sx3, row_ok, valid);
+        sz3 = in_grid(sz3, row_ok, valid);
+      }
+    }
+
+    // ---- level 2, velocity of row i-3 (step it+1)
+    if (k >= 6) {
+      const int r = i - 3;
+      const f4 rho2 = rows.seg_back(S2_RHO, 3);
+      const float rx = (r >= 2 && r < nx - 2) ? sx_dt : 0.0f;
+      const f4 ax = d4_rows(sx0, sx1, sx2, sx3), az = d4_cols_back(sz2);
+      f4 ds;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(az.v[e], rzb.v[e], ax.v[e] * rx);
+      if (ci2.row == r) inject_dt_y(inj2, r, c0, ci2, dt, ds);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) ud.v[e] = (bx2 * tbt.v[e]) * fmaf(ds.v[e], rho2.v[e], va.v[e]);
+      if (r >= m.ib && r < m.ie) {
+        st4_masked(at(p.vy1, r), ud, L.own);
+        probe_at(pr2, r, L, pi2, dt, [&](int, int e) { return pick4(ud, e); });
+      }
+    }
+
+    // ---- level 2, stress of row i-5 (step it+1)
+    if (k >= 9) {
+      const int r = i - 5;
+      const f4 mu2 = rows.seg_back(S2_MU, 3);
+      const float rx = (r >= 1 && r < nx - 2) ? sx_dt : 0.0f;
+      const f4 gx = d4_rows(ua, ub, uc, ud), gz = d4_cols_fwd(ub);
+      f4 sxy, szy;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        sxy.v[e] = fmaf(mu2.v[e], gx.v[e] * rx, sx0.v[e]);
+        szy.v[e] = fmaf(mu2.v[e], gz.v[e] * rzf.v[e], sz0.v[e]);
+      }
+      st4_masked(at(p.sxy1, r), sxy, L.own);
+      st4_masked(at(p.szy1, r), szy, L.own);
+    }
+
+    ua = ub; ub = uc; uc = ud;
+    sx0 = sx1; sx1 = sx2; sx2 = sx3;
+    sz0 = sz1; sz1 = sz2; sz2 = sz3;
+    va = vb; vb = vc; vc = vd;
+    xy0 = xy1; xy1 = xy2; xy2 = xy3;
+    zy0 = zy1; zy1 = zy2; zy2 = zy3;
+  }
+}
+
+template <class Loader>
+__device__ __forceinline__ void sh2_march(const ShStep& p, int gw, unsigned char* smem) {
+  const March m = march_of(p.g, gw);
+  if (!m.active) return;
+  int valid;
+  const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
+  sh2_body<Loader>(p, m, L, valid, smem);
+}
+
 }  // namespace
 
 template <class Loader>
@@ -332,13 +523,69 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(co
   psv2_march<Bulk2>(p, lw, smem);
 }
 
-cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, cudaStream_t s) {
+// The same for SH jobs (state slots vy, sxy, szy).
+__global__ void __launch_bounds__(kStepWarps * 32, 3) grouped_forward2_sh_kernel(const JobDesc* __restrict__ jobs,
+                                                                                 const GroupOp* __restrict__ ops,
+                                                                                 int nops) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int gw = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const GroupOp op = ops[group_op_of(ops, nops, gw)];
+  const JobDesc& J = jobs[op.job];
+  const int lw = gw - op.warp_begin;
+  if (lw >= J.g2.nstrips * J.g2.nchunks) return;
+  auto slot = [&](int s, int f) { return J.pool + s * J.slot_elems + f * J.field_elems + J.halo; };
+  ShStep p{};
+  p.g = J.g2;
+  p.vy0 = slot(op.a, 0); p.sxy0 = slot(op.a, 1); p.szy0 = slot(op.a, 2);
+  p.vy1 = slot(op.b, 0); p.sxy1 = slot(op.b, 1); p.szy1 = slot(op.b, 2);
+  p.rho = J.rho; p.mu = J.mu;
+  p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
+  p.inj = J.src;
+  p.inj.it = op.it;
+  p.probes = J.probes;
+  if (!(op.flags & 1)) p.probes.n = 0;
+  p.probes.it = op.it;
+  p.err = J.err;
+  sh2_march<ShBulk2>(p, lw, smem);
+}
+
+cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
+                                    cudaStream_t s) {
   if (nops <= 0 || warps <= 0) return cudaSuccess;
-  const size_t smem = smem_for<Bulk2>();
-  static const cudaError_t attr = prepare_kernel(grouped_forward2_kernel, smem);
+  const unsigned blocks = unsigned((warps + kStepWarps - 1) / kStepWarps);
+  if (psv) {
+    const size_t smem = smem_for<Bulk2>();
+    static const cudaError_t attr = prepare_kernel(grouped_forward2_kernel, smem);
+    if (attr != cudaSuccess) return attr;
+    grouped_forward2_kernel<<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+  } else {
+    const size_t smem = smem_for<ShBulk2>();
+    static const cudaError_t attr = prepare_kernel(grouped_forward2_sh_kernel, smem);
+    if (attr != cudaSuccess) return attr;
+    grouped_forward2_sh_kernel<<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+  }
+  return cudaGetLastError();
+}
+
+// SH two-step kernel: fewer registers than the PSV one (three CTAs per SM).
+__global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_kernel(const ShStep p) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  sh2_march<ShBulk2>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
+int sh_step2_blocks_per_sm() {
+  int n = 0;
+  const size_t smem = smem_for<ShBulk2>();
+  cudaError_t e = prepare_kernel(sh_step2_kernel, smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step2_kernel, kStepWarps * 32, smem);
+  return e == cudaSuccess ? n : 0;
+}
+
+cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s) {
+  const size_t smem = smem_for<ShBulk2>();
+  static const cudaError_t attr = prepare_kernel(sh_step2_kernel, smem);
   if (attr != cudaSuccess) return attr;
-  grouped_forward2_kernel<<<unsigned((warps + kStepWarps - 1) / kStepWarps), kStepWarps * 32, smem, s>>>(jobs, ops,
-                                                                                                         nops);
+  sh_step2_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
   return cudaGetLastError();
 }
 

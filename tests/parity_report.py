@@ -5,7 +5,7 @@ against the FP32 and FP64 oracles, as a markdown table (needs a GPU).
 
 Rows: the reference's three examples through the drop-in host API (fixtures
 are WGSL-path outputs), and seeded oracle cases for each kernel family (the
-step kernels, the two-step PSV kernel, the cluster kernel for small SH grids,
+step kernels, the two-step PSV and SH kernels, the cluster kernel for small SH grids,
 the spin kernel).  Columns: relative L2 and max|d|/peak against the fixture
 (where there is one), relative L2 against the FP32 oracle (reference operation
 order) and the FP64 oracle, and the FP32 oracle's own distance from FP64.
@@ -74,9 +74,13 @@ def oracle_cases(rows):
         ("SH 200 x 200, cluster kernel (whole run on chip)", 200, 200, 600, 10.0, 1.0e-3,
          [(100, 100, 10.0, 0.12, 0.0)], [(i, 20) for i in range(10, 191, 15)],
          dict(sh=True, psv=False, abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=20), {}),
-        ("SH 600 x 520, step kernels", 600, 520, 400, 10.0, 1.0e-3,
+        ("SH 600 x 520, two-step kernel", 600, 520, 400, 10.0, 1.0e-3,
          [(300, 260, 15.0, 0.08, 0.0)], [(i, 300) for i in range(240, 361, 15)],
          dict(sh=True, psv=False, abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=20), {}),
+        ("SH 600 x 520, one-step kernel", 600, 520, 400, 10.0, 1.0e-3,
+         [(300, 260, 15.0, 0.08, 0.0)], [(i, 300) for i in range(240, 361, 15)],
+         dict(sh=True, psv=False, abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=20),
+         {"two_step": 0}),
         ("PSV 512 x 480, two-step kernel", 512, 480, 400, 5.0, 4.0e-4,
          [(256, 50, 15.0, 0.05, 90.0)], [(i, 0) for i in range(0, 512, 32)] + [(256, 240)],
          dict(psv=True, abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=40), {}),

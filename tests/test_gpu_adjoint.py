@@ -90,24 +90,22 @@ def test_gradient_matches_fp64_oracle(phys):
 def test_checkpoint_interval_does_not_change_the_gradient(phys):
     """With one-step forward launches the recorded and the recomputed states
     are the same bits whatever the interval, so the gradient is bitwise equal.
-    The PSV default records two steps per launch (multiply-add contraction)
+    The default records two steps per launch (multiply-add contraction)
     between checkpoints, which changes the states by rounding only."""
     vp, vs, rho, flags, src, rec = _problem(phys, 1)
     obs = _observed(vp, vs, rho, flags, src, rec, -1)
     sim, _ = _sim(vp, vs, rho, flags, src, rec)
-    if phys == "psv":
-        sim.set_option("two_step", 0)
+    sim.set_option("two_step", 0)
     ref = _gpu_gradient(sim, flags, obs, -1, 1)[2]       # every state stored
     for k in (2, 7, 0, NT):                             # 2 and 7 steps, the default, one interval
         g = _gpu_gradient(sim, flags, obs, -1, k)[2]
         for p in g:
             assert np.array_equal(g[p], ref[p]), (k, p)
-    if phys == "psv":
-        sim.set_option("two_step", 1)
-        for k in (2, 7, 0, NT):
-            g = _gpu_gradient(sim, flags, obs, -1, k)[2]
-            for p in ("lambda", "mu", "buoyancy"):
-                assert rel_l2(g[p], ref[p]) <= 1e-5, (k, p)
+    sim.set_option("two_step", 1)
+    for k in (2, 7, 0, NT):
+        g = _gpu_gradient(sim, flags, obs, -1, k)[2]
+        for p in (("lambda", "mu", "buoyancy") if phys == "psv" else ("mu", "buoyancy")):
+            assert rel_l2(g[p], ref[p]) <= 1e-5, (k, p)
     sim.close()
 
 

@@ -21,6 +21,7 @@ def _run(nx, nz, nt, src, rec, cluster, snap=0, isrc=-1, graphs=None, **flags):
     stf = np.stack([sw.ricker(nt, dt, s[2], s[3], s[4], 1.0e10) for s in src], axis=1)
     with sw.Sim(nx, nz, nt, 10.0, 10.0, dt, sh=True, psv=False, **flags) as sim:
         sim.set_option("cluster", 1 if cluster else 0)
+        sim.set_option("two_step", 0)   # the one-step kernel where the cluster does not run
         if graphs is not None:
             sim.set_option("graphs", graphs)
         for k, v in _model(nx, nz, 3).items():
