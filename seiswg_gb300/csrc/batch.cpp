@@ -117,6 +117,7 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       jd.err = err_;
       descs_.push_back(jd);
       model_geom_.push_back(jd.g);
+      model_geom2_.push_back(jd.g2);
       jobs_.push_back(j);
     }
   }
@@ -129,13 +130,20 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
 void Batch::set_chunk_rows(int lx) {
   if (lx != 0 && lx < 4) throw std::invalid_argument("chunk_rows must be 0 or >= 4");
   SW_CUDA(cudaStreamSynchronize(stream_));
+  // The same rows for the one- and the two-step marches: in a batch many
+  // jobs share each launch, and its duration is the longest march.
   for (size_t q = 0; q < descs_.size(); ++q) {
-    Geom g = model_geom_[q];
+    Geom g = model_geom_[q], g2 = model_geom2_[q];
     if (lx > 0) {
       g.lx = lx;
       g.nchunks = (g.nx + lx - 1) / lx;
+      if (g2.lx > 0) {
+        g2.lx = lx;
+        g2.nchunks = (g2.nx + lx - 1) / lx;
+      }
     }
     descs_[q].g = g;
+    descs_[q].g2 = g2;
   }
   SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
@@ -165,18 +173,25 @@ double Batch::autotune(int slots) {
     const int lx = cand[c % cand.size()];
     two_step_ = c < int(cand.size());
     set_chunk_rows(lx);
-    // The same schedule positions for every candidate: the recording pass
-    // and a window of the reverse sweep.
-    const int w = std::min(slots, nslots_);
-    const int mid = std::min(std::max(0, nslots_ - w), nslots_ * 3 / 5);
+    // A window at the start of the recording pass and one in the middle of
+    // the reverse sweep, each scaled to its phase's slot count: two-step
+    // recording does twice the steps per slot in half the slots.
+    const int rec = std::max(1, rec_slots_), rest = std::max(1, nslots_ - rec_slots_);
+    const int w = std::min(slots, rec), rw = std::min(slots, rest);
+    const int mid = rec_slots_ + (rest - rw) / 2;
     enqueue_slots(0, std::min(2, nslots_));  // warm-up
+    float ms_rec = 0.0f, ms_rev = 0.0f;
     SW_CUDA(cudaEventRecord(e0, stream_));
     enqueue_slots(0, w);
-    enqueue_slots(mid, mid + w);
     SW_CUDA(cudaEventRecord(e1, stream_));
     SW_CUDA(cudaEventSynchronize(e1));
-    float ms = 0.0f;
-    SW_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    SW_CUDA(cudaEventElapsedTime(&ms_rec, e0, e1));
+    SW_CUDA(cudaEventRecord(e0, stream_));
+    enqueue_slots(mid, mid + rw);
+    SW_CUDA(cudaEventRecord(e1, stream_));
+    SW_CUDA(cudaEventSynchronize(e1));
+    SW_CUDA(cudaEventElapsedTime(&ms_rev, e0, e1));
+    const float ms = ms_rec / float(w) * float(rec) + ms_rev / float(rw) * float(rest);
     if (ms < best) { best = ms; best_lx = lx; best_two = two_step_; }
   }
   cudaEventDestroy(e0);
@@ -243,7 +258,12 @@ void Batch::build_schedule() {
     }
   }
   size_t T = 0;
-  for (auto& L : lists) T = std::max(T, L.size());
+  rec_slots_ = 0;
+  for (auto& L : lists) {
+    T = std::max(T, L.size());
+    for (size_t t = 0; t < L.size(); ++t)
+      if (L[t].kind == kMisfit) rec_slots_ = std::max(rec_slots_, int(t));
+  }
   nslots_ = int(T);
   std::vector<GroupOp> all;
   plan_.assign(T, {});

@@ -72,6 +72,7 @@ class Batch {
   void enqueue_slots(int t0, int t1);
   std::vector<JobDesc> descs_;   // host copy of d_jobs_
   std::vector<Geom> model_geom_; // each job's geometry from its problem's chunk model
+  std::vector<Geom> model_geom2_;  // ... of its two-step kernel (lx 0: none)
   int chunk_rows_ = 0;
   bool two_step_ = true;
   size_t ops_bytes_ = 0;
@@ -90,6 +91,7 @@ class Batch {
   };
   std::vector<std::vector<Launch>> plan_;
   int nslots_ = 0;
+  int rec_slots_ = 0;  // slots of the longest recording pass (before the misfit)
   std::vector<float*> sums_;   // per problem: 3 gradient fields
   std::vector<double> host_J_;
   size_t bytes_ = 0;
