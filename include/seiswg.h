@@ -205,7 +205,10 @@ int seiswg_batch_run(seiswg_batch* batch);
  * chunk rows 0, 16, 32, 48, 64, 96 and 128 with and without two-step
  * recording, timing `value` slots of the recording pass and of the reverse
  * sweep each, and keeps the one whose times, scaled to the slot counts of
- * the two phases, are the shortest.  Each drops the captured graph. */
+ * the two phases, are the shortest; "concurrent" (0/1): the launches of one
+ * schedule slot (one per kind of work: SH/PSV forward, reverse, misfit) run
+ * concurrently on forked streams (default 1) or one after another.  Each
+ * drops the captured graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
 /* The chunk rows in use (0: each problem's own chunk model), and whether
  * jobs record two steps per launch. */

@@ -449,7 +449,8 @@ class Batch:
         _check(lib().seiswg_batch_run(self._h))
 
     def set_option(self, key: str, value: int):
-        """"chunk_rows" (0: per-problem model), "two_step" (0/1) or "autotune" (slots per timing window)."""
+        """"chunk_rows" (0: per-problem model), "two_step" (0/1), "concurrent" (0/1) or "autotune"
+        (slots per timing window)."""
         _check(lib().seiswg_batch_set_option(self._h, key.encode(), int(value)))
 
     def gradient(self, problem: int, param: str):

@@ -23,6 +23,13 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
     SW_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     own_stream_ = true;
   }
+  aux_.assign(kKinds - 1, nullptr);
+  join_.assign(kKinds - 1, nullptr);
+  for (int k = 0; k < kKinds - 1; ++k) {
+    SW_CUDA(cudaStreamCreateWithFlags(&aux_[k], cudaStreamNonBlocking));
+    SW_CUDA(cudaEventCreateWithFlags(&join_[k], cudaEventDisableTiming));
+  }
+  SW_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
   for (size_t p = 0; p < problems_.size(); ++p) {
@@ -210,6 +217,9 @@ Batch::~Batch() {
       cudaFree(p);
   }
   for (float* s : sums_) cudaFree(s);
+  for (cudaStream_t a : aux_) if (a) cudaStreamDestroy(a);
+  for (cudaEvent_t e : join_) if (e) cudaEventDestroy(e);
+  if (fork_) cudaEventDestroy(fork_);
   cudaFree(d_jobs_);
   cudaFree(d_ops_);
   cudaFree(err_);
@@ -318,20 +328,40 @@ void Batch::enqueue_run() {
 
 void Batch::enqueue_slots(int t0, int t1) {
   for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
+    // Kinds of one slot touch different jobs: the first runs on the batch's
+    // stream, the others on forked streams that join before the next slot.
+    const bool fork = concurrent_ && plan_[t].size() > 1;
+    if (fork) SW_CUDA(cudaEventRecord(fork_, stream_));
+    int n = 0;
     for (const Launch& l : plan_[t]) {
       const GroupOp* ops = d_ops_ + l.offset;
-      switch (l.kind) {
-        case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
-        case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
-        case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
-        case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
-        case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, stream_)); break;
-        case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, stream_)); break;
-        case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, stream_)); break;
+      cudaStream_t s = stream_;
+      if (fork && n > 0) {
+        s = aux_[n - 1];
+        SW_CUDA(cudaStreamWaitEvent(s, fork_, 0));
       }
+      switch (l.kind) {
+        case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, s)); break;
+        case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, s)); break;
+        case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, s)); break;
+        case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, s)); break;
+        case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, s)); break;
+        case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, s)); break;
+        case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, s)); break;
+      }
+      if (fork && n > 0) SW_CUDA(cudaEventRecord(join_[n - 1], s));
       ++launches_per_run_;
+      ++n;
     }
+    for (int q = 1; fork && q < n; ++q) SW_CUDA(cudaStreamWaitEvent(stream_, join_[q - 1], 0));
   }
+}
+
+void Batch::set_concurrent(bool on) {
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  concurrent_ = on;
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
 }
 
 void Batch::run() {

@@ -44,10 +44,16 @@ class Batch {
   // timed launches leave results that the next run() overwrites.
   double autotune(int slots);
   int chunk_rows() const { return chunk_rows_; }
-  // PSV jobs record two steps per launch between checkpoints (default on);
-  // rebuilds the schedule.  The autotuner also tries both.
+  // Jobs (PSV alone, SH alone) record two steps per launch between
+  // checkpoints (default on); rebuilds the schedule.  The autotuner also
+  // tries both.
   void set_two_step(bool on);
   bool two_step() const { return two_step_; }
+  // The launches of one slot (one per kind of work) run concurrently on
+  // forked streams (default on), or one after another on the batch's stream.
+  // Drops the captured graph.
+  void set_concurrent(bool on);
+  bool concurrent() const { return concurrent_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -81,6 +87,10 @@ class Batch {
   std::vector<Job> jobs_;
   cudaStream_t stream_;
   bool own_stream_ = false;
+  bool concurrent_ = true;
+  std::vector<cudaStream_t> aux_;   // forked streams for a slot's other kinds
+  cudaEvent_t fork_ = nullptr;
+  std::vector<cudaEvent_t> join_;
   int ckpt_every_;
   JobDesc* d_jobs_ = nullptr;
   GroupOp* d_ops_ = nullptr;

@@ -493,6 +493,7 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     if (k == "chunk_rows") b->batch->set_chunk_rows(int(value));
     else if (k == "autotune") b->batch->autotune(int(value));
     else if (k == "two_step") b->batch->set_two_step(value != 0);
+    else if (k == "concurrent") b->batch->set_concurrent(value != 0);
     else throw std::invalid_argument("unknown batch option: " + k);
   });
 }
