@@ -650,7 +650,7 @@ def run_secondary(args):
                            "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
                            "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
-                           "concurrent_kinds": args.concurrent != 0,
+                           "concurrent": info.get("concurrent"),
                            "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
@@ -690,7 +690,8 @@ def main():
     ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--concurrent", type=int, default=-1,
-                    help="c5: a slot's launches on forked streams (1, the default) or one after another (0)")
+                    help="c5: launch order: 0 serial, 1 a slot's kinds on forked streams, 2 one stream per kind "
+                         "(-1: the default, 2)")
     ap.add_argument("--fd-check", type=int, default=0, help="c4: finite-difference check on this many cells")
     ap.add_argument("--fd-h", type=float, default=1e-3, help="c4: relative vp step of the finite differences")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],

@@ -205,15 +205,19 @@ int seiswg_batch_run(seiswg_batch* batch);
  * chunk rows 0, 16, 32, 48, 64, 96 and 128 with and without two-step
  * recording, timing `value` slots of the recording pass and of the reverse
  * sweep each, and keeps the one whose times, scaled to the slot counts of
- * the two phases, are the shortest; "concurrent" (0/1): the launches of one
- * schedule slot (one per kind of work: SH/PSV forward, reverse, misfit) run
- * concurrently on forked streams (default 1) or one after another.  Each
- * drops the captured graph. */
+ * the two phases, are the shortest; "concurrent": the order of the
+ * launches (one per schedule slot and kind of work: SH/PSV forward, reverse,
+ * misfit): 0 one after another, 1 a slot's launches on forked streams that
+ * join before the next slot, 2 (default) one stream per kind, a launch
+ * waiting only for the previous slot's launches of the kinds its jobs come
+ * from.  Each drops the captured graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
 /* The chunk rows in use (0: each problem's own chunk model), and whether
  * jobs record two steps per launch. */
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);
 int32_t seiswg_batch_two_step(const seiswg_batch* batch);
+/* The launch order in use ("concurrent": 0, 1 or 2). */
+int32_t seiswg_batch_concurrent(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */
 int seiswg_batch_gradient(seiswg_batch* batch, int32_t problem, const char* param, float* host);
 double seiswg_batch_misfit(const seiswg_batch* batch, int32_t problem);

@@ -30,6 +30,12 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
     SW_CUDA(cudaEventCreateWithFlags(&join_[k], cudaEventDisableTiming));
   }
   SW_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
+  kst_.assign(kKinds, nullptr);
+  kev_.assign(kKinds, nullptr);
+  for (int k = 0; k < kKinds; ++k) {
+    SW_CUDA(cudaStreamCreateWithFlags(&kst_[k], cudaStreamNonBlocking));
+    SW_CUDA(cudaEventCreateWithFlags(&kev_[k], cudaEventDisableTiming));
+  }
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
   for (size_t p = 0; p < problems_.size(); ++p) {
@@ -219,6 +225,8 @@ Batch::~Batch() {
   for (float* s : sums_) cudaFree(s);
   for (cudaStream_t a : aux_) if (a) cudaStreamDestroy(a);
   for (cudaEvent_t e : join_) if (e) cudaEventDestroy(e);
+  for (cudaStream_t a : kst_) if (a) cudaStreamDestroy(a);
+  for (cudaEvent_t e : kev_) if (e) cudaEventDestroy(e);
   if (fork_) cudaEventDestroy(fork_);
   cudaFree(d_jobs_);
   cudaFree(d_ops_);
@@ -279,10 +287,11 @@ void Batch::build_schedule() {
   plan_.assign(T, {});
   for (size_t t = 0; t < T; ++t) {
     for (int kind = 0; kind < kKinds; ++kind) {
-      Launch l{kind, int(all.size()), 0, 0};
+      Launch l{kind, int(all.size()), 0, 0, 0};
       for (size_t q = 0; q < jobs_.size(); ++q) {
         if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
         const HostOp& h = lists[q][t];
+        if (t > 0 && lists[q][t - 1].kind != kind) l.deps |= 1 << lists[q][t - 1].kind;
         const Geom& g = (kind == kFwd2Psv || kind == kFwd2Sh) ? descs_[q].g2 : descs_[q].g;
         all.push_back(GroupOp{int(q), h.it, h.a, h.b, h.flags, l.warps});
         l.warps += (kind == kMisfit) ? 1 : g.nstrips * g.nchunks;
@@ -327,39 +336,65 @@ void Batch::enqueue_run() {
 }
 
 void Batch::enqueue_slots(int t0, int t1) {
+  if (concurrent_ == 2) {
+    // One stream per kind, forked from and joined back into the batch's
+    // stream; a job that changes kind between slots makes its new kind's
+    // stream wait for its old kind's launch.
+    SW_CUDA(cudaEventRecord(fork_, stream_));
+    for (int k = 0; k < kKinds; ++k) SW_CUDA(cudaStreamWaitEvent(kst_[k], fork_, 0));
+    for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
+      for (const Launch& l : plan_[t]) {
+        cudaStream_t s = kst_[l.kind];
+        for (int a = 0; a < kKinds; ++a)
+          if (l.deps & (1 << a)) SW_CUDA(cudaStreamWaitEvent(s, kev_[a], 0));
+        launch_kind(l, s);
+        SW_CUDA(cudaEventRecord(kev_[l.kind], s));
+      }
+    }
+    for (int k = 0; k < kKinds; ++k) {
+      SW_CUDA(cudaEventRecord(kev_[k], kst_[k]));
+      SW_CUDA(cudaStreamWaitEvent(stream_, kev_[k], 0));
+    }
+    return;
+  }
   for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
     // Kinds of one slot touch different jobs: the first runs on the batch's
     // stream, the others on forked streams that join before the next slot.
-    const bool fork = concurrent_ && plan_[t].size() > 1;
+    const bool fork = concurrent_ == 1 && plan_[t].size() > 1;
     if (fork) SW_CUDA(cudaEventRecord(fork_, stream_));
     int n = 0;
     for (const Launch& l : plan_[t]) {
-      const GroupOp* ops = d_ops_ + l.offset;
       cudaStream_t s = stream_;
       if (fork && n > 0) {
         s = aux_[n - 1];
         SW_CUDA(cudaStreamWaitEvent(s, fork_, 0));
       }
-      switch (l.kind) {
-        case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, s)); break;
-        case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, s)); break;
-        case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, s)); break;
-        case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, s)); break;
-        case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, s)); break;
-        case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, s)); break;
-        case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, s)); break;
-      }
+      launch_kind(l, s);
       if (fork && n > 0) SW_CUDA(cudaEventRecord(join_[n - 1], s));
-      ++launches_per_run_;
       ++n;
     }
     for (int q = 1; fork && q < n; ++q) SW_CUDA(cudaStreamWaitEvent(stream_, join_[q - 1], 0));
   }
 }
 
-void Batch::set_concurrent(bool on) {
+void Batch::launch_kind(const Launch& l, cudaStream_t s) {
+  const GroupOp* ops = d_ops_ + l.offset;
+  switch (l.kind) {
+    case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, s)); break;
+    case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, s)); break;
+    case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, s)); break;
+    case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, s)); break;
+    case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, s)); break;
+    case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, s)); break;
+    case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, s)); break;
+  }
+  ++launches_per_run_;
+}
+
+void Batch::set_concurrent(int mode) {
+  if (mode < 0 || mode > 2) throw std::invalid_argument("concurrent must be 0, 1 or 2");
   SW_CUDA(cudaStreamSynchronize(stream_));
-  concurrent_ = on;
+  concurrent_ = mode;
   if (graph_) cudaGraphExecDestroy(graph_);
   graph_ = nullptr;
 }

@@ -49,11 +49,14 @@ class Batch {
   // tries both.
   void set_two_step(bool on);
   bool two_step() const { return two_step_; }
-  // The launches of one slot (one per kind of work) run concurrently on
-  // forked streams (default on), or one after another on the batch's stream.
+  // How the launches of the schedule are ordered.  0: one after another on
+  // the batch's stream.  1: the launches of one slot (one per kind of work)
+  // run concurrently on forked streams that join before the next slot.
+  // 2 (default): one stream per kind; a launch waits only for the previous
+  // slot's launches of the kinds its jobs come from, so the kinds pipeline.
   // Drops the captured graph.
-  void set_concurrent(bool on);
-  bool concurrent() const { return concurrent_; }
+  void set_concurrent(int mode);
+  int concurrent() const { return concurrent_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -87,10 +90,12 @@ class Batch {
   std::vector<Job> jobs_;
   cudaStream_t stream_;
   bool own_stream_ = false;
-  bool concurrent_ = true;
-  std::vector<cudaStream_t> aux_;   // forked streams for a slot's other kinds
+  int concurrent_ = 2;
+  std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
   cudaEvent_t fork_ = nullptr;
   std::vector<cudaEvent_t> join_;
+  std::vector<cudaStream_t> kst_;   // mode 2: one stream per kind
+  std::vector<cudaEvent_t> kev_;    // ... and its last launch
   int ckpt_every_;
   JobDesc* d_jobs_ = nullptr;
   GroupOp* d_ops_ = nullptr;
@@ -98,8 +103,10 @@ class Batch {
   // per slot and kind: [offset, count, warps] into d_ops_
   struct Launch {
     int kind, offset, count, warps;
+    int deps;  // kinds of the previous slot that some of this launch's jobs come from (bit mask)
   };
   std::vector<std::vector<Launch>> plan_;
+  void launch_kind(const Launch& l, cudaStream_t s);
   int nslots_ = 0;
   int rec_slots_ = 0;  // slots of the longest recording pass (before the misfit)
   std::vector<float*> sums_;   // per problem: 3 gradient fields
