@@ -616,6 +616,8 @@ def run_secondary(args):
         batch = sw.Batch(sims, obs)
         if args.concurrent >= 0:
             batch.set_option("concurrent", args.concurrent)
+        if args.stream_groups > 0:
+            batch.set_option("stream_groups", args.stream_groups)
         tune_ms = None
         if args.autotune:
             t0 = time.perf_counter()
@@ -650,7 +652,7 @@ def run_secondary(args):
                            "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
                            "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
-                           "concurrent": info.get("concurrent"),
+                           "concurrent": info.get("concurrent"), "stream_groups": info.get("stream_groups"),
                            "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
@@ -689,6 +691,7 @@ def main():
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
+    ap.add_argument("--stream-groups", type=int, default=0, help="c5: job groups with their own streams (0: default)")
     ap.add_argument("--concurrent", type=int, default=-1,
                     help="c5: launch order: 0 serial, 1 a slot's kinds on forked streams, 2 one stream per kind "
                          "(-1: the default, 2)")

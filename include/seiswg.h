@@ -210,14 +210,17 @@ int seiswg_batch_run(seiswg_batch* batch);
  * misfit): 0 one after another, 1 a slot's launches on forked streams that
  * join before the next slot, 2 (default) one stream per kind, a launch
  * waiting only for the previous slot's launches of the kinds its jobs come
- * from.  Each drops the captured graph. */
+ * from; "stream_groups" (1..4, default 1): jobs split round-robin into
+ * groups with their own launches (and streams in order 2).  Each drops the
+ * captured graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
 /* The chunk rows in use (0: each problem's own chunk model), and whether
  * jobs record two steps per launch. */
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);
 int32_t seiswg_batch_two_step(const seiswg_batch* batch);
-/* The launch order in use ("concurrent": 0, 1 or 2). */
+/* The launch order in use ("concurrent": 0, 1 or 2) and the job groups. */
 int32_t seiswg_batch_concurrent(const seiswg_batch* batch);
+int32_t seiswg_batch_stream_groups(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */
 int seiswg_batch_gradient(seiswg_batch* batch, int32_t problem, const char* param, float* host);
 double seiswg_batch_misfit(const seiswg_batch* batch, int32_t problem);

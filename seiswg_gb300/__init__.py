@@ -110,6 +110,7 @@ PROTOTYPES = [
     ("seiswg_batch_chunk_rows", _i32, [_vp]),
     ("seiswg_batch_two_step", _i32, [_vp]),
     ("seiswg_batch_concurrent", _i32, [_vp]),
+    ("seiswg_batch_stream_groups", _i32, [_vp]),
     ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
     ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
     ("seiswg_batch_info", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
@@ -450,8 +451,8 @@ class Batch:
         _check(lib().seiswg_batch_run(self._h))
 
     def set_option(self, key: str, value: int):
-        """"chunk_rows" (0: per-problem model), "two_step" (0/1), "concurrent" (0, 1, 2: launch order)
-        or "autotune" (slots per timing window)."""
+        """"chunk_rows" (0: per-problem model), "two_step" (0/1), "concurrent" (0, 1, 2: launch order),
+        "stream_groups" (1..4) or "autotune" (slots per timing window)."""
         _check(lib().seiswg_batch_set_option(self._h, key.encode(), int(value)))
 
     def gradient(self, problem: int, param: str):
@@ -469,7 +470,8 @@ class Batch:
         return dict(jobs=j.value, slots=s.value, launches_per_run=l.value, device_bytes=b.value,
                     chunk_rows=int(lib().seiswg_batch_chunk_rows(self._h)),
                     two_step=bool(lib().seiswg_batch_two_step(self._h)),
-                    concurrent=int(lib().seiswg_batch_concurrent(self._h)))
+                    concurrent=int(lib().seiswg_batch_concurrent(self._h)),
+                    stream_groups=int(lib().seiswg_batch_stream_groups(self._h)))
 
     @property
     def stream(self) -> int:

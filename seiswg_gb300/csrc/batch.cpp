@@ -23,16 +23,17 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
     SW_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     own_stream_ = true;
   }
-  aux_.assign(kKinds - 1, nullptr);
-  join_.assign(kKinds - 1, nullptr);
-  for (int k = 0; k < kKinds - 1; ++k) {
+  const int nstreams = kKinds * kMaxStreamGroups;
+  aux_.assign(nstreams - 1, nullptr);
+  join_.assign(nstreams - 1, nullptr);
+  for (int k = 0; k < nstreams - 1; ++k) {
     SW_CUDA(cudaStreamCreateWithFlags(&aux_[k], cudaStreamNonBlocking));
     SW_CUDA(cudaEventCreateWithFlags(&join_[k], cudaEventDisableTiming));
   }
   SW_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
-  kst_.assign(kKinds, nullptr);
-  kev_.assign(kKinds, nullptr);
-  for (int k = 0; k < kKinds; ++k) {
+  kst_.assign(nstreams, nullptr);
+  kev_.assign(nstreams, nullptr);
+  for (int k = 0; k < nstreams; ++k) {
     SW_CUDA(cudaStreamCreateWithFlags(&kst_[k], cudaStreamNonBlocking));
     SW_CUDA(cudaEventCreateWithFlags(&kev_[k], cudaEventDisableTiming));
   }
@@ -287,8 +288,9 @@ void Batch::build_schedule() {
   plan_.assign(T, {});
   for (size_t t = 0; t < T; ++t) {
     for (int kind = 0; kind < kKinds; ++kind) {
-      Launch l{kind, int(all.size()), 0, 0, 0};
-      for (size_t q = 0; q < jobs_.size(); ++q) {
+     for (int grp = 0; grp < groups_; ++grp) {
+      Launch l{kind, int(all.size()), 0, 0, 0, grp};
+      for (size_t q = grp; q < jobs_.size(); q += groups_) {
         if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
         const HostOp& h = lists[q][t];
         if (t > 0 && lists[q][t - 1].kind != kind) l.deps |= 1 << lists[q][t - 1].kind;
@@ -298,6 +300,7 @@ void Batch::build_schedule() {
         ++l.count;
       }
       if (l.count) plan_[t].push_back(l);
+     }
     }
   }
   SW_CUDA(cudaMalloc(&d_ops_, std::max<size_t>(1, all.size()) * sizeof(GroupOp)));
@@ -340,21 +343,26 @@ void Batch::enqueue_slots(int t0, int t1) {
     // One stream per kind, forked from and joined back into the batch's
     // stream; a job that changes kind between slots makes its new kind's
     // stream wait for its old kind's launch.
+    // Stream (kind, group) = kst_[kind * kMaxStreamGroups + group]; jobs stay
+    // in their group, so the waits are within a group.
+    auto sid = [](int kind, int grp) { return kind * kMaxStreamGroups + grp; };
     SW_CUDA(cudaEventRecord(fork_, stream_));
-    for (int k = 0; k < kKinds; ++k) SW_CUDA(cudaStreamWaitEvent(kst_[k], fork_, 0));
+    for (int k = 0; k < kKinds; ++k)
+      for (int g = 0; g < groups_; ++g) SW_CUDA(cudaStreamWaitEvent(kst_[sid(k, g)], fork_, 0));
     for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
       for (const Launch& l : plan_[t]) {
-        cudaStream_t s = kst_[l.kind];
+        cudaStream_t s = kst_[sid(l.kind, l.group)];
         for (int a = 0; a < kKinds; ++a)
-          if (l.deps & (1 << a)) SW_CUDA(cudaStreamWaitEvent(s, kev_[a], 0));
+          if (l.deps & (1 << a)) SW_CUDA(cudaStreamWaitEvent(s, kev_[sid(a, l.group)], 0));
         launch_kind(l, s);
-        SW_CUDA(cudaEventRecord(kev_[l.kind], s));
+        SW_CUDA(cudaEventRecord(kev_[sid(l.kind, l.group)], s));
       }
     }
-    for (int k = 0; k < kKinds; ++k) {
-      SW_CUDA(cudaEventRecord(kev_[k], kst_[k]));
-      SW_CUDA(cudaStreamWaitEvent(stream_, kev_[k], 0));
-    }
+    for (int k = 0; k < kKinds; ++k)
+      for (int g = 0; g < groups_; ++g) {
+        SW_CUDA(cudaEventRecord(kev_[sid(k, g)], kst_[sid(k, g)]));
+        SW_CUDA(cudaStreamWaitEvent(stream_, kev_[sid(k, g)], 0));
+      }
     return;
   }
   for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
@@ -389,6 +397,13 @@ void Batch::launch_kind(const Launch& l, cudaStream_t s) {
     case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, s)); break;
   }
   ++launches_per_run_;
+}
+
+void Batch::set_stream_groups(int groups) {
+  if (groups < 1 || groups > kMaxStreamGroups)
+    throw std::invalid_argument("stream_groups must be 1.." + std::to_string(kMaxStreamGroups));
+  groups_ = groups;
+  set_chunk_rows(chunk_rows_);  // rebuilds the schedule, drops the graph
 }
 
 void Batch::set_concurrent(int mode) {

@@ -57,6 +57,12 @@ class Batch {
   // Drops the captured graph.
   void set_concurrent(int mode);
   int concurrent() const { return concurrent_; }
+  // Jobs split round-robin into this many groups (1..kMaxStreamGroups), each
+  // with its own launches per slot and kind, and, in mode 2, its own streams:
+  // smaller launches that overlap more.  Rebuilds the schedule.
+  static constexpr int kMaxStreamGroups = 4;
+  void set_stream_groups(int groups);
+  int stream_groups() const { return groups_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -91,6 +97,7 @@ class Batch {
   cudaStream_t stream_;
   bool own_stream_ = false;
   int concurrent_ = 2;
+  int groups_ = 1;
   std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
   cudaEvent_t fork_ = nullptr;
   std::vector<cudaEvent_t> join_;
@@ -104,6 +111,7 @@ class Batch {
   struct Launch {
     int kind, offset, count, warps;
     int deps;  // kinds of the previous slot that some of this launch's jobs come from (bit mask)
+    int group;
   };
   std::vector<std::vector<Launch>> plan_;
   void launch_kind(const Launch& l, cudaStream_t s);

@@ -494,6 +494,7 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "autotune") b->batch->autotune(int(value));
     else if (k == "two_step") b->batch->set_two_step(value != 0);
     else if (k == "concurrent") b->batch->set_concurrent(int(value));
+    else if (k == "stream_groups") b->batch->set_stream_groups(int(value));
     else throw std::invalid_argument("unknown batch option: " + k);
   });
 }
@@ -503,6 +504,8 @@ int32_t seiswg_batch_chunk_rows(const seiswg_batch* b) { return b ? b->batch->ch
 int32_t seiswg_batch_two_step(const seiswg_batch* b) { return b && b->batch->two_step() ? 1 : 0; }
 
 int32_t seiswg_batch_concurrent(const seiswg_batch* b) { return b ? b->batch->concurrent() : 0; }
+
+int32_t seiswg_batch_stream_groups(const seiswg_batch* b) { return b ? b->batch->stream_groups() : 0; }
 
 int seiswg_batch_gradient(seiswg_batch* b, int32_t problem, const char* param, float* host) {
   if (!b || !param || !host) return fail(SEISWG_EINVAL, "seiswg_batch_gradient: null argument");

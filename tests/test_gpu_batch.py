@@ -124,9 +124,10 @@ def test_chunk_rows_and_autotune_leave_gradients_unchanged():
 
 def test_launch_orders_give_the_same_gradients():
     """Serial launches, a slot's kinds on forked streams, and one stream per
-    kind with cross-kind waits only where a job changes kind: the same cell
-    updates in an order the dependencies allow, so the gradients are bitwise
-    equal (a missing dependency would show as a difference)."""
+    kind (and job group) with cross-kind waits only where a job changes kind:
+    the same cell updates in an order the dependencies allow, so the
+    gradients are bitwise equal (a missing dependency would show as a
+    difference)."""
     import seiswg_gb300 as sw
 
     probs = _problems()
@@ -135,10 +136,11 @@ def test_launch_orders_give_the_same_gradients():
     try:
         assert batch.info()["concurrent"] == 2   # the default
         ref = None
-        for mode in (0, 1, 2, 2):                # the last run replays the graph of mode 2
+        for mode, groups in ((0, 1), (1, 1), (2, 1), (2, 1), (2, 2), (2, 4), (1, 3)):
             batch.set_option("concurrent", mode)
+            batch.set_option("stream_groups", groups)   # jobs split into stream groups
             assert batch.info()["concurrent"] == mode
-            batch.run()
+            batch.run()                          # (2, 1) twice: the second run replays the graph
             g = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
             J = [batch.misfit(i) for i in range(len(probs))]
             if ref is None:
@@ -148,8 +150,9 @@ def test_launch_orders_give_the_same_gradients():
             for i in range(len(probs)):
                 for p in g[i]:
                     assert np.array_equal(g[i][p], ref[0][i][p]), (mode, i, p)
-        with pytest.raises(sw.SeiswgError):
-            batch.set_option("concurrent", 3)
+        for key, bad in (("concurrent", 3), ("stream_groups", 0), ("stream_groups", 5)):
+            with pytest.raises(sw.SeiswgError):
+                batch.set_option(key, bad)
     finally:
         batch.close()
         for s in sims:
