@@ -38,10 +38,12 @@ class Batch {
   // Rows per warp chunk of every job (0: each problem's own chunk model).
   // Rebuilds the schedule; the captured graph is dropped.
   void set_chunk_rows(int lx);
-  // Empirical tuning of the chunk rows: times two windows of `slots` slots of
-  // the schedule (the recording forward pass, and the reverse sweep) for each
-  // candidate and keeps the fastest.  Returns its time in milliseconds.  The
-  // timed launches leave results that the next run() overwrites.
+  // Empirical tuning of the chunk rows and of one- or two-step recording:
+  // times a window of `slots` slots at the start of the recording pass and
+  // one in the middle of the reverse sweep for each candidate, scales each to
+  // its phase's slot count and keeps the candidate with the shortest total.
+  // Returns that projected time in milliseconds.  The timed launches leave
+  // results that the next run() overwrites.
   double autotune(int slots);
   int chunk_rows() const { return chunk_rows_; }
   // Jobs (PSV alone, SH alone) record two steps per launch between
