@@ -137,7 +137,7 @@ int seiswg_sim_adjoint_backward(seiswg_sim* sim, const float* adstf, int32_t adj
 int seiswg_sim_kernel_smooth(seiswg_sim* sim, float sigma);
 int seiswg_sim_kernel(seiswg_sim* sim, float* host);
 /* Exact discrete adjoint (no counterpart in the reference, which has only the
- * SH imaging condition above; SURVEY 8(a) "adjoint" row, extended).  The pair
+ * SH imaging condition above, solver.rs:1386-1498).  The pair
  * behaves like an autograd function: forward_op runs source isrc (-1: all)
  * and stores the wavefield every ckpt_every steps (0: ceil(sqrt(nt))); the
  * traces are then available through seiswg_sim_traces.  backward_op takes

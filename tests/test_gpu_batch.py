@@ -1,7 +1,8 @@
 """Batched gradients of uneven problems (grouped launches under one CUDA
 graph, on-device misfit) against the plain per-shot path, problem by
-problem.  The tolerance is the benchmark spec's gradient accuracy, relative L2
-1e-4; the two paths share their kernels, so they agree far closer."""
+problem.  The tolerance is the gradient accuracy the batched configuration
+asks for, relative L2 1e-4; the two paths share their kernels, so they agree
+far closer."""
 import numpy as np
 import pytest
 
