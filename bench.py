@@ -227,9 +227,10 @@ def run_reference(args, rank):
     if rank != 0:
         return
     W = make_workload(nx=args.grid, nz=args.grid, nt=args.nt)
+    phys = args.physics
     rates = []
     for _ in range(args.warmup):
-        cpu_oracle_rate(W, 2)
+        cpu_oracle_rate(W, 2, phys)
     for _ in range(args.steps):
         r, dtm, thr = cpu_oracle_rate(W, args.ref_sample, phys)
         rates.append(r)
@@ -238,7 +239,7 @@ def run_reference(args, rank):
         "impl": "reference", "metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dtm * 1e3 * args.nt / args.ref_sample,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(W, args.nt),
+        "config": workload_config(W, args.nt, phys),
         "cpu_baseline": {"value": val, "unit": METRIC, "cores": thr, "kind": "port",
                          "sample": f"full {W['nx']}x{W['nz']} grid, {args.ref_sample} of {args.nt} steps per "
                                    f"step (FP32 oracle restating fd2d.wgsl, OpenMP)"},
