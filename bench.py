@@ -274,6 +274,8 @@ def run_ours(args, rank, world):
         sim.set_option("two_step", args.two_step)
     if args.two_step_rows:
         sim.set_option("two_step_rows", args.two_step_rows)
+    if args.tma >= 0:
+        sim.set_option("tma", args.tma)
     two_step = args.two_step != 0   # the engine's default for PSV alone and SH alone is on
     sim.upload_model("vp", W["vp"])
     sim.upload_model("vs", W["vs"])
@@ -701,6 +703,7 @@ def main():
     ap.add_argument("--two-step", type=int, default=-1,
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
+    ap.add_argument("--tma", type=int, default=-1, help="c2: two-step rows by tensor copies (1) or bulk copies (0)")
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--stream-groups", type=int, default=0, help="c5: job groups with their own streams (0: default)")
     ap.add_argument("--concurrent", type=int, default=-1,

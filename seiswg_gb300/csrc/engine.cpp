@@ -186,6 +186,54 @@ int Sim::final_buffer(int every) const {
   return b;
 }
 
+namespace {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled() {
+  static const EncodeTiled fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      return EncodeTiled(nullptr);
+    }
+    return reinterpret_cast<EncodeTiled>(f);
+  }();
+  return fn;
+}
+
+// A 3-D map over nfields padded fields (columns ld, rows nx + 2 kHaloRows)
+// whose element (0, 0) pointers are `first` + f * stride floats, with boxes of
+// 128 columns x 1 row x box_fields fields.
+bool encode_fields(CUtensorMap* m, const float* first, ptrdiff_t stride, int nfields, int ld, int rows_alloc,
+                   int box_fields) {
+  const EncodeTiled fn = encode_tiled();
+  if (!fn || stride <= 0) return false;
+  const float* base = first - (size_t(kHaloRows) * size_t(ld) + kHaloCols);
+  const cuuint64_t dims[3] = {cuuint64_t(ld), cuuint64_t(rows_alloc), cuuint64_t(nfields)};
+  const cuuint64_t strides[2] = {cuuint64_t(ld) * sizeof(float), cuuint64_t(stride) * sizeof(float)};
+  const cuuint32_t box[3] = {128, 1, cuuint32_t(box_fields)};  // 32 lanes x 4 columns
+  const cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+void Sim::set_use_tma(bool on) {
+  use_tma_ = on;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
 void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList& inj_in,
                         const ProbeList& probes_in) {
   if (d_.sh) {
@@ -220,7 +268,24 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
     p.probes.list = probes_ + probe_split_;
     p.probes.n = nprobe_ - probe_split_;
   }
-  SW_CUDA(launch_psv_step2(p, stream_));
+  // Tensor copies where the state's five fields and the material's three
+  // lie at uniform strides (state buffers and checkpoint slots do).
+  const int rows_alloc = d_.nx + 2 * kHaloRows;
+  if (use_tma_ && tma_mat_ < 0) {
+    const ptrdiff_t dm = lam_ - rho_;
+    tma_mat_ = (mu_ - lam_ == dm && encode_fields(&tma_.rho, rho_, dm, 3, ld_, rows_alloc, 1) &&
+                encode_fields(&tma_.lm, rho_, dm, 3, ld_, rows_alloc, 2))
+                   ? 1
+                   : 0;
+  }
+  const ptrdiff_t ds = a.vz - a.vx;
+  if (use_tma_ && tma_mat_ == 1 && a.sxx - a.vz == ds && a.szz - a.sxx == ds && a.sxz - a.szz == ds &&
+      encode_fields(&tma_.sig, a.vx, ds, 5, ld_, rows_alloc, 3) &&
+      encode_fields(&tma_.vel, a.vx, ds, 5, ld_, rows_alloc, 2)) {
+    SW_CUDA(launch_psv_step2_tma(p, tma_, stream_));
+  } else {
+    SW_CUDA(launch_psv_step2(p, stream_));
+  }
   ++launches_;
 }
 

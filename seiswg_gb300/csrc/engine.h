@@ -178,6 +178,9 @@ class Sim {
   // Small SH grids run whole forward passes in one thread-block cluster when
   // state and material fit its shared memory (default on).
   void set_use_cluster(bool on) { use_cluster_ = on; }
+  // Two-step PSV launches fetch their rows with 3-D tensor copies where the
+  // state's fields lie at a uniform stride (default on).
+  void set_use_tma(bool on);
   int loader() const { return geom_.loader; }
   // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
   void check_device_error() const;
@@ -224,6 +227,9 @@ class Sim {
   Geom geom2_{};            // decomposition of the two-step kernel (lx 0: not yet modelled)
   bool two_step_ = false;
   bool use_cluster_ = true;
+  bool use_tma_ = true;
+  int tma_mat_ = -1;   // material tensor maps: -1 not yet encoded, 0 unavailable, 1 in tma_
+  Tma2 tma_{};         // rho and lm set once; sig and vel per launch
   int cluster_ctas_ = -1;   // CTAs of the cluster path (0: grid too large; -1: not yet queried)
   int adj_lx_[2] = {0, 0};  // reverse-step rows per chunk, per loader (0: not yet modelled)
   Arena arena_;

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cstddef>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fd_types.h"
@@ -94,6 +95,15 @@ cudaError_t launch_sh_cluster(const ShCluster& p, int ctas, cudaStream_t s);
 cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s);
 size_t step2_smem_bytes();
 int step2_blocks_per_sm();
+// Tensor maps (3-D: columns, rows, fields; 128 x 1 x n boxes) that let the
+// two-step PSV kernel fetch a row of several fields in one TMA copy: sigma^n
+// (sxx, szz, sxz of a state whose fields vx, vz, sxx, szz, sxz lie at a
+// uniform stride), v^n (vx, vz), 1/rho, and lambda, mu (material fields
+// 1/rho, lambda, mu at a uniform stride).  Encoded on the host.
+struct Tma2 {
+  CUtensorMap sig, vel, rho, lm;
+};
+cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s);
 // Two SH time steps per launch (fd_step2.cu), same decomposition as the PSV one.
 cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s);
 int sh_step2_blocks_per_sm();

@@ -3,6 +3,8 @@
 // Built with multiply-add contraction (the one-step kernels keep the
 // reference's separate multiply and add): the two-step march is bound by
 // instruction issue, not by HBM.
+#include <type_traits>
+
 #include "fd_fma.cuh"
 
 namespace seiswg {
@@ -27,7 +29,7 @@ namespace {
 // contraction the results differ from two one-step launches by rounding only.
 // --------------------------------------------------------------------------
 enum Psv2Seg {
-  P2_SXX = 0, P2_SXZ, P2_SZZ,  // sigma^n, row i+1
+  P2_SXX = 0, P2_SZZ, P2_SXZ,  // sigma^n, row i+1 (the order of the state's fields)
   P2_VX, P2_VZ,                // v^n, row i
   P2_RHO, P2_LAM, P2_MU,       // 1/rho row i, lambda/mu row i-2
   P2_NSEG
@@ -41,6 +43,85 @@ enum Psv2Seg {
 struct Bulk2 : BulkRows<P2_NSEG, 6, true, 3> {
   using SegsT = Segs<P2_NSEG>;
   using BulkRows<P2_NSEG, 6, true, 3>::BulkRows;
+};
+
+// The same ring filled by four 3-D tensor copies per row instead of eight
+// bulk copies (lane 0 issues them): sigma^n (3 fields, row i+1), v^n (2,
+// row i), 1/rho (row i), lambda and mu (2, row i-2) -- the stage layout of
+// Psv2Seg.  Coordinates are of the padded fields (halo columns and rows
+// included), so every x is the warp's first column plus kHaloCols: a
+// multiple of 4 floats, as the tensor copy requires.
+struct TmaRows2 {
+  static constexpr int S = 6, KEEP = 3, kAhead = S - 1 - KEEP, NSEG = P2_NSEG;
+  static constexpr int kStages = S;
+  static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
+  using SegsT = Segs<NSEG>;
+  const Tma2* tm = nullptr;
+  int x0, ib, lane, nk, cur, nxt;
+  uint32_t par;
+  float* buf;
+  uint64_t* bar;
+  __device__ TmaRows2(const SegsT&, size_t, int c0_, int ib_, int lane_, float* buf_, uint64_t* bar_, int nk_)
+      : x0(c0_ - 4 * lane_ + kHaloCols), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0), buf(buf_),
+        bar(bar_) {}
+  __device__ __forceinline__ static void tma3(float* dst, const CUtensorMap* map, int x, int y, int z,
+                                              uint64_t* b) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(b))
+        : "memory");
+  }
+  __device__ __forceinline__ void issue_at(int k, int st) {
+    const int y = ib - 1 + k + kHaloRows;  // padded row of iteration k
+    float* sb = buf + st * NSEG * kSegFloats;
+    mbar_expect_tx(&bar[st], kStageBytes);
+    tma3(sb + P2_SXX * kSegFloats, &tm->sig, x0, y + 1, 2, &bar[st]);
+    tma3(sb + P2_VX * kSegFloats, &tm->vel, x0, y, 0, &bar[st]);
+    tma3(sb + P2_RHO * kSegFloats, &tm->rho, x0, y, 0, &bar[st]);
+    tma3(sb + P2_LAM * kSegFloats, &tm->lm, x0, y - 2, 1, &bar[st]);
+  }
+  __device__ __forceinline__ void start() {
+    if (lane == 0) {
+      for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
+      fence_mbar_init();
+      for (int k = 0; k < kAhead && k < nk; ++k) issue_at(k, k % S);
+    }
+    __syncwarp();
+  }
+  __device__ __forceinline__ bool acquire(int k) {
+    __syncwarp();  // the previous iteration's seg_back reads are done
+    cur = nxt;
+    const uint32_t ph = par;
+    if (++nxt == S) {
+      nxt = 0;
+      par ^= 1u;
+    }
+    if (k + kAhead < nk && lane == 0) {
+      fence_proxy_async();
+      issue_at(k + kAhead, cur + kAhead < S ? cur + kAhead : cur + kAhead - S);
+    }
+    return __all_sync(kFull, mbar_wait(&bar[cur], ph));
+  }
+  __device__ __forceinline__ f4 seg_back(int q, int d) const {
+    const int st = cur >= d ? cur - d : cur + S - d;
+    const float4 t = *reinterpret_cast<const float4*>(buf + (st * NSEG + q) * kSegFloats + 4 * lane);
+    f4 r;
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    return r;
+  }
+  __device__ __forceinline__ f4 seg(int q) const {
+    const float4 t = *reinterpret_cast<const float4*>(buf + (cur * NSEG + q) * kSegFloats + 4 * lane);
+    f4 r;
+    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
+    return r;
+  }
+  __device__ __forceinline__ void release() { __syncwarp(); }
+  __device__ __forceinline__ void drain(int k) {
+    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
+    __syncwarp();
+  }
+  static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
 };
 
 __device__ __forceinline__ LaneCols lane_cols2(const Geom& g, int strip, int lane, int& valid) {
@@ -116,7 +197,7 @@ __device__ __forceinline__ void stress(const f4& u0, const f4& u1, const f4& u2,
 // fit the instruction cache.)
 template <class Loader, bool EDGE>
 __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, const LaneCols& L, int valid,
-                                          unsigned char* smem) {
+                                          unsigned char* smem, const Tma2* tm) {
   const Geom& g = p.g;
   const size_t ld = size_t(g.ld);
   const float dt = g.dt;
@@ -143,6 +224,7 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
+  if constexpr (std::is_same<Loader, TmaRows2>::value) rows.tm = tm;
   rows.start();
 
   // Column taper product, and dt folded into the difference factors:
@@ -289,12 +371,13 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
 }
 
 template <class Loader>
-__device__ __forceinline__ void psv2_march(const PsvStep& p, int gw, unsigned char* smem) {
+__device__ __forceinline__ void psv2_march(const PsvStep& p, int gw, unsigned char* smem,
+                                           const Tma2* tm = nullptr) {
   const March m = march_of(p.g, gw);
   if (!m.active) return;
   int valid;
   const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
-  psv2_body<Loader, true>(p, m, L, valid, smem);
+  psv2_body<Loader, true>(p, m, L, valid, smem, tm);
 }
 
 // --------------------------------------------------------------------------
@@ -568,6 +651,21 @@ cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int
     if (attr != cudaSuccess) return attr;
     grouped_forward2_sh_kernel<<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
   }
+  return cudaGetLastError();
+}
+
+// The two-step PSV kernel with its rows fetched by tensor copies.
+__global__ void __launch_bounds__(kStepWarps * 32, 2) psv_step2_tma_kernel(const __grid_constant__ PsvStep p,
+                                                                           const __grid_constant__ Tma2 t) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  psv2_march<TmaRows2>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem, &t);
+}
+
+cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s) {
+  const size_t smem = smem_for<TmaRows2>();
+  static const cudaError_t attr = prepare_kernel(psv_step2_tma_kernel, smem);
+  if (attr != cudaSuccess) return attr;
+  psv_step2_tma_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p, t);
   return cudaGetLastError();
 }
 
