@@ -228,6 +228,20 @@ bool encode_fields(CUtensorMap* m, const float* first, ptrdiff_t stride, int nfi
 
 }  // namespace
 
+// The material maps (1/rho, lambda, mu at a uniform stride), encoded once.
+bool Sim::tma_ready() {
+  if (!use_tma_) return false;
+  if (tma_mat_ < 0) {
+    const int rows_alloc = d_.nx + 2 * kHaloRows;
+    const ptrdiff_t dm = lam_ - rho_;
+    tma_mat_ = (mu_ - lam_ == dm && encode_fields(&tma_.rho, rho_, dm, 3, ld_, rows_alloc, 1) &&
+                encode_fields(&tma_.lm, rho_, dm, 3, ld_, rows_alloc, 2))
+                   ? 1
+                   : 0;
+  }
+  return tma_mat_ == 1;
+}
+
 void Sim::set_use_tma(bool on) {
   use_tma_ = on;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
@@ -249,7 +263,13 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
     p.probes.it = it;
     p.err = err_;
     if (probes_in.n) p.probes.n = probe_split_;
-    SW_CUDA(launch_sh_step2(p, stream_));
+    const ptrdiff_t ds = a.sxy - a.vy;
+    if (tma_ready() && a.szy - a.sxy == ds && encode_fields(&tma_.sig, a.vy, ds, 3, ld_, d_.nx + 2 * kHaloRows, 2) &&
+        encode_fields(&tma_.vel, a.vy, ds, 3, ld_, d_.nx + 2 * kHaloRows, 1)) {
+      SW_CUDA(launch_sh_step2_tma(p, tma_, stream_));
+    } else {
+      SW_CUDA(launch_sh_step2(p, stream_));
+    }
     ++launches_;
     return;
   }
@@ -271,15 +291,8 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
   // Tensor copies where the state's five fields and the material's three
   // lie at uniform strides (state buffers and checkpoint slots do).
   const int rows_alloc = d_.nx + 2 * kHaloRows;
-  if (use_tma_ && tma_mat_ < 0) {
-    const ptrdiff_t dm = lam_ - rho_;
-    tma_mat_ = (mu_ - lam_ == dm && encode_fields(&tma_.rho, rho_, dm, 3, ld_, rows_alloc, 1) &&
-                encode_fields(&tma_.lm, rho_, dm, 3, ld_, rows_alloc, 2))
-                   ? 1
-                   : 0;
-  }
   const ptrdiff_t ds = a.vz - a.vx;
-  if (use_tma_ && tma_mat_ == 1 && a.sxx - a.vz == ds && a.szz - a.sxx == ds && a.sxz - a.szz == ds &&
+  if (tma_ready() && a.sxx - a.vz == ds && a.szz - a.sxx == ds && a.sxz - a.szz == ds &&
       encode_fields(&tma_.sig, a.vx, ds, 5, ld_, rows_alloc, 3) &&
       encode_fields(&tma_.vel, a.vx, ds, 5, ld_, rows_alloc, 2)) {
     SW_CUDA(launch_psv_step2_tma(p, tma_, stream_));

@@ -181,6 +181,7 @@ class Sim {
   // Two-step PSV launches fetch their rows with 3-D tensor copies where the
   // state's fields lie at a uniform stride (default on).
   void set_use_tma(bool on);
+  bool tma_ready();
   int loader() const { return geom_.loader; }
   // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
   void check_device_error() const;

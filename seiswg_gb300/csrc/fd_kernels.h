@@ -104,6 +104,10 @@ struct Tma2 {
   CUtensorMap sig, vel, rho, lm;
 };
 cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s);
+// SH: sig = state fields vy, sxy, szy with boxes of 2 (sxy, szy), vel = the
+// same with boxes of 1 (vy), rho = material fields with boxes of 1 (1/rho,
+// and mu at field 2); lm unused.
+cudaError_t launch_sh_step2_tma(const ShStep& p, const Tma2& t, cudaStream_t s);
 // Two SH time steps per launch (fd_step2.cu), same decomposition as the PSV one.
 cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s);
 int sh_step2_blocks_per_sm();

@@ -45,14 +45,34 @@ struct Bulk2 : BulkRows<P2_NSEG, 6, true, 3> {
   using BulkRows<P2_NSEG, 6, true, 3>::BulkRows;
 };
 
-// The same ring filled by four 3-D tensor copies per row instead of eight
-// bulk copies (lane 0 issues them): sigma^n (3 fields, row i+1), v^n (2,
-// row i), 1/rho (row i), lambda and mu (2, row i-2) -- the stage layout of
-// Psv2Seg.  Coordinates are of the padded fields (halo columns and rows
-// included), so every x is the warp's first column plus kHaloCols: a
-// multiple of 4 floats, as the tensor copy requires.
-struct TmaRows2 {
-  static constexpr int S = 6, KEEP = 3, kAhead = S - 1 - KEEP, NSEG = P2_NSEG;
+// The same ring filled by 3-D tensor copies, issued by lane 0: one copy per
+// group of fields that lie next to each other in memory and share a row
+// offset (`Plan::issue`).  Coordinates are of the padded fields (halo columns
+// and rows included), so every x is the warp's first column plus kHaloCols:
+// a multiple of 4 floats, as the tensor copy requires.
+__device__ __forceinline__ void tma3(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* b) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(b))
+      : "memory");
+}
+
+// PSV: sigma^n (sxx, szz, sxz; row i+1), v^n (vx, vz; row i), 1/rho (row
+// i), lambda and mu (row i-2): four copies for the eight segments of Psv2Seg.
+struct PsvTmaPlan {
+  static constexpr int NSEG = P2_NSEG;
+  __device__ __forceinline__ static void issue(float* sb, const Tma2* tm, int x, int y, uint64_t* b) {
+    tma3(sb + P2_SXX * kSegFloats, &tm->sig, x, y + 1, 2, b);
+    tma3(sb + P2_VX * kSegFloats, &tm->vel, x, y, 0, b);
+    tma3(sb + P2_RHO * kSegFloats, &tm->rho, x, y, 0, b);
+    tma3(sb + P2_LAM * kSegFloats, &tm->lm, x, y - 2, 1, b);
+  }
+};
+
+template <class Plan>
+struct TmaRows {
+  static constexpr int S = 6, KEEP = 3, kAhead = S - 1 - KEEP, NSEG = Plan::NSEG;
   static constexpr int kStages = S;
   static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
   using SegsT = Segs<NSEG>;
@@ -61,25 +81,12 @@ struct TmaRows2 {
   uint32_t par;
   float* buf;
   uint64_t* bar;
-  __device__ TmaRows2(const SegsT&, size_t, int c0_, int ib_, int lane_, float* buf_, uint64_t* bar_, int nk_)
+  __device__ TmaRows(const SegsT&, size_t, int c0_, int ib_, int lane_, float* buf_, uint64_t* bar_, int nk_)
       : x0(c0_ - 4 * lane_ + kHaloCols), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0), buf(buf_),
         bar(bar_) {}
-  __device__ __forceinline__ static void tma3(float* dst, const CUtensorMap* map, int x, int y, int z,
-                                              uint64_t* b) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(b))
-        : "memory");
-  }
   __device__ __forceinline__ void issue_at(int k, int st) {
-    const int y = ib - 1 + k + kHaloRows;  // padded row of iteration k
-    float* sb = buf + st * NSEG * kSegFloats;
     mbar_expect_tx(&bar[st], kStageBytes);
-    tma3(sb + P2_SXX * kSegFloats, &tm->sig, x0, y + 1, 2, &bar[st]);
-    tma3(sb + P2_VX * kSegFloats, &tm->vel, x0, y, 0, &bar[st]);
-    tma3(sb + P2_RHO * kSegFloats, &tm->rho, x0, y, 0, &bar[st]);
-    tma3(sb + P2_LAM * kSegFloats, &tm->lm, x0, y - 2, 1, &bar[st]);
+    Plan::issue(buf + st * NSEG * kSegFloats, tm, x0, ib - 1 + k + kHaloRows, &bar[st]);
   }
   __device__ __forceinline__ void start() {
     if (lane == 0) {
@@ -123,6 +130,7 @@ struct TmaRows2 {
   }
   static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
 };
+using TmaRows2 = TmaRows<PsvTmaPlan>;
 
 __device__ __forceinline__ LaneCols lane_cols2(const Geom& g, int strip, int lane, int& valid) {
   LaneCols L;
@@ -393,6 +401,18 @@ enum Sh2Seg {
   S2_NSEG
 };
 
+// SH: sigma^n (sxy, szy; row i+1; the state's fields vy, sxy, szy), v^n (vy;
+// row i), 1/rho (row i) and mu (row i-2) of the material's 1/rho, lambda, mu.
+struct ShTmaPlan {
+  static constexpr int NSEG = S2_NSEG;
+  __device__ __forceinline__ static void issue(float* sb, const Tma2* tm, int x, int y, uint64_t* b) {
+    tma3(sb + S2_SXY * kSegFloats, &tm->sig, x, y + 1, 1, b);
+    tma3(sb + S2_VY * kSegFloats, &tm->vel, x, y, 0, b);
+    tma3(sb + S2_RHO * kSegFloats, &tm->rho, x, y, 0, b);
+    tma3(sb + S2_MU * kSegFloats, &tm->rho, x, y - 2, 2, b);
+  }
+};
+
 // Six stages: two rows in flight, the last three iterations kept (level 2
 // reads 1/rho of row i-3 and mu of row i-5 from them); lane q issues the
 // copy of segment q (288 against 265 Gcell-updates/s with lane 0 issuing
@@ -414,7 +434,7 @@ __device__ __forceinline__ void inject_dt_y(const InjectList& inj, int i, int c0
 
 template <class Loader>
 __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const LaneCols& L, int valid,
-                                         unsigned char* smem) {
+                                         unsigned char* smem, const Tma2* tm) {
   const Geom& g = p.g;
   const size_t ld = size_t(g.ld);
   const float dt = g.dt;
@@ -438,6 +458,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
+  if constexpr (std::is_same<Loader, TmaRows<ShTmaPlan>>::value) rows.tm = tm;
   rows.start();
 
   f4 tbt;
@@ -565,12 +586,12 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
 }
 
 template <class Loader>
-__device__ __forceinline__ void sh2_march(const ShStep& p, int gw, unsigned char* smem) {
+__device__ __forceinline__ void sh2_march(const ShStep& p, int gw, unsigned char* smem, const Tma2* tm = nullptr) {
   const March m = march_of(p.g, gw);
   if (!m.active) return;
   int valid;
   const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
-  sh2_body<Loader>(p, m, L, valid, smem);
+  sh2_body<Loader>(p, m, L, valid, smem, tm);
 }
 
 }  // namespace
@@ -673,6 +694,20 @@ cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s
 __global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_kernel(const ShStep p) {
   extern __shared__ __align__(128) unsigned char smem[];
   sh2_march<ShBulk2>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+}
+
+__global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_tma_kernel(const __grid_constant__ ShStep p,
+                                                                          const __grid_constant__ Tma2 t) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  sh2_march<TmaRows<ShTmaPlan>>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem, &t);
+}
+
+cudaError_t launch_sh_step2_tma(const ShStep& p, const Tma2& t, cudaStream_t s) {
+  const size_t smem = smem_for<TmaRows<ShTmaPlan>>();
+  static const cudaError_t attr = prepare_kernel(sh_step2_tma_kernel, smem);
+  if (attr != cudaSuccess) return attr;
+  sh_step2_tma_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p, t);
+  return cudaGetLastError();
 }
 
 int sh_step2_blocks_per_sm() {
