@@ -321,7 +321,9 @@ def run_ours(args, rank, world):
     # Algorithmic bytes: 52 B (PSV) or 32 B (SH) per cell-update, the one-step
     # scheme's minimum; the two-step kernels move about half of that
     # (traffic), so their fraction can exceed 1.
-    kernel = f"{phys}_step2_kernel" if two_step else f"{phys}_step_kernel"
+    # (two-step rows are fetched by tensor copies unless --tma 0)
+    kernel = (f"{phys}_step2_tma_kernel" if args.tma != 0 else f"{phys}_step2_kernel") if two_step \
+        else f"{phys}_step_kernel"
     per_launch = 2 if two_step else 1
     launch_s = ms_per_step / 1e3 / (nt / per_launch)
     achieved = BYTES_PER_CELL[phys] * per_launch * nx * nz / launch_s / 1e9
