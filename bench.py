@@ -476,6 +476,8 @@ def run_secondary(args):
             obs.append(sim_t.traces()[[0, 2]])
         sim_t.close()
         sim = W.make_sim()
+        if args.tma >= 0:
+            sim.set_option("tma", args.tma)
         stream = torch.cuda.ExternalStream(sim.stream)
         Js = []
 
@@ -705,7 +707,8 @@ def main():
     ap.add_argument("--two-step", type=int, default=-1,
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
-    ap.add_argument("--tma", type=int, default=-1, help="c2: two-step rows by tensor copies (1) or bulk copies (0)")
+    ap.add_argument("--tma", type=int, default=-1,
+                    help="c2, c4: rows of the two-step and reverse kernels by tensor copies (1) or bulk copies (0)")
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--stream-groups", type=int, default=0, help="c5: job groups with their own streams (0: default)")
     ap.add_argument("--concurrent", type=int, default=-1,

@@ -119,11 +119,11 @@ Sim::~Sim() {
   cudaFree(ck_store_);
   cudaFree(seg_store_);
   cudaFree(adj_store_);
+  cudaFree(snap_store_);
   cudaFree(u_tab_);
   cudaFree(obs_in_);
   cudaFree(j_tr_);
-  for (float* g : {g_lam_, g_mu_, g_b_})
-    if (g) cudaFree(g - size_t(kHaloRows) * ld_ - kHaloCols);
+  if (g_lam_) cudaFree(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols);  // the block of the three gradients
   if (kmu_) cudaFree(kmu_ - size_t(kHaloRows) * ld_ - kHaloCols);
   if (tmp_) cudaFree(tmp_ - size_t(kHaloRows) * ld_ - kHaloCols);
   if (own_stream_) cudaStreamDestroy(stream_);
@@ -240,6 +240,36 @@ bool Sim::tma_ready() {
                    : 0;
   }
   return tma_mat_ == 1;
+}
+
+// The PSV reverse step with its rows fetched by tensor copies, where the
+// forward state f, the incoming adjoint state a, the material and the
+// gradient block lie at uniform strides; false when they do not (the caller
+// launches the bulk-copy kernel).
+bool Sim::launch_adjoint_tma(const PsvAdjoint& p, const State& f, const State& a) {
+  if (!tma_ready()) return false;
+  const int rows_alloc = d_.nx + 2 * kHaloRows;
+  auto uniform = [](const State& x) {
+    const ptrdiff_t d = x.vz - x.vx;
+    return d > 0 && x.sxx - x.vz == d && x.szz - x.sxx == d && x.sxz - x.szz == d;
+  };
+  const ptrdiff_t dg = g_mu_ - g_lam_;
+  if (!uniform(f) || !uniform(a) || dg <= 0 || g_b_ - g_mu_ != dg) return false;
+  if (tma_grad_ != g_lam_) {
+    if (!encode_fields(&tma_adj_.g1, g_lam_, dg, 3, ld_, rows_alloc, 1) ||
+        !encode_fields(&tma_adj_.g2, g_lam_, dg, 3, ld_, rows_alloc, 2))
+      return false;
+    tma_grad_ = g_lam_;
+  }
+  tma_adj_.m1 = tma_.rho;
+  tma_adj_.m2 = tma_.lm;
+  if (!encode_fields(&tma_adj_.f1, f.vx, f.vz - f.vx, 5, ld_, rows_alloc, 1) ||
+      !encode_fields(&tma_adj_.f2, f.vx, f.vz - f.vx, 5, ld_, rows_alloc, 2) ||
+      !encode_fields(&tma_adj_.a3, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 3) ||
+      !encode_fields(&tma_adj_.a2, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 2))
+    return false;
+  SW_CUDA(launch_psv_adjoint_tma(p, tma_adj_, stream_));
+  return true;
 }
 
 void Sim::set_use_tma(bool on) {
@@ -860,12 +890,6 @@ void Sim::adjoint_forward(int isrc, int adj_interval) {
   const size_t fb = field_elems_ * sizeof(float);
   if (fwd_nsa_ != nsa) {
     cudaFree(fwd_store_);
-  cudaFree(ck_store_);
-  cudaFree(seg_store_);
-  cudaFree(adj_store_);
-  cudaFree(u_tab_);
-  for (float* g : {g_lam_, g_mu_, g_b_})
-    if (g) cudaFree(g - size_t(kHaloRows) * ld_ - kHaloCols);
     fwd_store_ = nullptr;
     fwd_bytes_ = size_t(nsa) * fb;
     SW_CUDA(cudaMalloc(&fwd_store_, fwd_bytes_));
@@ -1009,17 +1033,16 @@ void Sim::copy_state(const State& dst, const State& src) {
 
 void Sim::gradient_clear() {
   const size_t fb = field_elems_ * sizeof(float);
-  auto ensure = [&](float*& g) {
-    if (!g) {
-      float* a = nullptr;
-      SW_CUDA(cudaMalloc(&a, fb));
-      g = field_ptr(a);
-    }
-    SW_CUDA(cudaMemsetAsync(g - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
-  };
-  ensure(g_mu_);
-  ensure(g_b_);
-  if (d_.psv) ensure(g_lam_);
+  if (!g_mu_) {
+    // One block, fields lambda, mu, buoyancy at a uniform stride (the
+    // reverse step fetches rows of two of them with one tensor copy).
+    float* a = nullptr;
+    SW_CUDA(cudaMalloc(&a, 3 * fb));
+    g_lam_ = field_ptr(a);
+    g_mu_ = field_ptr(a + field_elems_);
+    g_b_ = field_ptr(a + 2 * field_elems_);
+  }
+  SW_CUDA(cudaMemsetAsync(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols, 0, 3 * fb, stream_));
 }
 
 int Sim::default_checkpoint_interval() const {
@@ -1223,7 +1246,7 @@ void Sim::run_backward() {
           p.src = s2;
           p.rec = r2;
           p.err = err_;
-          SW_CUDA(launch_psv_adjoint(p, stream_));
+          if (!launch_adjoint_tma(p, f, a)) SW_CUDA(launch_psv_adjoint(p, stream_));
         } else {
           ShAdjoint p{};
           p.g = ga;

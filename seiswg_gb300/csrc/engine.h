@@ -181,7 +181,6 @@ class Sim {
   // Two-step PSV launches fetch their rows with 3-D tensor copies where the
   // state's fields lie at a uniform stride (default on).
   void set_use_tma(bool on);
-  bool tma_ready();
   int loader() const { return geom_.loader; }
   // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
   void check_device_error() const;
@@ -231,6 +230,10 @@ class Sim {
   bool use_tma_ = true;
   int tma_mat_ = -1;   // material tensor maps: -1 not yet encoded, 0 unavailable, 1 in tma_
   Tma2 tma_{};         // rho and lm set once; sig and vel per launch
+  TmaAdj tma_adj_{};   // reverse step: g1, g2 for the gradient block at tma_grad_, the rest per launch
+  const float* tma_grad_ = nullptr;
+  bool tma_ready();
+  bool launch_adjoint_tma(const PsvAdjoint& p, const State& f, const State& a);
   int cluster_ctas_ = -1;   // CTAs of the cluster path (0: grid too large; -1: not yet queried)
   int adj_lx_[2] = {0, 0};  // reverse-step rows per chunk, per loader (0: not yet modelled)
   Arena arena_;

@@ -21,7 +21,10 @@
 //
 // Algorithmic bytes per cell-update (PSV): forward state 5 + adjoint state
 // 5 r+w + model 3 + gradients 3 r+w = 96 B (SH: 3 + 3 r+w + 2 + 2 r+w = 60 B).
+#include <type_traits>
+
 #include "fd_march.cuh"
+#include "fd_tma.cuh"
 
 namespace seiswg {
 
@@ -147,8 +150,32 @@ enum PsvAdjSeg {
   PA_NSEG
 };
 
+// Tensor copies of a PSV reverse-step row: eleven copies for the nineteen
+// segments (the forward sigma_xx, sigma_xz of row i+1 and sigma_zz of row i
+// one field each, the forward v, the incoming adjoint stresses of rows i+1
+// and i-2 and velocities of row i, the material, the gradients).
+struct AdjTmaPlan {
+  using Maps = TmaAdj;
+  static constexpr int NSEG = PA_NSEG;
+  __device__ __forceinline__ static void issue(float* sb, const TmaAdj* tm, int x, int y, uint64_t* b) {
+    tma3(sb + PA_SXX * kSegFloats, &tm->f1, x, y + 1, 2, b);
+    tma3(sb + PA_SXZ * kSegFloats, &tm->f1, x, y + 1, 4, b);
+    tma3(sb + PA_SZZ * kSegFloats, &tm->f1, x, y, 3, b);
+    tma3(sb + PA_VX * kSegFloats, &tm->f2, x, y, 0, b);
+    tma3(sb + PA_BXX * kSegFloats, &tm->a3, x, y + 1, 2, b);
+    tma3(sb + PA_WX * kSegFloats, &tm->a2, x, y, 0, b);
+    tma3(sb + PA_OXX * kSegFloats, &tm->a3, x, y - 2, 2, b);
+    tma3(sb + PA_B * kSegFloats, &tm->m1, x, y, 0, b);
+    tma3(sb + PA_LAM * kSegFloats, &tm->m2, x, y + 1, 1, b);
+    tma3(sb + PA_GB * kSegFloats, &tm->g1, x, y, 2, b);
+    tma3(sb + PA_GL * kSegFloats, &tm->g2, x, y - 2, 0, b);
+  }
+};
+using ATma = TmaRows<AdjTmaPlan, kAdjStages, 0>;
+
 template <class Loader>
-__device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, unsigned char* smem) {
+__device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, unsigned char* smem,
+                                                  const TmaAdj* tm = nullptr) {
   const Geom& g = p.g;
   const AMarch m = amarch(g, gw);
   if (!m.active) return;
@@ -179,6 +206,7 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
   segs.base[PA_GL] = p.g_lam; segs.roff[PA_GL] = -2;
   segs.base[PA_GM] = p.g_mu; segs.roff[PA_GM] = -2;
   Loader rows = make_aloader<Loader>(segs, g, m, L, smem);
+  if constexpr (std::is_same<Loader, ATma>::value) rows.tm = tm;
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
@@ -499,6 +527,12 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) psv_adjoint_kernel(const P
   psv_adjoint_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
 }
 
+__global__ void __launch_bounds__(kStepWarps * 32, 2) psv_adjoint_tma_kernel(const __grid_constant__ PsvAdjoint p,
+                                                                             const __grid_constant__ TmaAdj t) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  psv_adjoint_march<ATma>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem, &t);
+}
+
 template <class Loader>
 __global__ void __launch_bounds__(kStepWarps * 32, 2) sh_adjoint_kernel(const ShAdjoint p) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -649,6 +683,14 @@ int adjoint_blocks_per_sm(bool psv, int loader) {
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s) {
   if (p.g.loader == kLoaderBulk) return launch_psv_adj<ABulk<PA_NSEG>>(p, s);
   return launch_psv_adj<ADirect<PA_NSEG>>(p, s);
+}
+
+cudaError_t launch_psv_adjoint_tma(const PsvAdjoint& p, const TmaAdj& t, cudaStream_t s) {
+  const size_t smem = asmem<ATma>();
+  static const cudaError_t attr = aprep(psv_adjoint_tma_kernel, smem);
+  if (attr != cudaSuccess) return attr;
+  psv_adjoint_tma_kernel<<<ablocks(p.g), kStepWarps * 32, smem, s>>>(p, t);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s) {

@@ -104,6 +104,13 @@ struct Tma2 {
   CUtensorMap sig, vel, rho, lm;
 };
 cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s);
+// Tensor maps of the PSV reverse step: the forward state (vx, vz, sxx, szz,
+// sxz) with boxes of 1 and 2 fields, the incoming adjoint state (same field
+// order) with boxes of 3 and 2, the material (1/rho, lambda, mu) with boxes of
+// 1 and 2, and the gradients (lambda, mu, buoyancy) with boxes of 1 and 2.
+struct TmaAdj {
+  CUtensorMap f1, f2, a3, a2, m1, m2, g1, g2;
+};
 // SH: sig = state fields vy, sxy, szy with boxes of 2 (sxy, szy), vel = the
 // same with boxes of 1 (vy), rho = material fields with boxes of 1 (1/rho,
 // and mu at field 2); lm unused.
@@ -142,6 +149,7 @@ struct ShAdjoint {
 // Resident CTAs per SM of the reverse-step kernel for a loader (occupancy query).
 int adjoint_blocks_per_sm(bool psv, int loader);
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s);
+cudaError_t launch_psv_adjoint_tma(const PsvAdjoint& p, const TmaAdj& t, cudaStream_t s);
 cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s);
 
 // ---- grouped launches over many independent jobs (fd_step.cu, fd_adjoint.cu,

@@ -6,6 +6,7 @@
 #include <type_traits>
 
 #include "fd_fma.cuh"
+#include "fd_tma.cuh"
 
 namespace seiswg {
 
@@ -45,22 +46,10 @@ struct Bulk2 : BulkRows<P2_NSEG, 6, true, 3> {
   using BulkRows<P2_NSEG, 6, true, 3>::BulkRows;
 };
 
-// The same ring filled by 3-D tensor copies, issued by lane 0: one copy per
-// group of fields that lie next to each other in memory and share a row
-// offset (`Plan::issue`).  Coordinates are of the padded fields (halo columns
-// and rows included), so every x is the warp's first column plus kHaloCols:
-// a multiple of 4 floats, as the tensor copy requires.
-__device__ __forceinline__ void tma3(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* b) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-      "[%5];" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(b))
-      : "memory");
-}
-
 // PSV: sigma^n (sxx, szz, sxz; row i+1), v^n (vx, vz; row i), 1/rho (row
 // i), lambda and mu (row i-2): four copies for the eight segments of Psv2Seg.
 struct PsvTmaPlan {
+  using Maps = Tma2;
   static constexpr int NSEG = P2_NSEG;
   __device__ __forceinline__ static void issue(float* sb, const Tma2* tm, int x, int y, uint64_t* b) {
     tma3(sb + P2_SXX * kSegFloats, &tm->sig, x, y + 1, 2, b);
@@ -70,67 +59,7 @@ struct PsvTmaPlan {
   }
 };
 
-template <class Plan>
-struct TmaRows {
-  static constexpr int S = 6, KEEP = 3, kAhead = S - 1 - KEEP, NSEG = Plan::NSEG;
-  static constexpr int kStages = S;
-  static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
-  using SegsT = Segs<NSEG>;
-  const Tma2* tm = nullptr;
-  int x0, ib, lane, nk, cur, nxt;
-  uint32_t par;
-  float* buf;
-  uint64_t* bar;
-  __device__ TmaRows(const SegsT&, size_t, int c0_, int ib_, int lane_, float* buf_, uint64_t* bar_, int nk_)
-      : x0(c0_ - 4 * lane_ + kHaloCols), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0), buf(buf_),
-        bar(bar_) {}
-  __device__ __forceinline__ void issue_at(int k, int st) {
-    mbar_expect_tx(&bar[st], kStageBytes);
-    Plan::issue(buf + st * NSEG * kSegFloats, tm, x0, ib - 1 + k + kHaloRows, &bar[st]);
-  }
-  __device__ __forceinline__ void start() {
-    if (lane == 0) {
-      for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
-      fence_mbar_init();
-      for (int k = 0; k < kAhead && k < nk; ++k) issue_at(k, k % S);
-    }
-    __syncwarp();
-  }
-  __device__ __forceinline__ bool acquire(int k) {
-    __syncwarp();  // the previous iteration's seg_back reads are done
-    cur = nxt;
-    const uint32_t ph = par;
-    if (++nxt == S) {
-      nxt = 0;
-      par ^= 1u;
-    }
-    if (k + kAhead < nk && lane == 0) {
-      fence_proxy_async();
-      issue_at(k + kAhead, cur + kAhead < S ? cur + kAhead : cur + kAhead - S);
-    }
-    return __all_sync(kFull, mbar_wait(&bar[cur], ph));
-  }
-  __device__ __forceinline__ f4 seg_back(int q, int d) const {
-    const int st = cur >= d ? cur - d : cur + S - d;
-    const float4 t = *reinterpret_cast<const float4*>(buf + (st * NSEG + q) * kSegFloats + 4 * lane);
-    f4 r;
-    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
-    return r;
-  }
-  __device__ __forceinline__ f4 seg(int q) const {
-    const float4 t = *reinterpret_cast<const float4*>(buf + (cur * NSEG + q) * kSegFloats + 4 * lane);
-    f4 r;
-    r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
-    return r;
-  }
-  __device__ __forceinline__ void release() { __syncwarp(); }
-  __device__ __forceinline__ void drain(int k) {
-    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
-    __syncwarp();
-  }
-  static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
-};
-using TmaRows2 = TmaRows<PsvTmaPlan>;
+using TmaRows2 = TmaRows<PsvTmaPlan, 6, 3>;
 
 __device__ __forceinline__ LaneCols lane_cols2(const Geom& g, int strip, int lane, int& valid) {
   LaneCols L;
@@ -404,6 +333,7 @@ enum Sh2Seg {
 // SH: sigma^n (sxy, szy; row i+1; the state's fields vy, sxy, szy), v^n (vy;
 // row i), 1/rho (row i) and mu (row i-2) of the material's 1/rho, lambda, mu.
 struct ShTmaPlan {
+  using Maps = Tma2;
   static constexpr int NSEG = S2_NSEG;
   __device__ __forceinline__ static void issue(float* sb, const Tma2* tm, int x, int y, uint64_t* b) {
     tma3(sb + S2_SXY * kSegFloats, &tm->sig, x, y + 1, 1, b);
@@ -458,7 +388,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
-  if constexpr (std::is_same<Loader, TmaRows<ShTmaPlan>>::value) rows.tm = tm;
+  if constexpr (std::is_same<Loader, TmaRows<ShTmaPlan, 6, 3>>::value) rows.tm = tm;
   rows.start();
 
   f4 tbt;
@@ -699,11 +629,11 @@ __global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_kernel(const ShSt
 __global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_tma_kernel(const __grid_constant__ ShStep p,
                                                                           const __grid_constant__ Tma2 t) {
   extern __shared__ __align__(128) unsigned char smem[];
-  sh2_march<TmaRows<ShTmaPlan>>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem, &t);
+  sh2_march<TmaRows<ShTmaPlan, 6, 3>>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem, &t);
 }
 
 cudaError_t launch_sh_step2_tma(const ShStep& p, const Tma2& t, cudaStream_t s) {
-  const size_t smem = smem_for<TmaRows<ShTmaPlan>>();
+  const size_t smem = smem_for<TmaRows<ShTmaPlan, 6, 3>>();
   static const cudaError_t attr = prepare_kernel(sh_step2_tma_kernel, smem);
   if (attr != cudaSuccess) return attr;
   sh_step2_tma_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p, t);
