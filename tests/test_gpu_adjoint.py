@@ -271,3 +271,28 @@ def test_gradient_matches_fp64_oracle_in_the_c4_geometry():
     dm = W.extra["true_model"]["vp"].astype(np.float64) - W.model["vp"]
     d_ours, d_ref = float((ours[0] * dm).sum()), float((ref[0] * dm).sum())
     assert abs(d_ours - d_ref) <= 1e-3 * abs(d_ref)
+
+
+def test_exact_gradient_and_reference_adjoint_share_a_sim():
+    """The exact gradient, then the reference's SH imaging-condition adjoint
+    (its forward store sized by adj_interval), then the exact gradient again
+    on the same Sim: the workspaces of one path leave the other's intact, so
+    the two exact gradients are the same bits."""
+    import seiswg_gb300 as sw
+
+    vp, vs, rho, flags, src, rec = _problem("sh", 3)
+    obs = _observed(vp, vs, rho, flags, src, rec, 0)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    try:
+        first = _gpu_gradient(sim, flags, obs, 0, 0)[2]
+        for adj_interval in (5, 7):   # two store sizes: the store is resized once
+            sim.kernel_clear()
+            sim.adjoint_forward(0, adj_interval)
+            _, adstf = sw.waveform_misfit(sim.traces()[1], obs[0], DT)   # uy against the observed uy
+            sim.adjoint_backward(adstf, adj_interval)
+            assert np.isfinite(sim.kernel()).all()
+        again = _gpu_gradient(sim, flags, obs, 0, 0)[2]
+        for p in first:
+            assert np.array_equal(first[p], again[p]), p
+    finally:
+        sim.close()
