@@ -5,10 +5,10 @@
 // plus the spin state vy_c, syx_c, syy_c, syz_c and 1/J, nu, mu_c+nu_c
 // (fd2d.wgsl:308-399, 319-339, 405-445; 96 B per cell-update).
 //
-// The kernel is bound by instruction issue (230 registers, 8 warps per SM),
-// so it is built with multiply-add contraction and dt is folded into the
-// difference factors (dt/(8 h)); results match the reference's operation
-// order to rounding (relative L2 ~1e-7), not bitwise.
+// At 238 registers (8 warps per SM) the kernel is bound by latency; it is
+// built with multiply-add contraction and dt is folded into the difference
+// factors (dt/(8 h)), which cut its instructions by 16 %; results match the
+// reference's operation order to rounding (relative L2 ~1e-7), not bitwise.
 #include "fd_fma.cuh"
 
 namespace seiswg {
