@@ -175,7 +175,10 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * the two-step kernel; 0: its occupancy model), "cluster" (0/1: SH grids
  * whose state and material fit one thread-block cluster's shared memory run
  * each forward pass in one launch with the wavefield on chip; default on;
- * results are the one-step kernel's bits). */
+ * results are the one-step kernel's bits), "tma" (0/1: the two-step and the
+ * PSV reverse kernels fetch their rows with 3-D tensor copies where the
+ * fields lie at uniform strides, default on; 0: one bulk copy per field;
+ * the same results either way). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */
