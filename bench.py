@@ -635,6 +635,8 @@ def run_secondary(args):
             batch.set_option("concurrent", args.concurrent)
         if args.stream_groups > 0:
             batch.set_option("stream_groups", args.stream_groups)
+        if args.tma >= 0:
+            batch.set_option("tma", args.tma)
         tune_ms = None
         if args.autotune:
             t0 = time.perf_counter()
@@ -670,7 +672,7 @@ def run_secondary(args):
                            "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
                            "concurrent": info.get("concurrent"), "stream_groups": info.get("stream_groups"),
-                           "autotune_ms": tune_ms},
+                           "tma": args.tma != 0, "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
             small = min(range(len(problems)), key=lambda q: problems[q].cells)
@@ -708,7 +710,7 @@ def main():
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--tma", type=int, default=-1,
-                    help="c2, c4: rows of the two-step and reverse kernels by tensor copies (1) or bulk copies (0)")
+                    help="c2, c4, c5: rows of the two-step and reverse kernels by tensor copies (1) or bulk copies (0)")
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--stream-groups", type=int, default=0, help="c5: job groups with their own streams (0: default)")
     ap.add_argument("--concurrent", type=int, default=-1,

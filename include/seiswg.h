@@ -214,8 +214,11 @@ int seiswg_batch_run(seiswg_batch* batch);
  * join before the next slot, 2 (default) one stream per kind, a launch
  * waiting only for the previous slot's launches of the kinds its jobs come
  * from; "stream_groups" (1..4, default 1): jobs split round-robin into
- * groups with their own launches (and streams in order 2).  Each drops the
- * captured graph. */
+ * groups with their own launches (and streams in order 2); "tma" (0/1,
+ * default 1): the grouped two-step forward and PSV reverse launches fetch
+ * rows with 3-D tensor copies through each job's table of tensor maps, or
+ * with one bulk copy per field (the same bits).  Each drops the captured
+ * graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
 /* The chunk rows in use (0: each problem's own chunk model), and whether
  * jobs record two steps per launch. */

@@ -452,7 +452,8 @@ class Batch:
 
     def set_option(self, key: str, value: int):
         """"chunk_rows" (0: per-problem model), "two_step" (0/1), "concurrent" (0, 1, 2: launch order),
-        "stream_groups" (1..4) or "autotune" (slots per timing window)."""
+        "stream_groups" (1..4), "tma" (0/1: rows of the grouped two-step and reverse launches by tensor
+        copies or bulk copies) or "autotune" (slots per timing window)."""
         _check(lib().seiswg_batch_set_option(self._h, key.encode(), int(value)))
 
     def gradient(self, problem: int, param: str):

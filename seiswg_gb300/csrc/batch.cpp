@@ -129,6 +129,33 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       jd.nt = nt;
       jd.dt = d.dt;
       jd.err = err_;
+      // Tensor maps (JobDesc): state slots with boxes of 1, 2 and 3 fields,
+      // the adjoint slots (3, 2), the material (1, 2), the gradients (1, 2).
+      {
+        const int rows_alloc = d.nx + 2 * kHaloRows;
+        const int nf = j.nstate;
+        std::vector<CUtensorMap> maps(size_t(3) * j.nslot + kJobTmaTail);
+        bool ok = v.lam - v.rho == v.mu - v.lam && v.lam > v.rho;
+        for (int sl = 0; ok && sl < j.nslot; ++sl)
+          for (int b = 0; ok && b < 3; ++b)
+            ok = encode_fields(&maps[3 * sl + b], j.pool + sl * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc,
+                               std::min(b + 1, nf));
+        CUtensorMap* t = maps.data() + 3 * j.nslot;
+        for (int a = 0; ok && a < 2; ++a)
+          ok = encode_fields(&t[2 * a], j.adj + a * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc, std::min(3, nf)) &&
+               encode_fields(&t[2 * a + 1], j.adj + a * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc, 2);
+        ok = ok && encode_fields(&t[4], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
+             encode_fields(&t[5], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 2) &&
+             encode_fields(&t[6], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 1) &&
+             encode_fields(&t[7], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 2);
+        if (ok) {
+          SW_CUDA(cudaMalloc(&j.tm, maps.size() * sizeof(CUtensorMap)));
+          SW_CUDA(cudaMemcpy(j.tm, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+          bytes_ += maps.size() * sizeof(CUtensorMap);
+        }
+        jd.tm = j.tm;
+        jd.tm_nslot = j.nslot;
+      }
       descs_.push_back(jd);
       model_geom_.push_back(jd.g);
       model_geom2_.push_back(jd.g2);
@@ -220,7 +247,7 @@ Batch::~Batch() {
   if (graph_) cudaGraphExecDestroy(graph_);
   for (Job& j : jobs_) {
     for (void* p : {(void*)j.pool, (void*)j.adj, (void*)j.grads, (void*)j.acc, (void*)j.hist, (void*)j.obs,
-                    (void*)j.u_tab, (void*)j.J, (void*)j.src, (void*)j.rec})
+                    (void*)j.u_tab, (void*)j.J, (void*)j.src, (void*)j.rec, (void*)j.tm})
       cudaFree(p);
   }
   for (float* s : sums_) cudaFree(s);
@@ -404,6 +431,16 @@ void Batch::set_stream_groups(int groups) {
     throw std::invalid_argument("stream_groups must be 1.." + std::to_string(kMaxStreamGroups));
   groups_ = groups;
   set_chunk_rows(chunk_rows_);  // rebuilds the schedule, drops the graph
+}
+
+void Batch::set_tma(bool on) {
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  tma_ = on;
+  for (size_t q = 0; q < descs_.size(); ++q) descs_[q].tm = on ? jobs_[q].tm : nullptr;
+  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
 }
 
 void Batch::set_concurrent(int mode) {

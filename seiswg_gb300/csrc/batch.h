@@ -65,6 +65,10 @@ class Batch {
   static constexpr int kMaxStreamGroups = 4;
   void set_stream_groups(int groups);
   int stream_groups() const { return groups_; }
+  // Grouped launches fetch rows with 3-D tensor copies (default on) or one
+  // bulk copy per field; the same results.  Drops the captured graph.
+  void set_tma(bool on);
+  bool tma() const { return tma_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -78,6 +82,7 @@ class Batch {
   struct Job {
     int problem, shot, k, ncp, nslot, nt, nstate, ncomp, nrec;
     bool psv;
+    CUtensorMap* tm = nullptr;  // the job's tensor-map table in device memory (see JobDesc)
     float *pool = nullptr, *adj = nullptr, *grads = nullptr, *acc = nullptr, *hist = nullptr, *obs = nullptr,
           *u_tab = nullptr;
     double* J = nullptr;
@@ -99,6 +104,7 @@ class Batch {
   cudaStream_t stream_;
   bool own_stream_ = false;
   int concurrent_ = 2;
+  bool tma_ = true;   // grouped launches fetch rows by tensor copies where the job has a map table
   int groups_ = 1;
   std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
   cudaEvent_t fork_ = nullptr;

@@ -496,6 +496,7 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "two_step") b->batch->set_two_step(value != 0);
     else if (k == "concurrent") b->batch->set_concurrent(int(value));
     else if (k == "stream_groups") b->batch->set_stream_groups(int(value));
+    else if (k == "tma") b->batch->set_tma(value != 0);
     else throw std::invalid_argument("unknown batch option: " + k);
   });
 }

@@ -209,6 +209,8 @@ EncodeTiled encode_tiled() {
   return fn;
 }
 
+}  // namespace
+
 // A 3-D map over nfields padded fields (columns ld, rows nx + 2 kHaloRows)
 // whose element (0, 0) pointers are `first` + f * stride floats, with boxes of
 // 128 columns x 1 row x box_fields fields.
@@ -225,8 +227,6 @@ bool encode_fields(CUtensorMap* m, const float* first, ptrdiff_t stride, int nfi
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
-
-}  // namespace
 
 // The material maps (1/rho, lambda, mu at a uniform stride), encoded once.
 bool Sim::tma_ready() {

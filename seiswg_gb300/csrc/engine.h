@@ -59,6 +59,13 @@ class Arena {
   size_t plan_ = 0, used_ = 0;
 };
 
+// A 3-D tensor map over nfields padded fields (columns ld, rows rows_alloc)
+// whose element (0, 0) pointers are `first` + f * stride floats, with boxes of
+// 128 columns x 1 row x box_fields fields; false when the driver cannot
+// encode it.
+bool encode_fields(CUtensorMap* m, const float* first, ptrdiff_t stride, int nfields, int ld, int rows_alloc,
+                   int box_fields);
+
 class Sim {
  public:
   Sim(const SimDesc& d, cudaStream_t stream = nullptr);

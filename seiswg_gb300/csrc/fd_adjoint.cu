@@ -157,25 +157,26 @@ enum PsvAdjSeg {
 struct AdjTmaPlan {
   using Maps = TmaAdj;
   static constexpr int NSEG = PA_NSEG;
-  __device__ __forceinline__ static void issue(float* sb, const TmaAdj* tm, int x, int y, uint64_t* b) {
-    tma3(sb + PA_SXX * kSegFloats, &tm->f1, x, y + 1, 2, b);
-    tma3(sb + PA_SXZ * kSegFloats, &tm->f1, x, y + 1, 4, b);
-    tma3(sb + PA_SZZ * kSegFloats, &tm->f1, x, y, 3, b);
-    tma3(sb + PA_VX * kSegFloats, &tm->f2, x, y, 0, b);
-    tma3(sb + PA_BXX * kSegFloats, &tm->a3, x, y + 1, 2, b);
-    tma3(sb + PA_WX * kSegFloats, &tm->a2, x, y, 0, b);
-    tma3(sb + PA_OXX * kSegFloats, &tm->a3, x, y - 2, 2, b);
-    tma3(sb + PA_B * kSegFloats, &tm->m1, x, y, 0, b);
-    tma3(sb + PA_LAM * kSegFloats, &tm->m2, x, y + 1, 1, b);
-    tma3(sb + PA_GB * kSegFloats, &tm->g1, x, y, 2, b);
-    tma3(sb + PA_GL * kSegFloats, &tm->g2, x, y - 2, 0, b);
+  template <class M>
+  __device__ __forceinline__ static void issue(float* sb, const M* tm, int x, int y, uint64_t* b) {
+    tma3(sb + PA_SXX * kSegFloats, tmap(tm->f1), x, y + 1, 2, b);
+    tma3(sb + PA_SXZ * kSegFloats, tmap(tm->f1), x, y + 1, 4, b);
+    tma3(sb + PA_SZZ * kSegFloats, tmap(tm->f1), x, y, 3, b);
+    tma3(sb + PA_VX * kSegFloats, tmap(tm->f2), x, y, 0, b);
+    tma3(sb + PA_BXX * kSegFloats, tmap(tm->a3), x, y + 1, 2, b);
+    tma3(sb + PA_WX * kSegFloats, tmap(tm->a2), x, y, 0, b);
+    tma3(sb + PA_OXX * kSegFloats, tmap(tm->a3), x, y - 2, 2, b);
+    tma3(sb + PA_B * kSegFloats, tmap(tm->m1), x, y, 0, b);
+    tma3(sb + PA_LAM * kSegFloats, tmap(tm->m2), x, y + 1, 1, b);
+    tma3(sb + PA_GB * kSegFloats, tmap(tm->g1), x, y, 2, b);
+    tma3(sb + PA_GL * kSegFloats, tmap(tm->g2), x, y - 2, 0, b);
   }
 };
 using ATma = TmaRows<AdjTmaPlan, kAdjStages, 0>;
 
-template <class Loader>
+template <class Loader, class M = TmaAdj>
 __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, unsigned char* smem,
-                                                  const TmaAdj* tm = nullptr) {
+                                                  const M* tm = nullptr) {
   const Geom& g = p.g;
   const AMarch m = amarch(g, gw);
   if (!m.active) return;
@@ -206,7 +207,7 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
   segs.base[PA_GL] = p.g_lam; segs.roff[PA_GL] = -2;
   segs.base[PA_GM] = p.g_mu; segs.roff[PA_GM] = -2;
   Loader rows = make_aloader<Loader>(segs, g, m, L, smem);
-  if constexpr (std::is_same<Loader, ATma>::value) rows.tm = tm;
+  if constexpr (std::is_same<Loader, TmaRows<AdjTmaPlan, kAdjStages, 0, M>>::value) rows.tm = tm;
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
@@ -354,9 +355,13 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
         sxx.v[e] = oxx.v[e] + ax.v[e];
         szz.v[e] = ozz.v[e] + bz.v[e];
         sxz.v[e] = oxz.v[e] + (bx.v[e] + az.v[e]);
-        gl.v[e] = gl.v[e] + dt * (oxx.v[e] + ozz.v[e]) * (exx.v[e] + ezz.v[e]);
-        gm.v[e] = gm.v[e] + dt * (2.0f * oxx.v[e] * exx.v[e] + 2.0f * ozz.v[e] * ezz.v[e] +
-                                  oxz.v[e] * (exz.v[e] + ezx.v[e]));
+        // Explicitly rounded operations: the march is inlined into several
+        // kernels (bulk or tensor-copy rows, plain or grouped), and left to
+        // contraction the sums could round differently in each.
+        gl.v[e] = fmaf(__fmul_rn(dt, __fadd_rn(oxx.v[e], ozz.v[e])), __fadd_rn(exx.v[e], ezz.v[e]), gl.v[e]);
+        const float shear = __fmul_rn(oxz.v[e], __fadd_rn(exz.v[e], ezx.v[e]));
+        const float dev = fmaf(2.0f * oxx.v[e], exx.v[e], fmaf(2.0f * ozz.v[e], ezz.v[e], shear));
+        gm.v[e] = fmaf(dt, dev, gm.v[e]);
       }
       st4_masked(at(p.bxx1, r), sxx, L.own);
       st4_masked(at(p.bzz1, r), szz, L.own);
@@ -619,7 +624,14 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_adjoint_kernel(con
     p.src = src;
     p.rec = rec;
     p.err = J.err;
-    psv_adjoint_march<ABulk<PA_NSEG>>(p, lw, smem);
+    if (J.tm) {
+      const CUtensorMap* t = J.tm + 3 * J.tm_nslot;
+      const TmaAdjPtrs mp{J.tm + 3 * op.a + 0, J.tm + 3 * op.a + 1, t + 2 * in, t + 2 * in + 1,
+                          t + 4,               t + 5,               t + 6,      t + 7};
+      psv_adjoint_march<TmaRows<AdjTmaPlan, kAdjStages, 0, TmaAdjPtrs>, TmaAdjPtrs>(p, lw, smem, &mp);
+    } else {
+      psv_adjoint_march<ABulk<PA_NSEG>>(p, lw, smem);
+    }
   } else {
     ShAdjoint p{};
     p.g = J.g;

@@ -111,6 +111,13 @@ cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s
 struct TmaAdj {
   CUtensorMap f1, f2, a3, a2, m1, m2, g1, g2;
 };
+// The same maps as pointers into a table in device memory (grouped launches).
+struct Tma2Ptrs {
+  const CUtensorMap *sig, *vel, *rho, *lm;
+};
+struct TmaAdjPtrs {
+  const CUtensorMap *f1, *f2, *a3, *a2, *m1, *m2, *g1, *g2;
+};
 // SH: sig = state fields vy, sxy, szy with boxes of 2 (sxy, szy), vel = the
 // same with boxes of 1 (vy), rho = material fields with boxes of 1 (1/rho,
 // and mu at field 2); lm unused.
@@ -180,7 +187,14 @@ struct JobDesc {
   int nrec, nt;
   float dt;
   int* err;
+  // Tensor maps of the job (nullptr: bulk copies): for pool slot s, maps of
+  // its state fields with boxes of 1, 2 and 3 fields at tm[3 s + 0..2]; then,
+  // from tm[3 tm_nslot]: adjoint slot 0 (boxes of 3 and 2), adjoint slot 1
+  // (3, 2), the material (1, 2) and the gradient block (1, 2).
+  const CUtensorMap* tm;
+  int tm_nslot;
 };
+constexpr int kJobTmaTail = 8;  // maps after the slots' in a job's table
 
 // One operation of one job in a grouped launch.  Forward: step `it` from slot
 // a to slot b (flags & 1: record the probes).  Adjoint: reverse step `it` with

@@ -51,11 +51,12 @@ struct Bulk2 : BulkRows<P2_NSEG, 6, true, 3> {
 struct PsvTmaPlan {
   using Maps = Tma2;
   static constexpr int NSEG = P2_NSEG;
-  __device__ __forceinline__ static void issue(float* sb, const Tma2* tm, int x, int y, uint64_t* b) {
-    tma3(sb + P2_SXX * kSegFloats, &tm->sig, x, y + 1, 2, b);
-    tma3(sb + P2_VX * kSegFloats, &tm->vel, x, y, 0, b);
-    tma3(sb + P2_RHO * kSegFloats, &tm->rho, x, y, 0, b);
-    tma3(sb + P2_LAM * kSegFloats, &tm->lm, x, y - 2, 1, b);
+  template <class M>
+  __device__ __forceinline__ static void issue(float* sb, const M* tm, int x, int y, uint64_t* b) {
+    tma3(sb + P2_SXX * kSegFloats, tmap(tm->sig), x, y + 1, 2, b);
+    tma3(sb + P2_VX * kSegFloats, tmap(tm->vel), x, y, 0, b);
+    tma3(sb + P2_RHO * kSegFloats, tmap(tm->rho), x, y, 0, b);
+    tma3(sb + P2_LAM * kSegFloats, tmap(tm->lm), x, y - 2, 1, b);
   }
 };
 
@@ -132,9 +133,9 @@ __device__ __forceinline__ void stress(const f4& u0, const f4& u1, const f4& u2,
 // zeroed.  (A second, test-free instantiation for interior warps executed 17 %
 // fewer instructions but ran 8 % slower: two bodies of this size no longer
 // fit the instruction cache.)
-template <class Loader, bool EDGE>
+template <class Loader, bool EDGE, class M>
 __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, const LaneCols& L, int valid,
-                                          unsigned char* smem, const Tma2* tm) {
+                                          unsigned char* smem, const M* tm) {
   const Geom& g = p.g;
   const size_t ld = size_t(g.ld);
   const float dt = g.dt;
@@ -161,7 +162,7 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
-  if constexpr (std::is_same<Loader, TmaRows2>::value) rows.tm = tm;
+  if constexpr (std::is_same<Loader, TmaRows<PsvTmaPlan, 6, 3, M>>::value) rows.tm = tm;
   rows.start();
 
   // Column taper product, and dt folded into the difference factors:
@@ -307,14 +308,14 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
   }
 }
 
-template <class Loader>
+template <class Loader, class M = Tma2>
 __device__ __forceinline__ void psv2_march(const PsvStep& p, int gw, unsigned char* smem,
-                                           const Tma2* tm = nullptr) {
+                                           const M* tm = nullptr) {
   const March m = march_of(p.g, gw);
   if (!m.active) return;
   int valid;
   const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
-  psv2_body<Loader, true>(p, m, L, valid, smem, tm);
+  psv2_body<Loader, true, M>(p, m, L, valid, smem, tm);
 }
 
 // --------------------------------------------------------------------------
@@ -335,11 +336,12 @@ enum Sh2Seg {
 struct ShTmaPlan {
   using Maps = Tma2;
   static constexpr int NSEG = S2_NSEG;
-  __device__ __forceinline__ static void issue(float* sb, const Tma2* tm, int x, int y, uint64_t* b) {
-    tma3(sb + S2_SXY * kSegFloats, &tm->sig, x, y + 1, 1, b);
-    tma3(sb + S2_VY * kSegFloats, &tm->vel, x, y, 0, b);
-    tma3(sb + S2_RHO * kSegFloats, &tm->rho, x, y, 0, b);
-    tma3(sb + S2_MU * kSegFloats, &tm->rho, x, y - 2, 2, b);
+  template <class M>
+  __device__ __forceinline__ static void issue(float* sb, const M* tm, int x, int y, uint64_t* b) {
+    tma3(sb + S2_SXY * kSegFloats, tmap(tm->sig), x, y + 1, 1, b);
+    tma3(sb + S2_VY * kSegFloats, tmap(tm->vel), x, y, 0, b);
+    tma3(sb + S2_RHO * kSegFloats, tmap(tm->rho), x, y, 0, b);
+    tma3(sb + S2_MU * kSegFloats, tmap(tm->rho), x, y - 2, 2, b);
   }
 };
 
@@ -362,9 +364,9 @@ __device__ __forceinline__ void inject_dt_y(const InjectList& inj, int i, int c0
   for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(dt, fy.v[e], ds.v[e]);
 }
 
-template <class Loader>
+template <class Loader, class M>
 __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const LaneCols& L, int valid,
-                                         unsigned char* smem, const Tma2* tm) {
+                                         unsigned char* smem, const M* tm) {
   const Geom& g = p.g;
   const size_t ld = size_t(g.ld);
   const float dt = g.dt;
@@ -388,7 +390,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
-  if constexpr (std::is_same<Loader, TmaRows<ShTmaPlan, 6, 3>>::value) rows.tm = tm;
+  if constexpr (std::is_same<Loader, TmaRows<ShTmaPlan, 6, 3, M>>::value) rows.tm = tm;
   rows.start();
 
   f4 tbt;
@@ -515,13 +517,13 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
   }
 }
 
-template <class Loader>
-__device__ __forceinline__ void sh2_march(const ShStep& p, int gw, unsigned char* smem, const Tma2* tm = nullptr) {
+template <class Loader, class M = Tma2>
+__device__ __forceinline__ void sh2_march(const ShStep& p, int gw, unsigned char* smem, const M* tm = nullptr) {
   const March m = march_of(p.g, gw);
   if (!m.active) return;
   int valid;
   const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
-  sh2_body<Loader>(p, m, L, valid, smem, tm);
+  sh2_body<Loader, M>(p, m, L, valid, smem, tm);
 }
 
 }  // namespace
@@ -558,7 +560,13 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(co
   if (!(op.flags & 1)) p.probes.n = 0;
   p.probes.it = op.it;
   p.err = J.err;
-  psv2_march<Bulk2>(p, lw, smem);
+  if (J.tm) {
+    const CUtensorMap* t = J.tm + 3 * J.tm_nslot;
+    const Tma2Ptrs mp{J.tm + 3 * op.a + 2, J.tm + 3 * op.a + 1, t + 4, t + 5};
+    psv2_march<TmaRows<PsvTmaPlan, 6, 3, Tma2Ptrs>, Tma2Ptrs>(p, lw, smem, &mp);
+  } else {
+    psv2_march<Bulk2>(p, lw, smem);
+  }
 }
 
 // The same for SH jobs (state slots vy, sxy, szy).
@@ -584,7 +592,12 @@ __global__ void __launch_bounds__(kStepWarps * 32, 3) grouped_forward2_sh_kernel
   if (!(op.flags & 1)) p.probes.n = 0;
   p.probes.it = op.it;
   p.err = J.err;
-  sh2_march<ShBulk2>(p, lw, smem);
+  if (J.tm) {
+    const Tma2Ptrs mp{J.tm + 3 * op.a + 1, J.tm + 3 * op.a + 0, J.tm + 3 * J.tm_nslot + 4, nullptr};
+    sh2_march<TmaRows<ShTmaPlan, 6, 3, Tma2Ptrs>, Tma2Ptrs>(p, lw, smem, &mp);
+  } else {
+    sh2_march<ShBulk2>(p, lw, smem);
+  }
 }
 
 cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,

@@ -28,13 +28,20 @@ __device__ __forceinline__ void tma3(float* dst, const CUtensorMap* map, int x, 
       : "memory");
 }
 
-template <class Plan, int S_, int KEEP_>
+// A map given as a kernel parameter (its address) or as a pointer to a map in
+// global memory (the batch keeps one table per job there).
+__device__ __forceinline__ const CUtensorMap* tmap(const CUtensorMap& m) { return &m; }
+__device__ __forceinline__ const CUtensorMap* tmap(const CUtensorMap* m) { return m; }
+
+// Maps: a struct with the plan's named maps, as CUtensorMap members (kernel
+// parameter) or as pointers to maps in global memory.
+template <class Plan, int S_, int KEEP_, class Maps = typename Plan::Maps>
 struct TmaRows {
   static constexpr int S = S_, KEEP = KEEP_, kAhead = S - 1 - KEEP, NSEG = Plan::NSEG;
   static constexpr int kStages = S;
   static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
   using SegsT = Segs<NSEG>;
-  const typename Plan::Maps* tm = nullptr;
+  const Maps* tm = nullptr;
   int x0, ib, lane, nk, cur, nxt;
   uint32_t par;
   float* buf;

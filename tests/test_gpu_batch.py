@@ -125,10 +125,10 @@ def test_chunk_rows_and_autotune_leave_gradients_unchanged():
 
 def test_launch_orders_give_the_same_gradients():
     """Serial launches, a slot's kinds on forked streams, and one stream per
-    kind (and job group) with cross-kind waits only where a job changes kind:
-    the same cell updates in an order the dependencies allow, so the
-    gradients are bitwise equal (a missing dependency would show as a
-    difference)."""
+    kind (and job group) with cross-kind waits only where a job changes kind,
+    rows by tensor copies or by bulk copies: the same cell updates in an
+    order the dependencies allow, so the gradients are bitwise equal (a
+    missing dependency would show as a difference)."""
     import seiswg_gb300 as sw
 
     probs = _problems()
@@ -137,9 +137,11 @@ def test_launch_orders_give_the_same_gradients():
     try:
         assert batch.info()["concurrent"] == 2   # the default
         ref = None
-        for mode, groups in ((0, 1), (1, 1), (2, 1), (2, 1), (2, 2), (2, 4), (1, 3)):
+        for mode, groups, tma in ((0, 1, 1), (1, 1, 1), (2, 1, 1), (2, 1, 1), (2, 2, 1), (2, 4, 1), (1, 3, 1),
+                                  (2, 1, 0)):
             batch.set_option("concurrent", mode)
             batch.set_option("stream_groups", groups)   # jobs split into stream groups
+            batch.set_option("tma", tma)                 # rows by tensor copies or bulk copies
             assert batch.info()["concurrent"] == mode
             batch.run()                          # (2, 1) twice: the second run replays the graph
             g = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
