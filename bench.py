@@ -672,7 +672,7 @@ def run_secondary(args):
                            "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
                            "concurrent": info.get("concurrent"), "stream_groups": info.get("stream_groups"),
-                           "tma": args.tma != 0, "autotune_ms": tune_ms},
+                           "tma_jobs": info.get("tma_jobs"), "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
             small = min(range(len(problems)), key=lambda q: problems[q].cells)

@@ -227,6 +227,8 @@ int32_t seiswg_batch_two_step(const seiswg_batch* batch);
 /* The launch order in use ("concurrent": 0, 1 or 2) and the job groups. */
 int32_t seiswg_batch_concurrent(const seiswg_batch* batch);
 int32_t seiswg_batch_stream_groups(const seiswg_batch* batch);
+/* Jobs whose grouped launches fetch rows by tensor copies (0 with "tma" 0). */
+int32_t seiswg_batch_tma_jobs(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */
 int seiswg_batch_gradient(seiswg_batch* batch, int32_t problem, const char* param, float* host);
 double seiswg_batch_misfit(const seiswg_batch* batch, int32_t problem);

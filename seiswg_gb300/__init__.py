@@ -111,6 +111,7 @@ PROTOTYPES = [
     ("seiswg_batch_two_step", _i32, [_vp]),
     ("seiswg_batch_concurrent", _i32, [_vp]),
     ("seiswg_batch_stream_groups", _i32, [_vp]),
+    ("seiswg_batch_tma_jobs", _i32, [_vp]),
     ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
     ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
     ("seiswg_batch_info", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
@@ -472,7 +473,8 @@ class Batch:
                     chunk_rows=int(lib().seiswg_batch_chunk_rows(self._h)),
                     two_step=bool(lib().seiswg_batch_two_step(self._h)),
                     concurrent=int(lib().seiswg_batch_concurrent(self._h)),
-                    stream_groups=int(lib().seiswg_batch_stream_groups(self._h)))
+                    stream_groups=int(lib().seiswg_batch_stream_groups(self._h)),
+                    tma_jobs=int(lib().seiswg_batch_tma_jobs(self._h)))
 
     @property
     def stream(self) -> int:

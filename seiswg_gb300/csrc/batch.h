@@ -69,6 +69,14 @@ class Batch {
   // bulk copy per field; the same results.  Drops the captured graph.
   void set_tma(bool on);
   bool tma() const { return tma_; }
+  // Jobs whose grouped launches fetch rows by tensor copies: all with a map
+  // table while the option is on (a job whose fields do not lie at uniform
+  // strides has none), 0 while it is off.
+  int tma_jobs() const {
+    int n = 0;
+    for (const JobDesc& d : descs_) n += d.tm != nullptr;
+    return n;
+  }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run

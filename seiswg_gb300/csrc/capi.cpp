@@ -509,6 +509,8 @@ int32_t seiswg_batch_concurrent(const seiswg_batch* b) { return b ? b->batch->co
 
 int32_t seiswg_batch_stream_groups(const seiswg_batch* b) { return b ? b->batch->stream_groups() : 0; }
 
+int32_t seiswg_batch_tma_jobs(const seiswg_batch* b) { return b ? b->batch->tma_jobs() : 0; }
+
 int seiswg_batch_gradient(seiswg_batch* b, int32_t problem, const char* param, float* host) {
   if (!b || !param || !host) return fail(SEISWG_EINVAL, "seiswg_batch_gradient: null argument");
   return guarded([&] {

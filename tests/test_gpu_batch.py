@@ -143,6 +143,7 @@ def test_launch_orders_give_the_same_gradients():
             batch.set_option("stream_groups", groups)   # jobs split into stream groups
             batch.set_option("tma", tma)                 # rows by tensor copies or bulk copies
             assert batch.info()["concurrent"] == mode
+            assert batch.info()["tma_jobs"] == (batch.info()["jobs"] if tma else 0)
             batch.run()                          # (2, 1) twice: the second run replays the graph
             g = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
             J = [batch.misfit(i) for i in range(len(probs))]
