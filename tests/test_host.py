@@ -172,6 +172,11 @@ def test_infer_grid_matches_oracle():
     nx_ref, nz_ref = O.infer_grid(xs, zs)[:2]
     assert nx_ref * nz_ref != 3600 or (nx_ref, nz_ref) != (40, 90)
     assert sw.infer_grid(xs, zs) == (40, 90, 10.0, 1.0)
+    # a large grid (its extents scanned by several threads), origin off zero
+    xl = np.repeat(np.float32(-1234.5) + np.arange(2048, dtype=np.float32) * np.float32(12.5), 2048)
+    zl = np.tile(np.float32(77.25) + np.arange(2048, dtype=np.float32) * np.float32(12.5), 2048)
+    assert sw.infer_grid(xl, zl) == O.infer_grid(xl, zl)
+    assert sw.infer_grid(xl, zl)[:2] == (2048, 2048)
     # coordinates that form no grid: errors
     with pytest.raises(sw.SeiswgError) as e:
         sw.infer_grid(x, np.random.default_rng(0).random(x.size).astype(np.float32) * 100)
