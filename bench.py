@@ -396,7 +396,7 @@ def run_e2e(args, W, stf):
            f"sources = sources.dat\nstations = stations.dat\n")
     cfg = sw.Config.from_str(ini, "")
     h2d = 3 * nx * nz * 4 + 3 * nt * 4 + 2 * 256 * 4
-    d2h = 5 * 256 * nt * 4  # the five trace components of the recorded receivers
+    d2h = (1 if sh else 2) * len(W["rec_i"]) * nt * 4  # the trace components written out (uy; ux, uz)
 
     def one():
         s = sw.Solver(cfg, vfs, write_files=False)

@@ -851,10 +851,17 @@ void Sim::run_forward(int isrc, Snapshots* snaps) {
   }
 }
 
-void Sim::download_traces(float* host) const {
+void Sim::download_traces(float* host, unsigned comps) const {
   check_device_error();
   if (!nrec_) return;
-  SW_CUDA(cudaMemcpyAsync(host, obs_, size_t(5) * nrec_ * d_.nt * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+  const size_t n = size_t(nrec_) * d_.nt;
+  if ((comps & 0x1f) == 0x1f) {
+    SW_CUDA(cudaMemcpyAsync(host, obs_, 5 * n * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+  } else {
+    for (int c = 0; c < 5; ++c)
+      if (comps & (1u << c))
+        SW_CUDA(cudaMemcpyAsync(host + c * n, obs_ + c * n, n * sizeof(float), cudaMemcpyDeviceToHost, stream_));
+  }
   SW_CUDA(cudaStreamSynchronize(stream_));
 }
 

@@ -100,8 +100,10 @@ class Sim {
     std::vector<int> steps;
   };
   void run_forward(int isrc, Snapshots* snaps = nullptr);
-  // Traces of the last forward run, [5][nrec][nt] (x, y, z, yi, yc).
-  void download_traces(float* host) const;
+  // Traces of the last forward run, [5][nrec][nt] (x, y, z, yi, yc); only
+  // the components whose bit is set in `comps` are copied (the others of
+  // `host` are left as they are).
+  void download_traces(float* host, unsigned comps = 0x1f) const;
   // A wavefield component of the current state.
   void download_state(StateField f, float* host) const;
 

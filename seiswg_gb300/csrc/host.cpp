@@ -657,7 +657,11 @@ Vfs Solver::run_forward() {
 
   std::map<std::string, std::vector<float>> snap_bufs;
   uint32_t snap_count = 0;
-  std::vector<float> obs(size_t(5) * nrec * nt);
+  // The trace components written out: uy (1) for SH; ux, uz (0, 2) for PSV;
+  // with spin also ry, yi (1, 3).  Only those are copied back, into a buffer
+  // whose other components are never read (left uninitialised).
+  const unsigned comps = (sh ? 1u << 1 : 0u) | (psv ? (1u << 0) | (1u << 2) : 0u) | (spin ? (1u << 1) | (1u << 3) : 0u);
+  std::unique_ptr<float[]> obs(new float[size_t(5) * nrec * nt]);
   for (auto [isrc, idx] : runs) {
     log_info("Forward run  isrc=" + (isrc < 0 ? std::string("all") : std::to_string(isrc)) + "  (" +
              std::to_string(nt) + " time steps)");
@@ -689,10 +693,10 @@ Vfs Solver::run_forward() {
       ++snap_count;
     }
     // Traces (solver.rs:1047-1101).
-    sim_->download_traces(obs.data());
+    sim_->download_traces(obs.get(), comps);
     const size_t nobs = size_t(nrec) * nt;
     auto emit = [&](const std::string& name, int comp, bool npy) {
-      const float* c = obs.data() + size_t(comp) * nobs;
+      const float* c = obs.get() + size_t(comp) * nobs;
       std::string p = path_join(trace_dir, name + "_" + fmt6(uint32_t(idx)) + ".npy");
       Bytes b = npy ? make_npy(c, size_t(nrec), size_t(nt))
                     : Bytes(reinterpret_cast<const uint8_t*>(c), reinterpret_cast<const uint8_t*>(c + nobs));
