@@ -177,6 +177,14 @@ def test_infer_grid_matches_oracle():
     zl = np.tile(np.float32(77.25) + np.arange(2048, dtype=np.float32) * np.float32(12.5), 2048)
     assert sw.infer_grid(xl, zl) == O.infer_grid(xl, zl)
     assert sw.infer_grid(xl, zl)[:2] == (2048, 2048)
+    # extents as one in-order min/max pass: a NaN inside any thread's part is
+    # passed over, a NaN first element makes the extent NaN (an error)
+    zn = zl.copy()
+    zn[zn.size * 5 // 7] = np.nan
+    assert sw.infer_grid(xl, zn) == sw.infer_grid(xl, zl)
+    zn[0] = np.nan
+    with pytest.raises(sw.SeiswgError):
+        sw.infer_grid(xl, zn)
     # coordinates that form no grid: errors
     with pytest.raises(sw.SeiswgError) as e:
         sw.infer_grid(x, np.random.default_rng(0).random(x.size).astype(np.float32) * 100)
