@@ -13,6 +13,7 @@
 #include <fstream>
 #include <list>
 #include <sstream>
+#include <system_error>
 #include <thread>
 
 namespace seiswg {
@@ -428,12 +429,28 @@ float extent_of(const float* v, size_t n) {
   const unsigned nth = unsigned(std::min<size_t>({size_t(16), size_t(hw), (n + kPart - 1) / kPart}));
   std::vector<MinMax> part(nth);
   const size_t per = (n + nth - 1) / nth;
+  auto bounds = [&](unsigned t) {
+    const size_t b = std::min(n, size_t(t) * per);
+    return std::make_pair(b, std::min(n, b + per));
+  };
+  // Parts 1.. go to threads as long as threads can be started; this thread
+  // scans part 0 and every part no thread took.
   std::vector<std::thread> pool;
-  for (unsigned t = 1; t < nth; ++t) {
-    const size_t b = std::min(n, size_t(t) * per), e = std::min(n, b + per);
-    pool.emplace_back([&part, &scan, v, t, b, e] { part[t] = scan(v + b, e - b); });
+  unsigned handed = 1;
+  for (; handed < nth; ++handed) {
+    const auto [b, e] = bounds(handed);
+    const unsigned t = handed;
+    try {
+      pool.emplace_back([&part, &scan, v, t, b = b, e = e] { part[t] = scan(v + b, e - b); });
+    } catch (const std::system_error&) {
+      break;
+    }
   }
-  part[0] = scan(v, std::min(n, per));
+  for (unsigned t = 0; t < nth; ++t)
+    if (t == 0 || t >= handed) {
+      const auto [b, e] = bounds(t);
+      part[t] = scan(v + b, e - b);
+    }
   for (std::thread& th : pool) th.join();
   MinMax r = part[0];
   for (unsigned t = 1; t < nth; ++t) {
