@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 import subprocess
+import sys
 
 import seiswg_gb300 as sw
 
@@ -47,3 +48,36 @@ def test_exports_are_c_symbols():
 def test_cli_prints_usage():
     r = subprocess.run([sw.CLI_PATH], capture_output=True, text=True)
     assert r.returncode == 1 and "Usage" in r.stderr
+
+
+NULL_PROBE = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+import seiswg_gb300 as sw
+lib = sw.lib()
+# Calls that return a value rather than a status (0 for a null handle), and a
+# Ricker wavelet of zero samples (a valid empty request).
+values = {"seiswg_sim_checkpoint_interval", "seiswg_batch_chunk_rows", "seiswg_batch_two_step",
+          "seiswg_batch_concurrent", "seiswg_batch_stream_groups", "seiswg_batch_tma_jobs", "seiswg_ricker"}
+for name, res, args in sw.PROTOTYPES:
+    if res is not ctypes.c_int or name in values:
+        continue
+    vals = [a(0) if a in (ctypes.c_float, ctypes.c_int32, ctypes.c_size_t, ctypes.c_int64, ctypes.c_uint64)
+            else None for a in args]
+    rc = getattr(lib, name)(*vals)
+    msg = lib.seiswg_last_error() or b""
+    print(name, rc, len(msg), flush=True)
+"""
+
+
+def test_null_arguments_give_error_codes():
+    """Every status-returning call of the C ABI, given null handles and null
+    pointers (and zero sizes), returns an error code with a message; none
+    crashes (run in a child process so that a crash fails only this test).
+    Without a GPU none of these reaches the device."""
+    r = subprocess.run([sys.executable, "-c", NULL_PROBE, ROOT], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout[-2000:], r.stderr[-2000:])
+    lines = [ln.split() for ln in r.stdout.splitlines() if ln.startswith("seiswg_")]
+    assert len(lines) >= 40
+    bad = [(n, rc, m) for (n, rc, m) in lines if int(rc) == 0 or int(m) == 0]
+    assert not bad, bad
