@@ -5,17 +5,9 @@
 #include <cmath>
 #include <cstring>
 
+#include "batch_plan.h"
+
 namespace seiswg {
-
-namespace {
-
-enum Kind { kFwdSh = 0, kFwdPsv, kFwd2Sh, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
-
-struct HostOp {
-  int kind, it, a, b, flags;
-};
-
-}  // namespace
 
 Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStream_t stream)
     : problems_(problems), stream_(stream), ckpt_every_(ckpt_every) {
@@ -267,41 +259,7 @@ void Batch::build_schedule() {
   std::vector<std::vector<HostOp>> lists(jobs_.size());
   for (size_t q = 0; q < jobs_.size(); ++q) {
     const Job& j = jobs_[q];
-    const int k = j.k, ncp = j.ncp, nt = j.nt;
-    auto seg = [&](int m) { return ncp + m - 1; };  // interval buffer, m >= 1
-    auto pp = [&](int t) { return ncp + k - 1 + (t & 1); };
-    const int fwd = j.psv ? kFwdPsv : kFwdSh, adj = j.psv ? kAdjPsv : kAdjSh;
-    const bool two = two_step_ && descs_[q].g2.lx > 0;
-    const int fwd2 = j.psv ? kFwd2Psv : kFwd2Sh;
-    std::vector<HostOp>& L = lists[q];
-    // Recording pass: a step that ends on a checkpoint writes the checkpoint's
-    // slot, the others alternate between the two ping-pong slots; two steps
-    // per op where no checkpoint falls between them.
-    int cur = 0, ppi = 0;
-    for (int t = 0; t < nt;) {
-      const int n = (two && t + 1 < nt && (t + 1) % k != 0) ? 2 : 1;
-      const int e = t + n;
-      int dst;
-      if (e % k == 0 && e < nt) {
-        dst = e / k;
-      } else {
-        dst = pp(ppi);
-        ppi ^= 1;
-      }
-      L.push_back(HostOp{n == 2 ? fwd2 : fwd, t, cur, dst, 1});
-      cur = dst;
-      t = e;
-    }
-    L.push_back(HostOp{kMisfit, 0, 0, 0, 0});
-    int parity = 0;
-    for (int c = ncp - 1; c >= 0; --c) {
-      const int n0 = c * k, n1 = std::min(nt, n0 + k);
-      for (int m = 1; m <= n1 - n0 - 1; ++m) L.push_back(HostOp{fwd, n0 + m - 1, m == 1 ? c : seg(m - 1), seg(m), 0});
-      for (int n = n1 - 1; n >= n0; --n) {
-        L.push_back(HostOp{adj, n, n == n0 ? c : seg(n - n0), parity, 0});
-        parity ^= 1;
-      }
-    }
+    lists[q] = job_ops(j.nt, j.k, j.psv, two_step_ && descs_[q].g2.lx > 0);
   }
   size_t T = 0;
   rec_slots_ = 0;

@@ -1,0 +1,29 @@
+"""The batched gradient's per-job operation lists (seiswg_gb300/csrc/batch_plan.h,
+the host logic of Batch's schedule) replayed on a model of each job's slots
+for every step count up to 160, every checkpoint interval, both physics and
+both recording modes, plus the configurations' sizes: every forward and
+reverse step finds the state of its own step, checkpoints survive, the
+reverse sweep runs nt-1 .. 0 with alternating adjoint slots.  The replay
+program first shows that it reports planted mistakes.  CPU only (g++)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_job_operation_lists_replay_on_the_slots(tmp_path):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    exe = str(tmp_path / "batch_plan_check")
+    src = os.path.join(ROOT, "tests", "batch_plan_check.cpp")
+    inc = os.path.join(ROOT, "seiswg_gb300", "csrc")
+    b = subprocess.run([cxx, "-O2", "-std=c++17", "-Wall", "-Wextra", "-Werror", f"-I{inc}", src, "-o", exe],
+                       capture_output=True, text=True, timeout=300)
+    assert b.returncode == 0, b.stderr[-3000:]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout[-2000:]
+    assert r.stdout.startswith("ok ") and int(r.stdout.split()[1]) > 50000
