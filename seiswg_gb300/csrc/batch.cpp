@@ -270,22 +270,19 @@ void Batch::build_schedule() {
   }
   nslots_ = int(T);
   std::vector<GroupOp> all;
+  const std::vector<std::vector<PlanLaunch>> launches = plan_launches(lists, groups_);
   plan_.assign(T, {});
   for (size_t t = 0; t < T; ++t) {
-    for (int kind = 0; kind < kKinds; ++kind) {
-     for (int grp = 0; grp < groups_; ++grp) {
-      Launch l{kind, int(all.size()), 0, 0, 0, grp};
-      for (size_t q = grp; q < jobs_.size(); q += groups_) {
-        if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
+    for (const PlanLaunch& pl : launches[t]) {
+      Launch l{pl.kind, int(all.size()), 0, 0, pl.deps, pl.group};
+      for (int q : pl.jobs) {
         const HostOp& h = lists[q][t];
-        if (t > 0 && lists[q][t - 1].kind != kind) l.deps |= 1 << lists[q][t - 1].kind;
-        const Geom& g = (kind == kFwd2Psv || kind == kFwd2Sh) ? descs_[q].g2 : descs_[q].g;
-        all.push_back(GroupOp{int(q), h.it, h.a, h.b, h.flags, l.warps});
-        l.warps += (kind == kMisfit) ? 1 : g.nstrips * g.nchunks;
+        const Geom& g = (pl.kind == kFwd2Psv || pl.kind == kFwd2Sh) ? descs_[q].g2 : descs_[q].g;
+        all.push_back(GroupOp{q, h.it, h.a, h.b, h.flags, l.warps});
+        l.warps += (pl.kind == kMisfit) ? 1 : g.nstrips * g.nchunks;
         ++l.count;
       }
-      if (l.count) plan_[t].push_back(l);
-     }
+      plan_[t].push_back(l);
     }
   }
   SW_CUDA(cudaMalloc(&d_ops_, std::max<size_t>(1, all.size()) * sizeof(GroupOp)));

@@ -8,6 +8,7 @@
 // - 1 and ncp + k the recording pass's states between checkpoints.
 #pragma once
 
+#include <utility>
 #include <vector>
 
 namespace seiswg {
@@ -61,6 +62,37 @@ inline std::vector<HostOp> job_ops(int nt, int k, bool psv, bool two) {
     }
   }
   return L;
+}
+
+// One grouped launch of a schedule slot: the jobs (in the order of their
+// operations in the launch) whose operation at that slot is of this kind and
+// which belong to this group (job q is in group q % groups), and the kinds of
+// the previous slot that some of them come from (bit mask).
+struct PlanLaunch {
+  int kind, group, deps;
+  std::vector<int> jobs;
+};
+
+// The launches of every slot, kinds in ascending order and groups within a
+// kind: slot t holds operation t of every job that has one.
+inline std::vector<std::vector<PlanLaunch>> plan_launches(const std::vector<std::vector<HostOp>>& lists,
+                                                          int groups) {
+  size_t T = 0;
+  for (const auto& L : lists) T = L.size() > T ? L.size() : T;
+  std::vector<std::vector<PlanLaunch>> plan(T);
+  const size_t nj = lists.size();
+  for (size_t t = 0; t < T; ++t)
+    for (int kind = 0; kind < kKinds; ++kind)
+      for (int grp = 0; grp < groups; ++grp) {
+        PlanLaunch l{kind, grp, 0, {}};
+        for (size_t q = size_t(grp); q < nj; q += size_t(groups)) {
+          if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
+          if (t > 0 && lists[q][t - 1].kind != kind) l.deps |= 1 << lists[q][t - 1].kind;
+          l.jobs.push_back(int(q));
+        }
+        if (!l.jobs.empty()) plan[t].push_back(std::move(l));
+      }
+  return plan;
 }
 
 }  // namespace seiswg

@@ -11,7 +11,18 @@
 //   - every slot index lies in [0, ncp + k + 1).
 // The replay is first shown to catch planted mistakes (two reverse steps
 // swapped, a recomputation reading the wrong slot, the misfit dropped).
-// Prints "ok <cases>" and exits 0, or prints the first violation and exits 1.
+//
+// Then the launch plan of random mixes of jobs (plan_launches) is replayed
+// under launch order 2 of Batch: one stream per (kind, group), each launch
+// waiting for the events of the kinds in its dependency mask, each launch
+// recording its own stream's event.  Vector clocks over the streams give the
+// happens-before order; every job's operation at slot t must come after its
+// operation at slot t-1.  A dependency mask with a bit removed must be
+// reported.
+// Prints "ok <cases> <mixes>" and exits 0, or prints the first violation and
+// exits 1.
+#include <array>
+#include <cstdint>
 #include <cstdio>
 #include <utility>
 #include <vector>
@@ -103,6 +114,84 @@ static bool catches_planted_mistakes() {
   return ok;
 }
 
+// Launch order 2 (Batch::enqueue_slots): true when every job's operations
+// are ordered from slot to slot.  `drop`: clear this dependency bit of the
+// first launch that has it (a planted mistake), -1 for none.
+static bool order2_holds(const std::vector<std::vector<HostOp>>& lists, int groups, int drop) {
+  constexpr int kGroupsMax = 4, kStreams = kKinds * kGroupsMax;
+  using Clock = std::array<int, kStreams>;
+  auto plan = plan_launches(lists, groups);
+  if (drop >= 0) {
+    bool done = false;
+    for (auto& slot : plan)
+      for (auto& l : slot)
+        if (!done && (l.deps >> drop) & 1) {
+          l.deps &= ~(1 << drop);
+          done = true;
+        }
+    if (!done) return true;  // nothing to plant: the self-check fails
+  }
+  Clock zero{};
+  std::vector<Clock> stream(kStreams, zero), event(kStreams, zero);
+  std::array<int, kStreams> seq{};
+  // where[q] = (stream, seq) of the launch holding job q's previous operation
+  std::vector<std::pair<int, int>> where(lists.size(), {-1, 0});
+  for (size_t t = 0; t < plan.size(); ++t) {
+    std::vector<std::pair<int, int>> now(lists.size(), {-1, 0});
+    for (const PlanLaunch& l : plan[t]) {
+      const int s = l.kind * kGroupsMax + l.group;
+      Clock c = stream[s];
+      for (int a = 0; a < kKinds; ++a)
+        if ((l.deps >> a) & 1) {
+          const Clock& e = event[a * kGroupsMax + l.group];
+          for (int x = 0; x < kStreams; ++x) c[x] = c[x] > e[x] ? c[x] : e[x];
+        }
+      c[s] = ++seq[s];
+      for (int q : l.jobs) {
+        const auto [ps, pn] = where[q];
+        if (t > 0 && ps >= 0 && c[ps] < pn) return false;
+        now[q] = {s, c[s]};
+      }
+      stream[s] = c;
+      event[s] = c;
+    }
+    for (size_t q = 0; q < lists.size(); ++q)
+      if (now[q].first >= 0) where[q] = now[q];
+  }
+  return true;
+}
+
+static uint32_t rng_state = 12345u;
+static int rnd(int n) {  // 0 .. n-1
+  rng_state = rng_state * 1664525u + 1013904223u;
+  return int((rng_state >> 8) % uint32_t(n));
+}
+
+static int check_orders(int& mixes) {
+  for (int m = 0; m < 3000; ++m) {
+    const int nj = 1 + rnd(12), groups = 1 + rnd(4);
+    std::vector<std::vector<HostOp>> lists;
+    for (int q = 0; q < nj; ++q) {
+      const int nt = 1 + rnd(40), k = 1 + rnd(nt);
+      lists.push_back(job_ops(nt, k, rnd(2) != 0, rnd(2) != 0));
+    }
+    if (!order2_holds(lists, groups, -1)) {
+      std::printf("launch order 2 misses a dependency (mix %d)\n", m);
+      return 1;
+    }
+    ++mixes;
+  }
+  // Planted: removing one needed dependency bit must break the order for a
+  // mix where a job changes kind (recomputation to reverse steps).
+  std::vector<std::vector<HostOp>> lists = {job_ops(30, 6, true, true), job_ops(17, 4, false, false)};
+  for (int a : {kFwdPsv, kFwdSh, kFwd2Psv, kAdjPsv, kMisfit})
+    if (order2_holds(lists, 1, a)) {
+      std::printf("the order check misses a dropped dependency on kind %d\n", a);
+      return 1;
+    }
+  return 0;
+}
+
 int main() {
   if (!catches_planted_mistakes()) {
     std::printf("the replay misses a planted mistake\n");
@@ -124,6 +213,8 @@ int main() {
         if (check(nt, k, true, two != 0)) return 1;
         ++cases;
       }
-  std::printf("ok %d\n", cases);
+  int mixes = 0;
+  if (check_orders(mixes)) return 1;
+  std::printf("ok %d %d\n", cases, mixes);
   return 0;
 }
