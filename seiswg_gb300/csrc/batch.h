@@ -5,11 +5,12 @@
 // builds each job's operation list -- a recording forward pass writing a
 // checkpoint every k steps, the on-device misfit, then for each checkpoint
 // interval from the last one a forward recomputation followed by the reverse
-// steps -- and lays all lists side by side: global slot t holds operation t
-// of every job that has one.  Each slot is one grouped launch per kind
-// (forward SH, forward PSV, reverse SH, reverse PSV, misfit) whose warps
-// cover all jobs doing that kind of work, so that small problems share the
-// GPU.  The whole schedule is captured once as a CUDA graph and replayed.
+// steps (batch_plan.h) -- and lays all lists side by side: global slot t
+// holds operation t of every job that has one.  Each slot is one grouped
+// launch per kind (forward SH or PSV, one or two steps; reverse SH or PSV;
+// misfit) whose warps cover all jobs doing that kind of work, so that small
+// problems share the GPU.  The whole schedule is captured once as a CUDA
+// graph and replayed.
 #pragma once
 
 #include <memory>
@@ -54,8 +55,9 @@ class Batch {
   // How the launches of the schedule are ordered.  0: one after another on
   // the batch's stream.  1: the launches of one slot (one per kind of work)
   // run concurrently on forked streams that join before the next slot.
-  // 2 (default): one stream per kind; a launch waits only for the previous
-  // slot's launches of the kinds its jobs come from, so the kinds pipeline.
+  // 2 (default): one stream per kind; a launch waits only for the latest
+  // launches of the kinds its jobs come from (the previous slot's, or this
+  // slot's for a kind enqueued before it), so the kinds pipeline.
   // Drops the captured graph.
   void set_concurrent(int mode);
   int concurrent() const { return concurrent_; }
