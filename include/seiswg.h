@@ -212,8 +212,8 @@ int seiswg_batch_run(seiswg_batch* batch);
  * launches (one per schedule slot and kind of work: SH/PSV forward, reverse,
  * misfit): 0 one after another, 1 a slot's launches on forked streams that
  * join before the next slot, 2 (default) one stream per kind, a launch
- * waiting only for the previous slot's launches of the kinds its jobs come
- * from; "stream_groups" (1..4, default 1): jobs split round-robin into
+ * waiting only for the latest launches of the kinds its jobs come from (the
+ * previous slot's, or this slot's for a kind enqueued before it); "stream_groups" (1..4, default 1): jobs split round-robin into
  * groups with their own launches (and streams in order 2); "tma" (0/1,
  * default 1): the grouped two-step forward and PSV reverse launches fetch
  * rows with 3-D tensor copies through each job's table of tensor maps, or
