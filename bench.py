@@ -237,7 +237,11 @@ def run_reference(args, rank):
     val = float(np.median(rates))
     line = {
         "impl": "reference", "metric": METRIC, "value": val, "unit": METRIC, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dtm * 1e3 * args.nt / args.ref_sample,
+        "steps": args.steps, "warmup": args.warmup,
+        # one step of this arm is the bounded sample (ref_sample of the nt
+        # time steps on the full grid); the whole run by linear extrapolation:
+        "ms_per_step": dtm * 1e3,
+        "extrapolated_ms_per_full_run": dtm * 1e3 * args.nt / args.ref_sample,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(W, args.nt, phys),
         "cpu_baseline": {"value": val, "unit": METRIC, "cores": thr, "kind": "port",
@@ -318,17 +322,22 @@ def run_ours(args, rank, world):
     # steps (two-step kernel, nt even and no snapshots here); its average
     # duration is the timed region over its launches (memsets and the trace
     # kernel are < 0.1 % of it; see the launch lists under profiles/).
-    # Algorithmic bytes: 52 B (PSV) or 32 B (SH) per cell-update, the one-step
-    # scheme's minimum; the two-step kernels move about half of that
-    # (traffic), so their fraction can exceed 1.
+    # Algorithmic bytes of a launch: one pass over the state (read and
+    # written) and the material (read), 52 B (PSV) or 32 B (SH) per cell,
+    # whether the launch advances one step or two.
     # (two-step rows are fetched by tensor copies unless --tma 0)
     kernel = (f"{phys}_step2_tma_kernel" if args.tma != 0 else f"{phys}_step2_kernel") if two_step \
         else f"{phys}_step_kernel"
     per_launch = 2 if two_step else 1
     launch_s = ms_per_step / 1e3 / (nt / per_launch)
-    achieved = BYTES_PER_CELL[phys] * per_launch * nx * nz / launch_s / 1e9
+    achieved = BYTES_PER_CELL[phys] * nx * nz / launch_s / 1e9
     peak, peak_kind = _peaks()
     traffic = _traffic(kernel, nx, nz)
+
+    # ---- parity outside the timed region: a short run against the FP32 oracle
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = short_parity(W, phys, args.parity_nt)
 
     # ---- end to end through the reference-facing C ABI ---------------------
     e2e = None
@@ -353,8 +362,13 @@ def run_ours(args, rank, world):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(W, nt, phys),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": kernel, "bytes_per_cell_update": BYTES_PER_CELL[phys],
-                         "cell_updates_per_launch": per_launch * nx * nz, "peak_source": peak_kind},
+                         "traffic_source": "profile: dram__bytes_read.sum + dram__bytes_write.sum of one ncu "
+                                           "capture of this kernel (profiles/traffic.txt), scaled to the grid; "
+                                           "not measured in this run" if traffic else None,
+                         "kernel": kernel, "algorithmic_bytes_per_launch": BYTES_PER_CELL[phys] * nx * nz,
+                         "bytes_per_cell": BYTES_PER_CELL[phys], "cells_per_launch": nx * nz,
+                         "time_steps_per_launch": per_launch, "launch_us": launch_s * 1e6,
+                         "peak_source": peak_kind},
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "traces_finite": finite,
@@ -365,7 +379,49 @@ def run_ours(args, rank, world):
                            "api": "seiswg_config_load_str + seiswg_solver_new + seiswg_solver_run_forward"}
         if cpu:
             line["cpu_baseline"] = cpu
+        if parity:
+            line["parity"] = parity
         print(json.dumps(line), flush=True)
+
+
+def short_parity(W, phys, nt_p):
+    """The same grid, model, source and receivers for nt_p steps on the GPU and
+    in the FP32 oracle (reference operation order): relative L2 of the final
+    state fields (the top-row receivers' traces stay zero in both; the row is
+    decoupled by the edge rule)."""
+    import seiswg_gb300 as sw
+    from oracle import oracle as O
+
+    nx, nz = W["nx"], W["nz"]
+    sr = W["src"]
+    stf = sw.ricker(nt_p, W["dt"], sr["f0"], sr["t0"], sr["ang"], sr["amp"])[:, None, :]
+    flags = dict(sh=phys == "sh", psv=phys == "psv", abs_left=True, abs_right=True, abs_bottom=True, abs_top=True,
+                 abs_width=W["w"], abs_alpha=W["alpha"])
+    fields = ("vy", "sxy", "szy") if phys == "sh" else ("vx", "vz", "sxx", "szz", "sxz")
+    slots = dict(vy="VY", sxy="SXY", szy="SZY", vx="VX", vz="VZ", sxx="SXX", szz="SZZ", sxz="SXZ")
+    with sw.Sim(nx, nz, nt_p, W["dx"], W["dz"], W["dt"], **flags) as sim:
+        sim.upload_model("vp", W["vp"])
+        sim.upload_model("vs", W["vs"])
+        sim.upload_model("rho", W["rho"])
+        sim.prepare()
+        sim.set_sources([sr["i"]], [sr["j"]], stf)
+        sim.set_receivers(W["rec_i"], W["rec_j"])
+        sim.forward(0)
+        got = {f: sim.state(f) for f in fields}
+        tr = sim.traces()
+    s = O.Setup(nx, nz, nt_p, W["dx"], W["dz"], W["dt"], **flags)
+    o = O.FD2DOracle(s, [sr["i"] * nz + sr["j"]], stf.astype(np.float64), W["rec_i"] * nz + W["rec_j"], 32)
+    o.set_field("LAM", W["vp"])
+    o.set_field("MU", W["vs"])
+    o.set_field("RHO", W["rho"])
+    o.init_model()
+    o.run_forward(0)
+    errs = {f: float(np.linalg.norm(got[f] - o.field(slots[f])) / max(np.linalg.norm(o.field(slots[f])), 1e-300))
+            for f in fields}
+    comps = (1,) if phys == "sh" else (0, 2)
+    zero = bool(all(not np.any(tr[c]) and not np.any(o.obs(("X", "Y", "Z")[c])) for c in comps))
+    return {"rel_l2": max(errs.values()), "per_field": errs, "nt": nt_p, "against": "FP32 oracle",
+            "top_row_traces_zero_in_both": zero}
 
 
 def run_e2e(args, W, stf):
@@ -705,6 +761,8 @@ def main():
                     help="c2 grid and model with the SH system instead (the SH step kernel at scale)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--parity-nt", type=int, default=60, help="c2: steps of the parity run outside the timed region")
     ap.add_argument("--autotune", action="store_true", help="empirical loader/chunk tuning before timing")
     ap.add_argument("--two-step", type=int, default=-1,
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")

@@ -45,6 +45,8 @@ extern "C" {
 #define SEISWG_EIO 2       /* a file or VFS entry is missing or unreadable */
 #define SEISWG_ECUDA 3     /* CUDA runtime failure (no device, out of memory, launch error) */
 #define SEISWG_EINTERNAL 4
+#define SEISWG_ENUMERIC 5  /* the run's traces or gradients hold NaN or infinite values */
+#define SEISWG_ETIMEOUT 6  /* a kernel's bounded wait expired; the run's results are invalid */
 
 /* Message of the last failed call on this thread ("" after a success). */
 const char* seiswg_last_error(void);
@@ -113,8 +115,17 @@ void seiswg_sim_free(seiswg_sim* sim);
  * parameters by seiswg_sim_prepare, fd2d.wgsl:188-201) or "lambda", "mu",
  * "nu", "j", "lambda_c", "mu_c", "nu_c", "rho" for spin models. */
 int seiswg_sim_upload_model(seiswg_sim* sim, const char* name, const float* host, size_t n);
-/* vps2lm, mu_c+nu_c and the absorbing taper (fd2d.wgsl:188-235). */
+/* vps2lm, mu_c+nu_c and the absorbing taper (fd2d.wgsl:188-235).  Also
+ * checks stability before any run (the reference has no such check): fails
+ * with SEISWG_EINVAL when dt c (7/6) sqrt(1/dx^2 + 1/dz^2) > 1 (c the
+ * largest P speed with PSV, S speed with SH alone), when with spin (dt/2)
+ * sqrt(4 nu/J + (mu_c+nu_c)/J (7/3)^2 (1/dx^2 + 1/dz^2)) > 1, or when a
+ * squared wave speed is negative or not finite.  Option "stability_check" 0
+ * (set before this call) turns the rejection off. */
 int seiswg_sim_prepare(seiswg_sim* sim);
+/* The two stability numbers of the last seiswg_sim_prepare (spin: 0 without
+ * spin); a run is rejected above 1. */
+int seiswg_sim_stability(const seiswg_sim* sim, double* wave, double* spin);
 /* Sources at cells (i[s], j[s]); stf_xyz is [3][n][nt] (x, y, z components). */
 int seiswg_sim_set_sources(seiswg_sim* sim, int32_t n, const int32_t* i, const int32_t* j, const float* stf_xyz);
 int seiswg_sim_set_receivers(seiswg_sim* sim, int32_t n, const int32_t* i, const int32_t* j);
@@ -126,7 +137,9 @@ int seiswg_sim_set_receivers(seiswg_sim* sim, int32_t n, const int32_t* i, const
 int seiswg_sim_forward(seiswg_sim* sim, int32_t isrc, int32_t snap_every, int32_t nfields,
                        const char* const* fields, float* snaps_out, int32_t sync);
 /* Receiver traces of the last run, [5][nrec][nt]: x, y, z, yi, yc
- * (the reference's obs buffer, fd2d.wgsl:110-114). */
+ * (the reference's obs buffer, fd2d.wgsl:110-114).  Fails with
+ * SEISWG_ENUMERIC when they hold NaN or infinite values, and with
+ * SEISWG_ETIMEOUT when a kernel of the run gave up a bounded wait. */
 int seiswg_sim_traces(seiswg_sim* sim, float* host);
 /* Current wavefield component, nx*nz values. */
 int seiswg_sim_state(seiswg_sim* sim, const char* field, float* host);
@@ -160,7 +173,8 @@ int32_t seiswg_sim_checkpoint_interval(const seiswg_sim* sim);
 int seiswg_sim_set_observed(seiswg_sim* sim, const float* obs);
 int seiswg_sim_misfit_op(seiswg_sim* sim, double* J);
 int seiswg_sim_backward_op_device(seiswg_sim* sim);
-/* param: "lambda", "mu" or "buoyancy"; nx*nz values. */
+/* param: "lambda", "mu" or "buoyancy"; nx*nz values.  Fails with
+ * SEISWG_ENUMERIC when the gradients hold NaN or infinite values. */
 int seiswg_sim_gradient(seiswg_sim* sim, const char* param, float* host);
 /* Frees the checkpoint, adjoint and snapshot buffers until their next use
  * (gradients are kept). */
@@ -178,7 +192,13 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * results are the one-step kernel's bits), "tma" (0/1: the two-step and the
  * PSV reverse kernels fetch their rows with 3-D tensor copies where the
  * fields lie at uniform strides, default on; 0: one bulk copy per field;
- * the same results either way). */
+ * the same results either way), "stability_check" (0/1, default 1: see
+ * seiswg_sim_prepare), "wait_polls" (polls of a kernel's bounded wait for
+ * its row pipeline before it gives up and the run fails with
+ * SEISWG_ETIMEOUT; 0: the built-in 2^20), "test_arm_extra" (a test hook for
+ * that failure path: bytes armed on the first stage of every warp's row
+ * pipeline beyond its copies, so that every launch's first wait runs out
+ * while all copies still land; 0, the default, for real runs). */
 int seiswg_sim_set_option(seiswg_sim* sim, const char* key, int64_t value);
 int seiswg_sim_synchronize(seiswg_sim* sim);
 /* Number of kernels this handle has launched (graph nodes count per replay). */

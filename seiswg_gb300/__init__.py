@@ -22,7 +22,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libseiswg.so")
 CLI_PATH = os.path.join(_HERE, "_lib", "seiswg")
 
-OK, EINVAL, EIO, ECUDA, EINTERNAL = 0, 1, 2, 3, 4
+OK, EINVAL, EIO, ECUDA, EINTERNAL, ENUMERIC, ETIMEOUT = 0, 1, 2, 3, 4, 5, 6
 OBS_X, OBS_Y, OBS_Z, OBS_YI, OBS_YC = range(5)
 
 
@@ -75,6 +75,7 @@ PROTOTYPES = [
     ("seiswg_sim_free", None, [_vp]),
     ("seiswg_sim_upload_model", _c_int, [_vp, _cp, _pf, _sz]),
     ("seiswg_sim_prepare", _c_int, [_vp]),
+    ("seiswg_sim_stability", _c_int, [_vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("seiswg_sim_set_sources", _c_int, [_vp, _i32, _pi, _pi, _pf]),
     ("seiswg_sim_set_receivers", _c_int, [_vp, _i32, _pi, _pi]),
     ("seiswg_sim_forward", _c_int, [_vp, _i32, _i32, _i32, ctypes.POINTER(_cp), _pf, _i32]),
@@ -305,6 +306,12 @@ class Sim:
 
     def prepare(self):
         _check(lib().seiswg_sim_prepare(self._h))
+
+    def stability(self):
+        """(wave, spin) stability numbers of the last prepare(); above 1 is unstable."""
+        w, s = ctypes.c_double(), ctypes.c_double()
+        _check(lib().seiswg_sim_stability(self._h, ctypes.byref(w), ctypes.byref(s)))
+        return w.value, s.value
 
     def set_sources(self, i: Sequence[int], j: Sequence[int], stf_xyz):
         i = np.ascontiguousarray(i, np.int32)

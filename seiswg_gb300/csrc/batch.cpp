@@ -99,6 +99,7 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       jd.pool = j.pool;
       jd.adj = j.adj;
       jd.rho = v.rho; jd.lam = v.lam; jd.mu = v.mu;
+      jd.rho_dt = v.rho_dt;
       jd.taper_x = v.taper_x; jd.taper_zb = v.taper_zb; jd.taper_zt = v.taper_zt;
       jd.g_lam = j.grads + halo;
       jd.g_mu = j.grads + fe + halo;
@@ -122,7 +123,8 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       jd.dt = d.dt;
       jd.err = err_;
       // Tensor maps (JobDesc): state slots with boxes of 1, 2 and 3 fields,
-      // the adjoint slots (3, 2), the material (1, 2), the gradients (1, 2).
+      // the adjoint slots (3, 2), the material (1, 2), the gradients (1, 2),
+      // the dt-scaled material (1, 2).
       {
         const int rows_alloc = d.nx + 2 * kHaloRows;
         const int nf = j.nstate;
@@ -139,7 +141,9 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
         ok = ok && encode_fields(&t[4], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
              encode_fields(&t[5], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 2) &&
              encode_fields(&t[6], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 1) &&
-             encode_fields(&t[7], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 2);
+             encode_fields(&t[7], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 2) && v.rho_dt &&
+             encode_fields(&t[8], v.rho_dt, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
+             encode_fields(&t[9], v.rho_dt, v.lam - v.rho, 3, v.ld, rows_alloc, 2);
         if (ok) {
           SW_CUDA(cudaMalloc(&j.tm, maps.size() * sizeof(CUtensorMap)));
           SW_CUDA(cudaMemcpy(j.tm, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
@@ -423,6 +427,12 @@ void Batch::run() {
     SW_CUDA(e);
   }
   SW_CUDA(cudaGraphLaunch(graph_, stream_));
+  // NaN / infinity watchdog over every problem's gradient block.
+  for (size_t p = 0; p < problems_.size(); ++p) {
+    const Sim::View v = problems_[p].sim->view();
+    const long rows = 3L * (problems_[p].sim->desc().nx + 2 * kHaloRows);
+    SW_CUDA(launch_check_finite(sums_[p], rows, v.ld, v.ld, err_, kErrNonFiniteGradient, stream_));
+  }
   // Per-trace misfits, summed per problem in a fixed order.
   host_J_.assign(problems_.size(), 0.0);
   std::vector<double> buf;
@@ -435,7 +445,10 @@ void Batch::run() {
   }
   int e = 0;
   SW_CUDA(cudaMemcpy(&e, err_, sizeof(int), cudaMemcpyDeviceToHost));
-  if (e) throw CudaError("a batched kernel gave up waiting for its row pipeline (bounded wait expired)");
+  if (e) SW_CUDA(cudaMemset(err_, 0, sizeof(int)));  // reported once
+  if (e & kErrWaitTimeout)
+    throw WaitTimeout("a batched kernel gave up waiting for its row pipeline (bounded wait expired)");
+  if (e & kErrNonFiniteGradient) throw NumericError("a batched gradient holds NaN or infinite values");
 }
 
 void Batch::download_gradient(int problem, int which, float* host) const {

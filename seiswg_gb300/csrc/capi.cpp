@@ -52,6 +52,10 @@ int guarded(F&& f) {
     g_last_error.clear();
     f();
     return SEISWG_OK;
+  } catch (const seiswg::WaitTimeout& e) {
+    return fail(SEISWG_ETIMEOUT, e.what());
+  } catch (const seiswg::NumericError& e) {
+    return fail(SEISWG_ENUMERIC, e.what());
   } catch (const seiswg::CudaError& e) {
     return fail(SEISWG_ECUDA, e.what());
   } catch (const seiswg::Error& e) {
@@ -308,6 +312,14 @@ int seiswg_sim_prepare(seiswg_sim* s) {
   return guarded([&] { sim_of(s).prepare_model(); });
 }
 
+int seiswg_sim_stability(const seiswg_sim* s, double* wave, double* spin) {
+  if (!s || !s->sim) return fail(SEISWG_EINVAL, "null simulation handle");
+  if (wave) *wave = s->sim->stability_wave();
+  if (spin) *spin = s->sim->stability_spin();
+  g_last_error.clear();
+  return SEISWG_OK;
+}
+
 int seiswg_sim_set_sources(seiswg_sim* s, int32_t n, const int32_t* i, const int32_t* j, const float* stf) {
   return guarded([&] {
     if (n > 0 && (!i || !j || !stf)) throw std::invalid_argument("null source argument");
@@ -450,7 +462,14 @@ int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
     else if (k == "cluster") sim.set_use_cluster(value != 0);
     else if (k == "tma") sim.set_use_tma(value != 0);
     else if (k == "autotune") sim.autotune(int(value));
-    else throw std::invalid_argument("unknown option " + k);
+    else if (k == "stability_check") sim.set_stability_check(value != 0);
+    else if (k == "wait_polls") {
+      if (value < 0 || value > 0xffffffffLL) throw std::invalid_argument("wait_polls out of range");
+      sim.set_wait_polls(unsigned(value));
+    } else if (k == "test_arm_extra") {
+      if (value < 0 || value > (1 << 20)) throw std::invalid_argument("test_arm_extra out of range");
+      sim.set_arm_extra(unsigned(value));
+    } else throw std::invalid_argument("unknown option " + k);
   });
 }
 

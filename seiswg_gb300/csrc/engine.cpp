@@ -57,7 +57,10 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   const size_t fb = field_elems_ * sizeof(float);
 
   int nstate = (d.sh ? 3 : 0) + (d.psv ? 5 : 0) + (d.psv && d.spin ? 4 : 0);
-  int nmodel = 3 + (d.psv && d.spin ? 5 : 0);
+  // The two-step kernels (PSV alone, SH alone) read a dt-scaled copy of the
+  // material: dt/rho, dt*lambda, dt*mu.
+  const bool scaled = (d.psv && !d.sh && !d.spin) || (d.sh && !d.psv);
+  int nmodel = 3 + (d.psv && d.spin ? 5 : 0) + (scaled ? 3 : 0);
   for (int q = 0; q < 2 * nstate + nmodel; ++q) arena_.reserve(fb);
   arena_.reserve(rows_alloc * sizeof(float));
   arena_.reserve(size_t(ld_) * sizeof(float));
@@ -73,6 +76,7 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
     }
   }
   rho_ = alloc_field(); lam_ = alloc_field(); mu_ = alloc_field();
+  if (scaled) { rdt_ = alloc_field(); ldt_ = alloc_field(); mdt_ = alloc_field(); }
   if (d.psv && d.spin) { nu_ = alloc_field(); jm_ = alloc_field(); muc_ = alloc_field(); nuc_ = alloc_field(); mc_ = alloc_field(); }
   taper_x_ = static_cast<float*>(arena_.take(rows_alloc * sizeof(float))) + kHaloRows;
   taper_zb_ = static_cast<float*>(arena_.take(size_t(ld_) * sizeof(float))) + kHaloCols;
@@ -80,7 +84,7 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   // Zero everything; density and micro-inertia halos hold 1 so that the
   // (never used) halo velocities stay finite.
   zero_state();
-  for (float* f : {lam_, mu_, nu_, muc_, nuc_, mc_})
+  for (float* f : {lam_, mu_, nu_, muc_, nuc_, mc_, rdt_, ldt_, mdt_})
     if (f) SW_CUDA(cudaMemsetAsync(f - size_t(kHaloRows) * ld_ - kHaloCols, 0, fb, stream_));
   for (float* f : {rho_, jm_})
     if (f) SW_CUDA(launch_fill_rows(f - kHaloCols, -kHaloRows, d.nx + kHaloRows, ld_, 1.0f, stream_));
@@ -100,12 +104,14 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   if ((d.psv && !d.sh && !d.spin) || (d.sh && !d.psv)) set_two_step(true);
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
+  SW_CUDA(cudaMalloc(&red_, 4 * sizeof(unsigned)));
   use_graphs_ = (size_t(d.nx) * d.nz <= (size_t(1) << 20));
 }
 
 Sim::~Sim() {
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   cudaFree(err_);
+  cudaFree(red_);
   cudaFree(stf_);
   cudaFree(adstf_);
   cudaFree(inj_dev_[0]);
@@ -234,10 +240,12 @@ bool Sim::tma_ready() {
   if (tma_mat_ < 0) {
     const int rows_alloc = d_.nx + 2 * kHaloRows;
     const ptrdiff_t dm = lam_ - rho_;
-    tma_mat_ = (mu_ - lam_ == dm && encode_fields(&tma_.rho, rho_, dm, 3, ld_, rows_alloc, 1) &&
-                encode_fields(&tma_.lm, rho_, dm, 3, ld_, rows_alloc, 2))
-                   ? 1
-                   : 0;
+    bool ok = mu_ - lam_ == dm && encode_fields(&mat1_, rho_, dm, 3, ld_, rows_alloc, 1) &&
+              encode_fields(&mat2_, rho_, dm, 3, ld_, rows_alloc, 2);
+    if (ok && rdt_)  // the two-step kernels' dt-scaled material
+      ok = ldt_ - rdt_ == dm && mdt_ - ldt_ == dm && encode_fields(&tma_.rho, rdt_, dm, 3, ld_, rows_alloc, 1) &&
+           encode_fields(&tma_.lm, rdt_, dm, 3, ld_, rows_alloc, 2);
+    tma_mat_ = ok ? 1 : 0;
   }
   return tma_mat_ == 1;
 }
@@ -261,8 +269,8 @@ bool Sim::launch_adjoint_tma(const PsvAdjoint& p, const State& f, const State& a
       return false;
     tma_grad_ = g_lam_;
   }
-  tma_adj_.m1 = tma_.rho;
-  tma_adj_.m2 = tma_.lm;
+  tma_adj_.m1 = mat1_;
+  tma_adj_.m2 = mat2_;
   if (!encode_fields(&tma_adj_.f1, f.vx, f.vz - f.vx, 5, ld_, rows_alloc, 1) ||
       !encode_fields(&tma_adj_.f2, f.vx, f.vz - f.vx, 5, ld_, rows_alloc, 2) ||
       !encode_fields(&tma_adj_.a3, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 3) ||
@@ -285,7 +293,7 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
     p.g = geom2_;
     p.vy0 = a.vy; p.sxy0 = a.sxy; p.szy0 = a.szy;
     p.vy1 = o.vy; p.sxy1 = o.sxy; p.szy1 = o.szy;
-    p.rho = rho_; p.mu = mu_;
+    p.rho = rdt_; p.mu = mdt_;  // dt/rho, dt*mu
     p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
     p.inj = inj_in;
     p.inj.it = it;
@@ -307,7 +315,7 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
   p.g = geom2_;
   p.vx0 = a.vx; p.vz0 = a.vz; p.sxx0 = a.sxx; p.szz0 = a.szz; p.sxz0 = a.sxz;
   p.vx1 = o.vx; p.vz1 = o.vz; p.sxx1 = o.sxx; p.szz1 = o.szz; p.sxz1 = o.sxz;
-  p.rho = rho_; p.lam = lam_; p.mu = mu_;
+  p.rho = rdt_; p.lam = ldt_; p.mu = mdt_;  // dt/rho, dt*lambda, dt*mu
   p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
   p.inj = inj_in;
   p.inj.it = it;
@@ -386,6 +394,18 @@ double Sim::autotune(int steps) {
   return 1e3 * double(best) / steps;
 }
 
+void Sim::set_wait_polls(unsigned polls) {
+  geom_.wait_polls = geom2_.wait_polls = polls;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+void Sim::set_arm_extra(unsigned bytes) {
+  geom_.arm_extra = geom2_.arm_extra = bytes;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
 void Sim::set_loader(int loader) {
   if (loader != kLoaderDirect && loader != kLoaderBulk) throw std::invalid_argument("unknown loader");
   geom_.loader = loader;
@@ -393,13 +413,69 @@ void Sim::set_loader(int loader) {
   graphs_.clear();
 }
 
+// The device error word is reported once: it is cleared after it has been
+// read, so that the simulation stays usable for the next run.
 void Sim::check_device_error() const {
   int e = 0;
   SW_CUDA(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
+  if (!e) return;
+  SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
   if (e & kErrWaitTimeout)
-    throw CudaError("a step kernel gave up waiting for its row pipeline (bounded wait expired); "
-                    "results of this run are invalid");
+    throw WaitTimeout("a step kernel gave up waiting for its row pipeline (bounded wait expired); "
+                      "results of this run are invalid");
+  if (e & kErrNonFiniteTraces)
+    throw NumericError("the receiver traces hold NaN or infinite values (an unstable run or a bad model)");
+  if (e & kErrNonFiniteGradient)
+    throw NumericError("the gradient holds NaN or infinite values (an unstable run or a bad adjoint source)");
+}
+
+// Von Neumann limits of the staggered fourth-order scheme (leapfrog in time,
+// difference weights 9/8 and 1/24 whose magnitudes add up to 7/6):
+//   wave:  dt c (7/6) sqrt(1/dx^2 + 1/dz^2) <= 1, c the P speed sqrt((lambda
+//          + 2 mu)/rho) with PSV, the S speed sqrt(mu/rho) with SH alone;
+//   spin:  (dt/2) sqrt(w0^2 + cc^2 (7/3)^2 (1/dx^2 + 1/dz^2)) <= 1, w0 =
+//          sqrt(4 nu / J) the rotation rate and cc = sqrt((mu_c + nu_c)/J)
+//          the couple-wave speed.
+// Each is necessary for its own subsystem; the coupling terms are not
+// analysed.  A run that exceeds either, or a model with non-finite or
+// negative squared speeds, is rejected before it starts.
+void Sim::check_stability() {
+  unsigned h[4] = {0, 0, 0, 0};
+  SW_CUDA(cudaMemsetAsync(red_, 0, 4 * sizeof(unsigned), stream_));
+  SW_CUDA(launch_max_speeds(lam_, mu_, rho_, nu_, (d_.psv && d_.spin) ? jm_ : nullptr, mc_, d_.psv, d_.nx, d_.nz,
+                            ld_, red_, stream_));
+  SW_CUDA(cudaMemcpyAsync(h, red_, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  float c2, w2, q2;
+  std::memcpy(&c2, &h[0], 4);
+  std::memcpy(&w2, &h[1], 4);
+  std::memcpy(&q2, &h[2], 4);
+  const double k = std::sqrt(1.0 / (double(d_.dx) * d_.dx) + 1.0 / (double(d_.dz) * d_.dz));
+  const double dt = d_.dt;
+  cfl_wave_ = dt * std::sqrt(double(c2)) * (7.0 / 6.0) * k;
+  cfl_spin_ = (d_.psv && d_.spin) ? 0.5 * dt * std::sqrt(double(w2) + double(q2) * (7.0 / 3.0) * (7.0 / 3.0) * k * k)
+                                  : 0.0;
+  if (!stability_check_) return;
+  if (h[3])
+    throw std::invalid_argument("model: non-finite or negative squared wave speeds (check rho, vp/vs or the moduli)");
+  if (cfl_wave_ > 1.0) {
+    char m[256];
+    std::snprintf(m, sizeof m,
+                  "dt = %g is unstable: dt c (7/6) sqrt(1/dx^2 + 1/dz^2) = %.4f > 1 with c = %.6g m/s "
+                  "(largest dt %.6g)",
+                  dt, cfl_wave_, std::sqrt(double(c2)), dt / cfl_wave_);
+    throw std::invalid_argument(m);
+  }
+  if (cfl_spin_ > 1.0) {
+    char m[256];
+    std::snprintf(m, sizeof m,
+                  "dt = %g is unstable for the spin field: (dt/2) sqrt(4 nu/J + (mu_c+nu_c)/J (7/3)^2 "
+                  "(1/dx^2 + 1/dz^2)) = %.4f > 1 (largest dt %.6g)",
+                  dt, cfl_spin_, dt / cfl_spin_);
+    throw std::invalid_argument(m);
+  }
 }
 
 float* Sim::alloc_field() { return field_ptr(static_cast<float*>(arena_.take(field_elems_ * sizeof(float)))); }
@@ -445,7 +521,16 @@ void Sim::prepare_model() {
   // The step kernels read the buoyancy 1/rho and 1/J.
   SW_CUDA(launch_reciprocal(rho_, d_.nx, d_.nz, ld_, stream_));
   if (jm_) SW_CUDA(launch_reciprocal(jm_, d_.nx, d_.nz, ld_, stream_));
+  // The two-step kernels' material, dt/rho, dt*lambda, dt*mu (halos included).
+  if (rdt_) {
+    const size_t h = size_t(kHaloRows) * ld_ + kHaloCols;
+    const float dt = d_.dt;
+    SW_CUDA(launch_scale(rdt_ - h, rho_ - h, long(field_elems_), dt, stream_));
+    SW_CUDA(launch_scale(ldt_ - h, lam_ - h, long(field_elems_), dt, stream_));
+    SW_CUDA(launch_scale(mdt_ - h, mu_ - h, long(field_elems_), dt, stream_));
+  }
   prepared_ = true;
+  check_stability();
 
   // Absorbing taper, set_bound (fd2d.wgsl:205-235): b = ((1*eL)*eR)*eB*eT with
   // e = exp(-(alpha*d)^2); separable into a row factor (left, right) and two
@@ -736,7 +821,10 @@ void Sim::enqueue_traces() {
   t.hist = probe_hist_;
   t.obs = obs_;
   SW_CUDA(launch_assemble_traces(t, stream_));
-  ++launches_;
+  // NaN / infinity watchdog: a bit in the error word that the call reading
+  // the traces reports.
+  SW_CUDA(launch_check_finite(obs_, 5, nrec_ * d_.nt, long(nrec_) * d_.nt, err_, kErrNonFiniteTraces, stream_));
+  launches_ += 2;
 }
 
 void Sim::run_forward(int isrc, Snapshots* snaps) {
@@ -1272,6 +1360,10 @@ void Sim::run_backward() {
         cur ^= 1;
       }
     }
+    // NaN / infinity watchdog over the gradient block (lambda, mu, buoyancy).
+    SW_CUDA(launch_check_finite(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols, 3 * (d_.nx + 2 * kHaloRows), ld_, ld_,
+                                err_, kErrNonFiniteGradient, stream_));
+    ++launches_;
   });
 }
 
@@ -1314,6 +1406,7 @@ Sim::View Sim::view() const {
   v.ld = ld_;
   v.field_elems = field_elems_;
   v.rho = rho_; v.lam = lam_; v.mu = mu_;
+  v.rho_dt = rdt_;
   v.taper_x = taper_x_; v.taper_zb = taper_zb_; v.taper_zt = taper_zt_;
   v.stf = stf_;
   v.probes = probes_;

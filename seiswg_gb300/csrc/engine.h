@@ -22,6 +22,16 @@ struct CudaError : std::runtime_error {
   using std::runtime_error::runtime_error;
 };
 
+// A run whose results hold NaN or infinite values.
+struct NumericError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+
+// A kernel gave up a bounded wait; the run's results are invalid.
+struct WaitTimeout : CudaError {
+  using CudaError::CudaError;
+};
+
 void cuda_check(cudaError_t e, const char* what);
 #define SW_CUDA(call) ::seiswg::cuda_check((call), #call)
 
@@ -153,6 +163,7 @@ class Sim {
     int ld;
     size_t field_elems;
     const float *rho, *lam, *mu, *taper_x, *taper_zb, *taper_zt;
+    const float* rho_dt;    // dt/rho, then dt*lambda and dt*mu at the material's stride (null: no two-step kernel)
     const float* stf;       // [3][nsrc][nt]
     const Probe* probes;    // SH segment, then PSV segment
     int nprobe, probe_split;
@@ -191,8 +202,24 @@ class Sim {
   // state's fields lie at a uniform stride (default on).
   void set_use_tma(bool on);
   int loader() const { return geom_.loader; }
-  // Throws if a kernel recorded an error (e.g. a bounded wait ran out).
+  // Throws if a kernel recorded an error (a bounded wait ran out, or the
+  // traces or gradients of the last run hold NaN or infinite values); the
+  // error word is cleared once read.
   void check_device_error() const;
+  // Stability numbers of the model and dt (computed by prepare_model; the
+  // run is rejected above 1 while the check is on): the wave number dt c
+  // (7/6) sqrt(1/dx^2 + 1/dz^2) and, with spin, (dt/2) sqrt(4 nu/J +
+  // (mu_c+nu_c)/J (7/3)^2 (1/dx^2 + 1/dz^2)) (0 without spin).
+  double stability_wave() const { return cfl_wave_; }
+  double stability_spin() const { return cfl_spin_; }
+  // prepare_model rejects an unstable dt (default on).
+  void set_stability_check(bool on) { stability_check_ = on; }
+  // Polls of a bounded row-pipeline wait before a kernel gives up (0: the
+  // built-in limit).  arm_extra is a test hook: that many bytes are armed on
+  // the first stage of every warp's ring beyond its copies, so that every
+  // launch's first wait runs out (0 for normal runs).
+  void set_wait_polls(unsigned polls);
+  void set_arm_extra(unsigned bytes);
   int chunk_rows() const { return geom_.lx; }
   uint64_t kernel_launches() const { return launches_; }
   void synchronize() const;
@@ -238,7 +265,8 @@ class Sim {
   bool use_cluster_ = true;
   bool use_tma_ = true;
   int tma_mat_ = -1;   // material tensor maps: -1 not yet encoded, 0 unavailable, 1 in tma_
-  Tma2 tma_{};         // rho and lm set once; sig and vel per launch
+  Tma2 tma_{};         // rho and lm (the dt-scaled material) set once; sig and vel per launch
+  CUtensorMap mat1_{}, mat2_{};  // the material (1/rho, lambda, mu) with boxes of 1 and 2 fields
   TmaAdj tma_adj_{};   // reverse step: g1, g2 for the gradient block at tma_grad_, the rest per launch
   const float* tma_grad_ = nullptr;
   bool tma_ready();
@@ -247,7 +275,12 @@ class Sim {
   int adj_lx_[2] = {0, 0};  // reverse-step rows per chunk, per loader (0: not yet modelled)
   Arena arena_;
   State st_[2];
+  unsigned* red_ = nullptr;      // device scratch of the stability reduction
+  double cfl_wave_ = 0, cfl_spin_ = 0;
+  bool stability_check_ = true;
+  void check_stability();
   float *rho_ = nullptr, *lam_ = nullptr, *mu_ = nullptr;
+  float *rdt_ = nullptr, *ldt_ = nullptr, *mdt_ = nullptr;  // dt/rho, dt*lambda, dt*mu (two-step kernels)
   float *nu_ = nullptr, *jm_ = nullptr, *muc_ = nullptr, *nuc_ = nullptr, *mc_ = nullptr;
   float *taper_x_ = nullptr, *taper_zb_ = nullptr, *taper_zt_ = nullptr;
   float *kmu_ = nullptr, *tmp_ = nullptr;

@@ -208,6 +208,7 @@ __device__ __forceinline__ void psv_adjoint_march(const PsvAdjoint& p, int gw, u
   segs.base[PA_GM] = p.g_mu; segs.roff[PA_GM] = -2;
   Loader rows = make_aloader<Loader>(segs, g, m, L, smem);
   if constexpr (std::is_same<Loader, TmaRows<AdjTmaPlan, kAdjStages, 0, M>>::value) rows.tm = tm;
+  rows.configure(g);
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
@@ -419,6 +420,7 @@ __device__ __forceinline__ void sh_adjoint_march(const ShAdjoint& p, int gw, uns
   segs.base[SA_GB] = p.g_b; segs.roff[SA_GB] = 0;
   segs.base[SA_GM] = p.g_mu; segs.roff[SA_GM] = -2;
   Loader rows = make_aloader<Loader>(segs, g, m, L, smem);
+  rows.configure(g);
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);

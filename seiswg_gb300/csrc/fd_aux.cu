@@ -1,5 +1,6 @@
-// fd_aux.cu -- the non-step kernels: model set-up, trace assembly, the
-// reference adjoint's imaging condition and Gaussian kernel smoothing.
+// fd_aux.cu -- the non-step kernels: model set-up, the stability and
+// finite-value guards, trace assembly, the reference adjoint's imaging
+// condition and Gaussian kernel smoothing.
 #include "fd_kernels.h"
 
 namespace seiswg {
@@ -37,6 +38,63 @@ __global__ void reciprocal_kernel(float* f, int nx, int nz, int ld) {
     long k = (t / nz) * ld + (t % nz);
     f[k] = 1.0f / f[k];
   }
+}
+
+// out = in * factor over n consecutive floats (whole padded fields).
+__global__ void scale_kernel(float* out, const float* in, long n, float factor) {
+  for (long t = blockIdx.x * long(blockDim.x) + threadIdx.x; t < n; t += long(gridDim.x) * blockDim.x)
+    out[t] = in[t] * factor;
+}
+
+// Largest squared wave speeds over the interior, as the bits of non-negative
+// floats (which order like unsigned integers): out[0] P (PSV, (lambda +
+// 2 mu) b) or S (SH, mu b), out[1] the spin's rotation rate 4 nu / J,
+// out[2] its couple-wave speed (mu_c + nu_c) / J.  A non-finite or negative
+// value sets out[3].
+__global__ void speed_kernel(const float* lam, const float* mu, const float* b, const float* nu, const float* jinv,
+                             const float* mc, int psv, int nx, int nz, int ld, unsigned* out) {
+  long n = long(nx) * nz;
+  float m0 = 0.0f, m1 = 0.0f, m2 = 0.0f;
+  unsigned bad = 0;
+  for (long t = blockIdx.x * long(blockDim.x) + threadIdx.x; t < n; t += long(gridDim.x) * blockDim.x) {
+    const long k = (t / nz) * ld + (t % nz);
+    const float c2 = (psv ? lam[k] + 2.0f * mu[k] : mu[k]) * b[k];
+    float w2 = 0.0f, q2 = 0.0f;
+    if (jinv) {
+      w2 = 4.0f * nu[k] * jinv[k];
+      q2 = mc[k] * jinv[k];
+    }
+    if (!(c2 >= 0.0f && c2 < INFINITY && w2 >= 0.0f && w2 < INFINITY && q2 >= 0.0f && q2 < INFINITY)) bad = 1;
+    else {
+      m0 = fmaxf(m0, c2);
+      m1 = fmaxf(m1, w2);
+      m2 = fmaxf(m2, q2);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m0 = fmaxf(m0, __shfl_xor_sync(0xffffffffu, m0, o));
+    m1 = fmaxf(m1, __shfl_xor_sync(0xffffffffu, m1, o));
+    m2 = fmaxf(m2, __shfl_xor_sync(0xffffffffu, m2, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&out[0], __float_as_uint(m0));
+    atomicMax(&out[1], __float_as_uint(m1));
+    atomicMax(&out[2], __float_as_uint(m2));
+    if (bad) atomicOr(&out[3], 1u);
+  }
+}
+
+// Sets `bit` in *err when an element of rows x cols (row pitch ld) is not
+// finite.
+__global__ void finite_kernel(const float* f, long rows, int cols, long ld, int* err, int bit) {
+  const long n = rows * cols;
+  unsigned bad = 0;
+  for (long t = blockIdx.x * long(blockDim.x) + threadIdx.x; t < n; t += long(gridDim.x) * blockDim.x) {
+    const float v = f[(t / cols) * ld + (t % cols)];
+    if (!(fabsf(v) < INFINITY)) bad = 1;
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, bit);
 }
 
 __device__ __forceinline__ float fd4d(float a, float b, float c, float d, float den) {
@@ -135,6 +193,23 @@ cudaError_t launch_add_fields(float* out, const float* a, const float* b, int nx
 
 cudaError_t launch_reciprocal(float* f, int nx, int nz, int ld, cudaStream_t s) {
   reciprocal_kernel<<<grid_for(long(nx) * nz), 256, 0, s>>>(f, nx, nz, ld);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale(float* out, const float* in, long n, float factor, cudaStream_t s) {
+  scale_kernel<<<grid_for(n), 256, 0, s>>>(out, in, n, factor);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_speeds(const float* lam, const float* mu, const float* b, const float* nu, const float* jinv,
+                              const float* mc, bool psv, int nx, int nz, int ld, unsigned* out, cudaStream_t s) {
+  speed_kernel<<<grid_for(long(nx) * nz), 256, 0, s>>>(lam, mu, b, nu, jinv, mc, psv ? 1 : 0, nx, nz, ld, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_finite(const float* f, long rows, int cols, long ld, int* err, int bit, cudaStream_t s) {
+  if (rows <= 0 || cols <= 0) return cudaSuccess;
+  finite_kernel<<<grid_for(rows * cols), 256, 0, s>>>(f, rows, cols, ld, err, bit);
   return cudaGetLastError();
 }
 

@@ -98,8 +98,11 @@ int step2_blocks_per_sm();
 // Tensor maps (3-D: columns, rows, fields; 128 x 1 x n boxes) that let the
 // two-step PSV kernel fetch a row of several fields in one TMA copy: sigma^n
 // (sxx, szz, sxz of a state whose fields vx, vz, sxx, szz, sxz lie at a
-// uniform stride), v^n (vx, vz), 1/rho, and lambda, mu (material fields
-// 1/rho, lambda, mu at a uniform stride).  Encoded on the host.
+// uniform stride), v^n (vx, vz), dt/rho, and dt*lambda, dt*mu (the dt-scaled
+// material fields, at a uniform stride).  Encoded on the host.
+//
+// The two-step kernels (plain and grouped) read the material scaled by dt:
+// PsvStep/ShStep rho, lam, mu hold dt/rho, dt*lambda, dt*mu for them.
 struct Tma2 {
   CUtensorMap sig, vel, rho, lm;
 };
@@ -175,6 +178,7 @@ struct JobDesc {
   float* pool;
   float* adj;              // 2 adjoint slots
   const float *rho, *lam, *mu;
+  const float *rho_dt;     // dt/rho, dt*lambda, dt*mu at the material's stride (two-step kernels)
   const float *taper_x, *taper_zb, *taper_zt;
   float *g_b, *g_lam, *g_mu;
   InjectList src;          // the shot's source
@@ -190,11 +194,12 @@ struct JobDesc {
   // Tensor maps of the job (nullptr: bulk copies): for pool slot s, maps of
   // its state fields with boxes of 1, 2 and 3 fields at tm[3 s + 0..2]; then,
   // from tm[3 tm_nslot]: adjoint slot 0 (boxes of 3 and 2), adjoint slot 1
-  // (3, 2), the material (1, 2) and the gradient block (1, 2).
+  // (3, 2), the material (1, 2), the gradient block (1, 2) and the dt-scaled
+  // material (1, 2).
   const CUtensorMap* tm;
   int tm_nslot;
 };
-constexpr int kJobTmaTail = 8;  // maps after the slots' in a job's table
+constexpr int kJobTmaTail = 10;  // maps after the slots' in a job's table
 
 // One operation of one job in a grouped launch.  Forward: step `it` from slot
 // a to slot b (flags & 1: record the probes).  Adjoint: reverse step `it` with
@@ -257,6 +262,18 @@ cudaError_t launch_add_fields(float* out, const float* a, const float* b, int nx
                               cudaStream_t s);
 // f = 1/f over the nx x nz interior (buoyancy from density, 1/J).
 cudaError_t launch_reciprocal(float* f, int nx, int nz, int ld, cudaStream_t s);
+// out = in * factor over n consecutive floats.
+cudaError_t launch_scale(float* out, const float* in, long n, float factor, cudaStream_t s);
+// Largest squared speeds over the interior (bits of non-negative floats, max
+// taken into out[0..2], which the caller zeroes): out[0] (lambda + 2 mu) b
+// (psv) or mu b (SH), out[1] 4 nu / J and out[2] (mu_c + nu_c) / J when
+// jinv is given (spin; b and jinv hold 1/rho and 1/J); out[3] |= 1 when a
+// value is not finite or negative.
+cudaError_t launch_max_speeds(const float* lam, const float* mu, const float* b, const float* nu, const float* jinv,
+                              const float* mc, bool psv, int nx, int nz, int ld, unsigned* out, cudaStream_t s);
+// *err |= bit when an element of rows x cols (row pitch ld floats) is NaN or
+// infinite.
+cudaError_t launch_check_finite(const float* f, long rows, int cols, long ld, int* err, int bit, cudaStream_t s);
 
 // Receiver traces from probe histories (save_obs_* of fd2d.wgsl:295-301,
 // 463-492).  For each receiver r: obs[comp][r][it].

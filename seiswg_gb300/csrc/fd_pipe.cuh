@@ -9,9 +9,10 @@
 //               bulk copy (cp.async.bulk ... mbarrier::complete_tx::bytes),
 //               issued S-1 iterations ahead by lane 0 or, for many
 //               segments, lane q copying segment q; completion is tracked by
-//               one mbarrier per stage.  Waits are bounded: after kWaitLimit
-//               polls the warp records an error in *err, drains the copies it
-//               issued (again bounded) and leaves its march.
+//               one mbarrier per stage.  Waits are bounded: after a number
+//               of polls (Geom::wait_polls, kWaitLimit when 0) the warp
+//               records an error in *err, drains the copies it issued (again
+//               bounded) and leaves its march.
 #pragma once
 
 #include "fd_common.cuh"
@@ -19,7 +20,7 @@
 namespace seiswg {
 
 constexpr int kSegFloats = 128;  // 32 lanes x float4
-constexpr unsigned kWaitLimit = 1u << 20;
+constexpr unsigned kWaitLimit = 1u << 20;  // polls of a bounded wait unless Geom::wait_polls says otherwise
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -34,6 +35,14 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
+// Counts `bytes` as arrived on the barrier's transaction count, as a copy
+// completing would.  Used only to take back the bytes the wait-expiry test
+// hook armed beyond the copies, so that the barrier's phase then completes
+// exactly when the copies really issued have landed.
+__device__ __forceinline__ void mbar_complete_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
@@ -46,9 +55,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Bounded wait for the completion of phase `parity`.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (unsigned n = 0; n < kWaitLimit; ++n)
+// Bounded wait for the completion of phase `parity`: at most `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned limit) {
+  for (unsigned n = 0; n < limit; ++n)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -87,6 +96,7 @@ struct DirectRows {
   f4 v[NSEG];
   __device__ DirectRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int, float*, uint64_t*, int)
       : s(segs), ld(ld_), c0(c0_), ib(ib_) {}
+  __device__ __forceinline__ void configure(const Geom&) {}
   __device__ __forceinline__ void start() {}
   // Loads the stage of iteration k (row i = ib - 1 + k).
   __device__ __forceinline__ bool acquire(int k) {
@@ -121,6 +131,8 @@ struct BulkRows {
   uint32_t par;    // barrier phase parity of the next iteration to acquire
   float* buf;      // [S][NSEG][128]
   uint64_t* bar;   // [S]
+  unsigned lim = kWaitLimit;  // polls of a bounded wait
+  uint32_t extra = 0;         // test hook: bytes armed on stage 0 beyond its copies
   __device__ BulkRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int lane_, float* buf_,
                       uint64_t* bar_, int nk_)
       : s(segs), src(nullptr), roff(0), ld(ld_), col0(c0_ - 4 * lane_), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0),
@@ -141,15 +153,16 @@ struct BulkRows {
   // transaction count below zero transiently, which the barrier allows).
   // Called by the issuing lanes only.
   __device__ __forceinline__ void issue(int k) { issue_at(k, k % S); }
-  // As issue(k), with the stage st = k % S supplied by the caller.
-  __device__ __forceinline__ void issue_at(int k, int st) {
+  // As issue(k), with the stage st = k % S supplied by the caller; `add`
+  // bytes are armed beyond the stage's own (the wait-expiry test hook).
+  __device__ __forceinline__ void issue_at(int k, int st, uint32_t add = 0) {
     const int i = ib - 1 + k;
     if constexpr (kLaneIssue) {
-      if (lane == 0) mbar_expect_tx(&bar[st], kStageBytes);
+      if (lane == 0) mbar_expect_tx(&bar[st], kStageBytes + add);
       bulk_g2s(buf + (st * NSEG + lane) * kSegFloats, src + ptrdiff_t(i + roff) * ptrdiff_t(ld),
                kSegFloats * sizeof(float), &bar[st]);
     } else {
-      mbar_expect_tx(&bar[st], kStageBytes);
+      mbar_expect_tx(&bar[st], kStageBytes + add);
 #pragma unroll
       for (int q = 0; q < NSEG; ++q)
         bulk_g2s(buf + (st * NSEG + q) * kSegFloats, s.base[q] + ptrdiff_t(i + s.roff[q]) * ptrdiff_t(ld) + col0,
@@ -158,7 +171,15 @@ struct BulkRows {
   }
   __device__ __forceinline__ bool issuer() const { return kLaneIssue ? lane < NSEG : lane == 0; }
 
-  // Barrier set-up and the first S-1 stages.
+  // The launch's wait limit and test hook (Geom::wait_polls, arm_extra).
+  __device__ __forceinline__ void configure(const Geom& g) {
+    lim = g.wait_polls ? g.wait_polls : kWaitLimit;
+    extra = g.arm_extra;
+  }
+
+  // Barrier set-up and the first stages.  With the test hook on, stage 0 is
+  // armed for `extra` bytes more than its copies bring, so that the wait of
+  // iteration 0 runs out although every copy lands.
   __device__ __forceinline__ void start() {
     if (lane == 0) {
       for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
@@ -166,7 +187,7 @@ struct BulkRows {
     }
     __syncwarp();
     if (issuer())
-      for (int k = 0; k < kAhead && k < nk; ++k) issue(k);
+      for (int k = 0; k < kAhead && k < nk; ++k) issue_at(k, k % S, k == 0 ? extra : 0u);
     __syncwarp();
   }
 
@@ -187,7 +208,7 @@ struct BulkRows {
       fence_proxy_async();  // order the warp's reads of the old stage before the copy
       issue_at(k + kAhead, cur + kAhead < S ? cur + kAhead : cur + kAhead - S);
     }
-    return __all_sync(kFull, mbar_wait(&bar[cur], ph));
+    return __all_sync(kFull, mbar_wait(&bar[cur], ph, lim));
   }
   // Segment q of the stage of iteration (current - d), 1 <= d <= KEEP.
   __device__ __forceinline__ f4 seg_back(int q, int d) const {
@@ -207,9 +228,13 @@ struct BulkRows {
   // All lanes have read the stage; it may be refilled.
   __device__ __forceinline__ void release() { __syncwarp(); }
   // After a failed wait at iteration k: wait (bounded) for the copies still
-  // in flight so that none lands after the warp has left.
+  // in flight so that none lands after the warp has left.  With the test
+  // hook on, the wait of iteration 0 is the one that failed; its extra bytes
+  // are taken back first, so that stage 0 completes when its copies land.
   __device__ __forceinline__ void drain(int k) {
-    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
+    if (extra && k == 0 && lane == 0) mbar_complete_tx(&bar[0], extra);
+    __syncwarp();
+    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u, lim);
     __syncwarp();
   }
 };

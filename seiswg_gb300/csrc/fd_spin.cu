@@ -53,6 +53,7 @@ __device__ __forceinline__ void spin_march(const PsvStep& p, int gw, unsigned ch
   segs.base[SP_NU] = p.nu; segs.roff[SP_NU] = -2;
   segs.base[SP_MC] = p.mc; segs.roff[SP_MC] = -2;
   Loader rows = make_loader<Loader>(segs, g, m, L, smem);
+  rows.configure(g);
   rows.start();
 
   // Column taper product; dt/(8 dz) where the column derivative is allowed.

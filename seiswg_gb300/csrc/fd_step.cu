@@ -55,6 +55,7 @@ __device__ __forceinline__ void sh_march(const ShStep& p, int gw, unsigned char*
   segs.base[SH_RHO] = p.rho; segs.roff[SH_RHO] = 0;
   segs.base[SH_MU] = p.mu; segs.roff[SH_MU] = -2;
   Loader rows = make_loader<Loader>(segs, g, m, L, smem);
+  rows.configure(g);
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
@@ -151,6 +152,7 @@ __device__ __forceinline__ void psv_march(const PsvStep& p, int gw, unsigned cha
   segs.base[PV_LAM] = p.lam; segs.roff[PV_LAM] = -2;
   segs.base[PV_MU] = p.mu; segs.roff[PV_MU] = -2;
   Loader rows = make_loader<Loader>(segs, g, m, L, smem);
+  rows.configure(g);
   rows.start();
 
   const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);

@@ -3,6 +3,16 @@
 // Built with multiply-add contraction (the one-step kernels keep the
 // reference's separate multiply and add): the two-step march is bound by
 // instruction issue, not by HBM.
+//
+// The material these kernels read is scaled by dt on the host side of the
+// launch (dt/rho, dt*lambda, dt*mu; Sim::prepare_model), so that dt costs no
+// instruction per update and every intermediate keeps the magnitude of the
+// reference's own (fd2d.wgsl:362-363, 396-398: dt multiplies the divergence
+// after the division by 8 h).  Folding dt into the difference factors instead
+// (dt/(8 h) ~ 1e-5 times a raw difference) made the intermediates so small
+// that the leading edge of a wavefield underflowed into subnormals sooner
+// than in the reference, which moved trace samples ahead of the first arrival
+// by 1e-5 relative.
 #include <type_traits>
 
 #include "fd_fma.cuh"
@@ -21,6 +31,9 @@ namespace {
 // row i-5).  Only level-2 rows are written: per two steps each state field is
 // read and written once and each material field read twice (once per level,
 // the second time from L2), 26 B of HBM traffic per cell-update instead of 52.
+//
+// The divergence is added to v with the material's dt/rho and the sources
+// enter the divergence unscaled (stf_dsxz, fd2d.wgsl:344-352).
 //
 // Reach: two steps need level-1 values 3 columns and 4 rows beyond the
 // level-2 outputs, so a strip owns 112 columns (lanes 2..29) and a chunk of
@@ -93,9 +106,15 @@ __device__ __forceinline__ f4 in_grid(const f4& a, bool row_ok, int valid) {
   return o;
 }
 
-// dt times the stress divergence at a velocity row (div_sxz, fd2d.wgsl:315-316):
+// Sources of row i (stf_dsxz, fd2d.wgsl:344-352) added to the divergence.
+__device__ __forceinline__ void inject_add(const InjectList& inj, int i, int c0, Cursor& cur, f4& dsx, f4& dsz) {
+  inject_at<true, false, true>(inj, i, c0, cur, dsx, dsx, dsz);
+}
+
+// The stress divergence at a velocity row (div_sxz, fd2d.wgsl:309-317):
 // x from the sigma_xx / sigma_xz rows a0..a3 / b0..b3, z from the current
-// sigma_xz / sigma_zz rows cz / zz.  rx = dt/(8 dx) or 0, rz = dt/(8 dz) or 0.
+// sigma_xz / sigma_zz rows cz / zz.  rx = 1/(8 dx) or 0, rz = 1/(8 dz) or 0
+// (0 where the edge rule zeroes the derivative).
 __device__ __forceinline__ void vel_div(const f4& a0, const f4& a1, const f4& a2, const f4& a3, const f4& b0,
                                         const f4& b1, const f4& b2, const f4& b3, const f4& cz, const f4& zz,
                                         float rx, const f4& rz, f4& dsx, f4& dsz) {
@@ -110,8 +129,8 @@ __device__ __forceinline__ void vel_div(const f4& a0, const f4& a1, const f4& a2
 
 // Stress update of one row from the velocity rows u0..u3 (vx) and w0..w3 (vz)
 // (div_vxz and add_sxz, fd2d.wgsl:378-381, 396-398): sxx += (l+2m) dvx/dx +
-// l dvz/dz, szz += (l+2m) dvz/dz + l dvx/dx, sxz += m (dvx/dz + dvz/dx), the
-// derivatives carrying dt.
+// l dvz/dz, szz += (l+2m) dvz/dz + l dvx/dx, sxz += m (dvx/dz + dvz/dx), with
+// lam and mu holding dt*lambda and dt*mu.
 __device__ __forceinline__ void stress(const f4& u0, const f4& u1, const f4& u2, const f4& u3, const f4& w0,
                                        const f4& w1, const f4& w2, const f4& w3, float rx, const f4& rz,
                                        const f4& lam, const f4& mu, const f4& xx, const f4& zz, const f4& xz,
@@ -163,18 +182,19 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
   if constexpr (std::is_same<Loader, TmaRows<PsvTmaPlan, 6, 3, M>>::value) rows.tm = tm;
+  rows.configure(g);
   rows.start();
 
-  // Column taper product, and dt folded into the difference factors:
-  // dt/(8 dx) per row (0 where the row derivative is zeroed), dt/(8 dz) per
-  // column (0 where the column derivative is zeroed).
+  // Column taper product; difference factors 1/(8 dx) per row (0 where the
+  // row derivative is zeroed) and 1/(8 dz) per column (0 where the column
+  // derivative is zeroed).  rho, lam and mu hold dt/rho, dt*lambda, dt*mu.
   f4 tbt;
   {
     const f4 tb = ld4(p.taper_zb + c0), tt = ld4(p.taper_zt + c0);
 #pragma unroll
     for (int e = 0; e < 4; ++e) tbt.v[e] = tb.v[e] * tt.v[e];
   }
-  const float sx_dt = dt * g.rdx, sz_dt = dt * g.rdz;
+  const float sxr = g.rdx, szr = g.rdz;
   // sigma^n rings, rows i-2..i+1
   f4 xx0 = ld4(at(p.sxx0, i0 - 2)), xx1 = ld4(at(p.sxx0, i0 - 1)), xx2 = ld4(at(p.sxx0, i0)), xx3;
   f4 xz0 = ld4(at(p.sxz0, i0 - 2)), xz1 = ld4(at(p.sxz0, i0 - 1)), xz2 = ld4(at(p.sxz0, i0)), xz3;
@@ -196,8 +216,8 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
   f4 rzb, rzf;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
-    rzb.v[e] = (!EDGE || (L.zb & (1 << e))) ? sz_dt : 0.0f;
-    rzf.v[e] = (!EDGE || (L.zf & (1 << e))) ? sz_dt : 0.0f;
+    rzb.v[e] = (!EDGE || (L.zb & (1 << e))) ? szr : 0.0f;
+    rzf.v[e] = (!EDGE || (L.zf & (1 << e))) ? szr : 0.0f;
   }
   // Some lane holds columns outside the grid: level-1 values there are zeroed.
   const bool cols_out = EDGE && !__all_sync(kFull, valid == 0xF);
@@ -228,10 +248,10 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
 
     // ---- level 1, velocity of row i (step it)
     {
-      const float rx = (!EDGE || (i >= 2 && i < nx - 2)) ? sx_dt : 0.0f;
+      const float rx = (!EDGE || (i >= 2 && i < nx - 2)) ? sxr : 0.0f;
       f4 dsx, dsz;
       vel_div(xx0, xx1, xx2, xx3, xz0, xz1, xz2, xz3, xz2, zz2, rx, rzb, dsx, dsz);
-      if (ci1.row == i) inject_dt(p.inj, i, c0, ci1, dt, dsx, dsz);
+      if (ci1.row == i) inject_add(p.inj, i, c0, ci1, dsx, dsz);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float bb = bx1 * tbt.v[e];
@@ -251,7 +271,7 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     // ---- level 1, stress of row i-2 (step it)
     if (k >= 3) {
       const int r = i - 2;
-      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sx_dt : 0.0f;
+      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sxr : 0.0f;
       stress(xa, xb_, xc, xd, za, zb_, zc, zd, rx, rzf, lam, mu, xx0, zz0, xz0, sx3, sz3, sq3);
       const bool row_ok = (r >= 0 && r < nx);
       if (EDGE && (!row_ok || cols_out)) {
@@ -265,10 +285,10 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     if (k >= 6) {
       const int r = i - 3;
       const f4 rho2 = rows.seg_back(P2_RHO, 3);
-      const float rx = (!EDGE || (r >= 2 && r < nx - 2)) ? sx_dt : 0.0f;
+      const float rx = (!EDGE || (r >= 2 && r < nx - 2)) ? sxr : 0.0f;
       f4 dsx, dsz;
       vel_div(sx0, sx1, sx2, sx3, sq0, sq1, sq2, sq3, sq2, sz2, rx, rzb, dsx, dsz);
-      if (ci2.row == r) inject_dt(inj2, r, c0, ci2, dt, dsx, dsz);
+      if (ci2.row == r) inject_add(inj2, r, c0, ci2, dsx, dsz);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float bb = bx2 * tbt.v[e];
@@ -287,7 +307,7 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     if (k >= 9) {
       const int r = i - 5;
       const f4 lam2 = rows.seg_back(P2_LAM, 3), mu2 = rows.seg_back(P2_MU, 3);
-      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sx_dt : 0.0f;
+      const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sxr : 0.0f;
       f4 sxx, szz, sxz;
       stress(ua, ub, uc, ud, wa, wb, wc, wd, rx, rzf, lam2, mu2, sx0, sz0, sq0, sxx, szz, sxz);
       st4_masked(at(p.sxx1, r), sxx, L.own);
@@ -354,14 +374,9 @@ struct ShBulk2 : BulkRows<S2_NSEG, 6, true, 3> {
   using BulkRows<S2_NSEG, 6, true, 3>::BulkRows;
 };
 
-// Sources of row i (stf_dsy, fd2d.wgsl:248-266) added to dt times the
-// divergence.
-__device__ __forceinline__ void inject_dt_y(const InjectList& inj, int i, int c0, Cursor& cur, float dt, f4& ds) {
-  const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
-  f4 fy = z4;
-  inject_at<false, true, false>(inj, i, c0, cur, fy, fy, fy);
-#pragma unroll
-  for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(dt, fy.v[e], ds.v[e]);
+// Sources of row i (stf_dsy, fd2d.wgsl:253-260) added to the divergence.
+__device__ __forceinline__ void inject_add_y(const InjectList& inj, int i, int c0, Cursor& cur, f4& ds) {
+  inject_at<false, true, false>(inj, i, c0, cur, ds, ds, ds);
 }
 
 template <class Loader, class M>
@@ -391,6 +406,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
   }
   Loader rows(segs, ld, c0, i0 + 1, m.lane, buf, bar, nk);  // iteration k reads row i0 + k
   if constexpr (std::is_same<Loader, TmaRows<ShTmaPlan, 6, 3, M>>::value) rows.tm = tm;
+  rows.configure(g);
   rows.start();
 
   f4 tbt;
@@ -399,7 +415,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
 #pragma unroll
     for (int e = 0; e < 4; ++e) tbt.v[e] = tb.v[e] * tt.v[e];
   }
-  const float sx_dt = dt * g.rdx, sz_dt = dt * g.rdz;
+  const float sxr = g.rdx, szr = g.rdz;
   // sigma^n rings, rows i-2..i+1
   f4 xy0 = ld4(at(p.sxy0, i0 - 2)), xy1 = ld4(at(p.sxy0, i0 - 1)), xy2 = ld4(at(p.sxy0, i0)), xy3;
   f4 zy0 = ld4(at(p.szy0, i0 - 2)), zy1 = ld4(at(p.szy0, i0 - 1)), zy2 = ld4(at(p.szy0, i0)), zy3;
@@ -419,8 +435,8 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
   f4 rzb, rzf;
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
-    rzb.v[e] = (L.zb & (1 << e)) ? sz_dt : 0.0f;
-    rzf.v[e] = (L.zf & (1 << e)) ? sz_dt : 0.0f;
+    rzb.v[e] = (L.zb & (1 << e)) ? szr : 0.0f;
+    rzf.v[e] = (L.zf & (1 << e)) ? szr : 0.0f;
   }
   const bool cols_out = !__all_sync(kFull, valid == 0xF);
   float bx1_next = __ldg(p.taper_x + i0), bx2_next = __ldg(p.taper_x + i0 - 3);
@@ -444,12 +460,12 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
 
     // ---- level 1, velocity of row i (step it): div_sy, source, add_vy
     {
-      const float rx = (i >= 2 && i < nx - 2) ? sx_dt : 0.0f;
+      const float rx = (i >= 2 && i < nx - 2) ? sxr : 0.0f;
       const f4 ax = d4_rows(xy0, xy1, xy2, xy3), az = d4_cols_back(zy2);
       f4 ds;
 #pragma unroll
       for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(az.v[e], rzb.v[e], ax.v[e] * rx);
-      if (ci1.row == i) inject_dt_y(p.inj, i, c0, ci1, dt, ds);
+      if (ci1.row == i) inject_add_y(p.inj, i, c0, ci1, ds);
 #pragma unroll
       for (int e = 0; e < 4; ++e) vd.v[e] = (bx1 * tbt.v[e]) * fmaf(ds.v[e], rho.v[e], vo.v[e]);
       const bool row_ok = (i >= 0 && i < nx);
@@ -460,7 +476,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     // ---- level 1, stress of row i-2 (step it): div_vy, add_sy_sh
     if (k >= 3) {
       const int r = i - 2;
-      const float rx = (r >= 1 && r < nx - 2) ? sx_dt : 0.0f;
+      const float rx = (r >= 1 && r < nx - 2) ? sxr : 0.0f;
       const f4 gx = d4_rows(va, vb, vc, vd), gz = d4_cols_fwd(vb);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
@@ -478,12 +494,12 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     if (k >= 6) {
       const int r = i - 3;
       const f4 rho2 = rows.seg_back(S2_RHO, 3);
-      const float rx = (r >= 2 && r < nx - 2) ? sx_dt : 0.0f;
+      const float rx = (r >= 2 && r < nx - 2) ? sxr : 0.0f;
       const f4 ax = d4_rows(sx0, sx1, sx2, sx3), az = d4_cols_back(sz2);
       f4 ds;
 #pragma unroll
       for (int e = 0; e < 4; ++e) ds.v[e] = fmaf(az.v[e], rzb.v[e], ax.v[e] * rx);
-      if (ci2.row == r) inject_dt_y(inj2, r, c0, ci2, dt, ds);
+      if (ci2.row == r) inject_add_y(inj2, r, c0, ci2, ds);
 #pragma unroll
       for (int e = 0; e < 4; ++e) ud.v[e] = (bx2 * tbt.v[e]) * fmaf(ds.v[e], rho2.v[e], va.v[e]);
       if (r >= m.ib && r < m.ie) {
@@ -496,7 +512,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     if (k >= 9) {
       const int r = i - 5;
       const f4 mu2 = rows.seg_back(S2_MU, 3);
-      const float rx = (r >= 1 && r < nx - 2) ? sx_dt : 0.0f;
+      const float rx = (r >= 1 && r < nx - 2) ? sxr : 0.0f;
       const f4 gx = d4_rows(ua, ub, uc, ud), gz = d4_cols_fwd(ub);
       f4 sxy, szy;
 #pragma unroll
@@ -552,7 +568,8 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(co
   p.sxz0 = slot(op.a, 4);
   p.vx1 = slot(op.b, 0); p.vz1 = slot(op.b, 1); p.sxx1 = slot(op.b, 2); p.szz1 = slot(op.b, 3);
   p.sxz1 = slot(op.b, 4);
-  p.rho = J.rho; p.lam = J.lam; p.mu = J.mu;
+  const long long dm = J.lam - J.rho;  // the material's field stride
+  p.rho = J.rho_dt; p.lam = J.rho_dt + dm; p.mu = J.rho_dt + 2 * dm;
   p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
   p.inj = J.src;
   p.inj.it = op.it;
@@ -562,7 +579,7 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(co
   p.err = J.err;
   if (J.tm) {
     const CUtensorMap* t = J.tm + 3 * J.tm_nslot;
-    const Tma2Ptrs mp{J.tm + 3 * op.a + 2, J.tm + 3 * op.a + 1, t + 4, t + 5};
+    const Tma2Ptrs mp{J.tm + 3 * op.a + 2, J.tm + 3 * op.a + 1, t + 8, t + 9};
     psv2_march<TmaRows<PsvTmaPlan, 6, 3, Tma2Ptrs>, Tma2Ptrs>(p, lw, smem, &mp);
   } else {
     psv2_march<Bulk2>(p, lw, smem);
@@ -584,7 +601,7 @@ __global__ void __launch_bounds__(kStepWarps * 32, 3) grouped_forward2_sh_kernel
   p.g = J.g2;
   p.vy0 = slot(op.a, 0); p.sxy0 = slot(op.a, 1); p.szy0 = slot(op.a, 2);
   p.vy1 = slot(op.b, 0); p.sxy1 = slot(op.b, 1); p.szy1 = slot(op.b, 2);
-  p.rho = J.rho; p.mu = J.mu;
+  p.rho = J.rho_dt; p.mu = J.rho_dt + 2 * (J.lam - J.rho);
   p.taper_x = J.taper_x; p.taper_zb = J.taper_zb; p.taper_zt = J.taper_zt;
   p.inj = J.src;
   p.inj.it = op.it;
@@ -593,7 +610,7 @@ __global__ void __launch_bounds__(kStepWarps * 32, 3) grouped_forward2_sh_kernel
   p.probes.it = op.it;
   p.err = J.err;
   if (J.tm) {
-    const Tma2Ptrs mp{J.tm + 3 * op.a + 1, J.tm + 3 * op.a + 0, J.tm + 3 * J.tm_nslot + 4, nullptr};
+    const Tma2Ptrs mp{J.tm + 3 * op.a + 1, J.tm + 3 * op.a + 0, J.tm + 3 * J.tm_nslot + 8, nullptr};
     sh2_march<TmaRows<ShTmaPlan, 6, 3, Tma2Ptrs>, Tma2Ptrs>(p, lw, smem, &mp);
   } else {
     sh2_march<ShBulk2>(p, lw, smem);

@@ -46,18 +46,24 @@ struct TmaRows {
   uint32_t par;
   float* buf;
   uint64_t* bar;
+  unsigned lim = kWaitLimit;  // polls of a bounded wait
+  uint32_t extra = 0;         // test hook: bytes armed on stage 0 beyond its copies
   __device__ TmaRows(const SegsT&, size_t, int c0_, int ib_, int lane_, float* buf_, uint64_t* bar_, int nk_)
       : x0(c0_ - 4 * lane_ + kHaloCols), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0), buf(buf_),
         bar(bar_) {}
-  __device__ __forceinline__ void issue_at(int k, int st) {
-    mbar_expect_tx(&bar[st], kStageBytes);
+  __device__ __forceinline__ void issue_at(int k, int st, uint32_t add = 0) {
+    mbar_expect_tx(&bar[st], kStageBytes + add);
     Plan::issue(buf + st * NSEG * kSegFloats, tm, x0, ib - 1 + k + kHaloRows, &bar[st]);
+  }
+  __device__ __forceinline__ void configure(const Geom& g) {
+    lim = g.wait_polls ? g.wait_polls : kWaitLimit;
+    extra = g.arm_extra;
   }
   __device__ __forceinline__ void start() {
     if (lane == 0) {
       for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
       fence_mbar_init();
-      for (int k = 0; k < kAhead && k < nk; ++k) issue_at(k, k % S);
+      for (int k = 0; k < kAhead && k < nk; ++k) issue_at(k, k % S, k == 0 ? extra : 0u);
     }
     __syncwarp();
   }
@@ -73,7 +79,7 @@ struct TmaRows {
       fence_proxy_async();
       issue_at(k + kAhead, cur + kAhead < S ? cur + kAhead : cur + kAhead - S);
     }
-    return __all_sync(kFull, mbar_wait(&bar[cur], ph));
+    return __all_sync(kFull, mbar_wait(&bar[cur], ph, lim));
   }
   __device__ __forceinline__ f4 seg_back(int q, int d) const {
     const int st = cur >= d ? cur - d : cur + S - d;
@@ -89,8 +95,11 @@ struct TmaRows {
     return r;
   }
   __device__ __forceinline__ void release() { __syncwarp(); }
+  // As BulkRows::drain: the test hook's extra bytes are taken back first.
   __device__ __forceinline__ void drain(int k) {
-    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u);
+    if (extra && k == 0 && lane == 0) mbar_complete_tx(&bar[0], extra);
+    __syncwarp();
+    for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u, lim);
     __syncwarp();
   }
   static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }

@@ -60,6 +60,9 @@ struct Geom {
   float rdx;     // 1/(8*dx): reciprocal of the reference's denominator (fd2d.wgsl:156)
   float rdz;     // 1/(8*dz)
   int loader;    // kLoaderDirect or kLoaderBulk
+  unsigned wait_polls;  // polls of a bounded row-pipeline wait (0: kWaitLimit)
+  unsigned arm_extra;   // test hook: bytes armed on the first stage of every warp's
+                        // ring beyond its copies, so that its wait runs out (0 normally)
 };
 
 // Row loaders of the step kernels (fd_pipe.cuh).
@@ -68,6 +71,6 @@ constexpr int kPipeStages = 3;  // shared-memory stages per warp of the step ker
 constexpr int kAdjStages = 2;   // stages of the adjoint kernels (19 row segments per stage)
 
 // Bits of the device error word.
-enum { kErrWaitTimeout = 1 };
+enum { kErrWaitTimeout = 1, kErrNonFiniteTraces = 2, kErrNonFiniteGradient = 4 };
 
 }  // namespace seiswg

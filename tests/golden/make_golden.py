@@ -6,6 +6,7 @@ inputs that produced them, into compressed .npz files so that the parity tests
 run without the reference checkout (it is absent on the GPU machines).
 
     python tests/golden/make_golden.py /path/to/seiswg
+    SEISWG_REFERENCE=/path/to/seiswg python tests/golden/make_golden.py
 
 Contents
 --------
@@ -85,4 +86,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SEISWG_REFERENCE", "")
+    if not src:
+        sys.exit("usage: make_golden.py <seiswg checkout> (or set SEISWG_REFERENCE)")
+    main(src)

@@ -1,6 +1,8 @@
 """CUDA path against the FP32 CPU oracle on seeded inputs (relative L2 within
-1e-5, the tolerance of the FP32 wavefield; the FP64 oracle error is reported
-in the assertion message).  Cases cover the edge rules of fd2d.wgsl: grids
+1e-5, the FP32 tolerance the path is held to; the FP64 oracle error is
+reported in the assertion message; only the spin rotation yi, a difference of
+two displacement derivatives, may instead reach 3x the FP32 oracle's own
+distance from FP64).  Cases cover the edge rules of fd2d.wgsl: grids
 narrower than one warp strip, odd sizes, every taper edge, sources and
 receivers on and next to the boundary, co-located sources, per-shot source
 selection, SH+PSV together, spin, snapshots, and the reference adjoint with
@@ -33,7 +35,7 @@ _STATE = dict(vy="VY", sxy="SXY", szy="SZY", vx="VX", vz="VZ", sxx="SXX", szz="S
 
 
 def _run_pair(nx, nz, nt, dx, dt, src, rec, model, isrc=-1, snap=0, snap_fields=(), chunk_rows=None,
-              graphs=None, loader=None, **flags):
+              graphs=None, loader=None, two_step=None, **flags):
     """Runs the same problem on the GPU and in both oracles."""
     import seiswg_gb300 as sw
     from oracle import oracle as O
@@ -50,6 +52,8 @@ def _run_pair(nx, nz, nt, dx, dt, src, rec, model, isrc=-1, snap=0, snap_fields=
             sim.set_option("graphs", graphs)
         if loader is not None:
             sim.set_option("loader", loader)
+        if two_step is not None:
+            sim.set_option("two_step", two_step)
         for k, v in model.items():
             sim.upload_model(k, v)
         sim.prepare()
@@ -91,20 +95,22 @@ def _comps(flags):
 
 
 def _check(gpu, ref, flags, tol=L2_TOL):
-    # Tolerance: 1e-5 relative L2, or 3x the FP32 oracle's own distance from
-    # the FP64 oracle where FP32 cancellation makes that larger (the spin
-    # rotation yi = uy_c - curl/2 differences two displacement derivatives).
+    # Tolerance: 1e-5 relative L2 against the FP32 oracle.  The spin rotation
+    # yi = uy_c - curl/2 (component 3) differences two displacement
+    # derivatives; there FP32 cancellation can take the oracle itself past
+    # 1e-5 from FP64, and 3x that distance is allowed instead.
     for c in _comps(flags):
         e32 = rel_l2(gpu["traces"][c], ref[32]["obs"][c])
         e64 = rel_l2(gpu["traces"][c], ref[64]["obs"][c])
         floor = rel_l2(ref[32]["obs"][c], ref[64]["obs"][c])
-        assert e32 <= max(tol, 3 * floor), \
+        lim = max(tol, 3 * floor) if c == 3 else tol
+        assert e32 <= lim, \
             f"trace comp {c}: rel L2 {e32:.2e} vs FP32 oracle (FP64: {e64:.2e}, FP32 oracle vs FP64 {floor:.2e})"
     for f, a in gpu["state"].items():
         e32 = rel_l2(a, ref[32]["state"][f])
         e64 = rel_l2(a, ref[64]["state"][f])
         floor = rel_l2(ref[32]["state"][f], ref[64]["state"][f])
-        assert e32 <= max(tol, 3 * floor), \
+        assert e32 <= tol, \
             f"state {f}: rel L2 {e32:.2e} vs FP32 oracle (FP64: {e64:.2e}, FP32 oracle vs FP64 {floor:.2e})"
 
 
@@ -238,3 +244,26 @@ def test_reference_adjoint_and_smoothing():
         kmu = sim.kernel()
     np.testing.assert_allclose(gm, mis, rtol=1e-5)
     assert rel_l2(kmu, ref_kmu) <= L2_TOL
+
+
+@pytest.mark.parametrize("two_step", [1, 0], ids=["two_step", "one_step"])
+def test_c2_geometry_plain_tolerance(two_step):
+    """The headline workload's geometry at 512 x 480: PSV, absorbing width 40
+    on every edge, a 90-degree Ricker 50 cells below the top, receivers on the
+    top row and one at depth.  Traces and the final state within 1e-5 of the
+    FP32 oracle, for the two-step kernel (the default) and the one-step one.
+
+    The top row (j = 0) is decoupled from the grid by the edge rule (no z
+    difference reaches it or leaves it, fd2d.wgsl:151-180), so its traces
+    stay exactly zero; within 400 steps the deep receiver sees only the
+    signal ahead of the first arrival, whose ux is subnormal in FP32 -- the
+    most rounding-sensitive part of a trace."""
+    nx, nz, nt, dx, dt = 512, 480, 400, 5.0, 4.0e-4
+    flags = dict(psv=True, abs_left=True, abs_right=True, abs_bottom=True, abs_top=True, abs_width=40)
+    src = [(256, 50, 15.0, 0.05, 90.0)]
+    rec = [(i, 0) for i in range(0, 512, 32)] + [(256, 240)]
+    gpu, ref = _run_pair(nx, nz, nt, dx, dt, src, rec, _model(nx, nz, 11, dx=dx), two_step=two_step, **flags)
+    _check(gpu, ref, flags)
+    top = slice(0, 16)
+    for c in (0, 2):
+        assert not np.any(gpu["traces"][c][top]) and not np.any(ref[64]["obs"][c][top])
