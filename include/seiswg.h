@@ -161,8 +161,20 @@ int seiswg_sim_kernel(seiswg_sim* sim, float* host);
 int seiswg_sim_gradient_clear(seiswg_sim* sim);
 int seiswg_sim_forward_op(seiswg_sim* sim, int32_t isrc, int32_t ckpt_every);
 int seiswg_sim_backward_op(seiswg_sim* sim, const float* adj);
-/* The checkpoint interval of the last forward_op (0 before the first). */
+/* The checkpoint interval of the last forward_op (0 before the first, and
+ * under binomial checkpointing). */
 int32_t seiswg_sim_checkpoint_interval(const seiswg_sim* sim);
+/* The checkpoint plan of the last forward_op: binomial checkpointing slots
+ * (0: uniform checkpoints every `interval` steps), the forward steps the
+ * reverse sweep recomputes, and the device bytes the checkpoints hold.
+ * Binomial checkpointing (Griewank and Walther's revolve schedule; the
+ * reference has no checkpointing: it keeps the forward wavefield every
+ * adj_interval steps in host memory, solver.rs:1384, 1411-1414) stores S
+ * states and recomputes the fewest steps any schedule with S states can:
+ * F(nt, S-1) - (nt - 1) with F(n, s) = r n - C(s+1+r, r-1), r the least
+ * integer with C(s+1+r, r) >= n. */
+int seiswg_sim_checkpoint_plan(const seiswg_sim* sim, int32_t* slots, int32_t* interval, int64_t* recomputed,
+                               size_t* bytes);
 /* The misfit and adjoint source on the device (the host misfit of
  * solver.rs:432-467 without the trace download and the adjoint-source
  * upload).  set_observed copies the observed traces, [ncomp][nrec][nt] in the
@@ -192,7 +204,13 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * results are the one-step kernel's bits), "tma" (0/1: the two-step and the
  * PSV reverse kernels fetch their rows with 3-D tensor copies where the
  * fields lie at uniform strides, default on; 0: one bulk copy per field;
- * the same results either way), "stability_check" (0/1, default 1: see
+ * the same results either way), "checkpoint_slots" (forward_op with
+ * ckpt_every = 0 uses binomial checkpointing with this many stored states,
+ * 1 or more; 0, the default: uniform checkpoints every second step where half
+ * of the free HBM (or the budget below) holds them, else every ceil(sqrt(nt))
+ * steps, else binomial checkpointing with as many states as fit),
+ * "checkpoint_budget_mb" (the memory that default choice may give to
+ * checkpoints; 0: half of the free HBM), "stability_check" (0/1, default 1: see
  * seiswg_sim_prepare), "wait_polls" (polls of a kernel's bounded wait for
  * its row pipeline before it gives up and the run fails with
  * SEISWG_ETIMEOUT; 0: the built-in 2^20), "test_arm_extra" (a test hook for
@@ -265,7 +283,7 @@ void seiswg_batch_free(seiswg_batch* batch);
  * callers that cannot call cudaMalloc: hosts whose device memory all belongs
  * to their own pool allocator, or code where an allocation (which may
  * synchronise the device) is not allowed.  It allocates nothing; its scratch
- * is a fixed array in the library's device image (16 MiB + 64 KiB, held on
+ * is a fixed array in the library's device image (16 MiB + 112 KiB, held on
  * every GPU that loads the library until the process exits), which limits the
  * grid to 4,194,304 cells and 6144 per axis, and sigma to 511; larger
  * requests fail with SEISWG_EINVAL.  The first call on a device looks up the

@@ -119,12 +119,14 @@ def round_half_away(x):
 
 
 def infer_grid(x, z):
-    """solver.rs:646-656: nx, nz from the coordinate extents (f64 sqrt, f32 dx)."""
+    """solver.rs:646-656: nx, nz from the coordinate extents (f64 sqrt, f32 dx).
+    The extents fold f32::max / f32::min from -/+infinity (solver.rs:647-650),
+    which pass over NaN elements: nanmax / nanmin."""
     x = np.asarray(x, np.float32)
     z = np.asarray(z, np.float32)
     npt = x.size
-    lx = np.float32(x.max() - x.min())
-    lz = np.float32(z.max() - z.min())
+    lx = np.float32(np.nanmax(x) - np.nanmin(x))
+    lz = np.float32(np.nanmax(z) - np.nanmin(z))
     nx = int(round_half_away(np.float64(np.sqrt(np.float64(npt) * np.float64(lx) / np.float64(lz)))))
     nz = int(round_half_away(np.float64(np.sqrt(np.float64(npt) * np.float64(lz) / np.float64(lx)))))
     dx = np.float32(lx / np.float32(nx - 1))

@@ -90,6 +90,7 @@ PROTOTYPES = [
     ("seiswg_sim_forward_op", _c_int, [_vp, _i32, _i32]),
     ("seiswg_sim_backward_op", _c_int, [_vp, _pf]),
     ("seiswg_sim_checkpoint_interval", _i32, [_vp]),
+    ("seiswg_sim_checkpoint_plan", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_sz)]),
     ("seiswg_sim_set_observed", _c_int, [_vp, _pf]),
     ("seiswg_sim_misfit_op", _c_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     ("seiswg_sim_backward_op_device", _c_int, [_vp]),
@@ -383,6 +384,15 @@ class Sim:
     def checkpoint_interval(self) -> int:
         """Checkpoint interval of the last forward_op."""
         return int(lib().seiswg_sim_checkpoint_interval(self._h))
+
+    def checkpoint_plan(self):
+        """Of the last forward_op: dict(slots = binomial checkpointing slots
+        (0: uniform), interval, recomputed = forward steps the reverse sweep
+        recomputes, bytes = device memory of the checkpoints)."""
+        s, k, r, b = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int64(), ctypes.c_size_t()
+        _check(lib().seiswg_sim_checkpoint_plan(self._h, ctypes.byref(s), ctypes.byref(k), ctypes.byref(r),
+                                                ctypes.byref(b)))
+        return dict(slots=s.value, interval=k.value, recomputed=r.value, bytes=b.value)
 
     def set_observed(self, obs):
         """Observed traces [ncomp][nrec][nt] for misfit_op (kept on the device)."""

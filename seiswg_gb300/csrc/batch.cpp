@@ -23,12 +23,11 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
     SW_CUDA(cudaEventCreateWithFlags(&join_[k], cudaEventDisableTiming));
   }
   SW_CUDA(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming));
-  kst_.assign(nstreams, nullptr);
-  kev_.assign(nstreams, nullptr);
-  for (int k = 0; k < nstreams; ++k) {
-    SW_CUDA(cudaStreamCreateWithFlags(&kst_[k], cudaStreamNonBlocking));
-    SW_CUDA(cudaEventCreateWithFlags(&kev_[k], cudaEventDisableTiming));
-  }
+  static_assert(kMaxStreamGroups == kPlanGroupsMax, "stream groups of the batch and of its launch plan");
+  kst_.assign(kPlanStreams, nullptr);
+  kev_.assign(kPlanEvents, nullptr);
+  for (int k = 0; k < kPlanStreams; ++k) SW_CUDA(cudaStreamCreateWithFlags(&kst_[k], cudaStreamNonBlocking));
+  for (int k = 0; k < kPlanEvents; ++k) SW_CUDA(cudaEventCreateWithFlags(&kev_[k], cudaEventDisableTiming));
   SW_CUDA(cudaMalloc(&err_, sizeof(int)));
   SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
   for (size_t p = 0; p < problems_.size(); ++p) {
@@ -326,28 +325,31 @@ void Batch::enqueue_run() {
 
 void Batch::enqueue_slots(int t0, int t1) {
   if (concurrent_ == 2) {
-    // One stream per kind, forked from and joined back into the batch's
-    // stream; a job that changes kind between slots makes its new kind's
-    // stream wait for its old kind's launch.
-    // Stream (kind, group) = kst_[kind * kMaxStreamGroups + group]; jobs stay
-    // in their group, so the waits are within a group.
-    auto sid = [](int kind, int grp) { return kind * kMaxStreamGroups + grp; };
+    // One stream per (kind, group), forked from and joined back into the
+    // batch's stream; a job that changes kind between slots makes its new
+    // kind's stream wait for its old kind's launch of the previous slot
+    // (events per slot parity, batch_plan.h).  Jobs stay in their group, so
+    // the waits are within a group.
     SW_CUDA(cudaEventRecord(fork_, stream_));
     for (int k = 0; k < kKinds; ++k)
-      for (int g = 0; g < groups_; ++g) SW_CUDA(cudaStreamWaitEvent(kst_[sid(k, g)], fork_, 0));
-    for (int t = std::max(0, t0); t < std::min(t1, nslots_); ++t) {
+      for (int g = 0; g < groups_; ++g) SW_CUDA(cudaStreamWaitEvent(kst_[plan_stream(k, g)], fork_, 0));
+    const int ta = std::max(0, t0);
+    for (int t = ta; t < std::min(t1, nslots_); ++t) {
       for (const Launch& l : plan_[t]) {
-        cudaStream_t s = kst_[sid(l.kind, l.group)];
-        for (int a = 0; a < kKinds; ++a)
-          if (l.deps & (1 << a)) SW_CUDA(cudaStreamWaitEvent(s, kev_[sid(a, l.group)], 0));
+        cudaStream_t s = kst_[plan_stream(l.kind, l.group)];
+        // A window that starts at ta > 0 (the autotuner's) has no slot ta-1
+        // launches to wait for: the fork above orders it after them.
+        if (t > ta)
+          for (int a = 0; a < kKinds; ++a)
+            if (l.deps & (1 << a)) SW_CUDA(cudaStreamWaitEvent(s, kev_[plan_event(a, l.group, t - 1)], 0));
         launch_kind(l, s);
-        SW_CUDA(cudaEventRecord(kev_[sid(l.kind, l.group)], s));
+        SW_CUDA(cudaEventRecord(kev_[plan_event(l.kind, l.group, t)], s));
       }
     }
     for (int k = 0; k < kKinds; ++k)
       for (int g = 0; g < groups_; ++g) {
-        SW_CUDA(cudaEventRecord(kev_[sid(k, g)], kst_[sid(k, g)]));
-        SW_CUDA(cudaStreamWaitEvent(stream_, kev_[sid(k, g)], 0));
+        SW_CUDA(cudaEventRecord(kev_[plan_event(k, g, 0)], kst_[plan_stream(k, g)]));
+        SW_CUDA(cudaStreamWaitEvent(stream_, kev_[plan_event(k, g, 0)], 0));
       }
     return;
   }

@@ -55,16 +55,15 @@ class Batch {
   // How the launches of the schedule are ordered.  0: one after another on
   // the batch's stream.  1: the launches of one slot (one per kind of work)
   // run concurrently on forked streams that join before the next slot.
-  // 2 (default): one stream per kind; a launch waits only for the latest
-  // launches of the kinds its jobs come from (the previous slot's, or this
-  // slot's for a kind enqueued before it), so the kinds pipeline.
+  // 2 (default): one stream per kind; a launch waits only for the previous
+  // slot's launches of the kinds its jobs come from, so the kinds pipeline.
   // Drops the captured graph.
   void set_concurrent(int mode);
   int concurrent() const { return concurrent_; }
   // Jobs split round-robin into this many groups (1..kMaxStreamGroups), each
   // with its own launches per slot and kind, and, in mode 2, its own streams:
   // smaller launches that overlap more.  Rebuilds the schedule.
-  static constexpr int kMaxStreamGroups = 4;
+  static constexpr int kMaxStreamGroups = 4;  // = kPlanGroupsMax (batch_plan.h)
   void set_stream_groups(int groups);
   int stream_groups() const { return groups_; }
   // Grouped launches fetch rows with 3-D tensor copies (default on) or one
@@ -119,8 +118,8 @@ class Batch {
   std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
   cudaEvent_t fork_ = nullptr;
   std::vector<cudaEvent_t> join_;
-  std::vector<cudaStream_t> kst_;   // mode 2: one stream per kind
-  std::vector<cudaEvent_t> kev_;    // ... and its last launch
+  std::vector<cudaStream_t> kst_;   // mode 2: one stream per (kind, group)
+  std::vector<cudaEvent_t> kev_;    // ... one event per (kind, group, slot parity) (plan_event)
   int ckpt_every_;
   JobDesc* d_jobs_ = nullptr;
   GroupOp* d_ops_ = nullptr;

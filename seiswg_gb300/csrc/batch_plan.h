@@ -64,6 +64,160 @@ inline std::vector<HostOp> job_ops(int nt, int k, bool psv, bool two) {
   return L;
 }
 
+// ---------------------------------------------------------------------------
+// Binomial checkpointing (Griewank and Walther, "Algorithm 799: revolve",
+// ACM TOMS 26(1), 2000), restated for a job with S state slots.
+//
+// F(n, s): the fewest forward steps that give the reverse sweep of n steps
+// [a, a+n) every state it reads, starting from S^a (held) with s more free
+// slots.  With r the least number of repetitions such that
+// beta(s+1, r) = C(s+1+r, r) >= n, F(n, s) = r n - beta(s+2, r-1) (n >= 2,
+// s >= 1), F(1, s) = 0 and F(n, 0) = n (n-1) / 2.  The optimum obeys
+// F(n, s) = min over 1 <= m < n of m + F(n-m, s-1) + F(m, s): advance m steps,
+// store S^(a+m), reverse [a+m, a+n) with one slot fewer, then [a, a+m).
+// The recording pass of a gradient runs every step anyway, so the advances
+// along the right spine of that recursion cost nothing: the reverse phase
+// recomputes F(nt, S-1) - (nt - 1) steps.
+// ---------------------------------------------------------------------------
+inline unsigned long long revolve_beta_capped(long long s, long long r, unsigned long long cap) {
+  // C(s + r, r), or cap + 1 once it exceeds cap
+  unsigned long long b = 1;
+  for (long long q = 1; q <= r; ++q) {
+    b = b * (unsigned long long)(s + q) / (unsigned long long)q;  // exact: C(s+q, q) = C(s+q-1, q-1) (s+q) / q
+    if (b > cap) return cap + 1;
+  }
+  return b;
+}
+
+inline long long revolve_cost(long long n, long long s) {
+  if (n <= 1) return 0;
+  if (s <= 0) return n * (n - 1) / 2;
+  long long r = 0;
+  while (revolve_beta_capped(s + 1, r, (unsigned long long)n) < (unsigned long long)n) ++r;
+  return r * n - (long long)revolve_beta_capped(s + 2, r - 1, ~0ull >> 1);
+}
+
+// A split m (1 <= m < n) at which m + F(n-m, s-1) + F(m, s) = F(n, s); the
+// largest such m, which stores the next checkpoint as far ahead as the
+// optimum allows.
+inline int revolve_split(int n, int s) {
+  const long long best = revolve_cost(n, s);
+  for (int m = n - 1; m >= 1; --m)
+    if (m + revolve_cost(n - m, s - 1) + revolve_cost(m, s) == best) return m;
+  return 1;
+}
+
+// The operation list of a job under binomial checkpointing with S >= 1
+// checkpoint slots: slots 0..S-1 (slot 0 holds S^0, the zero state that no
+// step writes), then the working pair S and S+1.  The recording pass stores
+// the states of the recursion's right spine; the reverse phase then walks the
+// recursion, recomputing with one-step operations.  When the free slots run
+// out before the spine reaches step nt-1, the recording pass ends with a
+// one-step operation so that S^(nt-1) stays in a working slot for the first
+// reverse step.  The HostOp vocabulary and slot conventions are those of
+// job_ops; the reverse phase recomputes exactly F(nt, S-1) - (nt - 1) steps.
+inline std::vector<HostOp> job_ops_revolve(int nt, int S, bool psv, bool two) {
+  std::vector<HostOp> L;
+  if (nt <= 0 || S < 1) return L;
+  const int fwd = psv ? kFwdPsv : kFwdSh, adj = psv ? kAdjPsv : kAdjSh, fwd2 = psv ? kFwd2Psv : kFwd2Sh;
+  auto pp = [&](int q) { return S + (q & 1); };
+  // Right spine: node q reverses [a, a+n) from S^a in `slot`, with free
+  // checkpoint slots [lo, S); S^a of node q+1 goes to slot lo of node q.
+  struct Node { int a, n, slot, lo; };
+  std::vector<Node> spine{{0, nt, 0, 1}};
+  while (spine.back().n > 1 && spine.back().lo < S) {
+    const Node t = spine.back();
+    const int m = revolve_split(t.n, S - t.lo);
+    spine.push_back(Node{t.a + m, t.n - m, t.lo, t.lo + 1});
+  }
+  const Node deep = spine.back();
+  const bool keep_last = deep.n > 1;  // no free slot left: keep S^(nt-1) from the recording
+  // Recording pass: steps 0..nt, a step ending on a spine position writes its
+  // slot (two steps per operation where none falls between them).
+  std::vector<int> slot_at(size_t(nt) + 1, -1);
+  for (size_t q = 1; q < spine.size(); ++q) slot_at[size_t(spine[q].a)] = spine[q].slot;
+  int cur = 0, ppi = 0, last_slot = -1;
+  for (int t = 0; t < nt;) {
+    const bool pair = two && t + 1 < nt && slot_at[size_t(t) + 1] < 0 && !(keep_last && t + 2 == nt);
+    const int n = pair ? 2 : 1;
+    const int e = t + n;
+    int dst;
+    if (e < nt && slot_at[size_t(e)] >= 0) {
+      dst = slot_at[size_t(e)];
+    } else {
+      dst = pp(ppi);
+      ppi ^= 1;
+    }
+    if (e == nt - 1) last_slot = dst;
+    L.push_back(HostOp{pair ? fwd2 : fwd, t, cur, dst, 1});
+    cur = dst;
+    t = e;
+  }
+  L.push_back(HostOp{kMisfit, 0, 0, 0, 0});
+  int parity = 0;
+  auto rev = [&](int n, int slot) {
+    L.push_back(HostOp{adj, n, slot, parity, 0});
+    parity ^= 1;
+  };
+  // S^b from S^a in slot src, one step per operation, into slot dst (or, when
+  // dst is a working slot, into whichever working slot the alternation ends
+  // in); returns the slot holding S^b.
+  auto advance = [&](int src, int a, int b, int dst) {
+    int from = src, w = 0;
+    for (int it = a; it < b; ++it) {
+      int to = (it + 1 == b && dst < S) ? dst : pp(w++);
+      if (to == from) to = pp(w++);
+      L.push_back(HostOp{fwd, it, from, to, 0});
+      from = to;
+    }
+    return from;
+  };
+  // Reverse [a, a+n) from S^a in slot sa with free slots [lo, S).
+  struct Frame { int a, n, sa, lo, stage, m; };
+  auto reverse = [&](int a0, int n0, int sa0, int lo0) {
+    std::vector<Frame> fs{{a0, n0, sa0, lo0, 0, 0}};
+    while (!fs.empty()) {
+      const Frame f = fs.back();
+      fs.pop_back();
+      if (f.n == 1) {
+        rev(f.a, f.sa);
+      } else if (f.lo >= S) {  // no free slot: every state from S^a again
+        for (int j = f.a + f.n - 1; j >= f.a; --j) rev(j, j == f.a ? f.sa : advance(f.sa, f.a, j, S));
+      } else if (f.stage == 0) {
+        const int m = revolve_split(f.n, S - f.lo);
+        advance(f.sa, f.a, f.a + m, f.lo);
+        fs.push_back(Frame{f.a, f.n, f.sa, f.lo, 1, m});              // then [a, a+m)
+        fs.push_back(Frame{f.a + m, f.n - m, f.lo, f.lo + 1, 0, 0});  // first [a+m, a+n)
+      } else {
+        fs.push_back(Frame{f.a, f.m, f.sa, f.lo, 0, 0});  // the right part's slot is free again
+      }
+    }
+  };
+  // Deepest spine node first (the recording passed its whole segment), then
+  // each node's left part, whose right part is the next node's segment.
+  if (keep_last) {
+    rev(nt - 1, last_slot);
+    if (deep.n > 1) reverse(deep.a, deep.n - 1, deep.slot, deep.lo);
+  } else {
+    reverse(deep.a, deep.n, deep.slot, deep.lo);
+  }
+  for (size_t q = spine.size() - 1; q-- > 0;) reverse(spine[q].a, spine[q + 1].a - spine[q].a, spine[q].slot, spine[q].lo);
+  return L;
+}
+
+// Launch order 2 (Batch): one stream per (kind, group) and one event per
+// (kind, group, slot parity).  A launch of slot t records the event of its
+// slot's parity; a launch whose jobs come from kind a waits on kind a's event
+// of the other parity, i.e. on slot t-1's launch of kind a, and never on a
+// launch of its own slot (which the kind order may have enqueued before it).
+constexpr int kPlanGroupsMax = 4;
+inline int plan_stream(int kind, int group) { return kind * kPlanGroupsMax + group; }
+inline int plan_event(int kind, int group, int slot) {
+  return (slot & 1) * kKinds * kPlanGroupsMax + plan_stream(kind, group);
+}
+constexpr int kPlanStreams = kKinds * kPlanGroupsMax;
+constexpr int kPlanEvents = 2 * kPlanStreams;
+
 // One grouped launch of a schedule slot: the jobs (in the order of their
 // operations in the launch) whose operation at that slot is of this kind and
 // which belong to this group (job q is in group q % groups), and the kinds of

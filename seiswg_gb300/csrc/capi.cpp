@@ -418,6 +418,17 @@ int32_t seiswg_sim_checkpoint_interval(const seiswg_sim* s) {
   return s && s->sim ? s->sim->checkpoint_interval() : 0;
 }
 
+int seiswg_sim_checkpoint_plan(const seiswg_sim* s, int32_t* slots, int32_t* interval, int64_t* recomputed,
+                               size_t* bytes) {
+  if (!s || !s->sim) return fail(SEISWG_EINVAL, "null simulation handle");
+  if (slots) *slots = s->sim->checkpoint_slots();
+  if (interval) *interval = s->sim->checkpoint_interval();
+  if (recomputed) *recomputed = s->sim->recompute_steps();
+  if (bytes) *bytes = s->sim->checkpoint_bytes();
+  g_last_error.clear();
+  return SEISWG_OK;
+}
+
 int seiswg_sim_set_observed(seiswg_sim* s, const float* obs) {
   return guarded([&] {
     if (!obs) throw std::invalid_argument("null observed traces");
@@ -463,6 +474,13 @@ int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
     else if (k == "tma") sim.set_use_tma(value != 0);
     else if (k == "autotune") sim.autotune(int(value));
     else if (k == "stability_check") sim.set_stability_check(value != 0);
+    else if (k == "checkpoint_slots") {
+      if (value < 0 || value > (1 << 30)) throw std::invalid_argument("checkpoint_slots out of range");
+      sim.set_checkpoint_slots(int(value));
+    } else if (k == "checkpoint_budget_mb") {
+      if (value < 0) throw std::invalid_argument("checkpoint_budget_mb must be >= 0");
+      sim.set_checkpoint_budget(size_t(value) << 20);
+    }
     else if (k == "wait_polls") {
       if (value < 0 || value > 0xffffffffLL) throw std::invalid_argument("wait_polls out of range");
       sim.set_wait_polls(unsigned(value));

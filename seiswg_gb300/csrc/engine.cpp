@@ -2,6 +2,8 @@
 // simulation.  See engine.h.
 #include "engine.h"
 
+#include "batch_plan.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -124,6 +126,7 @@ Sim::~Sim() {
   cudaFree(fwd_store_);
   cudaFree(ck_store_);
   cudaFree(seg_store_);
+  cudaFree(rv_store_);
   cudaFree(adj_store_);
   cudaFree(snap_store_);
   cudaFree(u_tab_);
@@ -1140,20 +1143,86 @@ void Sim::gradient_clear() {
   SW_CUDA(cudaMemsetAsync(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols, 0, 3 * fb, stream_));
 }
 
+// The checkpoint scheme of a forward_op with ckpt_every = 0: uniform
+// checkpoints every second step where the budget holds them (with the
+// forward pass running two steps per launch this recomputes half a forward
+// pass per gradient), else every ceil(sqrt(nt)) steps (one forward pass),
+// else binomial checkpointing with as many slots as the budget holds.
+// Budget: the "checkpoint_budget_mb" option, or half of the free memory plus
+// what the current checkpoints hold.  Returns k > 0 (uniform interval) or
+// -S (binomial, S slots).
 int Sim::default_checkpoint_interval() const {
   const int nt = std::max(d_.nt, 1);
   const int k_sqrt = std::max(1, int(std::ceil(std::sqrt(double(nt)))));
-  // Where HBM allows, checkpoint every second step: with the forward pass
-  // running two steps per launch this recomputes half a forward pass per
-  // gradient instead of a whole one.  Budget: half of the free memory plus
-  // what the current checkpoints hold.
-  size_t free_b = 0, total_b = 0;
-  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return k_sqrt;
   const double state_b = double(nstate()) * double(field_elems_) * sizeof(float);
-  const double budget = 0.5 * double(free_b) + double(ck_bytes_);
+  double budget = double(ck_budget_);
+  if (ck_budget_ == 0) {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return k_sqrt;
+    budget = 0.5 * double(free_b) + double(ck_bytes_);
+  }
   const int k2 = std::min(2, nt);
   if ((double((nt + k2 - 1) / k2) + k2) * state_b <= budget) return k2;
-  return k_sqrt;
+  if ((double((nt + k_sqrt - 1) / k_sqrt) + k_sqrt) * state_b <= budget) return k_sqrt;
+  return -std::max(1, std::min(nt, int(budget / state_b)));
+}
+
+void Sim::free_checkpoints() {
+  for (float** p : {&ck_store_, &seg_store_, &rv_store_}) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  ck_k_ = ck_n_ = rv_slots_ = 0;
+  ck_bytes_ = 0;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+// Binomial checkpointing (job_ops_revolve, batch_plan.h): slots 0..S-1 of
+// rv_store_ (slot 0 the zero state), slots S and S+1 the two state buffers.
+Sim::State Sim::rv_slot(int q) const {
+  const size_t state_elems = size_t(nstate()) * field_elems_;
+  return q < rv_slots_ ? slot_state(rv_store_ + size_t(q) * state_elems) : st_[q - rv_slots_];
+}
+
+void Sim::forward_op_binomial(int isrc, int S) {
+  const int nt = d_.nt;
+  S = std::max(1, std::min(S, std::max(nt, 1)));
+  const size_t state_elems = size_t(nstate()) * field_elems_;
+  if (S != rv_slots_ || !rv_store_) {
+    free_checkpoints();
+    SW_CUDA(cudaMalloc(&rv_store_, size_t(S) * state_elems * sizeof(float)));
+    // Halos stay zero; so does slot 0 (the zero initial state), which no
+    // operation writes.
+    SW_CUDA(cudaMemsetAsync(rv_store_, 0, size_t(S) * state_elems * sizeof(float), stream_));
+    rv_slots_ = S;
+    ck_bytes_ = size_t(S) * state_elems * sizeof(float);
+  }
+  rv_ops_ = job_ops_revolve(nt, S, d_.psv, two_step_);
+  recompute_steps_ = 0;
+  for (const HostOp& o : rv_ops_)
+    if (!(o.flags & 1) && (o.kind == kFwdPsv || o.kind == kFwdSh)) ++recompute_steps_;
+  if (!g_mu_) gradient_clear();
+  InjectList inj = source_injections(isrc);
+  ProbeList pl = probe_list();
+  zero_state();
+  if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
+  int last = -1;
+  const std::string key = "fop/rv/" + std::to_string(inj.n) + "/" + std::to_string(S) + (two_step_ ? "/2" : "");
+  run_loop(key, [&] {
+    for (const HostOp& o : rv_ops_) {
+      if (o.kind == kMisfit) break;
+      if (o.kind == kFwd2Psv || o.kind == kFwd2Sh) enqueue_step2(o.it, rv_slot(o.a), rv_slot(o.b), inj, pl);
+      else enqueue_step_states(o.it, rv_slot(o.a), rv_slot(o.b), inj, pl, false);
+    }
+    enqueue_traces();
+  });
+  for (const HostOp& o : rv_ops_) {
+    if (o.kind == kMisfit) break;
+    last = o.b;
+  }
+  cur_buf_ = last >= S ? last - S : 0;  // the step that ends at nt writes a state buffer
+  ck_isrc_ = isrc;
 }
 
 void Sim::forward_op(int isrc, int ckpt_every) {
@@ -1161,15 +1230,16 @@ void Sim::forward_op(int isrc, int ckpt_every) {
   if (d_.spin) throw std::invalid_argument("the exact adjoint is defined for SH or PSV without spin");
   if (d_.sh && d_.psv) throw std::invalid_argument("the exact adjoint runs one of SH or PSV at a time");
   const int nt = d_.nt;
-  int k = ckpt_every > 0 ? ckpt_every : default_checkpoint_interval();
+  int k = ckpt_every > 0 ? ckpt_every : rv_force_ > 0 ? -rv_force_ : default_checkpoint_interval();
+  if (k < 0) {
+    forward_op_binomial(isrc, -k);
+    return;
+  }
   k = std::max(1, std::min(k, std::max(nt, 1)));
   const int ncp = (nt + k - 1) / k;
   const size_t state_elems = size_t(nstate()) * field_elems_;
-  if (k != ck_k_ || ncp != ck_n_) {
-    cudaFree(ck_store_);
-    cudaFree(seg_store_);
-    ck_store_ = seg_store_ = nullptr;
-    ck_bytes_ = 0;
+  if (k != ck_k_ || ncp != ck_n_ || rv_slots_) {
+    free_checkpoints();
     SW_CUDA(cudaMalloc(&ck_store_, std::max(1, ncp) * state_elems * sizeof(float)));
     SW_CUDA(cudaMalloc(&seg_store_, size_t(k) * state_elems * sizeof(float)));
     // Halos of every stored state stay zero; so does checkpoint 0 (the zero
@@ -1179,9 +1249,8 @@ void Sim::forward_op(int isrc, int ckpt_every) {
     ck_k_ = k;
     ck_n_ = ncp;
     ck_bytes_ = (size_t(ncp) + size_t(k)) * state_elems * sizeof(float);
-    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
-    graphs_.clear();
   }
+  recompute_steps_ = nt - ncp;  // every interval but its checkpoint, once
   if (!g_mu_) gradient_clear();
   InjectList inj = source_injections(isrc);
   ProbeList pl = probe_list();
@@ -1285,6 +1354,43 @@ void Sim::backward_op_device() {
   run_backward();
 }
 
+// One reverse step n: forward state f = S^n, incoming adjoint state a,
+// outgoing o.
+void Sim::enqueue_reverse(int n, const State& f, const State& a, const State& o, const InjectList& src,
+                          const InjectList& rec, const Geom& ga) {
+  InjectList s2 = src, r2 = rec;
+  s2.it = n;
+  r2.it = n;
+  if (d_.psv) {
+    PsvAdjoint p{};
+    p.g = ga;
+    p.vx = f.vx; p.vz = f.vz; p.sxx = f.sxx; p.szz = f.szz; p.sxz = f.sxz;
+    p.wx0 = a.vx; p.wz0 = a.vz; p.bxx0 = a.sxx; p.bzz0 = a.szz; p.bxz0 = a.sxz;
+    p.wx1 = o.vx; p.wz1 = o.vz; p.bxx1 = o.sxx; p.bzz1 = o.szz; p.bxz1 = o.sxz;
+    p.rho = rho_; p.lam = lam_; p.mu = mu_;
+    p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+    p.g_b = g_b_; p.g_lam = g_lam_; p.g_mu = g_mu_;
+    p.src = s2;
+    p.rec = r2;
+    p.err = err_;
+    if (!launch_adjoint_tma(p, f, a)) SW_CUDA(launch_psv_adjoint(p, stream_));
+  } else {
+    ShAdjoint p{};
+    p.g = ga;
+    p.vy = f.vy; p.sxy = f.sxy; p.szy = f.szy;
+    p.w0 = a.vy; p.bxy0 = a.sxy; p.bzy0 = a.szy;
+    p.w1 = o.vy; p.bxy1 = o.sxy; p.bzy1 = o.szy;
+    p.rho = rho_; p.mu = mu_;
+    p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
+    p.g_b = g_b_; p.g_mu = g_mu_;
+    p.src = s2;
+    p.rec = r2;
+    p.err = err_;
+    SW_CUDA(launch_sh_adjoint(p, stream_));
+  }
+  ++launches_;
+}
+
 void Sim::run_backward() {
   const int nt = d_.nt;
   const size_t nrt = size_t(nrec_) * nt;
@@ -1310,6 +1416,24 @@ void Sim::run_backward() {
   const Geom ga = adjoint_geom();
   SW_CUDA(cudaStreamSynchronize(stream_));  // host tables above are released after this call
 
+  if (rv_slots_ > 0) {  // binomial checkpointing: the operation list after the misfit
+    const std::string key = "bop/rv/" + std::to_string(src.n) + "/" + std::to_string(rec.n) + "/" +
+                            std::to_string(rv_slots_) + (two_step_ ? "/2" : "");
+    run_loop(key, [&] {
+      bool after = false;
+      for (const HostOp& o : rv_ops_) {
+        if (o.kind == kMisfit) { after = true; continue; }
+        if (!after) continue;
+        if (o.kind == kFwdPsv || o.kind == kFwdSh) enqueue_step_states(o.it, rv_slot(o.a), rv_slot(o.b), src, none, false);
+        else enqueue_reverse(o.it, rv_slot(o.a), adj[o.b], adj[1 - o.b], src, rec, ga);
+      }
+      SW_CUDA(launch_check_finite(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols, 3 * (d_.nx + 2 * kHaloRows), ld_,
+                                  ld_, err_, kErrNonFiniteGradient, stream_));
+      ++launches_;
+    });
+    return;
+  }
+
   const std::string key = "bop/" + std::to_string(src.n) + "/" + std::to_string(rec.n) + "/" + std::to_string(k);
   run_loop(key, [&] {
     int cur = 0;
@@ -1323,40 +1447,7 @@ void Sim::run_backward() {
       };
       for (int n = n0; n < n1 - 1; ++n) enqueue_step_states(n, fstate(n), fstate(n + 1), src, none, false);
       for (int n = n1 - 1; n >= n0; --n) {
-        const State f = fstate(n);
-        const State& a = adj[cur];
-        const State& o = adj[1 - cur];
-        InjectList s2 = src, r2 = rec;
-        s2.it = n;
-        r2.it = n;
-        if (d_.psv) {
-          PsvAdjoint p{};
-          p.g = ga;
-          p.vx = f.vx; p.vz = f.vz; p.sxx = f.sxx; p.szz = f.szz; p.sxz = f.sxz;
-          p.wx0 = a.vx; p.wz0 = a.vz; p.bxx0 = a.sxx; p.bzz0 = a.szz; p.bxz0 = a.sxz;
-          p.wx1 = o.vx; p.wz1 = o.vz; p.bxx1 = o.sxx; p.bzz1 = o.szz; p.bxz1 = o.sxz;
-          p.rho = rho_; p.lam = lam_; p.mu = mu_;
-          p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
-          p.g_b = g_b_; p.g_lam = g_lam_; p.g_mu = g_mu_;
-          p.src = s2;
-          p.rec = r2;
-          p.err = err_;
-          if (!launch_adjoint_tma(p, f, a)) SW_CUDA(launch_psv_adjoint(p, stream_));
-        } else {
-          ShAdjoint p{};
-          p.g = ga;
-          p.vy = f.vy; p.sxy = f.sxy; p.szy = f.szy;
-          p.w0 = a.vy; p.bxy0 = a.sxy; p.bzy0 = a.szy;
-          p.w1 = o.vy; p.bxy1 = o.sxy; p.bzy1 = o.szy;
-          p.rho = rho_; p.mu = mu_;
-          p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
-          p.g_b = g_b_; p.g_mu = g_mu_;
-          p.src = s2;
-          p.rec = r2;
-          p.err = err_;
-          SW_CUDA(launch_sh_adjoint(p, stream_));
-        }
-        ++launches_;
+        enqueue_reverse(n, fstate(n), adj[cur], adj[1 - cur], src, rec, ga);
         cur ^= 1;
       }
     }
@@ -1371,11 +1462,11 @@ void Sim::release_workspace() {
   SW_CUDA(cudaStreamSynchronize(stream_));
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
-  for (float** p : {&ck_store_, &seg_store_, &adj_store_, &fwd_store_, &snap_store_}) {
+  for (float** p : {&ck_store_, &seg_store_, &rv_store_, &adj_store_, &fwd_store_, &snap_store_}) {
     cudaFree(*p);
     *p = nullptr;
   }
-  ck_k_ = ck_n_ = 0;
+  ck_k_ = ck_n_ = rv_slots_ = 0;
   ck_isrc_ = -2;
   ck_bytes_ = 0;
   fwd_nsa_ = 0;

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "batch_plan.h"
 #include "fd_kernels.h"
 
 namespace seiswg {
@@ -150,6 +151,16 @@ class Sim {
   // which: 0 lambda, 1 mu, 2 buoyancy
   void download_gradient(int which, float* host) const;
   int checkpoint_interval() const { return ck_k_; }
+  // Binomial checkpointing slots of the last forward_op (0: uniform
+  // checkpoints every checkpoint_interval() steps), the forward steps its
+  // reverse sweep recomputes, and the bytes its checkpoints hold.
+  int checkpoint_slots() const { return rv_slots_; }
+  long long recompute_steps() const { return recompute_steps_; }
+  // Options of the checkpoint scheme: binomial checkpointing with S slots
+  // (0: the default choice), and the memory the default choice may use for
+  // checkpoints (0: half of the free HBM).
+  void set_checkpoint_slots(int S) { rv_force_ = S > 0 ? S : 0; }
+  void set_checkpoint_budget(size_t bytes) { ck_budget_ = bytes; }
   // Frees the checkpoint, interval, adjoint and snapshot buffers (they are
   // allocated again on the next use); gradients are kept.
   void release_workspace();
@@ -324,6 +335,17 @@ class Sim {
   bool u_ready_ = false;        // u_tab_ holds the adjoint source of the last forward_op
   void run_backward();
   void ensure_u_tab();
+  void enqueue_reverse(int n, const State& f, const State& a, const State& o, const InjectList& src,
+                       const InjectList& rec, const Geom& ga);
+  // binomial checkpointing (batch_plan.h job_ops_revolve)
+  int rv_slots_ = 0, rv_force_ = 0;
+  size_t ck_budget_ = 0;
+  long long recompute_steps_ = 0;
+  float* rv_store_ = nullptr;              // rv_slots_ states
+  std::vector<HostOp> rv_ops_;
+  State rv_slot(int q) const;
+  void forward_op_binomial(int isrc, int S);
+  void free_checkpoints();
 
   bool use_graphs_ = true;
   std::map<std::string, cudaGraphExec_t> graphs_;

@@ -198,7 +198,9 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
   // sigma^n rings, rows i-2..i+1
   f4 xx0 = ld4(at(p.sxx0, i0 - 2)), xx1 = ld4(at(p.sxx0, i0 - 1)), xx2 = ld4(at(p.sxx0, i0)), xx3;
   f4 xz0 = ld4(at(p.sxz0, i0 - 2)), xz1 = ld4(at(p.sxz0, i0 - 1)), xz2 = ld4(at(p.sxz0, i0)), xz3;
-  f4 zz0 = ld4(at(p.szz0, i0 - 2)), zz1 = ld4(at(p.szz0, i0 - 1)), zz2 = ld4(at(p.szz0, i0)), zz3;
+  // sigma_zz^n: row i (zz2, for the z difference); row i-2, which the stress
+  // update adds to, is read from the stage kept three iterations back.
+  f4 zz2 = ld4(at(p.szz0, i0)), zz3;
   const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
   f4 xa = z4, xb_ = z4, xc = z4, xd = z4, za = z4, zb_ = z4, zc = z4, zd = z4;  // level-1 v rows i-3..i
   f4 sx0 = z4, sx1 = z4, sx2 = z4, sx3 = z4;    // level-1 sxx rows i-5..i-2
@@ -272,7 +274,7 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     if (k >= 3) {
       const int r = i - 2;
       const float rx = (!EDGE || (r >= 1 && r < nx - 2)) ? sxr : 0.0f;
-      stress(xa, xb_, xc, xd, za, zb_, zc, zd, rx, rzf, lam, mu, xx0, zz0, xz0, sx3, sz3, sq3);
+      stress(xa, xb_, xc, xd, za, zb_, zc, zd, rx, rzf, lam, mu, xx0, rows.seg_back(P2_SZZ, 3), xz0, sx3, sz3, sq3);
       const bool row_ok = (r >= 0 && r < nx);
       if (EDGE && (!row_ok || cols_out)) {
         sx3 = in_grid(sx3, row_ok, valid);
@@ -324,7 +326,7 @@ __device__ __forceinline__ void psv2_body(const PsvStep& p, const March& m, cons
     za = zb_; zb_ = zc; zc = zd;
     xx0 = xx1; xx1 = xx2; xx2 = xx3;
     xz0 = xz1; xz1 = xz2; xz2 = xz3;
-    zz0 = zz1; zz1 = zz2; zz2 = zz3;
+    zz2 = zz3;
   }
 }
 
@@ -418,7 +420,9 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
   const float sxr = g.rdx, szr = g.rdz;
   // sigma^n rings, rows i-2..i+1
   f4 xy0 = ld4(at(p.sxy0, i0 - 2)), xy1 = ld4(at(p.sxy0, i0 - 1)), xy2 = ld4(at(p.sxy0, i0)), xy3;
-  f4 zy0 = ld4(at(p.szy0, i0 - 2)), zy1 = ld4(at(p.szy0, i0 - 1)), zy2 = ld4(at(p.szy0, i0)), zy3;
+  // sigma_zy^n: row i (zy2, for the z difference); row i-2, which the stress
+  // update adds to, is read from the stage kept three iterations back.
+  f4 zy2 = ld4(at(p.szy0, i0)), zy3;
   const f4 z4 = {{0.0f, 0.0f, 0.0f, 0.0f}};
   f4 va = z4, vb = z4, vc = z4, vd = z4;        // level-1 vy rows i-3..i
   f4 sx0 = z4, sx1 = z4, sx2 = z4, sx3 = z4;    // level-1 sxy rows i-5..i-2
@@ -478,6 +482,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
       const int r = i - 2;
       const float rx = (r >= 1 && r < nx - 2) ? sxr : 0.0f;
       const f4 gx = d4_rows(va, vb, vc, vd), gz = d4_cols_fwd(vb);
+      const f4 zy0 = rows.seg_back(S2_SZY, 3);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         sx3.v[e] = fmaf(mu.v[e], gx.v[e] * rx, xy0.v[e]);
@@ -529,7 +534,7 @@ __device__ __forceinline__ void sh2_body(const ShStep& p, const March& m, const 
     sz0 = sz1; sz1 = sz2; sz2 = sz3;
     va = vb; vb = vc; vc = vd;
     xy0 = xy1; xy1 = xy2; xy2 = xy3;
-    zy0 = zy1; zy1 = zy2; zy2 = zy3;
+    zy2 = zy3;
   }
 }
 

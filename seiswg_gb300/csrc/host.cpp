@@ -14,6 +14,7 @@
 #include <list>
 #include <sstream>
 #include <system_error>
+#include <limits>
 #include <thread>
 
 namespace seiswg {
@@ -389,23 +390,25 @@ bool grid_from_layout(const ModelData& x, const ModelData& z, GridInfo& g) {
 
 }  // namespace
 
-// max - min of n > 0 floats.  Every partial minimum and maximum starts from
-// v[0] and takes an element only when it compares below / above, as
-// std::min / std::max do, so the result is that of one pass in order (NaN
-// elements are passed over; a NaN v[0] gives NaN).  Coordinate files of large
-// grids (4096 x 4096: 64 MB each) are scanned by up to 16 threads over
-// contiguous parts, each in 16 independent lanes that the compiler
-// vectorises.
+// max - min of n > 0 floats, as the reference folds them (solver.rs:647-650:
+// f32::max from -infinity, f32::min from +infinity): NaN elements are passed
+// over wherever they are, the first included.  Every partial minimum and
+// maximum starts from +/-infinity and takes an element only when it compares
+// below / above, which a NaN never does.  Coordinate files of large grids
+// (4096 x 4096: 64 MB each) are scanned by up to 16 threads over contiguous
+// parts, each in 16 independent lanes that the compiler vectorises.
 namespace {
 float extent_of(const float* v, size_t n) {
   struct MinMax {
     float lo, hi;
   };
-  const float v0 = v[0];
-  auto scan = [v0](const float* p, size_t m) {
+  auto scan = [](const float* p, size_t m) {
     constexpr int W = 16;
     float lo[W], hi[W];
-    for (int q = 0; q < W; ++q) lo[q] = hi[q] = v0;
+    for (int q = 0; q < W; ++q) {
+      lo[q] = std::numeric_limits<float>::infinity();
+      hi[q] = -std::numeric_limits<float>::infinity();
+    }
     const size_t mw = m / W * W;
     for (size_t k = 0; k < mw; k += W)
       for (int q = 0; q < W; ++q) {
@@ -489,6 +492,16 @@ GridInfo infer_grid(const ModelData& x, const ModelData& z) {
   // Rectangular cells (dx != dz), where the aspect-ratio rule cannot work:
   // the grid read from the coordinate layout.
   if (have_layout) return lay;
+  // Otherwise the reference's result wherever it tiles npt, as the reference
+  // itself takes it without looking at the layout (coordinates stored z
+  // first, or x values that differ by rounding within a column).
+  if (g.nx >= 2 && g.nz >= 2 && size_t(g.nx) * size_t(g.nz) == x.size()) {
+    log_info("grid inferred from the coordinate extents (" + std::to_string(g.nx) + " x " + std::to_string(g.nz) +
+             "); the coordinates do not follow the layout k = i*nz + j exactly");
+    g.dx = lx / float(g.nx - 1);
+    g.dz = lz / float(g.nz - 1);
+    return g;
+  }
   throw Error("cannot infer a rectangular grid from the coordinates (nx=" + std::to_string(g.nx) +
               ", nz=" + std::to_string(g.nz) + ", npt=" + std::to_string(x.size()) + ")");
 }

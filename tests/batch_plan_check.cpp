@@ -14,13 +14,22 @@
 //
 // Then the launch plan of random mixes of jobs (plan_launches) is replayed
 // under launch order 2 of Batch: one stream per (kind, group), each launch
-// waiting for the events of the kinds in its dependency mask, each launch
-// recording its own stream's event.  Vector clocks over the streams give the
-// happens-before order; every job's operation at slot t must come after its
-// operation at slot t-1.  A dependency mask with a bit removed must be
+// waiting for the previous slot's events of the kinds in its dependency mask
+// (plan_event, one event per kind, group and slot parity), each launch
+// recording its own event of its slot's parity.  Vector clocks over the
+// streams give the happens-before order; every job's operation at slot t must
+// come after its operation at slot t-1, and every wait must find an event
+// recorded by a launch of slot t-1 (not of slot t, which would serialise
+// launches of the same slot).  A dependency mask with a bit removed must be
 // reported.
-// Prints "ok <cases> <mixes>" and exits 0, or prints the first violation and
-// exits 1.
+// Binomial checkpointing (job_ops_revolve): the closed-form cost F(n, s) is
+// checked against a brute-force minimisation of its recursion for n <= 60,
+// s <= 6; the operation lists for many step counts and slot counts are
+// replayed on S + 2 slots (every reverse step finds its state, recomputation
+// reads the state of its step, slot 0 keeps the zero state), and the steps
+// recomputed must equal F(nt, S-1) - (nt - 1) exactly.
+// Prints "ok <cases> <mixes> <revolve cases>" and exits 0, or prints the
+// first violation and exits 1.
 #include <array>
 #include <cstdint>
 #include <cstdio>
@@ -88,6 +97,94 @@ static int replay(int nt, int k, bool psv, bool two, const std::vector<HostOp>& 
 static int check(int nt, int k, bool psv, bool two) { return replay(nt, k, psv, two, job_ops(nt, k, psv, two)); }
 
 // Each planted mistake must be reported.
+// Replays a binomial schedule on S + 2 slots; *recomputed = forward steps of
+// the reverse phase.
+static int replay_revolve(int nt, int S, bool psv, bool two, const std::vector<HostOp>& L, long long* recomputed) {
+  const int nslot = S + 2;
+  std::vector<int> slot(nslot, -1);
+  slot[0] = 0;
+  const int fwd = psv ? kFwdPsv : kFwdSh, fwd2 = psv ? kFwd2Psv : kFwd2Sh, adj = psv ? kAdjPsv : kAdjSh;
+  int rec = 0, rev = nt - 1, parity = 0;
+  bool misfit = false;
+  *recomputed = 0;
+  for (size_t q = 0; q < L.size(); ++q) {
+    const HostOp& o = L[q];
+    if (o.a < 0 || o.a >= nslot) return fail(nt, S, two, q, "revolve: source slot out of range");
+    if (o.kind == fwd || o.kind == fwd2) {
+      const int n = o.kind == fwd2 ? 2 : 1;
+      if (o.b < 1 || o.b >= nslot) return fail(nt, S, two, q, "revolve: destination out of range (or slot 0)");
+      if (o.a == o.b) return fail(nt, S, two, q, "revolve: a step reads and writes the same slot");
+      if (slot[o.a] != o.it) return fail(nt, S, two, q, "revolve: forward step does not find its state");
+      if (!misfit) {
+        if (o.it != rec || !(o.flags & 1)) return fail(nt, S, two, q, "revolve: recording out of order");
+        rec += n;
+      } else {
+        if (o.kind != fwd || (o.flags & 1)) return fail(nt, S, two, q, "revolve: recomputation not one plain step");
+        *recomputed += 1;
+      }
+      slot[o.b] = o.it + n;
+    } else if (o.kind == kMisfit) {
+      if (misfit || rec != nt) return fail(nt, S, two, q, "revolve: misfit before the end of the recording");
+      misfit = true;
+    } else if (o.kind == adj) {
+      if (!misfit || o.it != rev) return fail(nt, S, two, q, "revolve: reverse steps out of order");
+      if (slot[o.a] != o.it) return fail(nt, S, two, q, "revolve: reverse step does not find its state");
+      if (o.b != parity) return fail(nt, S, two, q, "revolve: adjoint slots do not alternate");
+      parity ^= 1;
+      --rev;
+    } else {
+      return fail(nt, S, two, q, "revolve: unexpected kind");
+    }
+  }
+  if (!misfit || rev != -1) return fail(nt, S, two, L.size(), "revolve: reverse sweep incomplete");
+  return 0;
+}
+
+static long long brute_cost(int n, int s, std::vector<std::vector<long long>>& memo) {
+  if (n <= 1) return 0;
+  if (s == 0) return (long long)n * (n - 1) / 2;
+  long long& m = memo[size_t(n)][size_t(s)];
+  if (m >= 0) return m;
+  long long best = -1;
+  for (int k = 1; k < n; ++k) {
+    const long long c = k + brute_cost(n - k, s - 1, memo) + brute_cost(k, s, memo);
+    if (best < 0 || c < best) best = c;
+  }
+  return m = best;
+}
+
+static int check_revolve(int& cases) {
+  std::vector<std::vector<long long>> memo(61, std::vector<long long>(7, -1));
+  for (int n = 1; n <= 60; ++n)
+    for (int sl = 0; sl <= 6; ++sl)
+      if (brute_cost(n, sl, memo) != revolve_cost(n, sl)) {
+        std::printf("revolve_cost(%d, %d) = %lld, the recursion gives %lld\n", n, sl, revolve_cost(n, sl),
+                    brute_cost(n, sl, memo));
+        return 1;
+      }
+  auto one = [&](int nt, int S, bool two) {
+    long long rc = 0;
+    if (replay_revolve(nt, S, true, two, job_ops_revolve(nt, S, true, two), &rc)) return 1;
+    const long long want = revolve_cost(nt, S - 1) - (nt - 1);
+    if (rc != want) {
+      std::printf("revolve nt=%d S=%d two=%d: %lld steps recomputed, the optimum is %lld\n", nt, S, int(two), rc,
+                  want);
+      return 1;
+    }
+    ++cases;
+    return 0;
+  };
+  for (int nt = 1; nt <= 120; ++nt)
+    for (int S = 1; S <= 12; ++S)
+      for (int two = 0; two < 2; ++two)
+        if (one(nt, S, two != 0)) return 1;
+  for (int nt : {1000, 3000, 4000})
+    for (int S : {2, 3, 10, 40, 56, 110, 1502})
+      for (int two = 0; two < 2; ++two)
+        if (one(nt, S, two != 0)) return 1;
+  return 0;
+}
+
 static bool catches_planted_mistakes() {
   const int nt = 23, k = 5;
   quiet = true;
@@ -118,7 +215,7 @@ static bool catches_planted_mistakes() {
 // are ordered from slot to slot.  `drop`: clear this dependency bit of the
 // first launch that has it (a planted mistake), -1 for none.
 static bool order2_holds(const std::vector<std::vector<HostOp>>& lists, int groups, int drop) {
-  constexpr int kGroupsMax = 4, kStreams = kKinds * kGroupsMax;
+  constexpr int kStreams = kPlanStreams;
   using Clock = std::array<int, kStreams>;
   auto plan = plan_launches(lists, groups);
   if (drop >= 0) {
@@ -132,18 +229,24 @@ static bool order2_holds(const std::vector<std::vector<HostOp>>& lists, int grou
     if (!done) return true;  // nothing to plant: the self-check fails
   }
   Clock zero{};
-  std::vector<Clock> stream(kStreams, zero), event(kStreams, zero);
+  std::vector<Clock> stream(kStreams, zero), event(kPlanEvents, zero);
+  std::vector<int> event_slot(kPlanEvents, -1);  // slot of the launch that last recorded the event
   std::array<int, kStreams> seq{};
   // where[q] = (stream, seq) of the launch holding job q's previous operation
   std::vector<std::pair<int, int>> where(lists.size(), {-1, 0});
   for (size_t t = 0; t < plan.size(); ++t) {
     std::vector<std::pair<int, int>> now(lists.size(), {-1, 0});
     for (const PlanLaunch& l : plan[t]) {
-      const int s = l.kind * kGroupsMax + l.group;
+      const int s = plan_stream(l.kind, l.group);
       Clock c = stream[s];
       for (int a = 0; a < kKinds; ++a)
         if ((l.deps >> a) & 1) {
-          const Clock& e = event[a * kGroupsMax + l.group];
+          const int ev = plan_event(a, l.group, int(t) - 1);
+          if (event_slot[ev] != int(t) - 1) {
+            if (!quiet) std::printf("slot %zu: a launch waits on an event not recorded at slot %zu\n", t, t - 1);
+            return false;
+          }
+          const Clock& e = event[ev];
           for (int x = 0; x < kStreams; ++x) c[x] = c[x] > e[x] ? c[x] : e[x];
         }
       c[s] = ++seq[s];
@@ -153,7 +256,8 @@ static bool order2_holds(const std::vector<std::vector<HostOp>>& lists, int grou
         now[q] = {s, c[s]};
       }
       stream[s] = c;
-      event[s] = c;
+      event[plan_event(l.kind, l.group, int(t))] = c;
+      event_slot[plan_event(l.kind, l.group, int(t))] = int(t);
     }
     for (size_t q = 0; q < lists.size(); ++q)
       if (now[q].first >= 0) where[q] = now[q];
@@ -184,11 +288,13 @@ static int check_orders(int& mixes) {
   // Planted: removing one needed dependency bit must break the order for a
   // mix where a job changes kind (recomputation to reverse steps).
   std::vector<std::vector<HostOp>> lists = {job_ops(30, 6, true, true), job_ops(17, 4, false, false)};
+  quiet = true;
   for (int a : {kFwdPsv, kFwdSh, kFwd2Psv, kAdjPsv, kMisfit})
     if (order2_holds(lists, 1, a)) {
       std::printf("the order check misses a dropped dependency on kind %d\n", a);
       return 1;
     }
+  quiet = false;
   return 0;
 }
 
@@ -215,6 +321,8 @@ int main() {
       }
   int mixes = 0;
   if (check_orders(mixes)) return 1;
-  std::printf("ok %d %d\n", cases, mixes);
+  int rcases = 0;
+  if (check_revolve(rcases)) return 1;
+  std::printf("ok %d %d %d\n", cases, mixes, rcases);
   return 0;
 }

@@ -314,3 +314,74 @@ def test_reverse_step_tensor_copies_give_the_same_gradient():
             assert np.array_equal(g[0][p], g[1][p]), p
     finally:
         sim.close()
+
+
+def _revolve_cost(n, s):
+    """F(n, s) of binomial checkpointing (Griewank and Walther's revolve):
+    forward steps that reverse n steps from the first state with s more
+    free slots."""
+    from math import comb
+
+    if n <= 1:
+        return 0
+    if s <= 0:
+        return n * (n - 1) // 2
+    r = 0
+    while comb(s + 1 + r, r) < n:
+        r += 1
+    return r * n - comb(s + 1 + r, r - 1)
+
+
+@pytest.mark.parametrize("phys", ["psv", "sh"])
+def test_binomial_checkpointing_gives_the_uniform_gradient(phys):
+    """With one-step recording every stored or recomputed state is the same
+    bits whatever the schedule, so binomial checkpointing with any number of
+    slots gives the gradient of uniform checkpoints bit for bit, recomputing
+    exactly F(nt, S-1) - (nt - 1) steps.  With the default two-step recording
+    the states differ by rounding only."""
+    vp, vs, rho, flags, src, rec = _problem(phys, 3)
+    obs = _observed(vp, vs, rho, flags, src, rec, -1)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    sim.set_option("two_step", 0)
+    ref = _gpu_gradient(sim, flags, obs, -1, 1)[2]
+    params = ("lambda", "mu", "buoyancy") if phys == "psv" else ("mu", "buoyancy")
+    for S in (1, 2, 3, 7, 40, NT):
+        sim.set_option("checkpoint_slots", S)
+        g = _gpu_gradient(sim, flags, obs, -1, 0)[2]
+        plan = sim.checkpoint_plan()
+        assert plan["slots"] == S and plan["interval"] == 0
+        assert plan["recomputed"] == _revolve_cost(NT, S - 1) - (NT - 1), (S, plan)
+        for p in params:
+            assert np.array_equal(g[p], ref[p]), (S, p)
+    sim.set_option("two_step", 1)
+    for S in (2, 13):
+        sim.set_option("checkpoint_slots", S)
+        g = _gpu_gradient(sim, flags, obs, -1, 0)[2]
+        for p in params:
+            assert rel_l2(g[p], ref[p]) <= 1e-5, (S, p)
+    sim.close()
+
+
+def test_checkpoint_budget_selects_the_scheme():
+    """The default scheme under a memory budget: every second step where it
+    fits, every ceil(sqrt(nt)) steps where that fits, else binomial
+    checkpointing with as many states as fit (the same gradient)."""
+    vp, vs, rho, flags, src, rec = _problem("psv", 4)
+    obs = _observed(vp, vs, rho, flags, src, rec, 0)
+    sim, _ = _sim(vp, vs, rho, flags, src, rec)
+    ref = _gpu_gradient(sim, flags, obs, 0, 1)[2]
+    g0 = _gpu_gradient(sim, flags, obs, 0, 0)[2]
+    plan = sim.checkpoint_plan()
+    assert plan["interval"] == 2 and plan["slots"] == 0     # the test grid fits every second step
+    state = plan["bytes"] / (NT // 2 + 2)
+    for states, want in ((40, "sqrt"), (12, "binomial")):
+        sim.set_option("checkpoint_budget_mb", max(1, int(states * state) >> 20))
+        g = _gpu_gradient(sim, flags, obs, 0, 0)[2]
+        plan = sim.checkpoint_plan()
+        if want == "sqrt":
+            assert plan["interval"] == int(np.ceil(np.sqrt(NT))) and plan["slots"] == 0, plan
+        else:
+            assert plan["slots"] >= 1 and plan["interval"] == 0 and plan["bytes"] <= states * state, plan
+        for p in ("lambda", "mu", "buoyancy"):
+            assert rel_l2(g[p], ref[p]) <= 1e-5 and rel_l2(g0[p], ref[p]) <= 1e-5
+    sim.close()

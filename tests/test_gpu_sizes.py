@@ -108,7 +108,7 @@ def test_c4_full_grid_gradient():
     J, adj = sw.l2_misfit(syn, obs, w.dt)
     sim.backward_op(adj)
     g = {p: sim.gradient(p) for p in ("lambda", "mu", "buoyancy")}
-    ck = sim.checkpoint_interval()
+    ck = sim.checkpoint_interval
     sim.close()
     assert J > 0 and ck >= 1
 

@@ -177,14 +177,27 @@ def test_infer_grid_matches_oracle():
     zl = np.tile(np.float32(77.25) + np.arange(2048, dtype=np.float32) * np.float32(12.5), 2048)
     assert sw.infer_grid(xl, zl) == O.infer_grid(xl, zl)
     assert sw.infer_grid(xl, zl)[:2] == (2048, 2048)
-    # extents as one in-order min/max pass: a NaN inside any thread's part is
-    # passed over, a NaN first element makes the extent NaN (an error)
+    # extents as the reference folds them (f32::max / f32::min from
+    # -/+infinity): a NaN anywhere is passed over, the first element included
     zn = zl.copy()
     zn[zn.size * 5 // 7] = np.nan
     assert sw.infer_grid(xl, zn) == sw.infer_grid(xl, zl)
     zn[0] = np.nan
+    assert sw.infer_grid(xl, zn) == sw.infer_grid(xl, zl)
+    xn = xl.copy()
+    xn[0] = np.nan            # the smallest x, also held by the rest of the first column
+    assert sw.infer_grid(xn, zl) == O.infer_grid(xn, zl)
     with pytest.raises(sw.SeiswgError):
-        sw.infer_grid(xl, zn)
+        sw.infer_grid(np.full(16, np.nan, np.float32), zl[:16])
+    # square cells that the layout check cannot read, which the reference
+    # accepts by its aspect-ratio rule: coordinates stored z first, and x
+    # values jittered by rounding within a column
+    xz = np.tile(np.arange(30, dtype=np.float32) * 7.0, 50)
+    zz = np.repeat(np.arange(50, dtype=np.float32) * 7.0, 30)
+    assert sw.infer_grid(xz, zz) == O.infer_grid(xz, zz) == (30, 50, 7.0, 7.0)
+    xj = x + (np.random.default_rng(1).random(x.size).astype(np.float32) - 0.5) * np.float32(1e-3)
+    xj[0], xj[-1] = x[0], x[-1]
+    assert sw.infer_grid(xj, z) == O.infer_grid(xj, z)
     # coordinates that form no grid: errors
     with pytest.raises(sw.SeiswgError) as e:
         sw.infer_grid(x, np.random.default_rng(0).random(x.size).astype(np.float32) * 100)

@@ -12,12 +12,12 @@ from tests.examples import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def _unsmoothed_and_smoothed_kernel(sigma):
+def _unsmoothed_and_smoothed_kernel(sigma, nx, nz):
     """kmu of a two-shot reference adjoint before and after
     seiswg_sim_kernel_smooth (the allocating path)."""
     import seiswg_gb300 as sw
 
-    nx, nz, nt, dx, dt, adj = 64, 150, 200, 10.0, 1.5e-3, 10
+    nt, dx, dt, adj = 200, 10.0, 1.5e-3, 10
     src_i, src_j = np.array([20, 44], np.int32), np.array([20, 20], np.int32)
     rec_i, rec_j = np.arange(5, 60, 6, dtype=np.int32), np.full(10, 30, np.int32)
     stf = np.stack([sw.ricker(nt, dt, 20.0, 0.05, 0.0, 1.0e10)] * 2, axis=1)
@@ -43,14 +43,20 @@ def _unsmoothed_and_smoothed_kernel(sigma):
     return k0, k1
 
 
-def test_smooth_noalloc_matches_allocating_path_twice():
+# (nx, nz, sigma): a tall grid with radius 8 sigma = 40 inside both axes;
+# nx > nz with the radius clamped to max(nx, nz) - 1 = 89 (8 sigma = 160) and
+# normaliser tables of different lengths
+CASES = [(64, 150, 5.0), (90, 40, 20.0)]
+
+
+@pytest.mark.parametrize("nx,nz,sigma", CASES)
+def test_smooth_noalloc_matches_allocating_path_twice(nx, nz, sigma):
     torch = pytest.importorskip("torch")
     import seiswg_gb300 as sw
 
-    sigma = 5.0
-    k0, k1 = _unsmoothed_and_smoothed_kernel(sigma)
+    k0, k1 = _unsmoothed_and_smoothed_kernel(sigma, nx, nz)
     assert np.abs(k0).max() > 0 and not np.allclose(k0, k1)
-    nx, nz = k0.shape
+    assert k0.shape == (nx, nz)
     x = torch.from_numpy(np.ascontiguousarray(k0)).cuda()
     y = torch.empty_like(x)
     stream = torch.cuda.current_stream()
