@@ -534,6 +534,10 @@ def run_secondary(args):
         sim = W.make_sim()
         if args.tma >= 0:
             sim.set_option("tma", args.tma)
+        if args.checkpoint_slots:
+            sim.set_option("checkpoint_slots", args.checkpoint_slots)
+        if args.checkpoint_budget_mb:
+            sim.set_option("checkpoint_budget_mb", args.checkpoint_budget_mb)
         stream = torch.cuda.ExternalStream(sim.stream)
         Js = []
 
@@ -571,6 +575,11 @@ def run_secondary(args):
                    higher_is_better=True, wall_s_per_gradient=wall,
                    gcell_updates_per_s=cell_updates / (ms / 1e3) / 1e9,
                    config={"workload": W.name, "checkpoint_interval": sim.checkpoint_interval,
+                           "checkpoint_plan": {**sim.checkpoint_plan(),
+                                               "scheme": "binomial (revolve)" if sim.checkpoint_plan()["slots"]
+                                               else "uniform",
+                                               "recomputed_per_shot_of_nt": sim.checkpoint_plan()["recomputed"] / W.nt,
+                                               "budget_mb": args.checkpoint_budget_mb or None},
                            "misfit": "L2 waveform, ux+uz, " + ("host" if args.host_misfit else "on the device"),
                            "J_per_shot": list(Js),
                            "receivers": int(W.rec_i.size), "shots": nshot},
@@ -693,6 +702,8 @@ def run_secondary(args):
             batch.set_option("stream_groups", args.stream_groups)
         if args.tma >= 0:
             batch.set_option("tma", args.tma)
+        if args.checkpoint_slots:
+            batch.set_option("checkpoint_slots", args.checkpoint_slots)
         tune_ms = None
         if args.autotune:
             t0 = time.perf_counter()
@@ -725,7 +736,10 @@ def run_secondary(args):
                    config={"workload": f"c5: {len(problems)} problems, 256..1536 per axis, nt 1000..3000, SH/PSV, "
                                        "1-4 shots",
                            "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
-                           "device_bytes": info["device_bytes"], "checkpoints": "ceil(sqrt(nt)) per job",
+                           "device_bytes": info["device_bytes"],
+                           "checkpoints": (f"binomial (revolve), {info['checkpoint_slots']} states per job"
+                                           if info["checkpoint_slots"] else "ceil(sqrt(nt)) per job"),
+                           "recomputed_steps_per_run": info["recomputed_steps"],
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
                            "concurrent": info.get("concurrent"), "stream_groups": info.get("stream_groups"),
                            "tma_jobs": info.get("tma_jobs"), "autotune_ms": tune_ms},
@@ -775,6 +789,10 @@ def main():
                     help="c5: launch order: 0 serial, 1 a slot's kinds on forked streams, 2 one stream per kind "
                          "(-1: the default, 2)")
     ap.add_argument("--fd-check", type=int, default=0, help="c4: finite-difference check on this many cells")
+    ap.add_argument("--checkpoint-slots", type=int, default=0,
+                    help="c4, c5: binomial checkpointing with this many stored states (per shot / per job)")
+    ap.add_argument("--checkpoint-budget-mb", type=int, default=0,
+                    help="c4: the memory the default checkpoint choice may use (binomial below sqrt(nt) states)")
     ap.add_argument("--host-misfit", action="store_true", help="c4: misfit and adjoint source on the host")
     ap.add_argument("--fd-h", type=float, default=1e-3, help="c4: relative vp step of the finite differences")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],

@@ -13,6 +13,7 @@
  *   Solver::new             (src/solver.rs:578)   seiswg_solver_new
  *   Solver::run_forward     (src/solver.rs:941)   seiswg_solver_run_forward
  *   Solver::run_adjoint     (src/solver.rs:1298)  seiswg_solver_run_adjoint
+ *   mode = inversion        (src/main.rs:93-94, planned)  seiswg_solver_run_inversion
  *   fields/idata/obs/stf bindings and the per-step kernel chain
  *     (shaders/fd2d.wgsl:123-127, src/solver.rs:984-1044)   seiswg_sim_*
  *   ricker                  (src/solver.rs:350)   seiswg_ricker
@@ -89,6 +90,18 @@ int seiswg_solver_run_forward(seiswg_solver* s, seiswg_vfs* out);
 /* Solver::run_adjoint: observed uy traces from `vfs` (or disk); writes
  * proc000000_kmu.bin and gradient_kmu.bin into `out`. */
 int seiswg_solver_run_adjoint(seiswg_solver* s, const seiswg_vfs* vfs, seiswg_vfs* out);
+/* `[workflow] mode = inversion`, which the reference lists as planned
+ * (README.md:61) and rejects (src/main.rs:93-94): steepest descent from the
+ * initial model ([path] model_init) toward the observed traces ([path]
+ * traces: uy_NNNNNN.npy for SH, ux_ and uz_NNNNNN.npy for PSV, one per shot),
+ * each gradient the exact discrete adjoint summed over the shots and smoothed,
+ * with a backtracking line search.  New keys, which the reference ignores,
+ * under [inversion]: iterations (5), parameters ("vp,vs"; of vp, vs, rho),
+ * step (0.02, the first relative model change), max_step (0.1),
+ * line_search_trials (6), smooth (gradient smoothing sigma in cells; default
+ * [solver] smooth).  Writes proc000000_{vp,vs,rho,x,z}.bin and
+ * inversion_misfit.txt to [path] output.  SH or PSV alone. */
+int seiswg_solver_run_inversion(seiswg_solver* s, const seiswg_vfs* vfs, seiswg_vfs* out);
 int seiswg_solver_info(const seiswg_solver* s, int32_t* nx, int32_t* nz, float* dx, float* dz, int32_t* nsrc,
                        int32_t* nrec);
 /* Total waveform misfit of the last run_adjoint (solver.rs:1503). */
@@ -255,9 +268,15 @@ int seiswg_batch_run(seiswg_batch* batch);
  * groups with their own launches (and streams in order 2); "tma" (0/1,
  * default 1): the grouped two-step forward and PSV reverse launches fetch
  * rows with 3-D tensor copies through each job's table of tensor maps, or
- * with one bulk copy per field (the same bits).  Each drops the captured
- * graph. */
+ * with one bulk copy per field (the same bits); "checkpoint_slots" (S >= 1:
+ * every job keeps S + 2 states and follows the binomial checkpointing
+ * schedule of seiswg_sim_checkpoint_plan; 0: back to the uniform checkpoints
+ * of seiswg_batch_create), which reallocates the jobs' state pools.  Each
+ * drops the captured graph. */
 int seiswg_batch_set_option(seiswg_batch* batch, const char* key, int64_t value);
+/* The binomial checkpointing slots per job (0: uniform checkpoints) and the
+ * forward steps the reverse sweeps of all jobs recompute in one run. */
+int seiswg_batch_checkpoint_plan(const seiswg_batch* batch, int32_t* slots, int64_t* recomputed);
 /* The chunk rows in use (0: each problem's own chunk model), and whether
  * jobs record two steps per launch. */
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);

@@ -67,6 +67,7 @@ PROTOTYPES = [
     ("seiswg_solver_set_write_files", _c_int, [_vp, _c_int]),
     ("seiswg_solver_run_forward", _c_int, [_vp, _vp]),
     ("seiswg_solver_run_adjoint", _c_int, [_vp, _vp, _vp]),
+    ("seiswg_solver_run_inversion", _c_int, [_vp, _vp, _vp]),
     ("seiswg_solver_info", _c_int, [_vp, _pi, _pi, _pf, _pf, _pi, _pi]),
     ("seiswg_solver_total_misfit", ctypes.c_double, [_vp]),
     ("seiswg_solver_sim", _vp, [_vp]),
@@ -114,6 +115,7 @@ PROTOTYPES = [
     ("seiswg_batch_concurrent", _i32, [_vp]),
     ("seiswg_batch_stream_groups", _i32, [_vp]),
     ("seiswg_batch_tma_jobs", _i32, [_vp]),
+    ("seiswg_batch_checkpoint_plan", _c_int, [_vp, _pi, ctypes.POINTER(ctypes.c_int64)]),
     ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
     ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
     ("seiswg_batch_info", _c_int, [_vp, _pi, _pi, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_sz)]),
@@ -240,6 +242,13 @@ class Solver:
     def run_adjoint(self, vfs: Optional[Vfs] = None) -> Dict[str, bytes]:
         out = Vfs()
         _check(lib().seiswg_solver_run_adjoint(self._h, vfs._h if vfs else None, out._h))
+        return out.to_dict()
+
+    def run_inversion(self, vfs: Optional[Vfs] = None) -> Dict[str, bytes]:
+        """`mode = inversion` (seiswg_solver_run_inversion): the final model
+        files and inversion_misfit.txt."""
+        out = Vfs()
+        _check(lib().seiswg_solver_run_inversion(self._h, vfs._h if vfs else None, out._h))
         return out.to_dict()
 
     def info(self):
@@ -491,7 +500,14 @@ class Batch:
                     two_step=bool(lib().seiswg_batch_two_step(self._h)),
                     concurrent=int(lib().seiswg_batch_concurrent(self._h)),
                     stream_groups=int(lib().seiswg_batch_stream_groups(self._h)),
-                    tma_jobs=int(lib().seiswg_batch_tma_jobs(self._h)))
+                    tma_jobs=int(lib().seiswg_batch_tma_jobs(self._h)), **self.checkpoint_plan())
+
+    def checkpoint_plan(self):
+        """dict(checkpoint_slots = binomial slots per job (0: uniform),
+        recomputed_steps = forward steps recomputed per run over all jobs)."""
+        s, r = _i32(), ctypes.c_int64()
+        _check(lib().seiswg_batch_checkpoint_plan(self._h, ctypes.byref(s), ctypes.byref(r)))
+        return dict(checkpoint_slots=s.value, recomputed_steps=r.value)
 
     @property
     def stream(self) -> int:

@@ -64,8 +64,6 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       j.nslot = j.ncp + j.k + 1;
       const size_t slot = size_t(j.nstate) * fe;
       const size_t ntr = size_t(ncomp) * nrec;
-      SW_CUDA(cudaMalloc(&j.pool, size_t(j.nslot) * slot * sizeof(float)));
-      SW_CUDA(cudaMemsetAsync(j.pool, 0, size_t(j.nslot) * slot * sizeof(float), stream_));
       SW_CUDA(cudaMalloc(&j.adj, 2 * slot * sizeof(float)));
       SW_CUDA(cudaMemsetAsync(j.adj, 0, 2 * slot * sizeof(float), stream_));
       SW_CUDA(cudaMalloc(&j.grads, 3 * fe * sizeof(float)));
@@ -77,7 +75,7 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       SW_CUDA(cudaMalloc(&j.J, std::max<size_t>(1, ntr) * sizeof(double)));
       SW_CUDA(cudaMalloc(&j.src, sizeof(Inject)));
       SW_CUDA(cudaMalloc(&j.rec, std::max(1, nrec) * sizeof(Inject)));
-      bytes_ += (size_t(j.nslot) + 2) * slot * sizeof(float) + 3 * fe * sizeof(float) +
+      bytes_ += 2 * slot * sizeof(float) + 3 * fe * sizeof(float) +
                 (size_t(v.nprobe) * (nt + 1) + 2 * ntr * nt) * sizeof(float);
       const Inject src{v.src_i[s], v.src_j[s], s, 0};
       SW_CUDA(cudaMemcpyAsync(j.src, &src, sizeof(Inject), cudaMemcpyHostToDevice, stream_));
@@ -121,46 +119,102 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
       jd.nt = nt;
       jd.dt = d.dt;
       jd.err = err_;
-      // Tensor maps (JobDesc): state slots with boxes of 1, 2 and 3 fields,
-      // the adjoint slots (3, 2), the material (1, 2), the gradients (1, 2),
-      // the dt-scaled material (1, 2).
-      {
-        const int rows_alloc = d.nx + 2 * kHaloRows;
-        const int nf = j.nstate;
-        std::vector<CUtensorMap> maps(size_t(3) * j.nslot + kJobTmaTail);
-        bool ok = v.lam - v.rho == v.mu - v.lam && v.lam > v.rho;
-        for (int sl = 0; ok && sl < j.nslot; ++sl)
-          for (int b = 0; ok && b < 3; ++b)
-            ok = encode_fields(&maps[3 * sl + b], j.pool + sl * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc,
-                               std::min(b + 1, nf));
-        CUtensorMap* t = maps.data() + 3 * j.nslot;
-        for (int a = 0; ok && a < 2; ++a)
-          ok = encode_fields(&t[2 * a], j.adj + a * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc, std::min(3, nf)) &&
-               encode_fields(&t[2 * a + 1], j.adj + a * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc, 2);
-        ok = ok && encode_fields(&t[4], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
-             encode_fields(&t[5], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 2) &&
-             encode_fields(&t[6], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 1) &&
-             encode_fields(&t[7], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 2) && v.rho_dt &&
-             encode_fields(&t[8], v.rho_dt, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
-             encode_fields(&t[9], v.rho_dt, v.lam - v.rho, 3, v.ld, rows_alloc, 2);
-        if (ok) {
-          SW_CUDA(cudaMalloc(&j.tm, maps.size() * sizeof(CUtensorMap)));
-          SW_CUDA(cudaMemcpy(j.tm, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
-          bytes_ += maps.size() * sizeof(CUtensorMap);
-        }
-        jd.tm = j.tm;
-        jd.tm_nslot = j.nslot;
-      }
       descs_.push_back(jd);
       model_geom_.push_back(jd.g);
       model_geom2_.push_back(jd.g2);
       jobs_.push_back(j);
+      alloc_pool(jobs_.size() - 1);
     }
   }
   SW_CUDA(cudaMalloc(&d_jobs_, std::max<size_t>(1, descs_.size()) * sizeof(JobDesc)));
   SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
   build_schedule();
+}
+
+// The job's pool of state slots (uniform checkpoints: ncp + k + 1; binomial
+// checkpointing: S + 2) and its table of tensor maps (JobDesc): state slots
+// with boxes of 1, 2 and 3 fields, the adjoint slots (3, 2), the material
+// (1, 2), the gradients (1, 2), the dt-scaled material (1, 2).
+void Batch::alloc_pool(size_t q) {
+  Job& j = jobs_[q];
+  JobDesc& jd = descs_[q];
+  const Sim::View v = problems_[j.problem].sim->view();
+  const SimDesc& d = problems_[j.problem].sim->desc();
+  const size_t fe = v.field_elems;
+  const size_t halo = size_t(kHaloRows) * v.ld + kHaloCols;
+  const size_t slot = size_t(j.nstate) * fe;
+  if (j.pool) {
+    bytes_ -= size_t(j.pool_slots) * slot * sizeof(float);
+    cudaFree(j.pool);
+    j.pool = nullptr;
+  }
+  if (j.tm) {
+    bytes_ -= (size_t(3) * j.pool_slots + kJobTmaTail) * sizeof(CUtensorMap);
+    cudaFree(j.tm);
+    j.tm = nullptr;
+  }
+  SW_CUDA(cudaMalloc(&j.pool, size_t(j.nslot) * slot * sizeof(float)));
+  SW_CUDA(cudaMemsetAsync(j.pool, 0, size_t(j.nslot) * slot * sizeof(float), stream_));
+  j.pool_slots = j.nslot;
+  bytes_ += size_t(j.nslot) * slot * sizeof(float);
+  jd.pool = j.pool;
+  {
+    const int rows_alloc = d.nx + 2 * kHaloRows;
+    const int nf = j.nstate;
+    std::vector<CUtensorMap> maps(size_t(3) * j.nslot + kJobTmaTail);
+    bool ok = v.lam - v.rho == v.mu - v.lam && v.lam > v.rho;
+    for (int sl = 0; ok && sl < j.nslot; ++sl)
+      for (int b = 0; ok && b < 3; ++b)
+        ok = encode_fields(&maps[3 * sl + b], j.pool + sl * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc,
+                           std::min(b + 1, nf));
+    CUtensorMap* t = maps.data() + 3 * j.nslot;
+    for (int a = 0; ok && a < 2; ++a)
+      ok = encode_fields(&t[2 * a], j.adj + a * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc, std::min(3, nf)) &&
+           encode_fields(&t[2 * a + 1], j.adj + a * slot + halo, ptrdiff_t(fe), nf, v.ld, rows_alloc, 2);
+    ok = ok && encode_fields(&t[4], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
+         encode_fields(&t[5], v.rho, v.lam - v.rho, 3, v.ld, rows_alloc, 2) &&
+         encode_fields(&t[6], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 1) &&
+         encode_fields(&t[7], j.grads + halo, ptrdiff_t(fe), 3, v.ld, rows_alloc, 2) && v.rho_dt &&
+         encode_fields(&t[8], v.rho_dt, v.lam - v.rho, 3, v.ld, rows_alloc, 1) &&
+         encode_fields(&t[9], v.rho_dt, v.lam - v.rho, 3, v.ld, rows_alloc, 2);
+    if (ok) {
+      SW_CUDA(cudaMalloc(&j.tm, maps.size() * sizeof(CUtensorMap)));
+      SW_CUDA(cudaMemcpy(j.tm, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice));
+      bytes_ += maps.size() * sizeof(CUtensorMap);
+    }
+    jd.tm = tma_ ? j.tm : nullptr;
+    jd.tm_nslot = j.nslot;
+  }
+}
+
+void Batch::set_checkpoint_slots(int S) {
+  if (S < 0) throw std::invalid_argument("checkpoint_slots must be >= 0");
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  for (size_t q = 0; q < jobs_.size(); ++q) {
+    Job& j = jobs_[q];
+    j.S = S > 0 ? std::min(S, std::max(j.nt, 1)) : 0;
+    j.nslot = j.S > 0 ? j.S + 2 : j.ncp + j.k + 1;
+    alloc_pool(q);
+  }
+  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  checkpoint_slots_ = S;
+  set_chunk_rows(chunk_rows_);  // rebuilds the schedule, drops the graph
+}
+
+long long Batch::recompute_steps() const {
+  long long n = 0;
+  for (size_t q = 0; q < jobs_.size(); ++q) {
+    const Job& j = jobs_[q];
+    const std::vector<HostOp> L = j.S > 0 ? job_ops_revolve(j.nt, j.S, j.psv, false) : job_ops(j.nt, j.k, j.psv, false);
+    bool after = false;
+    for (const HostOp& o : L) {
+      if (o.kind == kMisfit) after = true;
+      else if (after && (o.kind == kFwdPsv || o.kind == kFwdSh)) ++n;
+    }
+  }
+  return n;
 }
 
 void Batch::set_chunk_rows(int lx) {
@@ -262,7 +316,8 @@ void Batch::build_schedule() {
   std::vector<std::vector<HostOp>> lists(jobs_.size());
   for (size_t q = 0; q < jobs_.size(); ++q) {
     const Job& j = jobs_[q];
-    lists[q] = job_ops(j.nt, j.k, j.psv, two_step_ && descs_[q].g2.lx > 0);
+    const bool two = two_step_ && descs_[q].g2.lx > 0;
+    lists[q] = j.S > 0 ? job_ops_revolve(j.nt, j.S, j.psv, two) : job_ops(j.nt, j.k, j.psv, two);
   }
   size_t T = 0;
   rec_slots_ = 0;

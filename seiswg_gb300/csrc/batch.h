@@ -78,6 +78,13 @@ class Batch {
     for (const JobDesc& d : descs_) n += d.tm != nullptr;
     return n;
   }
+  // Binomial checkpointing (job_ops_revolve, batch_plan.h) with S state
+  // slots per job (plus the two working slots); 0 returns to uniform
+  // checkpoints.  Reallocates every job's pool and rebuilds the schedule.
+  void set_checkpoint_slots(int S);
+  int checkpoint_slots() const { return checkpoint_slots_; }
+  // Forward steps the reverse sweeps of all jobs recompute per run.
+  long long recompute_steps() const;
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -90,6 +97,8 @@ class Batch {
  private:
   struct Job {
     int problem, shot, k, ncp, nslot, nt, nstate, ncomp, nrec;
+    int S = 0;           // binomial checkpointing slots (0: uniform checkpoints every k steps)
+    int pool_slots = 0;  // slots of the allocated pool
     bool psv;
     CUtensorMap* tm = nullptr;  // the job's tensor-map table in device memory (see JobDesc)
     float *pool = nullptr, *adj = nullptr, *grads = nullptr, *acc = nullptr, *hist = nullptr, *obs = nullptr,
@@ -99,6 +108,8 @@ class Batch {
     Inject* rec = nullptr;
   };
   void build_schedule();
+  void alloc_pool(size_t q);
+  int checkpoint_slots_ = 0;
   void enqueue_run();
   void enqueue_slots(int t0, int t1);
   std::vector<JobDesc> descs_;   // host copy of d_jobs_

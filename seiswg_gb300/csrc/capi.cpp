@@ -239,6 +239,16 @@ int seiswg_solver_run_adjoint(seiswg_solver* s, const seiswg_vfs* vfs, seiswg_vf
   });
 }
 
+int seiswg_solver_run_inversion(seiswg_solver* s, const seiswg_vfs* vfs, seiswg_vfs* out) {
+  if (!s) return fail(SEISWG_EINVAL, "null solver");
+  return guarded([&] {
+    static const seiswg::Vfs empty;
+    seiswg::Vfs r = s->solver->run_inversion(vfs ? vfs->map : empty);
+    if (out)
+      for (auto& kv : r) out->map[kv.first] = std::move(kv.second);
+  });
+}
+
 int seiswg_solver_info(const seiswg_solver* s, int32_t* nx, int32_t* nz, float* dx, float* dz, int32_t* nsrc,
                        int32_t* nrec) {
   if (!s) return fail(SEISWG_EINVAL, "null solver");
@@ -534,7 +544,10 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "concurrent") b->batch->set_concurrent(int(value));
     else if (k == "stream_groups") b->batch->set_stream_groups(int(value));
     else if (k == "tma") b->batch->set_tma(value != 0);
-    else throw std::invalid_argument("unknown batch option: " + k);
+    else if (k == "checkpoint_slots") {
+      if (value < 0 || value > (1 << 30)) throw std::invalid_argument("checkpoint_slots out of range");
+      b->batch->set_checkpoint_slots(int(value));
+    } else throw std::invalid_argument("unknown batch option: " + k);
   });
 }
 
@@ -547,6 +560,14 @@ int32_t seiswg_batch_concurrent(const seiswg_batch* b) { return b ? b->batch->co
 int32_t seiswg_batch_stream_groups(const seiswg_batch* b) { return b ? b->batch->stream_groups() : 0; }
 
 int32_t seiswg_batch_tma_jobs(const seiswg_batch* b) { return b ? b->batch->tma_jobs() : 0; }
+
+int seiswg_batch_checkpoint_plan(const seiswg_batch* b, int32_t* slots, int64_t* recomputed) {
+  if (!b) return fail(SEISWG_EINVAL, "null batch");
+  return guarded([&] {
+    if (slots) *slots = b->batch->checkpoint_slots();
+    if (recomputed) *recomputed = b->batch->recompute_steps();
+  });
+}
 
 int seiswg_batch_gradient(seiswg_batch* b, int32_t problem, const char* param, float* host) {
   if (!b || !param || !host) return fail(SEISWG_EINVAL, "seiswg_batch_gradient: null argument");
@@ -606,22 +627,7 @@ int seiswg_npy_encode(const float* data, size_t nrows, size_t ncols, void* out, 
 
 int seiswg_l2_misfit(const float* syn, const float* obs, int32_t ntr, int32_t nt, float dt, float* adj, double* J) {
   if (ntr < 0 || nt < 2 || !syn || !obs || !adj || !J) return fail(SEISWG_EINVAL, "seiswg_l2_misfit: bad argument");
-  // Taper of solver.rs:442-459 (in double here).
-  const double t_end = double(nt - 1) * double(dt), tw = t_end / 10.0, pi = 3.14159265358979323846;
-  double sum = 0.0;
-  for (int it = 0; it < nt; ++it) {
-    const double t = double(it) * double(dt);
-    double tau = 1.0;
-    if (t <= tw) tau = 0.5 + 0.5 * std::cos(pi * (tw - t) / tw);
-    else if (t >= t_end - tw) tau = 0.5 + 0.5 * std::cos(pi * ((t_end - tw) - t) / tw);
-    for (int r = 0; r < ntr; ++r) {
-      const size_t k = size_t(r) * nt + it;
-      const double d = (double(syn[k]) - double(obs[k])) * tau;
-      sum += d * d;
-      adj[k] = float(2.0 * d * tau);
-    }
-  }
-  *J = sum;
+  *J = seiswg::l2_misfit(syn, obs, ntr, nt, dt, adj);
   g_last_error.clear();
   return SEISWG_OK;
 }
@@ -630,13 +636,7 @@ int seiswg_velocity_gradients(const float* g_lam, const float* g_mu, const float
                               const float* vs, const float* rho, size_t n, float* g_vp, float* g_vs, float* g_rho) {
   if (!g_lam || !g_mu || !g_b || !vp || !vs || !rho || !g_vp || !g_vs || !g_rho)
     return fail(SEISWG_EINVAL, "seiswg_velocity_gradients: null argument");
-  for (size_t k = 0; k < n; ++k) {
-    const double a = vp[k], b = vs[k], r = rho[k], gl = g_lam[k], gm = g_mu[k], gb = g_b[k];
-    const bool live = a > b;  // vps2lm sets lambda to 0 otherwise (fd2d.wgsl:196-200)
-    g_vp[k] = float(live ? gl * 2.0 * r * a : 0.0);
-    g_vs[k] = float((live ? gl * (-4.0 * r * b) : 0.0) + gm * 2.0 * r * b);
-    g_rho[k] = float((live ? gl * (a * a - 2.0 * b * b) : 0.0) + gm * b * b - gb / (r * r));
-  }
+  seiswg::velocity_gradients(g_lam, g_mu, g_b, vp, vs, rho, n, g_vp, g_vs, g_rho);
   g_last_error.clear();
   return SEISWG_OK;
 }

@@ -1,6 +1,8 @@
 // cli.cpp -- `seiswg <config.ini>`, the command-line entry of the reference
 // (src/main.rs:33-99): load the config, pre-load the model directory,
-// sources, stations and observed traces into a VFS, then run the workflow.
+// sources, stations and observed traces into a VFS, then run the workflow:
+// forward, adjoint, or inversion (which the reference rejects as not yet
+// implemented, main.rs:93-94).
 #include <dirent.h>
 #include <sys/stat.h>
 
@@ -76,6 +78,8 @@ int main(int argc, char** argv) {
     if (seiswg_solver_run_forward(s, nullptr) != SEISWG_OK) rc = die("forward");
   } else if (workflow == "adjoint") {
     if (seiswg_solver_run_adjoint(s, vfs, nullptr) != SEISWG_OK) rc = die("adjoint");
+  } else if (workflow == "inversion") {
+    if (seiswg_solver_run_inversion(s, vfs, nullptr) != SEISWG_OK) rc = die("inversion");
   } else {
     std::fprintf(stderr, "Error: Workflow '%s' is not yet implemented in seiswg\n", workflow.c_str());
     rc = 1;

@@ -1090,6 +1090,14 @@ void Sim::smooth_kmu(float sigma) {
   cudaFree(dw);
 }
 
+void Sim::smooth_field(float* host, float sigma) {
+  clear_kmu();
+  SW_CUDA(cudaMemcpy2DAsync(kmu_, size_t(ld_) * sizeof(float), host, size_t(d_.nz) * sizeof(float),
+                            size_t(d_.nz) * sizeof(float), size_t(d_.nx), cudaMemcpyHostToDevice, stream_));
+  smooth_kmu(sigma);
+  download_kmu(host);
+}
+
 void Sim::download_kmu(float* host) const {
   if (!kmu_) {
     std::fill(host, host + size_t(d_.nx) * d_.nz, 0.0f);

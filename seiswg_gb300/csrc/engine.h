@@ -127,6 +127,9 @@ class Sim {
   void adjoint_backward(const float* adstf_host, int adj_interval);
   void clear_kmu();
   void smooth_kmu(float sigma);
+  // The same Gaussian smoothing of a host field (nx*nz values, in place),
+  // through the kmu buffer (whose contents it replaces).
+  void smooth_field(float* host, float sigma);
   void download_kmu(float* host) const;
 
   // ---- exact discrete adjoint with checkpointing --------------------------

@@ -215,6 +215,12 @@ Config parse_config(const Ini& ini, const std::string& base) {
   if (ini_get(ini, "cuda", "chunk_rows", &v) && parse_u32(v, &u)) c.chunk_rows = int(u);
   if (ini_get(ini, "cuda", "graphs", &v)) c.graphs = lower(trim(v)) == "yes" ? 1 : 0;
   if (ini_get(ini, "cuda", "two_step", &v)) c.two_step = lower(trim(v)) == "yes" ? 1 : 0;
+  c.inv_iterations = get_u32_or(ini, "inversion", "iterations", c.inv_iterations);
+  c.inv_step = get_f32_or(ini, "inversion", "step", c.inv_step);
+  c.inv_max_step = get_f32_or(ini, "inversion", "max_step", c.inv_max_step);
+  c.inv_trials = get_u32_or(ini, "inversion", "line_search_trials", c.inv_trials);
+  c.inv_smooth = get_f32_or(ini, "inversion", "smooth", c.inv_smooth);
+  if (ini_get(ini, "inversion", "parameters", &v)) c.inv_parameters = lower(trim(v));
   return c;
 }
 
@@ -359,6 +365,36 @@ double waveform_misfit(const float* syn, const float* obs, int nrec, int nt, flo
     }
   }
   return std::sqrt(misfit);
+}
+
+double l2_misfit(const float* syn, const float* obs, int ntr, int nt, float dt, float* adj) {
+  // Taper of solver.rs:442-459, in double here.
+  const double t_end = double(nt - 1) * double(dt), tw = t_end / 10.0, pi = 3.14159265358979323846;
+  double sum = 0.0;
+  for (int it = 0; it < nt; ++it) {
+    const double t = double(it) * double(dt);
+    double tau = 1.0;
+    if (t <= tw) tau = 0.5 + 0.5 * std::cos(pi * (tw - t) / tw);
+    else if (t >= t_end - tw) tau = 0.5 + 0.5 * std::cos(pi * ((t_end - tw) - t) / tw);
+    for (int r = 0; r < ntr; ++r) {
+      const size_t k = size_t(r) * nt + it;
+      const double d = (double(syn[k]) - double(obs[k])) * tau;
+      sum += d * d;
+      if (adj) adj[k] = float(2.0 * d * tau);
+    }
+  }
+  return sum;
+}
+
+void velocity_gradients(const float* g_lam, const float* g_mu, const float* g_b, const float* vp, const float* vs,
+                        const float* rho, size_t n, float* g_vp, float* g_vs, float* g_rho) {
+  for (size_t k = 0; k < n; ++k) {
+    const double a = vp[k], b = vs[k], r = rho[k], gl = g_lam[k], gm = g_mu[k], gb = g_b[k];
+    const bool live = a > b;  // vps2lm sets lambda to 0 otherwise (fd2d.wgsl:196-200)
+    g_vp[k] = float(live ? gl * 2.0 * r * a : 0.0);
+    g_vs[k] = float((live ? gl * (-4.0 * r * b) : 0.0) + gm * 2.0 * r * b);
+    g_rho[k] = float((live ? gl * (a * a - 2.0 * b * b) : 0.0) + gm * b * b - gb / (r * r));
+  }
 }
 
 namespace {
@@ -827,6 +863,194 @@ Vfs Solver::run_adjoint(const Vfs& vfs) {
   out[kp] = std::move(raw);
   out[gp] = std::move(with_header);
   log_info("Adjoint: gradient saved to " + kp);
+  return out;
+}
+
+// ---- inversion ---------------------------------------------------------------
+// Steepest descent in relative model units with a backtracking line search:
+//   s_p  = m_p g_p / max over p and cells |m_p g_p|   (p: the inverted fields)
+//   m_p <- m_p (1 - alpha s_p)                         (largest relative change alpha)
+//   accept when J(m_new) <= J(m) + c1 sum g (m_new - m)  (Armijo, c1 = 1e-4),
+//   else alpha <- alpha / 2, at most [inversion] line_search_trials times;
+//   after an acceptance at the first trial the next step starts 1.5x larger.
+// J is the L2 waveform misfit (l2_misfit) summed over the shots; its gradient
+// is the exact discrete adjoint (Sim::forward_op / backward_op, checkpointed),
+// mapped to vp, vs, rho and smoothed with the Gaussian of the reference's
+// kernel smoothing (fd2d.wgsl:515-609).  A trial model that fails the
+// stability check counts as a rejected trial.
+Vfs Solver::run_inversion(const Vfs& vfs) {
+  if (cfg_.spin || cfg_.sh == cfg_.psv) throw Error("the inversion workflow runs SH or PSV alone (no spin)");
+  if (!cfg_.has_traces) throw Error("config [path] traces is required for the inversion workflow");
+  const bool psv = cfg_.psv;
+  const int nt = int(cfg_.nt), nrec = this->nrec(), nsrc = this->nsrc();
+  const int ncomp = psv ? 2 : 1;
+  const size_t npt = size_t(grid_.nx) * grid_.nz, nobs = size_t(nrec) * nt;
+  std::vector<std::string> params;
+  {
+    std::stringstream ss(cfg_.inv_parameters);
+    std::string t;
+    while (std::getline(ss, t, ',')) {
+      t = trim(t);
+      if (t.empty()) continue;
+      if (t != "vp" && t != "vs" && t != "rho") throw Error("[inversion] parameters: unknown field " + t);
+      params.push_back(t);
+    }
+  }
+  if (params.empty()) throw Error("[inversion] parameters lists no field");
+  if (cfg_.inv_step <= 0.0f || cfg_.inv_max_step <= 0.0f) throw Error("[inversion] step and max_step must be > 0");
+
+  // Shots as in run_adjoint, and their observed traces ([path] traces:
+  // uy_NNNNNN.npy for SH; ux_ and uz_NNNNNN.npy for PSV, the forward
+  // workflow's output names).
+  std::vector<std::pair<int, int>> runs;
+  if (cfg_.combine_sources) runs.push_back({-1, 0});
+  else for (int s = 0; s < nsrc; ++s) runs.push_back({s, s});
+  std::vector<std::vector<float>> obs(runs.size());
+  for (size_t q = 0; q < runs.size(); ++q) {
+    for (const char* c : psv ? std::vector<const char*>{"ux", "uz"} : std::vector<const char*>{"uy"}) {
+      const std::string p = path_join(cfg_.traces, std::string(c) + "_" + fmt6(uint32_t(runs[q].second)) + ".npy");
+      Bytes b;
+      try {
+        b = lookup(vfs, p);
+      } catch (const Error&) {
+        throw Error("Cannot load observed traces " + p);
+      }
+      std::vector<float> t = parse_npy(b, p);
+      if (t.size() != nobs)
+        throw Error("observed traces " + p + " hold " + std::to_string(t.size()) + " samples, expected " +
+                    std::to_string(nobs));
+      obs[q].insert(obs[q].end(), t.begin(), t.end());
+    }
+  }
+  // The initial model, as read by the constructor.
+  const std::string model_dir = cfg_.has_model_init ? cfg_.model_init : cfg_.model_true;
+  std::map<std::string, std::vector<float>> model;
+  Bytes x_bytes, z_bytes;
+  for (const char* f : {"vp", "vs", "rho"}) {
+    const std::string p = path_join(model_dir, std::string("proc000000_") + f + ".bin");
+    model[f] = parse_model_bin(lookup(vfs, p), p);
+    if (model[f].size() != npt) throw Error("a model file does not match the grid");
+  }
+  x_bytes = lookup(vfs, path_join(model_dir, "proc000000_x.bin"));
+  z_bytes = lookup(vfs, path_join(model_dir, "proc000000_z.bin"));
+  const float sigma = cfg_.inv_smooth >= 0.0f ? cfg_.inv_smooth : cfg_.smooth;
+  const unsigned comp_mask = psv ? (1u << 0) | (1u << 2) : (1u << 1);
+  std::vector<float> tr(size_t(5) * nobs), syn(size_t(ncomp) * nobs), adj(size_t(ncomp) * nobs);
+  auto gather = [&]() {
+    sim_->download_traces(tr.data(), comp_mask);
+    if (psv) {
+      std::copy(tr.begin(), tr.begin() + long(nobs), syn.begin());
+      std::copy(tr.begin() + 2 * long(nobs), tr.begin() + 3 * long(nobs), syn.begin() + long(nobs));
+    } else {
+      std::copy(tr.begin() + long(nobs), tr.begin() + 2 * long(nobs), syn.begin());
+    }
+  };
+  auto upload = [&](const std::map<std::string, std::vector<float>>& m) {
+    sim_->upload_model(ModelField::VP, m.at("vp").data());
+    sim_->upload_model(ModelField::VS, m.at("vs").data());
+    sim_->upload_model(ModelField::RHO, m.at("rho").data());
+    try {
+      sim_->prepare_model();
+    } catch (const std::invalid_argument& e) {
+      log_info(std::string("Inversion: trial model rejected: ") + e.what());
+      return false;
+    }
+    return true;
+  };
+  auto misfit = [&](const std::map<std::string, std::vector<float>>& m) {
+    if (!upload(m)) return std::numeric_limits<double>::infinity();
+    double J = 0.0;
+    for (size_t q = 0; q < runs.size(); ++q) {
+      sim_->run_forward(runs[q].first);
+      gather();
+      J += l2_misfit(syn.data(), obs[q].data(), ncomp * nrec, nt, cfg_.dt, nullptr);
+    }
+    return J;
+  };
+  std::map<std::string, std::vector<float>> grad;
+  auto gradient = [&](const std::map<std::string, std::vector<float>>& m) {
+    if (!upload(m)) throw Error("the current inversion model fails the stability check");
+    sim_->gradient_clear();
+    double J = 0.0;
+    for (size_t q = 0; q < runs.size(); ++q) {
+      sim_->forward_op(runs[q].first, 0);
+      gather();
+      J += l2_misfit(syn.data(), obs[q].data(), ncomp * nrec, nt, cfg_.dt, adj.data());
+      sim_->backward_op(adj.data());
+    }
+    std::vector<float> gl(npt), gm(npt), gb(npt);
+    sim_->download_gradient(0, gl.data());
+    sim_->download_gradient(1, gm.data());
+    sim_->download_gradient(2, gb.data());
+    for (const char* f : {"vp", "vs", "rho"}) grad[f].assign(npt, 0.0f);
+    velocity_gradients(gl.data(), gm.data(), gb.data(), m.at("vp").data(), m.at("vs").data(), m.at("rho").data(),
+                       npt, grad["vp"].data(), grad["vs"].data(), grad["rho"].data());
+    if (sigma > 0.0f)
+      for (const std::string& p : params) sim_->smooth_field(grad[p].data(), sigma);
+    return J;
+  };
+
+  inv_history_.clear();
+  float alpha0 = std::min(cfg_.inv_step, cfg_.inv_max_step);
+  for (uint32_t iter = 0; iter < cfg_.inv_iterations; ++iter) {
+    const double J = gradient(model);
+    double scale = 0.0;
+    for (const std::string& p : params)
+      for (size_t k = 0; k < npt; ++k) scale = std::max(scale, std::fabs(double(model[p][k]) * grad[p][k]));
+    InversionStep rec{J, J, 0.0, 0, false};
+    if (scale > 0.0) {
+      float alpha = alpha0;
+      for (uint32_t trial = 1; trial <= cfg_.inv_trials; ++trial) {
+        auto cand = model;
+        double slope = 0.0;
+        for (const std::string& p : params)
+          for (size_t k = 0; k < npt; ++k) {
+            const double m0 = model[p][k], sp = m0 * grad[p][k] / scale;
+            cand[p][k] = float(m0 * (1.0 - double(alpha) * sp));
+            slope += double(grad[p][k]) * (double(cand[p][k]) - m0);
+          }
+        const double Jn = misfit(cand);
+        rec.trials = int(trial);
+        if (std::isfinite(Jn) && Jn <= J + 1e-4 * slope) {
+          rec = InversionStep{J, Jn, double(alpha), int(trial), true};
+          model = std::move(cand);
+          alpha0 = std::min(alpha * (trial == 1 ? 1.5f : 1.0f), cfg_.inv_max_step);
+          break;
+        }
+        alpha *= 0.5f;
+        alpha0 = alpha;
+      }
+    }
+    inv_history_.push_back(rec);
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "Inversion: iteration %u misfit %.6e -> %.6e (step %.4g, %s after %d trial%s)",
+                  iter + 1, rec.misfit, rec.new_misfit, rec.step, rec.accepted ? "accepted" : "rejected",
+                  rec.trials, rec.trials == 1 ? "" : "s");
+    log_info(buf);
+    if (!rec.accepted) break;  // no descent found along the gradient: stop
+  }
+  upload(model);  // the simulation holds the final model
+
+  Vfs out;
+  if (write_files_) mkdirs(cfg_.output);
+  auto emit = [&](const std::string& name, Bytes b) {
+    const std::string p = path_join(cfg_.output, name);
+    if (write_files_) write_file(p, b);
+    out[p] = std::move(b);
+  };
+  for (const char* f : {"vp", "vs", "rho"}) emit(std::string("proc000000_") + f + ".bin", make_model_bin(model[f]));
+  emit("proc000000_x.bin", x_bytes);
+  emit("proc000000_z.bin", z_bytes);
+  std::string log = "# iteration misfit new_misfit step trials accepted\n";
+  for (size_t q = 0; q < inv_history_.size(); ++q) {
+    char buf[160];
+    const InversionStep& r = inv_history_[q];
+    std::snprintf(buf, sizeof buf, "%zu %.9e %.9e %.6g %d %d\n", q + 1, r.misfit, r.new_misfit, r.step, r.trials,
+                  int(r.accepted));
+    log += buf;
+  }
+  emit("inversion_misfit.txt", Bytes(log.begin(), log.end()));
+  log_info("Inversion: model saved to " + cfg_.output);
   return out;
 }
 

@@ -43,6 +43,14 @@ struct Config {
   int chunk_rows = 0;   // 0: engine default
   int graphs = -1;      // -1: engine default, 0 off, 1 on
   int two_step = -1;    // [cuda] two_step: -1 engine default (on for PSV alone), 0 off, 1 on
+  // [inversion] -- the workflow the reference lists as planned (README.md:61,
+  // main.rs:93-94); keys the reference does not read
+  uint32_t inv_iterations = 5;  // descent steps
+  float inv_step = 0.02f;       // first relative model change of the line search
+  float inv_max_step = 0.1f;    // largest relative model change of a step
+  uint32_t inv_trials = 6;      // misfit evaluations per line search
+  float inv_smooth = -1.0f;     // gradient smoothing sigma in cells (< 0: [solver] smooth)
+  std::string inv_parameters = "vp,vs";  // inverted fields, of vp, vs, rho
 };
 
 // config::load (config.rs:118) and config::load_from_str (config.rs:132).
@@ -67,6 +75,13 @@ std::vector<std::vector<double>> parse_table(const std::string& text);
 void ricker(float t, float f0, float t0, float ang_deg, float amp, float* x, float* y, float* z);
 // Waveform misfit and time-reversed adjoint source (solver.rs:432-467).
 double waveform_misfit(const float* syn, const float* obs, int nrec, int nt, float dt, float* adstf);
+// J = sum (taper * (syn - obs))^2 over ntr traces of nt samples with the
+// misfit taper of solver.rs:442-459, and adj = dJ/dsyn (not time-reversed).
+double l2_misfit(const float* syn, const float* obs, int ntr, int nt, float dt, float* adj);
+// Chain rule from (lambda, mu, buoyancy) gradients to (vp, vs, rho) for
+// lambda = rho (vp^2 - 2 vs^2) (0 where vp <= vs), mu = rho vs^2 (fd2d.wgsl:188-201).
+void velocity_gradients(const float* g_lam, const float* g_mu, const float* g_b, const float* vp, const float* vs,
+                        const float* rho, size_t n, float* g_vp, float* g_vs, float* g_rho);
 
 // Grid inference from coordinate extents (solver.rs:646-656).
 struct GridInfo {
@@ -105,6 +120,21 @@ class Solver {
   Vfs run_forward();
   // Solver::run_adjoint (solver.rs:1298).
   Vfs run_adjoint(const Vfs& vfs);
+  // `mode = inversion`, which the reference lists as planned (README.md:61)
+  // and rejects (main.rs:93-94): steepest descent on the [inversion]
+  // parameters from the initial model, each gradient the exact discrete
+  // adjoint summed over the shots, smoothed, with a backtracking (Armijo)
+  // line search; writes the final model (proc000000_<param>.bin with x, z)
+  // to [path] output.  SH or PSV alone.
+  Vfs run_inversion(const Vfs& vfs);
+  // Misfit J of each accepted or rejected inversion step: (J before, J
+  // after, relative step; 0 when rejected).
+  struct InversionStep {
+    double misfit, new_misfit, step;
+    int trials;
+    bool accepted;
+  };
+  const std::vector<InversionStep>& inversion_history() const { return inv_history_; }
 
   void set_write_files(bool on) { write_files_ = on; }
   Sim& sim() { return *sim_; }
@@ -132,6 +162,7 @@ class Solver {
   bool write_files_ = true;
   std::vector<double> misfits_;
   double total_misfit_ = 0.0;
+  std::vector<InversionStep> inv_history_;
 };
 
 // Logging (env RUST_LOG-like level via SEISWG_LOG: error|warn|info; default info).

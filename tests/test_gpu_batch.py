@@ -161,3 +161,38 @@ def test_launch_orders_give_the_same_gradients():
         batch.close()
         for s in sims:
             s.close()
+
+
+def test_batch_binomial_checkpointing_gives_the_same_gradients():
+    """Every job under binomial checkpointing (S state slots, the revolve
+    schedule of job_ops_revolve) against the uniform checkpoints of the
+    default batch: with one-step recording every stored or recomputed state
+    is the same bits, so the gradients are equal bit for bit; the pools
+    shrink to S + 2 states per job and the recomputed steps are those the
+    schedule states."""
+    import seiswg_gb300 as sw
+
+    probs = _problems()
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    batch.set_option("two_step", 0)
+    batch.run()
+    ref = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
+    bytes_uniform = batch.info()["device_bytes"]
+    for S in (2, 5):
+        batch.set_option("checkpoint_slots", S)
+        info = batch.info()
+        assert info["checkpoint_slots"] == S and info["device_bytes"] < bytes_uniform
+        assert info["recomputed_steps"] > 0
+        batch.run()
+        for i in range(len(probs)):
+            for p in ("lambda", "mu", "buoyancy"):
+                assert np.array_equal(batch.gradient(i, p), ref[i][p]), (S, i, p)
+    batch.set_option("two_step", 1)
+    batch.run()
+    for i in range(len(probs)):
+        for p in ("mu", "buoyancy"):
+            assert rel_l2(batch.gradient(i, p), ref[i][p]) <= 1e-5
+    batch.close()
+    for s in sims:
+        s.close()

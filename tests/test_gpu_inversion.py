@@ -1,6 +1,8 @@
 """The inversion loop on the GPU: a few descent steps on a small PSV problem
 with three shots reduce the waveform misfit and move vp toward the anomaly of
 the true model."""
+import os
+
 import numpy as np
 import pytest
 
@@ -51,3 +53,62 @@ def test_descent_reduces_misfit_and_finds_the_anomaly():
     ptrue = true["vp"].astype(np.float64) - 3000.0
     corr = float((dvp * ptrue).sum() / (np.linalg.norm(dvp) * np.linalg.norm(ptrue)))
     assert corr > 0.3, corr
+
+
+def _write_model(d, nx, nz, dx, vp, vs, rho):
+    from tests.examples import write_bin
+
+    os.makedirs(d, exist_ok=True)
+    x = np.repeat(np.arange(nx, dtype=np.float32) * np.float32(dx), nz)
+    z = np.tile(np.arange(nz, dtype=np.float32) * np.float32(dx), nx)
+    for name, a in (("x", x), ("z", z), ("vp", vp), ("vs", vs), ("rho", rho)):
+        write_bin(os.path.join(d, f"proc000000_{name}.bin"), a)
+
+
+def test_cli_inversion_lowers_the_misfit(tmp_path):
+    """`mode = inversion` through the drop-in command line (the reference
+    rejects it as not yet implemented, main.rs:93-94): observed traces from a
+    forward run of the true model, then three descent steps from the
+    homogeneous initial model; the misfit falls at every accepted step and
+    the final model files are written."""
+    import subprocess
+
+    import seiswg_gb300 as sw
+
+    W, true = _problem()
+    d = str(tmp_path)
+    n, dx = W.nx, W.dx
+    _write_model(os.path.join(d, "model_true"), n, n, dx, true["vp"], true["vs"], true["rho"])
+    _write_model(os.path.join(d, "model_init"), n, n, dx, W.model["vp"], W.model["vs"], W.model["rho"])
+    with open(os.path.join(d, "sources.dat"), "w") as f:
+        for (i, j, f0, t0, ang, amp) in W.sources:
+            f.write(f"{i * dx} {j * dx} 0 {f0} {t0} {ang} {amp}\n")
+    with open(os.path.join(d, "stations.dat"), "w") as f:
+        for i, j in zip(W.rec_i, W.rec_j):
+            f.write(f"{i * dx} {j * dx}\n")
+    solver = (f"[solver]\nsh = no\npsv = yes\nnt = {W.nt}\ndt = {W.dt!r}\nabs_left = yes\nabs_right = yes\n"
+              f"abs_bottom = yes\nabs_top = yes\nabs_width = {W.flags['abs_width']}\ncombine_sources = no\n")
+    open(os.path.join(d, "forward.ini"), "w").write(
+        "[workflow]\nmode = forward\n" + solver +
+        "[path]\noutput = fwd\noutput_traces = obs\nmodel_true = model_true\nsources = sources.dat\n"
+        "stations = stations.dat\n")
+    open(os.path.join(d, "inversion.ini"), "w").write(
+        "[workflow]\nmode = inversion\n" + solver +
+        "[path]\noutput = inv\nmodel_init = model_init\nsources = sources.dat\nstations = stations.dat\n"
+        "traces = obs\n[inversion]\niterations = 3\nparameters = vp, vs\nstep = 0.01\nmax_step = 0.03\n"
+        "smooth = 3\n")
+    for ini in ("forward.ini", "inversion.ini"):
+        r = subprocess.run([sw.CLI_PATH, os.path.join(d, ini)], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr[-3000:]
+    rows = [ln.split() for ln in open(os.path.join(d, "inv", "inversion_misfit.txt")) if not ln.startswith("#")]
+    J0, J1, acc = [float(r[1]) for r in rows], [float(r[2]) for r in rows], [int(r[5]) for r in rows]
+    assert len(rows) >= 2 and sum(acc) >= 2, rows
+    assert all(b < a for a, b, ok in zip(J0, J1, acc) if ok)
+    assert J1[-1] < 0.9 * J0[0]
+    vp = np.fromfile(os.path.join(d, "inv", "proc000000_vp.bin"), "<f4")
+    assert int(vp[:1].view(np.int32)[0]) == n * n and vp.size == n * n + 1
+    dvp = vp[1:].reshape(n, n).astype(np.float64) - 3000.0
+    ptrue = true["vp"].astype(np.float64) - 3000.0
+    assert float((dvp * ptrue).sum() / (np.linalg.norm(dvp) * np.linalg.norm(ptrue))) > 0.2
+    for f in ("vs", "rho", "x", "z"):
+        assert os.path.exists(os.path.join(d, "inv", f"proc000000_{f}.bin"))

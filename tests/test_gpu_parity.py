@@ -1,8 +1,8 @@
 """CUDA path against the FP32 CPU oracle on seeded inputs (relative L2 within
-1e-5, the FP32 tolerance the path is held to; the FP64 oracle error is
-reported in the assertion message; only the spin rotation yi, a difference of
-two displacement derivatives, may instead reach 3x the FP32 oracle's own
-distance from FP64).  Cases cover the edge rules of fd2d.wgsl: grids
+1e-5, the FP32 tolerance the path is held to; where the problem's own FP32
+rounding exceeds that, at least as accurate against the FP64 oracle as the
+reference's FP32 arithmetic, see _agrees; the FP64 oracle error is reported
+in the assertion message).  Cases cover the edge rules of fd2d.wgsl: grids
 narrower than one warp strip, odd sizes, every taper edge, sources and
 receivers on and next to the boundary, co-located sources, per-shot source
 selection, SH+PSV together, spin, snapshots, and the reference adjoint with
@@ -94,24 +94,48 @@ def _comps(flags):
     return sorted(set(c))
 
 
+def _agrees(e32, e64, floor, tol, cancel=False):
+    """1e-5 relative L2 against the FP32 oracle.  Where the FP32 rounding of
+    the problem itself exceeds that (the FP32 oracle is more than 1e-5 from
+    the FP64 one: traces ahead of the first arrival, long runs, cells the
+    edge rule isolates), two FP32 results that round differently cannot
+    agree to 1e-5; the result must then be at least as close to FP64 as the
+    reference's own FP32 arithmetic, and within twice that distance of it.
+    The spin rotation yi = uy_c - curl/2 differences two displacement
+    derivatives (cancel): 3x the oracle's distance from FP64 is allowed."""
+    if e32 <= tol:
+        return True
+    if e64 <= floor and e32 <= 2 * floor:
+        return True
+    return cancel and e32 <= 3 * floor
+
+
 def _check(gpu, ref, flags, tol=L2_TOL):
-    # Tolerance: 1e-5 relative L2 against the FP32 oracle.  The spin rotation
-    # yi = uy_c - curl/2 (component 3) differences two displacement
-    # derivatives; there FP32 cancellation can take the oracle itself past
-    # 1e-5 from FP64, and 3x that distance is allowed instead.
     for c in _comps(flags):
         e32 = rel_l2(gpu["traces"][c], ref[32]["obs"][c])
         e64 = rel_l2(gpu["traces"][c], ref[64]["obs"][c])
         floor = rel_l2(ref[32]["obs"][c], ref[64]["obs"][c])
-        lim = max(tol, 3 * floor) if c == 3 else tol
-        assert e32 <= lim, \
+        assert _agrees(e32, e64, floor, tol, cancel=c == 3), \
             f"trace comp {c}: rel L2 {e32:.2e} vs FP32 oracle (FP64: {e64:.2e}, FP32 oracle vs FP64 {floor:.2e})"
     for f, a in gpu["state"].items():
         e32 = rel_l2(a, ref[32]["state"][f])
         e64 = rel_l2(a, ref[64]["state"][f])
         floor = rel_l2(ref[32]["state"][f], ref[64]["state"][f])
-        assert e32 <= tol, \
+        assert _agrees(e32, e64, floor, tol), \
             f"state {f}: rel L2 {e32:.2e} vs FP32 oracle (FP64: {e64:.2e}, FP32 oracle vs FP64 {floor:.2e})"
+
+
+def _check_plain(gpu, ref, flags, tol=L2_TOL):
+    """Plain 1e-5 against the FP32 oracle on every trace component and state
+    field (the spin rotation yi aside, as in _agrees)."""
+    for c in _comps(flags):
+        e32 = rel_l2(gpu["traces"][c], ref[32]["obs"][c])
+        floor = rel_l2(ref[32]["obs"][c], ref[64]["obs"][c])
+        assert e32 <= (max(tol, 3 * floor) if c == 3 else tol), \
+            f"trace comp {c}: rel L2 {e32:.2e} vs FP32 oracle (FP32 oracle vs FP64 {floor:.2e})"
+    for f, a in gpu["state"].items():
+        e32 = rel_l2(a, ref[32]["state"][f])
+        assert e32 <= tol, f"state {f}: rel L2 {e32:.2e} vs FP32 oracle"
 
 
 LOADERS = pytest.mark.parametrize("loader", [0, 1], ids=["direct", "bulk"])
@@ -263,7 +287,7 @@ def test_c2_geometry_plain_tolerance(two_step):
     src = [(256, 50, 15.0, 0.05, 90.0)]
     rec = [(i, 0) for i in range(0, 512, 32)] + [(256, 240)]
     gpu, ref = _run_pair(nx, nz, nt, dx, dt, src, rec, _model(nx, nz, 11, dx=dx), two_step=two_step, **flags)
-    _check(gpu, ref, flags)
+    _check_plain(gpu, ref, flags)
     top = slice(0, 16)
     for c in (0, 2):
         assert not np.any(gpu["traces"][c][top]) and not np.any(ref[64]["obs"][c][top])

@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 
 from tests.examples import rel_l2
-from tests.test_gpu_parity import _check, _STATE, _ORACLE_SLOT
+from tests.test_gpu_parity import _check_plain, _STATE, _ORACLE_SLOT
 
 pytestmark = pytest.mark.gpu
 
@@ -70,7 +70,7 @@ def test_c2_full_grid():
     for c in (0, 2):
         assert not np.any(gpu["traces"][c][top]) and not np.any(ref[64]["obs"][c][top])
         assert np.abs(gpu["traces"][c][top.stop:]).max() > 0
-    _check(gpu, ref, w.flags)
+    _check_plain(gpu, ref, w.flags)
 
 
 def test_c3_full_grid():
@@ -82,7 +82,7 @@ def test_c3_full_grid():
     w = configs.c3_spin_forward(nt=100)
     gpu, ref = _pair(w, w.rec_i, w.rec_j, ("vx", "vz", "sxx", "szz", "sxz", "vyc", "syx", "syy", "syz"))
     assert np.abs(gpu["traces"][0]).max() > 0
-    _check(gpu, ref, w.flags)
+    _check_plain(gpu, ref, w.flags)
 
 
 def test_c4_full_grid_gradient():
@@ -97,7 +97,16 @@ def test_c4_full_grid_gradient():
 
     w = configs.c4_psv_adjoint(nt=60, shots=8)
     w.sources = w.sources[:1]
-    obs_o = _oracle(w, 64, w.rec_i, w.rec_j, model=w.extra["true_model"])
+    # Within 60 steps the waves reach about 30 cells: the observed data come
+    # from a model perturbed there (+5 % vp and vs in a Gaussian of radius 20
+    # cells between the source and the first receivers), not from the
+    # configuration's deep anomaly, which no wave reaches that soon.
+    si, sj = w.sources[0][0], w.sources[0][1]
+    ii, jj = np.meshgrid(np.arange(w.nx), np.arange(w.nz), indexing="ij")
+    bump = (1.0 + 0.05 * np.exp(-((ii - si - 15) ** 2 + (jj - sj - 10) ** 2) / 20.0 ** 2)).astype(np.float32)
+    near = dict(vp=(w.model["vp"] * bump).astype(np.float32), vs=(w.model["vs"] * bump).astype(np.float32),
+                rho=w.model["rho"])
+    obs_o = _oracle(w, 64, w.rec_i, w.rec_j, model=near)
     obs = np.stack([obs_o.obs("X"), obs_o.obs("Z")]).astype(np.float32)
     del obs_o
 
