@@ -742,6 +742,7 @@ def run_secondary(args):
                            "recomputed_steps_per_run": info["recomputed_steps"],
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
                            "concurrent": info.get("concurrent"), "stream_groups": info.get("stream_groups"),
+                           "queue_units": info.get("queue_units"), "queue_blocks": info.get("queue_blocks"),
                            "tma_jobs": info.get("tma_jobs"), "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
@@ -786,8 +787,8 @@ def main():
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--stream-groups", type=int, default=0, help="c5: job groups with their own streams (0: default)")
     ap.add_argument("--concurrent", type=int, default=-1,
-                    help="c5: launch order: 0 serial, 1 a slot's kinds on forked streams, 2 one stream per kind "
-                         "(-1: the default, 2)")
+                    help="c5: 0 serial grouped launches, 1 a slot's kinds on forked streams, 2 one stream per "
+                         "kind, 3 one persistent launch over a device queue (-1: the default, 3)")
     ap.add_argument("--fd-check", type=int, default=0, help="c4: finite-difference check on this many cells")
     ap.add_argument("--checkpoint-slots", type=int, default=0,
                     help="c4, c5: binomial checkpointing with this many stored states (per shot / per job)")

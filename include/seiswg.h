@@ -256,15 +256,23 @@ int seiswg_batch_run(seiswg_batch* batch);
  * chunk model); "two_step" (0/1): jobs whose problem runs two steps per
  * launch (PSV alone, SH alone) record their forward pass that way (default
  * 1); "autotune": tries
- * chunk rows 0, 16, 32, 48, 64, 96 and 128 with and without two-step
+ * chunk rows 0, 16 (not in order 3), 32, 48, 64, 96 and 128 with and without two-step
  * recording, timing `value` slots of the recording pass and of the reverse
  * sweep each, and keeps the one whose times, scaled to the slot counts of
- * the two phases, are the shortest; "concurrent": the order of the
- * launches (one per schedule slot and kind of work: SH/PSV forward, reverse,
- * misfit): 0 one after another, 1 a slot's launches on forked streams that
- * join before the next slot, 2 (default) one stream per kind, a launch
- * waiting only for the latest launches of the kinds its jobs come from (the
- * previous slot's, or this slot's for a kind enqueued before it); "stream_groups" (1..4, default 1): jobs split round-robin into
+ * the two phases, are the shortest (in order 3, the queue's units of those
+ * slots); "concurrent": how the schedule runs -- as grouped launches (one
+ * per schedule slot and kind of work: SH/PSV forward, reverse, misfit), 0
+ * one after another, 1 a slot's launches on forked streams that join before
+ * the next slot, 2 one stream per kind, a launch waiting only for the
+ * previous slot's launches of the kinds its jobs come from; or 3 (default)
+ * as one persistent launch whose warps work through a device queue of every
+ * job's units (one warp's march over one strip and chunk of one operation),
+ * each unit waiting only for the chunks its rows reach of its job's previous
+ * operation; "queue_wait_us" (order 3, default 2 s): the bound of one such
+ * wait, after which the run fails with SEISWG_ETIMEOUT;
+ * "test_queue_need_extra" (a test hook, default 0): added to every such
+ * dependency after a job's first operation, so that those waits run out;
+ * "stream_groups" (1..4, default 1): jobs split round-robin into
  * groups with their own launches (and streams in order 2); "tma" (0/1,
  * default 1): the grouped two-step forward and PSV reverse launches fetch
  * rows with 3-D tensor copies through each job's table of tensor maps, or
@@ -281,9 +289,12 @@ int seiswg_batch_checkpoint_plan(const seiswg_batch* batch, int32_t* slots, int6
  * jobs record two steps per launch. */
 int32_t seiswg_batch_chunk_rows(const seiswg_batch* batch);
 int32_t seiswg_batch_two_step(const seiswg_batch* batch);
-/* The launch order in use ("concurrent": 0, 1 or 2) and the job groups. */
+/* The launch order in use ("concurrent": 0 to 3) and the job groups. */
 int32_t seiswg_batch_concurrent(const seiswg_batch* batch);
 int32_t seiswg_batch_stream_groups(const seiswg_batch* batch);
+/* Launch order 3: the units in the device queue and the CTAs of the
+ * persistent launch (0 and 0 in the other orders). */
+int seiswg_batch_queue(const seiswg_batch* batch, int64_t* units, int32_t* blocks);
 /* Jobs whose grouped launches fetch rows by tensor copies (0 with "tma" 0). */
 int32_t seiswg_batch_tma_jobs(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */

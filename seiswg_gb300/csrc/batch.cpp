@@ -129,7 +129,7 @@ Batch::Batch(const std::vector<BatchProblem>& problems, int ckpt_every, cudaStre
   SW_CUDA(cudaMalloc(&d_jobs_, std::max<size_t>(1, descs_.size()) * sizeof(JobDesc)));
   SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
-  build_schedule();
+  set_chunk_rows(0);  // each problem's own chunk model; builds the schedule
 }
 
 // The job's pool of state slots (uniform checkpoints: ncp + k + 1; binomial
@@ -232,6 +232,11 @@ void Batch::set_chunk_rows(int lx) {
         g2.nchunks = (g2.nx + lx - 1) / lx;
       }
     }
+    if (concurrent_ == 3 && g2.lx > 0 && g2.lx != g.lx) {  // the queue counts finished units per chunk
+      const int l = std::max(g.lx, g2.lx);
+      g.lx = g2.lx = l;
+      g.nchunks = g2.nchunks = (g.nx + l - 1) / l;
+    }
     descs_[q].g = g;
     descs_[q].g2 = g2;
   }
@@ -252,7 +257,10 @@ void Batch::set_two_step(bool on) {
 
 double Batch::autotune(int slots) {
   if (slots < 1) slots = 1;
-  std::vector<int> cand = {0, 16, 32, 48, 64, 96, 128};
+  // The device queue counts units per chunk: short chunks multiply its units
+  // (and their claims and waits), so it starts at 32 rows.
+  std::vector<int> cand = concurrent_ == 3 ? std::vector<int>{0, 32, 48, 64, 96, 128}
+                                           : std::vector<int>{0, 16, 32, 48, 64, 96, 128};
   cudaEvent_t e0, e1;
   SW_CUDA(cudaEventCreate(&e0));
   SW_CUDA(cudaEventCreate(&e1));
@@ -294,6 +302,7 @@ double Batch::autotune(int slots) {
 
 Batch::~Batch() {
   if (graph_) cudaGraphExecDestroy(graph_);
+  free_queue();
   for (Job& j : jobs_) {
     for (void* p : {(void*)j.pool, (void*)j.adj, (void*)j.grads, (void*)j.acc, (void*)j.hist, (void*)j.obs,
                     (void*)j.u_tab, (void*)j.J, (void*)j.src, (void*)j.rec, (void*)j.tm})
@@ -348,6 +357,124 @@ void Batch::build_schedule() {
   SW_CUDA(cudaStreamSynchronize(stream_));
   bytes_ += all.size() * sizeof(GroupOp) - ops_bytes_;
   ops_bytes_ = all.size() * sizeof(GroupOp);
+  if (concurrent_ == 3) build_queue(lists);
+  else free_queue();
+}
+
+// Launch order 3: the queue of every job's units (plan_queue), the jobs'
+// operations with their dependency counts, one counter per job and chunk,
+// and the claim counter; each job's descriptor points at its part.
+void Batch::build_queue(const std::vector<std::vector<HostOp>>& lists) {
+  free_queue();
+  std::vector<QueueShape> shapes;
+  for (const JobDesc& d : descs_) {
+    if (d.g2.lx > 0 && (d.g2.lx != d.g.lx || d.g2.nchunks != d.g.nchunks))
+      throw std::logic_error("the device queue needs the same chunks for a job's one- and two-step geometries");
+    shapes.push_back(QueueShape{d.g.nchunks, d.g.lx, d.g.nstrips, d.g2.lx > 0 ? d.g2.nstrips : d.g.nstrips});
+  }
+  QueuePlan Q = plan_queue(lists, shapes);
+  std::vector<QueueOp> ops;
+  std::vector<size_t> op_off;
+  need_at_.assign(jobs_.size(), {});
+  cnt_off_.assign(jobs_.size(), 0);
+  ncnt_ = 0;
+  for (size_t q = 0; q < jobs_.size(); ++q) {
+    op_off.push_back(ops.size());
+    ops.insert(ops.end(), Q.ops[q].begin(), Q.ops[q].end());
+    int total = 0;
+    for (const QueueOp& o : Q.ops[q]) need_at_[q].push_back(o.need);
+    if (!Q.ops[q].empty()) total = Q.ops[q].back().need + queue_units_per_chunk(Q.ops[q].back().kind, shapes[q]);
+    need_at_[q].push_back(total);
+    cnt_off_[q] = ncnt_;
+    ncnt_ += shapes[q].nchunks;
+  }
+  nunits_ = (long long)Q.units.size();
+  slot_begin_ = Q.slot_begin;
+  SW_CUDA(cudaMalloc(&d_units_, std::max<size_t>(1, Q.units.size()) * sizeof(QueueUnit)));
+  SW_CUDA(cudaMemcpy(d_units_, Q.units.data(), Q.units.size() * sizeof(QueueUnit), cudaMemcpyHostToDevice));
+  SW_CUDA(cudaMalloc(&d_qops_, std::max<size_t>(1, ops.size()) * sizeof(QueueOp)));
+  SW_CUDA(cudaMemcpy(d_qops_, ops.data(), ops.size() * sizeof(QueueOp), cudaMemcpyHostToDevice));
+  SW_CUDA(cudaMalloc(&d_qcnt_, std::max(1, ncnt_) * sizeof(int)));
+  SW_CUDA(cudaMalloc(&d_next_, sizeof(unsigned long long)));
+  queue_bytes_ = Q.units.size() * sizeof(QueueUnit) + ops.size() * sizeof(QueueOp) + size_t(ncnt_) * sizeof(int) +
+                 sizeof(unsigned long long);
+  bytes_ += queue_bytes_;
+  bool all_maps = true;
+  for (size_t q = 0; q < jobs_.size(); ++q) {
+    descs_[q].qops = d_qops_ + op_off[q];
+    descs_[q].qcnt = d_qcnt_ + cnt_off_[q];
+    descs_[q].qreach = queue_reach(descs_[q].g.lx);
+    all_maps = all_maps && jobs_[q].tm != nullptr;
+  }
+  queue_tma_ = tma_ && all_maps;
+  int dev = 0, sms = 0;
+  SW_CUDA(cudaGetDevice(&dev));
+  SW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  queue_blocks_ = batch_queue_blocks_per_sm(queue_tma_) * sms;
+  if (queue_blocks_ <= 0) throw CudaError("the batch's queue kernel cannot be resident on this GPU");
+  SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
+  SW_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Batch::free_queue() {
+  for (void* p : {(void*)d_units_, (void*)d_qops_, (void*)d_qcnt_, (void*)d_next_}) cudaFree(p);
+  for (JobDesc& d : descs_) {  // the device copy keeps its stale pointers until the next upload; unused
+    d.qops = nullptr;
+    d.qcnt = nullptr;
+  }
+  d_units_ = nullptr;
+  d_qops_ = nullptr;
+  d_qcnt_ = nullptr;
+  d_next_ = nullptr;
+  bytes_ -= queue_bytes_;
+  queue_bytes_ = 0;
+  nunits_ = 0;
+  slot_begin_.clear();
+  need_at_.clear();
+  cnt_off_.clear();
+  ncnt_ = 0;
+  queue_blocks_ = 0;
+}
+
+// The units of slots [t0, t1) as one launch.  Every job's counters start at
+// the count its first operation at or after slot t0 waits for, as if the
+// slots before t0 had run (the autotuner's windows; a whole run starts at 0).
+void Batch::enqueue_queue(int t0, int t1) {
+  t0 = std::max(0, t0);
+  t1 = std::min(t1, nslots_);
+  if (t0 >= t1 || !d_units_) return;
+  if (t0 == 0) {
+    SW_CUDA(cudaMemsetAsync(d_qcnt_, 0, std::max(1, ncnt_) * sizeof(int), stream_));
+    SW_CUDA(cudaMemsetAsync(d_next_, 0, sizeof(unsigned long long), stream_));
+  } else {
+    std::vector<int> cnt(size_t(std::max(1, ncnt_)), 0);
+    for (size_t q = 0; q < jobs_.size(); ++q) {
+      const std::vector<int>& n = need_at_[q];
+      const int v = n[std::min(size_t(t0), n.size() - 1)];
+      std::fill(cnt.begin() + cnt_off_[q], cnt.begin() + cnt_off_[q] + descs_[q].g.nchunks, v);
+    }
+    const unsigned long long first = (unsigned long long)slot_begin_[size_t(t0)];
+    SW_CUDA(cudaMemcpy(d_qcnt_, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice));
+    SW_CUDA(cudaMemcpy(d_next_, &first, sizeof(first), cudaMemcpyHostToDevice));
+  }
+  SW_CUDA(launch_batch_queue(d_jobs_, d_units_, slot_begin_[size_t(t1)], d_next_, err_, queue_tma_, queue_wait_ns_,
+                             queue_need_extra_, queue_blocks_, stream_));
+  ++launches_per_run_;
+}
+
+void Batch::set_queue_wait_ns(unsigned long long ns) {
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  queue_wait_ns_ = ns;
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
+}
+
+void Batch::set_queue_need_extra(int n) {
+  if (n < 0) throw std::invalid_argument("queue need_extra must be >= 0");
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  queue_need_extra_ = n;
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
 }
 
 void Batch::enqueue_run() {
@@ -379,6 +506,10 @@ void Batch::enqueue_run() {
 }
 
 void Batch::enqueue_slots(int t0, int t1) {
+  if (concurrent_ == 3) {
+    enqueue_queue(t0, t1);
+    return;
+  }
   if (concurrent_ == 2) {
     // One stream per (kind, group), forked from and joined back into the
     // batch's stream; a job that changes kind between slots makes its new
@@ -452,7 +583,18 @@ void Batch::set_stream_groups(int groups) {
 void Batch::set_tma(bool on) {
   SW_CUDA(cudaStreamSynchronize(stream_));
   tma_ = on;
-  for (size_t q = 0; q < descs_.size(); ++q) descs_[q].tm = on ? jobs_[q].tm : nullptr;
+  bool all_maps = true;
+  for (size_t q = 0; q < descs_.size(); ++q) {
+    descs_[q].tm = on ? jobs_[q].tm : nullptr;
+    all_maps = all_maps && jobs_[q].tm != nullptr;
+  }
+  if (d_units_) {
+    queue_tma_ = on && all_maps;
+    int dev = 0, sms = 0;
+    SW_CUDA(cudaGetDevice(&dev));
+    SW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    queue_blocks_ = batch_queue_blocks_per_sm(queue_tma_) * sms;
+  }
   SW_CUDA(cudaMemcpyAsync(d_jobs_, descs_.data(), descs_.size() * sizeof(JobDesc), cudaMemcpyHostToDevice, stream_));
   SW_CUDA(cudaStreamSynchronize(stream_));
   if (graph_) cudaGraphExecDestroy(graph_);
@@ -460,11 +602,13 @@ void Batch::set_tma(bool on) {
 }
 
 void Batch::set_concurrent(int mode) {
-  if (mode < 0 || mode > 2) throw std::invalid_argument("concurrent must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) throw std::invalid_argument("concurrent must be 0, 1, 2 or 3");
   SW_CUDA(cudaStreamSynchronize(stream_));
+  const bool rebuild = (mode == 3) != (concurrent_ == 3);
   concurrent_ = mode;
   if (graph_) cudaGraphExecDestroy(graph_);
   graph_ = nullptr;
+  if (rebuild) set_chunk_rows(chunk_rows_);
 }
 
 void Batch::run() {
@@ -504,7 +648,9 @@ void Batch::run() {
   SW_CUDA(cudaMemcpy(&e, err_, sizeof(int), cudaMemcpyDeviceToHost));
   if (e) SW_CUDA(cudaMemset(err_, 0, sizeof(int)));  // reported once
   if (e & kErrWaitTimeout)
-    throw WaitTimeout("a batched kernel gave up waiting for its row pipeline (bounded wait expired)");
+    throw WaitTimeout(
+        "a batched kernel gave up waiting for its row pipeline or, in the device queue, for a unit's dependencies "
+        "(bounded wait expired)");
   if (e & kErrNonFiniteGradient) throw NumericError("a batched gradient holds NaN or infinite values");
 }
 

@@ -16,6 +16,7 @@
 #include <memory>
 #include <vector>
 
+#include "batch_plan.h"
 #include "engine.h"
 
 namespace seiswg {
@@ -52,12 +53,16 @@ class Batch {
   // tries both.
   void set_two_step(bool on);
   bool two_step() const { return two_step_; }
-  // How the launches of the schedule are ordered.  0: one after another on
-  // the batch's stream.  1: the launches of one slot (one per kind of work)
-  // run concurrently on forked streams that join before the next slot.
-  // 2 (default): one stream per kind; a launch waits only for the previous
-  // slot's launches of the kinds its jobs come from, so the kinds pipeline.
-  // Drops the captured graph.
+  // How the schedule runs.  0: one grouped launch per (slot, kind), one
+  // after another on the batch's stream.  1: the launches of one slot run
+  // concurrently on forked streams that join before the next slot.  2: one
+  // stream per kind; a launch waits only for the previous slot's launches of
+  // the kinds its jobs come from, so the kinds pipeline.  3 (default): one
+  // persistent launch over a device work queue of every job's units
+  // (fd_queue.cu, plan_queue in batch_plan.h); the one- and two-step
+  // geometries of a job then share their rows per chunk (the larger of the
+  // two).  Entering or leaving mode 3 rebuilds the schedule; every change
+  // drops the captured graph.
   void set_concurrent(int mode);
   int concurrent() const { return concurrent_; }
   // Jobs split round-robin into this many groups (1..kMaxStreamGroups), each
@@ -85,6 +90,14 @@ class Batch {
   int checkpoint_slots() const { return checkpoint_slots_; }
   // Forward steps the reverse sweeps of all jobs recompute per run.
   long long recompute_steps() const;
+  // Launch order 3: the bound of a dependency wait in the queue kernel
+  // (nanoseconds), and a test hook added to every dependency after a job's
+  // first operation so that those waits run out (0 normally).
+  void set_queue_wait_ns(unsigned long long ns);
+  void set_queue_need_extra(int n);
+  // Units in the device queue (0 outside launch order 3) and its CTAs.
+  long long queue_units() const { return nunits_; }
+  int queue_blocks() const { return queue_blocks_; }
   // which: 0 lambda, 1 mu, 2 buoyancy (zero for lambda of SH problems).
   void download_gradient(int problem, int which, float* host) const;
   double misfit(int problem) const;  // sum over the problem's shots and traces of the last run
@@ -123,7 +136,7 @@ class Batch {
   std::vector<Job> jobs_;
   cudaStream_t stream_;
   bool own_stream_ = false;
-  int concurrent_ = 2;
+  int concurrent_ = 3;
   bool tma_ = true;   // grouped launches fetch rows by tensor copies where the job has a map table
   int groups_ = 1;
   std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
@@ -150,6 +163,25 @@ class Batch {
   size_t bytes_ = 0;
   cudaGraphExec_t graph_ = nullptr;
   uint64_t launches_per_run_ = 0;
+
+  // Launch order 3: the device queue (plan_queue).
+  void build_queue(const std::vector<std::vector<HostOp>>& lists);
+  void free_queue();
+  void enqueue_queue(int t0, int t1);  // the units of slots [t0, t1)
+  QueueUnit* d_units_ = nullptr;
+  QueueOp* d_qops_ = nullptr;
+  int* d_qcnt_ = nullptr;
+  unsigned long long* d_next_ = nullptr;
+  long long nunits_ = 0;
+  size_t queue_bytes_ = 0;
+  std::vector<long long> slot_begin_;       // first unit of each slot
+  std::vector<std::vector<int>> need_at_;   // per job: need of each operation, then the total
+  std::vector<int> cnt_off_;                // per job: its first counter
+  int ncnt_ = 0;
+  int queue_blocks_ = 0;
+  bool queue_tma_ = false;
+  unsigned long long queue_wait_ns_ = 2000000000ull;
+  int queue_need_extra_ = 0;
 };
 
 }  // namespace seiswg

@@ -8,13 +8,14 @@
 // - 1 and ncp + k the recording pass's states between checkpoints.
 #pragma once
 
+#include <stdexcept>
 #include <utility>
 #include <vector>
 
+#include "fd_types.h"
+
 namespace seiswg {
 
-// Kinds of work; one grouped launch per (schedule slot, kind).
-enum BatchKind { kFwdSh = 0, kFwdPsv, kFwd2Sh, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
 
 // Forward: step `it` (two steps for kFwd2*) from slot a to slot b, flags & 1
 // records the probes.  Reverse: reverse step `it` with the forward state of
@@ -247,6 +248,89 @@ inline std::vector<std::vector<PlanLaunch>> plan_launches(const std::vector<std:
         if (!l.jobs.empty()) plan[t].push_back(std::move(l));
       }
   return plan;
+}
+
+// ---------------------------------------------------------------------------
+// Launch order 3 (Batch): the whole schedule as one persistent launch over a
+// device work queue (fd_queue.cu).
+//
+// Every operation of a job is split into units: one per (strip, chunk) of
+// the operation's geometry, unit = strip + nstrips * chunk, or one unit for
+// the misfit.  The one- and two-step geometries of a job share their chunks
+// (the same rows per chunk), so a chunk names the same rows for every kind.
+// Units are laid out slot-major -- slot t holds operation t of every job,
+// kinds in BatchKind order, jobs in index order, units in index order -- so
+// that every unit a unit depends on comes earlier in the queue.  A job keeps
+// one counter of finished units per chunk; the units of its operation t wait
+// until the counter of every chunk within `reach` chunks of theirs (of every
+// chunk, for the misfit) shows need[t], the units per chunk of operations
+// 0..t-1.  A counter can reach need[t] only once operation t-1 has finished
+// on that chunk (operation t-1's own units waited for t-2 there, and so on),
+// so a unit starts only after every earlier operation of its job has
+// finished on the chunks its rows reach: what it reads is written, and what
+// it overwrites (a chunk of its own rows) has been read.  Warps claim units
+// in queue order and run them in that order, so the first unfinished unit
+// always has its dependencies finished and is held by a running warp: the
+// queue cannot deadlock, whether or not all CTAs are resident.
+// ---------------------------------------------------------------------------
+
+// Chunks and rows per chunk of a job's one- and two-step geometries, and
+// their strips.
+struct QueueShape {
+  int nchunks, lx, nstrips1, nstrips2;
+};
+
+// Rows a unit reads beyond its chunk: the two-step marches read from 9 rows
+// above to 5 below their chunk, the one-step and reverse marches from 3
+// above to 2 below.
+constexpr int kQueueReachRows = 9;
+inline int queue_reach(int lx) { return (kQueueReachRows + lx - 1) / lx; }
+
+inline int queue_units_per_chunk(int kind, const QueueShape& s) {
+  if (kind == kMisfit) return 1;
+  return (kind == kFwd2Psv || kind == kFwd2Sh) ? s.nstrips2 : s.nstrips1;
+}
+inline int queue_units(int kind, const QueueShape& s) {
+  return kind == kMisfit ? 1 : queue_units_per_chunk(kind, s) * s.nchunks;
+}
+
+struct QueuePlan {
+  std::vector<std::vector<QueueOp>> ops;  // per job, its operations with their `need`
+  std::vector<QueueUnit> units;           // the queue
+  std::vector<long long> slot_begin;      // first unit of each slot, then units.size()
+};
+
+inline QueuePlan plan_queue(const std::vector<std::vector<HostOp>>& lists, const std::vector<QueueShape>& shapes) {
+  QueuePlan Q;
+  const size_t nj = lists.size();
+  if (nj > 65536) throw std::invalid_argument("the device queue holds at most 65536 jobs");
+  size_t T = 0, total = 0;
+  Q.ops.resize(nj);
+  for (size_t q = 0; q < nj; ++q) {
+    T = lists[q].size() > T ? lists[q].size() : T;
+    if (size_t(shapes[q].nstrips1) * shapes[q].nchunks > 65536 ||
+        size_t(shapes[q].nstrips2) * shapes[q].nchunks > 65536)
+      throw std::invalid_argument("a job has more than 65536 warp units per operation (chunk_rows too small)");
+    int need = 0;
+    for (const HostOp& h : lists[q]) {
+      Q.ops[q].push_back(QueueOp{h.kind, h.it, h.a, h.b, h.flags, need});
+      need += queue_units_per_chunk(h.kind, shapes[q]);
+      total += size_t(queue_units(h.kind, shapes[q]));
+    }
+  }
+  Q.units.reserve(total);
+  Q.slot_begin.reserve(T + 1);
+  for (size_t t = 0; t < T; ++t) {
+    Q.slot_begin.push_back((long long)Q.units.size());
+    for (int kind = 0; kind < kKinds; ++kind)
+      for (size_t q = 0; q < nj; ++q) {
+        if (t >= lists[q].size() || lists[q][t].kind != kind) continue;
+        const int n = queue_units(kind, shapes[q]);
+        for (int u = 0; u < n; ++u) Q.units.push_back(QueueUnit{(unsigned short)q, (unsigned short)u, unsigned(t)});
+      }
+  }
+  Q.slot_begin.push_back((long long)Q.units.size());
+  return Q;
 }
 
 }  // namespace seiswg

@@ -544,6 +544,13 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "concurrent") b->batch->set_concurrent(int(value));
     else if (k == "stream_groups") b->batch->set_stream_groups(int(value));
     else if (k == "tma") b->batch->set_tma(value != 0);
+    else if (k == "queue_wait_us") {
+      if (value < 1 || value > (int64_t(1) << 40)) throw std::invalid_argument("queue_wait_us out of range");
+      b->batch->set_queue_wait_ns((unsigned long long)value * 1000ull);
+    } else if (k == "test_queue_need_extra") {
+      if (value < 0 || value > (1 << 30)) throw std::invalid_argument("test_queue_need_extra out of range");
+      b->batch->set_queue_need_extra(int(value));
+    }
     else if (k == "checkpoint_slots") {
       if (value < 0 || value > (1 << 30)) throw std::invalid_argument("checkpoint_slots out of range");
       b->batch->set_checkpoint_slots(int(value));
@@ -560,6 +567,13 @@ int32_t seiswg_batch_concurrent(const seiswg_batch* b) { return b ? b->batch->co
 int32_t seiswg_batch_stream_groups(const seiswg_batch* b) { return b ? b->batch->stream_groups() : 0; }
 
 int32_t seiswg_batch_tma_jobs(const seiswg_batch* b) { return b ? b->batch->tma_jobs() : 0; }
+
+int seiswg_batch_queue(const seiswg_batch* b, int64_t* units, int32_t* blocks) {
+  if (!b) return fail(SEISWG_EINVAL, "null batch");
+  if (units) *units = b->batch->queue_units();
+  if (blocks) *blocks = b->batch->queue_blocks();
+  return SEISWG_OK;
+}
 
 int seiswg_batch_checkpoint_plan(const seiswg_batch* b, int32_t* slots, int64_t* recomputed) {
   if (!b) return fail(SEISWG_EINVAL, "null batch");

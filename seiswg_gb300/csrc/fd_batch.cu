@@ -5,35 +5,14 @@
 // receiver) is reduced by one thread: d^n from the probe history, J_trace =
 // sum_n (tau_n (d^n - o^n))^2 with the cosine taper of solver.rs:442-459, and
 // the reverse cumulative adjoint source dt * U^n, U^n = sum_{m >= n}
-// 2 tau_m^2 (d^m - o^m), which the reverse sweep injects at the receiver.
-// Sums run in double; the arithmetic matches seiswg_l2_misfit on the host.
-#include <cmath>
+// 2 tau_m^2 (d^m - o^m), which the reverse sweep injects at the receiver
+// (misfit_trace, fd_misfit.cuh).
 
-#include "fd_kernels.h"
+#include "fd_misfit.cuh"
 
 namespace seiswg {
 
 namespace {
-
-// One trace: J_trace = sum_n (tau_n (d^n - o^n))^2 and u^n = dt * U^n with
-// U^n = sum_{m >= n} float(2 tau_m^2 (d^m - o^m)), summed in double from the
-// last sample down (the order of seiswg_l2_misfit's host loop).
-__device__ double misfit_trace(const float* __restrict__ d, const float* __restrict__ o, float* __restrict__ u,
-                               int nt, double dt) {
-  const double t_end = double(nt - 1) * dt, tw = t_end / 10.0, pi = 3.14159265358979323846;
-  double sum = 0.0, acc = 0.0;
-  for (int it = nt - 1; it >= 0; --it) {
-    const double t = double(it) * dt;
-    double tau = 1.0;
-    if (t <= tw) tau = 0.5 + 0.5 * cos(pi * (tw - t) / tw);
-    else if (t >= t_end - tw) tau = 0.5 + 0.5 * cos(pi * ((t_end - tw) - t) / tw);
-    const double e = (double(d[it]) - double(o[it])) * tau;
-    sum += e * e;
-    acc += double(float(2.0 * e * tau));
-    u[it] = float(dt * acc);
-  }
-  return sum;
-}
 
 __global__ void grouped_misfit_kernel(const JobDesc* __restrict__ jobs, const GroupOp* __restrict__ ops) {
   const GroupOp op = ops[blockIdx.x];

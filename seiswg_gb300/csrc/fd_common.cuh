@@ -22,12 +22,32 @@ struct f4 {
   float v[4];
 };
 
+// Loads of state rows and of values other launches write.  In the batch's
+// queue kernel (fd_queue.cu, which defines SEISWG_COHERENT_LOADS) other warps
+// of the same launch write them, so they go through L2 (ld.global.cg); the
+// step kernels read them through the read-only path (ld.global.nc), which
+// is valid only for data no thread of the launch writes.
+namespace {
+#ifdef SEISWG_COHERENT_LOADS
+__device__ __forceinline__ f4 ld4(const float* p) {
+  const float4 t = __ldcg(reinterpret_cast<const float4*>(p));
+#else
 __device__ __forceinline__ f4 ld4(const float* __restrict__ p) {
-  float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+#endif
   f4 r;
   r.v[0] = t.x; r.v[1] = t.y; r.v[2] = t.z; r.v[3] = t.w;
   return r;
 }
+
+__device__ __forceinline__ float ld1(const float* p) {
+#ifdef SEISWG_COHERENT_LOADS
+  return __ldcg(p);
+#else
+  return __ldg(p);
+#endif
+}
+}  // namespace
 
 __device__ __forceinline__ void st4(float* p, const f4& a) {
   *reinterpret_cast<float4*>(p) = make_float4(a.v[0], a.v[1], a.v[2], a.v[3]);

@@ -198,6 +198,12 @@ struct JobDesc {
   // material (1, 2).
   const CUtensorMap* tm;
   int tm_nslot;
+  // The device work queue (launch order 3 of the batch): the job's
+  // operations, its counters of finished units (one per chunk) and how many
+  // chunks to each side a unit's rows reach.
+  const QueueOp* qops;
+  int* qcnt;
+  int qreach;
 };
 constexpr int kJobTmaTail = 10;  // maps after the slots' in a job's table
 
@@ -250,6 +256,21 @@ cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int
 cudaError_t launch_sim_misfit(const float* syn, const float* obs, float* u_tab, double* J, int nrec, int nt,
                               bool psv, float dt, cudaStream_t s);
 cudaError_t launch_grouped_misfit(const JobDesc* jobs, const GroupOp* ops, int nops, cudaStream_t s);
+
+// The batch's persistent queue kernel (fd_queue.cu): `blocks` CTAs whose
+// warps claim units units[*next], units[*next + 1], ... below `end` in order
+// (*next and the jobs' counters are set by the caller), wait for each unit's
+// dependencies -- bounded by wait_ns nanoseconds, after which the error word
+// gets kErrWaitTimeout and the warp leaves -- and run its march.  `tma`:
+// two-step and PSV reverse units fetch rows by tensor copies (every job has
+// a map table), else by bulk copies.  need_extra (a test hook, 0 normally)
+// is added to every dependency after a job's first operation, so that those
+// waits run out.
+cudaError_t launch_batch_queue(const JobDesc* jobs, const QueueUnit* units, long long end, unsigned long long* next,
+                               int* err, bool tma, unsigned long long wait_ns, int need_extra, int blocks,
+                               cudaStream_t s);
+// CTAs of the queue kernel resident per SM (its grid is that times the SMs).
+int batch_queue_blocks_per_sm(bool tma);
 
 // ---- auxiliary kernels (fd_aux.cu) ----------------------------------------
 

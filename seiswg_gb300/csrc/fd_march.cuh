@@ -37,9 +37,9 @@ __device__ __forceinline__ void inject_row(const InjectList& inj, int i, int c0,
     const int e = __ldg(&inj.list[ci].j) - c0;
     if (e >= 0 && e < 4) {
       const size_t o = size_t(__ldg(&inj.list[ci].row)) * inj.nt + inj.it;
-      const float ax = X ? __ldg(&inj.val_x[o]) : 0.0f;
-      const float ay = Y ? __ldg(&inj.val_y[o]) : 0.0f;
-      const float az = Z ? __ldg(&inj.val_z[o]) : 0.0f;
+      const float ax = X ? ld1(&inj.val_x[o]) : 0.0f;
+      const float ay = Y ? ld1(&inj.val_y[o]) : 0.0f;
+      const float az = Z ? ld1(&inj.val_z[o]) : 0.0f;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         if (q == e) {
@@ -92,7 +92,11 @@ __device__ __forceinline__ void probe_row(const ProbeList& pr, int i, const Lane
     if (e >= 0 && e < 4 && (L.own & (1 << e))) {
       int idx = __ldg(&pr.list[pi].idx);
       float v = pick(__ldg(&pr.list[pi].comp), e);
+#ifdef SEISWG_COHERENT_LOADS
+      float u = __ldcg(&pr.acc[idx]) + v * dt;  // af(F_U*, k, v * dt), fd2d.wgsl:270
+#else
       float u = pr.acc[idx] + v * dt;  // af(F_U*, k, v * dt), fd2d.wgsl:270
+#endif
       pr.acc[idx] = u;
       pr.hist[size_t(idx) * pr.nt + pr.it] = u;
     }
@@ -125,18 +129,13 @@ struct BulkL : BulkRows<NSEG, kPipeStages> {
   using BulkRows<NSEG, kPipeStages>::BulkRows;
 };
 
-// Per-warp slices of the CTA's dynamic shared memory: [warps][S][NSEG][128]
-// floats, then [warps][S] mbarriers.
+// The warp's loader over its slice of shared memory (warp_slice).
 template <class Loader>
 __device__ __forceinline__ Loader make_loader(const typename Loader::SegsT& segs, const Geom& g, const March& m,
-                                              const LaneCols& L, unsigned char* smem) {
+                                              const LaneCols& L, unsigned char* slice) {
   float* buf = nullptr;
   uint64_t* bar = nullptr;
-  if (Loader::kStages > 0) {
-    const size_t per = size_t(Loader::kStages) * Loader::kStageBytes;
-    buf = reinterpret_cast<float*>(smem + per * m.warp);
-    bar = reinterpret_cast<uint64_t*>(smem + per * (blockDim.x >> 5)) + Loader::kStages * m.warp;
-  }
+  if (Loader::kStages > 0) slice_ring<Loader>(slice, buf, bar);
   return Loader(segs, size_t(g.ld), L.c0, m.ib, m.lane, buf, bar, m.ie - m.ib + 3);
 }
 

@@ -79,6 +79,27 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// A warp's slice of the CTA's dynamic shared memory: the S stages of its row
+// ring, then S mbarriers, rounded up to 128 bytes so that the stages of every
+// warp stay 128-byte aligned, as tensor copies require.  Warp w's slice
+// starts at w times the kernel's per-warp stride: its loader's own size in
+// the step kernels, the largest loader's in the batch's queue kernel.
+__host__ __device__ constexpr size_t warp_ring_bytes(int stages, uint32_t stage_bytes) {
+  return (size_t(stages) * stage_bytes + size_t(stages) * 8 + 127) / 128 * 128;
+}
+
+template <class Loader>
+__device__ __forceinline__ unsigned char* warp_slice(unsigned char* smem) {
+  return smem + size_t(threadIdx.x >> 5) * Loader::smem_bytes_per_warp();
+}
+
+// The ring of a slice: stages first, barriers after them.
+template <class Loader>
+__device__ __forceinline__ void slice_ring(unsigned char* slice, float*& buf, uint64_t*& bar) {
+  buf = reinterpret_cast<float*>(slice);
+  bar = reinterpret_cast<uint64_t*>(slice + size_t(Loader::kStages) * Loader::kStageBytes);
+}
+
 // Segment table: base pointer (element (0,0)) and row offset of each field.
 template <int NSEG>
 struct Segs {
@@ -89,7 +110,7 @@ struct Segs {
 template <int NSEG>
 struct DirectRows {
   static constexpr int kStages = 0;
-  static constexpr size_t smem_bytes_per_warp() { return 0; }
+  __host__ __device__ static constexpr size_t smem_bytes_per_warp() { return 0; }
   Segs<NSEG> s;
   size_t ld;
   int c0, ib;
@@ -120,7 +141,9 @@ struct BulkRows {
   static constexpr int kAhead = S - 1 - KEEP;
   static constexpr int kStages = S;
   static constexpr uint32_t kStageBytes = NSEG * kSegFloats * sizeof(float);
-  static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
+  __host__ __device__ static constexpr size_t smem_bytes_per_warp() {
+    return warp_ring_bytes(S, kStageBytes);
+  }
   Segs<NSEG> s;      // serial issue: every segment's field
   const float* src;  // lane issue, lane q < NSEG: segment q's field at row 0, the warp's first column
   int roff;          // lane issue, lane q < NSEG: segment q's row offset
@@ -135,8 +158,8 @@ struct BulkRows {
   uint32_t extra = 0;         // test hook: bytes armed on stage 0 beyond its copies
   __device__ BulkRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int lane_, float* buf_,
                       uint64_t* bar_, int nk_)
-      : s(segs), src(nullptr), roff(0), ld(ld_), col0(c0_ - 4 * lane_), ib(ib_), lane(lane_), nk(nk_), cur(0), nxt(0), par(0),
-        buf(buf_), bar(bar_) {
+      : s(segs), src(nullptr), roff(0), ld(ld_), col0(c0_ - 4 * lane_), ib(ib_), lane(lane_), nk(nk_), cur(0),
+        nxt(0), par(0), buf(buf_), bar(bar_) {
     if constexpr (kLaneIssue) {
 #pragma unroll
       for (int q = 0; q < NSEG; ++q)

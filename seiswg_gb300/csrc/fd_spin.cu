@@ -191,7 +191,7 @@ __device__ __forceinline__ void spin_march(const PsvStep& p, int gw, unsigned ch
 template <class Loader>
 __global__ void __launch_bounds__(kStepWarps * 32) psv_spin_step_kernel(const PsvStep p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  spin_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), smem);
+  spin_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<Loader>(smem));
 }
 
 namespace {

@@ -102,7 +102,9 @@ struct TmaRows {
     for (int kk = k; kk <= k + kAhead && kk < nk; ++kk) (void)mbar_wait(&bar[kk % S], uint32_t(kk / S) & 1u, lim);
     __syncwarp();
   }
-  static constexpr size_t smem_bytes_per_warp() { return size_t(S) * kStageBytes + size_t(S) * 8; }
+  __host__ __device__ static constexpr size_t smem_bytes_per_warp() {
+    return warp_ring_bytes(S, kStageBytes);
+  }
 };
 }  // namespace
 }  // namespace seiswg

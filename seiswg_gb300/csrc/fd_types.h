@@ -73,4 +73,22 @@ constexpr int kAdjStages = 2;   // stages of the adjoint kernels (19 row segment
 // Bits of the device error word.
 enum { kErrWaitTimeout = 1, kErrNonFiniteTraces = 2, kErrNonFiniteGradient = 4 };
 
+// Kinds of work of a batched job (batch_plan.h): one grouped launch per
+// (schedule slot, kind), or the kind of a queue operation.
+enum BatchKind { kFwdSh = 0, kFwdPsv, kFwd2Sh, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
+
+// The batch's device work queue (batch_plan.h, fd_queue.cu).  QueueOp: one
+// operation of a job -- its kind (BatchKind), step, slots and flags as in
+// GroupOp (fd_kernels.h) -- and `need`, the count of finished units that the
+// counter of every chunk its rows reach must show before one of its units
+// may start.  QueueUnit: unit `unit` (warp index strip + nstrips * chunk of
+// the operation's geometry; 0 for the misfit) of operation `op` of job `job`.
+struct QueueOp {
+  int kind, it, a, b, flags, need;
+};
+struct QueueUnit {
+  unsigned short job, unit;
+  unsigned op;
+};
+
 }  // namespace seiswg

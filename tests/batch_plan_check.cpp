@@ -28,11 +28,30 @@
 // replayed on S + 2 slots (every reverse step finds its state, recomputation
 // reads the state of its step, slot 0 keeps the zero state), and the steps
 // recomputed must equal F(nt, S-1) - (nt - 1) exactly.
-// Prints "ok <cases> <mixes> <revolve cases>" and exits 0, or prints the
-// first violation and exits 1.
+// Launch order 3, the device queue (plan_queue): random mixes of jobs (uniform
+// and binomial checkpointing, SH and PSV, one- and two-step recording,
+// uneven grids and chunk rows) are run by a discrete-event model of the
+// queue kernel -- W warps claim units in queue order, each claiming its next
+// unit as it starts one; a unit starts once the job's counters of the chunks
+// within `reach` of its chunk (all chunks, for the misfit) show its `need`,
+// runs for a random time and then counts itself on its chunk -- and every
+// unit's accesses are checked against the job's sequential program at the
+// rows the marches really touch (two-step: 9 rows above to 5 below the chunk;
+// one-step and reverse: 3 above, 2 below): a state or adjoint slot, the
+// probe histories, the adjoint sources and the gradients, per chunk.  Every
+// read must start after the last earlier write of its cell has ended, every
+// write after every earlier access of its cell has ended; the run must end
+// with every unit done (no deadlock).  Planted: a queue whose dependencies
+// cover only the unit's own chunk must be reported, and so must a queue with
+// a unit moved ahead of one it depends on, which deadlocks one warp.
+// Prints "ok <cases> <mixes> <revolve cases> <queue mixes>" and exits 0, or
+// prints the first violation and exits 1.
+#include <algorithm>
 #include <array>
 #include <cstdint>
 #include <cstdio>
+#include <map>
+#include <queue>
 #include <utility>
 #include <vector>
 
@@ -298,6 +317,243 @@ static int check_orders(int& mixes) {
   return 0;
 }
 
+// ---- launch order 3: the device queue ---------------------------------------
+
+struct QJob {
+  int nx, lx, nchunks, nstrips1, nstrips2;
+  std::vector<HostOp> ops;
+};
+
+// Buffers of a job: pool slots 0..63, adjoint slots 64, 65, the probe
+// histories 66, the adjoint sources 67 (one cell), the gradients 68.
+enum { kBufAdj = 64, kBufProbe = 66, kBufU = 67, kBufGrad = 68 };
+
+struct Access {
+  int buf, c0, c1;  // chunks [c0, c1)
+  bool write;
+};
+
+// The cells a unit of operation o at chunk c touches (chunks of the rows the
+// march reads or writes).
+static std::vector<Access> unit_accesses(const QJob& J, const HostOp& o, int c) {
+  std::vector<Access> A;
+  const int ib = c * J.lx, ie = std::min(J.nx, ib + J.lx);
+  auto span = [&](int above, int below) {
+    const int lo = std::max(0, ib - above), hi = std::min(J.nx - 1, ie - 1 + below);
+    return std::make_pair(lo / J.lx, hi / J.lx + 1);
+  };
+  if (o.kind == kMisfit) {
+    A.push_back({kBufProbe, 0, J.nchunks, false});
+    A.push_back({kBufU, 0, 1, true});
+  } else if (o.kind == kAdjSh || o.kind == kAdjPsv) {
+    const auto r = span(3, 2);
+    A.push_back({o.a, r.first, r.second, false});
+    A.push_back({kBufAdj + (o.b & 1), r.first, r.second, false});
+    A.push_back({kBufU, 0, 1, false});
+    A.push_back({kBufGrad, c, c + 1, true});  // read, modified and written by the unit alone
+    A.push_back({kBufAdj + 1 - (o.b & 1), c, c + 1, true});
+  } else {
+    const bool two = o.kind == kFwd2Sh || o.kind == kFwd2Psv;
+    const auto r = two ? span(9, 5) : span(3, 2);
+    A.push_back({o.a, r.first, r.second, false});
+    A.push_back({o.b, c, c + 1, true});
+    if (o.flags & 1) A.push_back({kBufProbe, c, c + 1, true});  // accumulators: the unit's own rows
+  }
+  return A;
+}
+
+// Runs the queue with W warps and random unit times (seeded), then checks
+// the access order.  reach_override >= 0 replaces every job's reach (the
+// planted mistake).  Returns 0, 1 (hazard) or 2 (deadlock).
+static int replay_queue(const std::vector<QJob>& jobs, const QueuePlan& Q, int W, int reach_override) {
+  const size_t nu = Q.units.size();
+  std::vector<std::vector<int>> cnt(jobs.size());
+  for (size_t q = 0; q < jobs.size(); ++q) cnt[q].assign(size_t(jobs[q].nchunks), 0);
+  std::vector<double> t_start(nu, -1.0), t_end(nu, -1.0);
+  auto chunk_of = [&](const QueueUnit& u) {
+    const QJob& J = jobs[u.job];
+    const HostOp& o = J.ops[u.op];
+    if (o.kind == kMisfit) return 0;
+    return int(u.unit) / ((o.kind == kFwd2Sh || o.kind == kFwd2Psv) ? J.nstrips2 : J.nstrips1);
+  };
+  auto ready = [&](size_t p) {
+    const QueueUnit& u = Q.units[p];
+    const QJob& J = jobs[u.job];
+    const QueueOp& op = Q.ops[u.job][u.op];
+    const int reach = reach_override >= 0 ? reach_override : queue_reach(J.lx);
+    int c0 = 0, c1 = J.nchunks;
+    if (op.kind != kMisfit) {
+      const int c = chunk_of(u);
+      c0 = std::max(0, c - reach);
+      c1 = std::min(J.nchunks, c + reach + 1);
+    }
+    for (int c = c0; c < c1; ++c)
+      if (cnt[u.job][size_t(c)] < op.need) return false;
+    return true;
+  };
+  // Warps: the unit held (claimed, not started or running) and the next.
+  struct W8 { long long cur = -1, next = -1; bool running = false; };
+  std::vector<W8> warps(static_cast<size_t>(W));
+  long long claim = 0;
+  auto take = [&]() -> long long { return claim < (long long)nu ? claim++ : -1; };
+  for (W8& w : warps) w.cur = take();
+  using Ev = std::pair<double, int>;  // (end time, warp)
+  std::priority_queue<Ev, std::vector<Ev>, std::greater<Ev>> evq;
+  double now = 0.0;
+  size_t done = 0;
+  for (;;) {
+    // Start every waiting warp whose unit is ready (in warp order).
+    bool progress = true;
+    while (progress) {
+      progress = false;
+      for (int w = 0; w < W; ++w) {
+        W8& s = warps[size_t(w)];
+        if (s.running || s.cur < 0 || !ready(size_t(s.cur))) continue;
+        s.running = true;
+        s.next = take();  // claimed as the unit starts, as the kernel does
+        t_start[size_t(s.cur)] = now;
+        evq.push({now + 1.0 + rnd(1000) / 100.0, w});
+        progress = true;
+      }
+    }
+    if (evq.empty()) break;
+    const Ev e = evq.top();
+    evq.pop();
+    now = e.first;
+    W8& s = warps[size_t(e.second)];
+    const size_t p = size_t(s.cur);
+    t_end[p] = now;
+    ++done;
+    const QueueUnit& u = Q.units[p];
+    if (jobs[u.job].ops[u.op].kind == kMisfit) {
+      for (int& c : cnt[u.job]) ++c;
+    } else {
+      ++cnt[u.job][size_t(chunk_of(u))];
+    }
+    s.running = false;
+    s.cur = s.next;
+    s.next = -1;
+  }
+  if (done != nu) return 2;
+  // Per job and cell, the accesses in program order: every access must start
+  // after the conflicting accesses of earlier operations have ended.
+  for (size_t q = 0; q < jobs.size(); ++q) {
+    const QJob& J = jobs[q];
+    // cell -> per operation: (min start, max end) of its reading and of its writing units
+    struct OpAcc { double rs = 1e300, re = -1.0, ws = 1e300, we = -1.0; };
+    std::map<std::pair<int, int>, std::map<int, OpAcc>> cells;
+    for (size_t p = 0; p < nu; ++p) {
+      const QueueUnit& u = Q.units[p];
+      if (u.job != q) continue;
+      for (const Access& a : unit_accesses(J, J.ops[u.op], chunk_of(u)))
+        for (int c = a.c0; c < a.c1; ++c) {
+          OpAcc& x = cells[{a.buf, c}][int(u.op)];
+          if (a.write) { x.ws = std::min(x.ws, t_start[p]); x.we = std::max(x.we, t_end[p]); }
+          else { x.rs = std::min(x.rs, t_start[p]); x.re = std::max(x.re, t_end[p]); }
+        }
+    }
+    for (const auto& cell : cells) {
+      double last_write_end = -1.0, reads_end = -1.0;
+      for (const auto& oa : cell.second) {
+        const OpAcc& x = oa.second;
+        if (x.re >= 0.0 && x.rs < last_write_end) {
+          if (!quiet)
+            std::printf("job %zu buffer %d chunk %d: op %d reads before the last write ended\n", q, cell.first.first,
+                        cell.first.second, oa.first);
+          return 1;
+        }
+        if (x.we >= 0.0) {
+          if (x.ws < last_write_end || x.ws < reads_end) {
+            if (!quiet)
+              std::printf("job %zu buffer %d chunk %d: op %d writes before earlier accesses ended\n", q,
+                          cell.first.first, cell.first.second, oa.first);
+            return 1;
+          }
+          last_write_end = x.we;
+          reads_end = -1.0;
+        }
+        if (x.re >= 0.0) reads_end = std::max(reads_end, x.re);
+      }
+    }
+  }
+  return 0;
+}
+
+static QJob random_qjob() {
+  QJob J;
+  J.nx = 12 + rnd(120);
+  const int lxs[] = {4, 5, 8, 9, 12, 16, 32};
+  J.lx = lxs[rnd(7)];
+  J.nchunks = (J.nx + J.lx - 1) / J.lx;
+  J.nstrips1 = 1 + rnd(3);
+  J.nstrips2 = 1 + rnd(3);
+  const int nt = 1 + rnd(24);
+  const bool psv = rnd(2) != 0, two = rnd(2) != 0;
+  if (rnd(3) == 0) J.ops = job_ops_revolve(nt, 1 + rnd(5), psv, two);
+  else J.ops = job_ops(nt, 1 + rnd(nt), psv, two);
+  return J;
+}
+
+static QueuePlan plan_of(const std::vector<QJob>& jobs) {
+  std::vector<std::vector<HostOp>> lists;
+  std::vector<QueueShape> shapes;
+  for (const QJob& J : jobs) {
+    lists.push_back(J.ops);
+    shapes.push_back(QueueShape{J.nchunks, J.lx, J.nstrips1, J.nstrips2});
+  }
+  return plan_queue(lists, shapes);
+}
+
+static int check_queue(int& mixes) {
+  for (int m = 0; m < 1500; ++m) {
+    std::vector<QJob> jobs;
+    const int nj = 1 + rnd(6);
+    for (int q = 0; q < nj; ++q) jobs.push_back(random_qjob());
+    const QueuePlan Q = plan_of(jobs);
+    // slot-major: every unit's operation index equals its slot
+    for (size_t t = 0; t + 1 < Q.slot_begin.size(); ++t)
+      for (long long p = Q.slot_begin[t]; p < Q.slot_begin[t + 1]; ++p)
+        if (Q.units[size_t(p)].op != t) {
+          std::printf("queue mix %d: unit %lld of slot %zu holds operation %u\n", m, p, t, Q.units[size_t(p)].op);
+          return 1;
+        }
+    const int W = 1 + rnd(48);
+    const int r = replay_queue(jobs, Q, W, -1);
+    if (r) {
+      std::printf("queue mix %d (%d warps): %s\n", m, W, r == 2 ? "deadlock" : "access out of order");
+      return 1;
+    }
+    ++mixes;
+  }
+  // Planted: dependencies on the unit's own chunk only (reach 0) must give a
+  // hazard in a multi-chunk two-step job run by many warps.
+  quiet = true;
+  {
+    QJob J;
+    J.nx = 96; J.lx = 8; J.nchunks = 12; J.nstrips1 = 2; J.nstrips2 = 2;
+    J.ops = job_ops(20, 4, true, true);
+    const std::vector<QJob> jobs{J};
+    const QueuePlan Q = plan_of(jobs);
+    bool caught = false;
+    for (int trial = 0; trial < 20 && !caught; ++trial) caught = replay_queue(jobs, Q, 32, 0) == 1;
+    if (!caught) {
+      std::printf("the queue replay misses a dependency that does not cover the rows read\n");
+      return 1;
+    }
+    // A unit of operation 1 moved to the front: with one warp it waits for
+    // operation 0, which no warp can reach.
+    QueuePlan bad = Q;
+    const long long p1 = bad.slot_begin[1];
+    std::rotate(bad.units.begin(), bad.units.begin() + p1, bad.units.begin() + p1 + 1);
+    if (replay_queue(jobs, bad, 1, -1) != 2) {
+      std::printf("the queue replay misses a deadlock\n");
+      return 1;
+    }
+  }
+  quiet = false;
+  return 0;
+}
+
 int main() {
   if (!catches_planted_mistakes()) {
     std::printf("the replay misses a planted mistake\n");
@@ -323,6 +579,8 @@ int main() {
   if (check_orders(mixes)) return 1;
   int rcases = 0;
   if (check_revolve(rcases)) return 1;
-  std::printf("ok %d %d %d\n", cases, mixes, rcases);
+  int qmixes = 0;
+  if (check_queue(qmixes)) return 1;
+  std::printf("ok %d %d %d %d\n", cases, mixes, rcases, qmixes);
   return 0;
 }

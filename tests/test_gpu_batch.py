@@ -1,8 +1,9 @@
-"""Batched gradients of uneven problems (grouped launches under one CUDA
-graph, on-device misfit) against the plain per-shot path, problem by
-problem.  The tolerance is the gradient accuracy the batched configuration
-asks for, relative L2 1e-4; the two paths share their kernels, so they agree
-far closer."""
+"""Batched gradients of uneven problems (by default one persistent launch over
+a device work queue, else grouped launches; one CUDA graph per run, misfit on
+the device) against the plain per-shot path, problem by problem.  The
+tolerance is the gradient accuracy the batched configuration asks for,
+relative L2 1e-4; the two paths share their marches, so they agree far
+closer."""
 import numpy as np
 import pytest
 
@@ -124,18 +125,37 @@ def test_chunk_rows_and_autotune_leave_gradients_unchanged():
 
 
 def test_launch_orders_give_the_same_gradients():
-    """Serial launches, a slot's kinds on forked streams, and one stream per
-    kind (and job group) with cross-kind waits only where a job changes kind,
-    rows by tensor copies or by bulk copies: the same cell updates in an
-    order the dependencies allow, so the gradients are bitwise equal (a
-    missing dependency would show as a difference)."""
+    """The grouped launch orders -- serial launches, a slot's kinds on forked
+    streams, and one stream per kind (and job group) with cross-kind waits
+    only where a job changes kind, rows by tensor copies or by bulk copies --
+    make the same cell updates in an order the dependencies allow, so their
+    gradients are bitwise equal (a missing dependency would show as a
+    difference).  The device queue (order 3, the default) gives the same bits
+    with tensor or bulk copies, run after run, and agrees with the grouped
+    launches to rounding: it builds its one-step recomputation with
+    multiply-add contraction."""
     import seiswg_gb300 as sw
 
     probs = _problems()
     sims = [w.make_sim() for (w, _, _) in probs]
     batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
     try:
-        assert batch.info()["concurrent"] == 2   # the default
+        info = batch.info()
+        assert info["concurrent"] == 3   # the default: one persistent launch over the device queue
+        assert info["queue_units"] > 0 and info["queue_blocks"] > 0
+        queue = None
+        for tma in (1, 0, 1):
+            batch.set_option("tma", tma)
+            batch.run()
+            g = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
+            J = [batch.misfit(i) for i in range(len(probs))]
+            if queue is None:
+                queue = (g, J)
+                continue
+            assert J == queue[1], tma
+            for i in range(len(probs)):
+                for p in g[i]:
+                    assert np.array_equal(g[i][p], queue[0][i][p]), ("queue", tma, i, p)
         ref = None
         for mode, groups, tma in ((0, 1, 1), (1, 1, 1), (2, 1, 1), (2, 1, 1), (2, 2, 1), (2, 4, 1), (1, 3, 1),
                                   (2, 1, 0)):
@@ -147,6 +167,7 @@ def test_launch_orders_give_the_same_gradients():
             batch.run()                          # (2, 1) twice: the second run replays the graph
             g = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
             J = [batch.misfit(i) for i in range(len(probs))]
+            assert batch.info()["queue_units"] == 0
             if ref is None:
                 ref = (g, J)
                 continue
@@ -154,7 +175,13 @@ def test_launch_orders_give_the_same_gradients():
             for i in range(len(probs)):
                 for p in g[i]:
                     assert np.array_equal(g[i][p], ref[0][i][p]), (mode, i, p)
-        for key, bad in (("concurrent", 3), ("stream_groups", 0), ("stream_groups", 5)):
+        for i in range(len(probs)):
+            assert abs(queue[1][i] - ref[1][i]) <= 1e-6 * ref[1][i]
+            params = ("lambda", "mu", "buoyancy") if probs[i][0].flags["psv"] else ("mu", "buoyancy")
+            for p in params:
+                assert rel_l2(queue[0][i][p], ref[0][i][p]) <= 1e-5, ("queue vs grouped", i, p)
+        for key, bad in (("concurrent", 4), ("concurrent", -1), ("stream_groups", 0), ("stream_groups", 5),
+                         ("queue_wait_us", 0), ("test_queue_need_extra", -1)):
             with pytest.raises(sw.SeiswgError):
                 batch.set_option(key, bad)
     finally:
@@ -196,3 +223,33 @@ def test_batch_binomial_checkpointing_gives_the_same_gradients():
     batch.close()
     for s in sims:
         s.close()
+
+
+def test_queue_wait_expiry_reports_a_timeout_and_the_batch_recovers():
+    """The queue kernel's dependency waits are bounded.  With the test hook
+    adding one to every dependency after a job's first operation, no such
+    wait can be met: each runs out after queue_wait_us, the run fails with
+    SEISWG_ETIMEOUT, and no GPU fault or hang results.  With the hook off the
+    same batch runs again and gives the gradients of a run before."""
+    import seiswg_gb300 as sw
+
+    probs = _problems()[:2]
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    try:
+        batch.run()
+        ref = [batch.gradient(i, "mu") for i in range(len(probs))]
+        batch.set_option("queue_wait_us", 2000)
+        batch.set_option("test_queue_need_extra", 1)
+        with pytest.raises(sw.SeiswgError) as e:
+            batch.run()
+        assert e.value.code == sw.ETIMEOUT
+        batch.set_option("test_queue_need_extra", 0)
+        batch.set_option("queue_wait_us", 2000000)
+        batch.run()
+        for i in range(len(probs)):
+            assert np.array_equal(batch.gradient(i, "mu"), ref[i]), i
+    finally:
+        batch.close()
+        for s in sims:
+            s.close()
