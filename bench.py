@@ -663,7 +663,8 @@ def run_secondary(args):
                                              f"gradient, every step's strains kept, OpenMP), {dtm:.1f} s; "
                                              f"extrapolated to {nshot} shots x {W.nt} steps by cell-updates"}
     elif args.workload == "c5":
-        problems = configs.c5_batch(count=args.count)
+        problems = configs.c5_batch(count=args.count, lo=min(256, args.c5_hi), hi=args.c5_hi,
+                                    nt_lo=min(1000, args.c5_nt_hi), nt_hi=args.c5_nt_hi)
         comps = [[0, 2] if w.flags["psv"] else [1] for w in problems]
         obs = []
         for w, c in zip(problems, comps):   # observed data from the true models (untimed)
@@ -702,6 +703,8 @@ def run_secondary(args):
             batch.set_option("stream_groups", args.stream_groups)
         if args.tma >= 0:
             batch.set_option("tma", args.tma)
+        if args.queue_band >= 0:
+            batch.set_option("queue_band", args.queue_band)
         if args.checkpoint_slots:
             batch.set_option("checkpoint_slots", args.checkpoint_slots)
         tune_ms = None
@@ -733,7 +736,8 @@ def run_secondary(args):
                    plain={"problem_gradients_per_s": len(problems) / plain_s, "shot_gradients_per_s": nshots / plain_s,
                           "gcell_updates_per_s": cells / plain_s / 1e9, "seconds": plain_s},
                    speedup=plain_s / wall, max_rel_l2_mu_vs_plain=max(errs),
-                   config={"workload": f"c5: {len(problems)} problems, 256..1536 per axis, nt 1000..3000, SH/PSV, "
+                   config={"workload": f"c5: {len(problems)} problems, {min(256, args.c5_hi)}..{args.c5_hi} per axis, "
+                                       f"nt {min(1000, args.c5_nt_hi)}..{args.c5_nt_hi}, SH/PSV, "
                                        "1-4 shots",
                            "jobs": info["jobs"], "slots": info["slots"], "launches_per_run": info["launches_per_run"],
                            "device_bytes": info["device_bytes"],
@@ -743,6 +747,7 @@ def run_secondary(args):
                            "chunk_rows": info.get("chunk_rows"), "two_step_recording": info.get("two_step"),
                            "concurrent": info.get("concurrent"), "stream_groups": info.get("stream_groups"),
                            "queue_units": info.get("queue_units"), "queue_blocks": info.get("queue_blocks"),
+                           "queue_band": info.get("queue_band"),
                            "tma_jobs": info.get("tma_jobs"), "autotune_ms": tune_ms},
                    clocks=clk.summary())
         if not args.no_cpu:
@@ -785,10 +790,16 @@ def main():
     ap.add_argument("--tma", type=int, default=-1,
                     help="c2, c4, c5: rows of the two-step and reverse kernels by tensor copies (1) or bulk copies (0)")
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
+    ap.add_argument("--c5-hi", type=int, default=1536,
+                    help="c5: largest grid edge (1536 = the configuration; smaller for profiling captures)")
+    ap.add_argument("--c5-nt-hi", type=int, default=3000,
+                    help="c5: most time steps (3000 = the configuration; smaller for profiling captures)")
+    ap.add_argument("--queue-band", type=int, default=-1,
+                    help="c5: slots per band of the device queue's order (0 slot-major; -1: the default)")
     ap.add_argument("--stream-groups", type=int, default=0, help="c5: job groups with their own streams (0: default)")
     ap.add_argument("--concurrent", type=int, default=-1,
                     help="c5: 0 serial grouped launches, 1 a slot's kinds on forked streams, 2 one stream per "
-                         "kind, 3 one persistent launch over a device queue (-1: the default, 3)")
+                         "kind, 3 one persistent launch over a device queue (-1: the default, 2)")
     ap.add_argument("--fd-check", type=int, default=0, help="c4: finite-difference check on this many cells")
     ap.add_argument("--checkpoint-slots", type=int, default=0,
                     help="c4, c5: binomial checkpointing with this many stored states (per shot / per job)")

@@ -263,13 +263,17 @@ int seiswg_batch_run(seiswg_batch* batch);
  * slots); "concurrent": how the schedule runs -- as grouped launches (one
  * per schedule slot and kind of work: SH/PSV forward, reverse, misfit), 0
  * one after another, 1 a slot's launches on forked streams that join before
- * the next slot, 2 one stream per kind, a launch waiting only for the
- * previous slot's launches of the kinds its jobs come from; or 3 (default)
- * as one persistent launch whose warps work through a device queue of every
+ * the next slot, 2 (default) one stream per kind, a launch waiting only for
+ * the previous slot's launches of the kinds its jobs come from; or 3 as one
+ * persistent launch whose warps work through a device queue of every
  * job's units (one warp's march over one strip and chunk of one operation),
  * each unit waiting only for the chunks its rows reach of its job's previous
  * operation; "queue_wait_us" (order 3, default 2 s): the bound of one such
- * wait, after which the run fails with SEISWG_ETIMEOUT;
+ * wait, after which the run fails with SEISWG_ETIMEOUT; "queue_band" (order
+ * 3, default 0): the queue's units slot after slot (0), or in bands of that
+ * many slots within which each job's units run diagonally across its
+ * operations and chunks, so that an operation reads the rows the previous
+ * one wrote while they are still in L2;
  * "test_queue_need_extra" (a test hook, default 0): added to every such
  * dependency after a job's first operation, so that those waits run out;
  * "stream_groups" (1..4, default 1): jobs split round-robin into
@@ -293,8 +297,9 @@ int32_t seiswg_batch_two_step(const seiswg_batch* batch);
 int32_t seiswg_batch_concurrent(const seiswg_batch* batch);
 int32_t seiswg_batch_stream_groups(const seiswg_batch* batch);
 /* Launch order 3: the units in the device queue and the CTAs of the
- * persistent launch (0 and 0 in the other orders). */
-int seiswg_batch_queue(const seiswg_batch* batch, int64_t* units, int32_t* blocks);
+ * persistent launch (0 and 0 in the other orders), and the "queue_band"
+ * option. */
+int seiswg_batch_queue(const seiswg_batch* batch, int64_t* units, int32_t* blocks, int32_t* band);
 /* Jobs whose grouped launches fetch rows by tensor copies (0 with "tma" 0). */
 int32_t seiswg_batch_tma_jobs(const seiswg_batch* batch);
 /* param: "lambda", "mu" or "buoyancy"; nx*nz values of the problem. */

@@ -115,7 +115,7 @@ PROTOTYPES = [
     ("seiswg_batch_concurrent", _i32, [_vp]),
     ("seiswg_batch_stream_groups", _i32, [_vp]),
     ("seiswg_batch_tma_jobs", _i32, [_vp]),
-    ("seiswg_batch_queue", _i32, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_i32)]),
+    ("seiswg_batch_queue", _i32, [_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
     ("seiswg_batch_checkpoint_plan", _c_int, [_vp, _pi, ctypes.POINTER(ctypes.c_int64)]),
     ("seiswg_batch_gradient", _c_int, [_vp, _i32, _cp, _pf]),
     ("seiswg_batch_misfit", ctypes.c_double, [_vp, _i32]),
@@ -482,7 +482,8 @@ class Batch:
         """"chunk_rows" (0: per-problem model), "two_step" (0/1), "concurrent" (0, 1, 2: grouped
         launches in that order; 3: one persistent launch over a device queue), "stream_groups" (1..4),
         "tma" (0/1: rows of the two-step and reverse marches by tensor copies or bulk copies),
-        "queue_wait_us" (bound of a queue dependency wait), "test_queue_need_extra" (test hook),
+        "queue_wait_us" (bound of a queue dependency wait), "queue_band" (slots per band of the queue's
+        order, 0: slot-major), "test_queue_need_extra" (test hook),
         "checkpoint_slots" or "autotune" (slots per timing window)."""
         _check(lib().seiswg_batch_set_option(self._h, key.encode(), int(value)))
 
@@ -506,11 +507,11 @@ class Batch:
                     tma_jobs=int(lib().seiswg_batch_tma_jobs(self._h)), **self.queue(), **self.checkpoint_plan())
 
     def queue(self):
-        """dict(queue_units = units in the device queue, queue_blocks = CTAs of the persistent launch);
-        both 0 outside launch order 3."""
-        u, b = ctypes.c_int64(), _i32()
-        _check(lib().seiswg_batch_queue(self._h, ctypes.byref(u), ctypes.byref(b)))
-        return dict(queue_units=u.value, queue_blocks=b.value)
+        """dict(queue_units = units in the device queue, queue_blocks = CTAs of the persistent launch
+        (both 0 outside launch order 3), queue_band = slots per band of the queue's order)."""
+        u, b, k = ctypes.c_int64(), _i32(), _i32()
+        _check(lib().seiswg_batch_queue(self._h, ctypes.byref(u), ctypes.byref(b), ctypes.byref(k)))
+        return dict(queue_units=u.value, queue_blocks=b.value, queue_band=k.value)
 
     def checkpoint_plan(self):
         """dict(checkpoint_slots = binomial slots per job (0: uniform),

@@ -372,7 +372,7 @@ void Batch::build_queue(const std::vector<std::vector<HostOp>>& lists) {
       throw std::logic_error("the device queue needs the same chunks for a job's one- and two-step geometries");
     shapes.push_back(QueueShape{d.g.nchunks, d.g.lx, d.g.nstrips, d.g2.lx > 0 ? d.g2.nstrips : d.g.nstrips});
   }
-  QueuePlan Q = plan_queue(lists, shapes);
+  QueuePlan Q = plan_queue(lists, shapes, queue_band_);
   std::vector<QueueOp> ops;
   std::vector<size_t> op_off;
   need_at_.assign(jobs_.size(), {});
@@ -436,13 +436,18 @@ void Batch::free_queue() {
   queue_blocks_ = 0;
 }
 
-// The units of slots [t0, t1) as one launch.  Every job's counters start at
-// the count its first operation at or after slot t0 waits for, as if the
-// slots before t0 had run (the autotuner's windows; a whole run starts at 0).
+// The units of slots [t0, t1), widened to whole bands, as one launch.  Every
+// job's counters start at the count its first operation at or after slot t0
+// waits for, as if the slots before t0 had run (the autotuner's windows; a
+// whole run starts at 0).
 void Batch::enqueue_queue(int t0, int t1) {
   t0 = std::max(0, t0);
   t1 = std::min(t1, nslots_);
   if (t0 >= t1 || !d_units_) return;
+  if (queue_band_ > 0) {
+    t0 -= t0 % queue_band_;
+    t1 = std::min(nslots_, (t1 + queue_band_ - 1) / queue_band_ * queue_band_);
+  }
   if (t0 == 0) {
     SW_CUDA(cudaMemsetAsync(d_qcnt_, 0, std::max(1, ncnt_) * sizeof(int), stream_));
     SW_CUDA(cudaMemsetAsync(d_next_, 0, sizeof(unsigned long long), stream_));
@@ -467,6 +472,12 @@ void Batch::set_queue_wait_ns(unsigned long long ns) {
   queue_wait_ns_ = ns;
   if (graph_) cudaGraphExecDestroy(graph_);
   graph_ = nullptr;
+}
+
+void Batch::set_queue_band(int slots) {
+  if (slots < 0) throw std::invalid_argument("queue_band must be >= 0");
+  queue_band_ = slots;
+  set_chunk_rows(chunk_rows_);  // rebuilds the schedule, drops the graph
 }
 
 void Batch::set_queue_need_extra(int n) {

@@ -57,7 +57,7 @@ class Batch {
   // after another on the batch's stream.  1: the launches of one slot run
   // concurrently on forked streams that join before the next slot.  2: one
   // stream per kind; a launch waits only for the previous slot's launches of
-  // the kinds its jobs come from, so the kinds pipeline.  3 (default): one
+  // the kinds its jobs come from, so the kinds pipeline (default).  3: one
   // persistent launch over a device work queue of every job's units
   // (fd_queue.cu, plan_queue in batch_plan.h); the one- and two-step
   // geometries of a job then share their rows per chunk (the larger of the
@@ -95,6 +95,10 @@ class Batch {
   // first operation so that those waits run out (0 normally).
   void set_queue_wait_ns(unsigned long long ns);
   void set_queue_need_extra(int n);
+  // Launch order 3: slots per band of the queue's order (plan_queue; 0:
+  // slot-major).  Rebuilds the schedule.
+  void set_queue_band(int slots);
+  int queue_band() const { return queue_band_; }
   // Units in the device queue (0 outside launch order 3) and its CTAs.
   long long queue_units() const { return nunits_; }
   int queue_blocks() const { return queue_blocks_; }
@@ -136,7 +140,7 @@ class Batch {
   std::vector<Job> jobs_;
   cudaStream_t stream_;
   bool own_stream_ = false;
-  int concurrent_ = 3;
+  int concurrent_ = 2;
   bool tma_ = true;   // grouped launches fetch rows by tensor copies where the job has a map table
   int groups_ = 1;
   std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
@@ -182,6 +186,7 @@ class Batch {
   bool queue_tma_ = false;
   unsigned long long queue_wait_ns_ = 2000000000ull;
   int queue_need_extra_ = 0;
+  int queue_band_ = 0;
 };
 
 }  // namespace seiswg

@@ -8,6 +8,7 @@
 // - 1 and ncp + k the recording pass's states between checkpoints.
 #pragma once
 
+#include <algorithm>
 #include <stdexcept>
 #include <utility>
 #include <vector>
@@ -259,8 +260,12 @@ inline std::vector<std::vector<PlanLaunch>> plan_launches(const std::vector<std:
 // the misfit.  The one- and two-step geometries of a job share their chunks
 // (the same rows per chunk), so a chunk names the same rows for every kind.
 // Units are laid out slot-major -- slot t holds operation t of every job,
-// kinds in BatchKind order, jobs in index order, units in index order -- so
-// that every unit a unit depends on comes earlier in the queue.  A job keeps
+// kinds in BatchKind order, jobs in index order, units in index order -- or
+// in bands of `band` slots, within which each job's units follow a diagonal
+// across its operations and chunks (plan_queue), so that operation t+1 of a
+// chunk comes soon after operation t of the chunks below it and finds their
+// rows still in L2.  Either way every unit a unit depends on comes earlier in
+// the queue.  A job keeps
 // one counter of finished units per chunk; the units of its operation t wait
 // until the counter of every chunk within `reach` chunks of theirs (of every
 // chunk, for the misfit) shows need[t], the units per chunk of operations
@@ -297,10 +302,22 @@ inline int queue_units(int kind, const QueueShape& s) {
 struct QueuePlan {
   std::vector<std::vector<QueueOp>> ops;  // per job, its operations with their `need`
   std::vector<QueueUnit> units;           // the queue
-  std::vector<long long> slot_begin;      // first unit of each slot, then units.size()
+  // First unit of each slot's band (of each slot, slot-major), then
+  // units.size(): the units of slots [t0, t1) are [slot_begin[t0],
+  // slot_begin[t1]) when t0 and t1 start bands.
+  std::vector<long long> slot_begin;
 };
 
-inline QueuePlan plan_queue(const std::vector<std::vector<HostOp>>& lists, const std::vector<QueueShape>& shapes) {
+// band 0: slot-major.  band K > 0: slots [bK, (b+1)K) form band b; a job's
+// unit of operation t and chunk c in the band gets the key
+//   c + (R + 1) (t - bK) + N m,
+// R its reach in chunks, N its chunks and m the misfits of the job in the
+// band before t (a misfit gets N - 1 + (R + 1) (t - bK) + N m), and the
+// band's units are ordered by key, then job, operation and unit.  A unit's
+// dependencies (operation t-1 within R chunks, or every chunk before a
+// misfit) have smaller keys or lie in an earlier band.
+inline QueuePlan plan_queue(const std::vector<std::vector<HostOp>>& lists, const std::vector<QueueShape>& shapes,
+                            int band = 0) {
   QueuePlan Q;
   const size_t nj = lists.size();
   if (nj > 65536) throw std::invalid_argument("the device queue holds at most 65536 jobs");
@@ -320,6 +337,36 @@ inline QueuePlan plan_queue(const std::vector<std::vector<HostOp>>& lists, const
   }
   Q.units.reserve(total);
   Q.slot_begin.reserve(T + 1);
+  if (band > 0) {
+    std::vector<std::pair<long long, QueueUnit>> v;
+    for (size_t t0 = 0; t0 < T; t0 += size_t(band)) {
+      const size_t t1 = std::min(T, t0 + size_t(band));
+      v.clear();
+      for (size_t q = 0; q < nj; ++q) {
+        const QueueShape& sh = shapes[q];
+        const long long R1 = queue_reach(sh.lx) + 1, N = sh.nchunks;
+        long long shift = 0;
+        for (size_t t = t0; t < std::min(t1, lists[q].size()); ++t) {
+          const int kind = lists[q][t].kind;
+          const long long tau = (long long)(t - t0);
+          if (kind == kMisfit) {
+            v.push_back({N - 1 + R1 * tau + shift, QueueUnit{(unsigned short)q, 0, unsigned(t)}});
+            shift += N;
+            continue;
+          }
+          const int ns = queue_units_per_chunk(kind, sh), n = queue_units(kind, sh);
+          for (int u = 0; u < n; ++u)
+            v.push_back({u / ns + R1 * tau + shift, QueueUnit{(unsigned short)q, (unsigned short)u, unsigned(t)}});
+        }
+      }
+      std::stable_sort(v.begin(), v.end(), [](const std::pair<long long, QueueUnit>& a,
+                                               const std::pair<long long, QueueUnit>& b) { return a.first < b.first; });
+      for (size_t t = t0; t < t1; ++t) Q.slot_begin.push_back((long long)Q.units.size());
+      for (const auto& e : v) Q.units.push_back(e.second);
+    }
+    Q.slot_begin.push_back((long long)Q.units.size());
+    return Q;
+  }
   for (size_t t = 0; t < T; ++t) {
     Q.slot_begin.push_back((long long)Q.units.size());
     for (int kind = 0; kind < kKinds; ++kind)

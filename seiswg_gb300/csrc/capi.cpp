@@ -547,6 +547,9 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "queue_wait_us") {
       if (value < 1 || value > (int64_t(1) << 40)) throw std::invalid_argument("queue_wait_us out of range");
       b->batch->set_queue_wait_ns((unsigned long long)value * 1000ull);
+    } else if (k == "queue_band") {
+      if (value < 0 || value > (1 << 20)) throw std::invalid_argument("queue_band out of range");
+      b->batch->set_queue_band(int(value));
     } else if (k == "test_queue_need_extra") {
       if (value < 0 || value > (1 << 30)) throw std::invalid_argument("test_queue_need_extra out of range");
       b->batch->set_queue_need_extra(int(value));
@@ -568,10 +571,11 @@ int32_t seiswg_batch_stream_groups(const seiswg_batch* b) { return b ? b->batch-
 
 int32_t seiswg_batch_tma_jobs(const seiswg_batch* b) { return b ? b->batch->tma_jobs() : 0; }
 
-int seiswg_batch_queue(const seiswg_batch* b, int64_t* units, int32_t* blocks) {
+int seiswg_batch_queue(const seiswg_batch* b, int64_t* units, int32_t* blocks, int32_t* band) {
   if (!b) return fail(SEISWG_EINVAL, "null batch");
   if (units) *units = b->batch->queue_units();
   if (blocks) *blocks = b->batch->queue_blocks();
+  if (band) *band = b->batch->queue_band();
   return SEISWG_OK;
 }
 

@@ -43,7 +43,8 @@
 // write after every earlier access of its cell has ended; the run must end
 // with every unit done (no deadlock).  Planted: a queue whose dependencies
 // cover only the unit's own chunk must be reported, and so must a queue with
-// a unit moved ahead of one it depends on, which deadlocks one warp.
+// a unit moved ahead of one it depends on, which deadlocks one warp.  The
+// queues are laid out slot-major or in diagonal bands of 1 to 64 slots.
 // Prints "ok <cases> <mixes> <revolve cases> <queue mixes>" and exits 0, or
 // prints the first violation and exits 1.
 #include <algorithm>
@@ -494,14 +495,14 @@ static QJob random_qjob() {
   return J;
 }
 
-static QueuePlan plan_of(const std::vector<QJob>& jobs) {
+static QueuePlan plan_of(const std::vector<QJob>& jobs, int band = 0) {
   std::vector<std::vector<HostOp>> lists;
   std::vector<QueueShape> shapes;
   for (const QJob& J : jobs) {
     lists.push_back(J.ops);
     shapes.push_back(QueueShape{J.nchunks, J.lx, J.nstrips1, J.nstrips2});
   }
-  return plan_queue(lists, shapes);
+  return plan_queue(lists, shapes, band);
 }
 
 static int check_queue(int& mixes) {
@@ -509,18 +510,26 @@ static int check_queue(int& mixes) {
     std::vector<QJob> jobs;
     const int nj = 1 + rnd(6);
     for (int q = 0; q < nj; ++q) jobs.push_back(random_qjob());
-    const QueuePlan Q = plan_of(jobs);
-    // slot-major: every unit's operation index equals its slot
-    for (size_t t = 0; t + 1 < Q.slot_begin.size(); ++t)
-      for (long long p = Q.slot_begin[t]; p < Q.slot_begin[t + 1]; ++p)
-        if (Q.units[size_t(p)].op != t) {
+    const int bands[] = {0, 0, 1, 2, 3, 5, 8, 64};
+    const int band = bands[rnd(8)];
+    const QueuePlan Q = plan_of(jobs, band);
+    // slot-major: every unit's operation index equals its slot; bands: every
+    // unit between two band starts holds an operation of that band
+    const size_t T = Q.slot_begin.size() - 1, B = band > 0 ? size_t(band) : 1;
+    for (size_t t = 0; t < T; t += B)
+      for (long long p = Q.slot_begin[t]; p < Q.slot_begin[std::min(T, t + B)]; ++p)
+        if (Q.units[size_t(p)].op < t || Q.units[size_t(p)].op >= t + B) {
           std::printf("queue mix %d: unit %lld of slot %zu holds operation %u\n", m, p, t, Q.units[size_t(p)].op);
           return 1;
         }
+    if (Q.units.size() != size_t(Q.slot_begin[T])) {
+      std::printf("queue mix %d: %zu units, the plan counts %lld\n", m, Q.units.size(), Q.slot_begin[T]);
+      return 1;
+    }
     const int W = 1 + rnd(48);
     const int r = replay_queue(jobs, Q, W, -1);
     if (r) {
-      std::printf("queue mix %d (%d warps): %s\n", m, W, r == 2 ? "deadlock" : "access out of order");
+      std::printf("queue mix %d (%d warps, band %d): %s\n", m, W, band, r == 2 ? "deadlock" : "access out of order");
       return 1;
     }
     ++mixes;

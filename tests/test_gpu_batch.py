@@ -130,7 +130,7 @@ def test_launch_orders_give_the_same_gradients():
     only where a job changes kind, rows by tensor copies or by bulk copies --
     make the same cell updates in an order the dependencies allow, so their
     gradients are bitwise equal (a missing dependency would show as a
-    difference).  The device queue (order 3, the default) gives the same bits
+    difference).  The device queue (order 3) gives the same bits
     with tensor or bulk copies, run after run, and agrees with the grouped
     launches to rounding: it builds its one-step recomputation with
     multiply-add contraction."""
@@ -140,8 +140,10 @@ def test_launch_orders_give_the_same_gradients():
     sims = [w.make_sim() for (w, _, _) in probs]
     batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
     try:
+        assert batch.info()["concurrent"] == 2   # the default
+        batch.set_option("concurrent", 3)        # one persistent launch over the device queue
         info = batch.info()
-        assert info["concurrent"] == 3   # the default: one persistent launch over the device queue
+        assert info["concurrent"] == 3 and info["queue_band"] == 0
         assert info["queue_units"] > 0 and info["queue_blocks"] > 0
         queue = None
         for tma in (1, 0, 1):
@@ -156,6 +158,13 @@ def test_launch_orders_give_the_same_gradients():
             for i in range(len(probs)):
                 for p in g[i]:
                     assert np.array_equal(g[i][p], queue[0][i][p]), ("queue", tma, i, p)
+        batch.set_option("queue_band", 4)        # diagonal bands of 4 slots: the same bits
+        assert batch.info()["queue_band"] == 4
+        batch.run()
+        for i in range(len(probs)):
+            assert batch.misfit(i) == queue[1][i]
+            for p in queue[0][i]:
+                assert np.array_equal(batch.gradient(i, p), queue[0][i][p]), ("band", i, p)
         ref = None
         for mode, groups, tma in ((0, 1, 1), (1, 1, 1), (2, 1, 1), (2, 1, 1), (2, 2, 1), (2, 4, 1), (1, 3, 1),
                                   (2, 1, 0)):
@@ -237,6 +246,7 @@ def test_queue_wait_expiry_reports_a_timeout_and_the_batch_recovers():
     sims = [w.make_sim() for (w, _, _) in probs]
     batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
     try:
+        batch.set_option("concurrent", 3)
         batch.run()
         ref = [batch.gradient(i, "mu") for i in range(len(probs))]
         batch.set_option("queue_wait_us", 2000)
