@@ -143,24 +143,32 @@ __device__ void queue_misfit(const JobDesc& J) {
   }
 }
 
-// The units of each kind, each in a function of its own (not inlined): the
-// queue loop's few live values are saved around the call, and each march
-// gets the registers it has in its own kernel instead of sharing one
-// allocation with every other kind.  False when a bounded wait expired.
-__device__ __noinline__ bool unit_psv1(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+// The units of each kind.  The job table is passed as a restrict pointer
+// (read-only for the whole launch), so that the march's parameters can be
+// reloaded from it instead of being spilled.  Built inline: as calls of
+// functions of their own they spilled more (each kind's march runs in a
+// kernel that holds every kind, at 255 registers).  False when a bounded
+// wait expired.
+__device__ __forceinline__ bool unit_psv1(const JobDesc* __restrict__ jobs, int job, const QueueOp op, int unit,
+                                          unsigned char* slice) {
+  const JobDesc& J = jobs[job];
   if (!psv_march<QPsv1>(job_psv_step(J, op.it, op.a, op.b, op.flags), unit, slice)) return false;
   inval_ring<QPsv1>(slice);
   return true;
 }
 
-__device__ __noinline__ bool unit_sh1(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+__device__ __forceinline__ bool unit_sh1(const JobDesc* __restrict__ jobs, int job, const QueueOp op, int unit,
+                                         unsigned char* slice) {
+  const JobDesc& J = jobs[job];
   if (!sh_march<QSh1>(job_sh_step(J, op.it, op.a, op.b, op.flags), unit, slice)) return false;
   inval_ring<QSh1>(slice);
   return true;
 }
 
 template <bool TMA>
-__device__ __noinline__ bool unit_psv2(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+__device__ __forceinline__ bool unit_psv2(const JobDesc* __restrict__ jobs, int job, const QueueOp op, int unit,
+                                          unsigned char* slice) {
+  const JobDesc& J = jobs[job];
   const PsvStep p = job_psv_step2(J, op.it, op.a, op.b, op.flags);
   if constexpr (TMA) {
     const Tma2Ptrs mp = job_psv2_maps(J, op.a);
@@ -174,7 +182,9 @@ __device__ __noinline__ bool unit_psv2(const JobDesc& J, const QueueOp& op, int 
 }
 
 template <bool TMA>
-__device__ __noinline__ bool unit_sh2(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+__device__ __forceinline__ bool unit_sh2(const JobDesc* __restrict__ jobs, int job, const QueueOp op, int unit,
+                                         unsigned char* slice) {
+  const JobDesc& J = jobs[job];
   const ShStep p = job_sh_step2(J, op.it, op.a, op.b, op.flags);
   if constexpr (TMA) {
     const Tma2Ptrs mp = job_sh2_maps(J, op.a);
@@ -188,7 +198,9 @@ __device__ __noinline__ bool unit_sh2(const JobDesc& J, const QueueOp& op, int u
 }
 
 template <bool TMA>
-__device__ __noinline__ bool unit_adj_psv(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+__device__ __forceinline__ bool unit_adj_psv(const JobDesc* __restrict__ jobs, int job, const QueueOp op, int unit,
+                                             unsigned char* slice) {
+  const JobDesc& J = jobs[job];
   const PsvAdjoint p = job_psv_adjoint(J, op.it, op.a, op.b);
   if constexpr (TMA) {
     const TmaAdjPtrs mp = job_adj_maps(J, op.a, op.b);
@@ -201,27 +213,30 @@ __device__ __noinline__ bool unit_adj_psv(const JobDesc& J, const QueueOp& op, i
   return true;
 }
 
-__device__ __noinline__ bool unit_adj_sh(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+__device__ __forceinline__ bool unit_adj_sh(const JobDesc* __restrict__ jobs, int job, const QueueOp op, int unit,
+                                            unsigned char* slice) {
+  const JobDesc& J = jobs[job];
   if (!sh_adjoint_march<QAdjSh>(job_sh_adjoint(J, op.it, op.a, op.b), unit, slice)) return false;
   inval_ring<QAdjSh>(slice);
   return true;
 }
 
-__device__ __noinline__ bool unit_misfit(const JobDesc& J) {
-  queue_misfit(J);
+__device__ __forceinline__ bool unit_misfit(const JobDesc* __restrict__ jobs, int job) {
+  queue_misfit(jobs[job]);
   return true;
 }
 
 template <bool TMA>
-__device__ __forceinline__ bool run_unit(const JobDesc& J, const QueueOp& op, int unit, unsigned char* slice) {
+__device__ __forceinline__ bool run_unit(const JobDesc* __restrict__ jobs, int job, const QueueOp& op, int unit,
+                                         unsigned char* slice) {
   switch (op.kind) {
-    case kFwdPsv: return unit_psv1(J, op, unit, slice);
-    case kFwdSh: return unit_sh1(J, op, unit, slice);
-    case kFwd2Psv: return unit_psv2<TMA>(J, op, unit, slice);
-    case kFwd2Sh: return unit_sh2<TMA>(J, op, unit, slice);
-    case kAdjPsv: return unit_adj_psv<TMA>(J, op, unit, slice);
-    case kAdjSh: return unit_adj_sh(J, op, unit, slice);
-    default: return unit_misfit(J);
+    case kFwdPsv: return unit_psv1(jobs, job, op, unit, slice);
+    case kFwdSh: return unit_sh1(jobs, job, op, unit, slice);
+    case kFwd2Psv: return unit_psv2<TMA>(jobs, job, op, unit, slice);
+    case kFwd2Sh: return unit_sh2<TMA>(jobs, job, op, unit, slice);
+    case kAdjPsv: return unit_adj_psv<TMA>(jobs, job, op, unit, slice);
+    case kAdjSh: return unit_adj_sh(jobs, job, op, unit, slice);
+    default: return unit_misfit(jobs, job);
   }
 }
 
@@ -230,40 +245,53 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2)
     batch_queue_kernel(const JobDesc* __restrict__ jobs, const QueueUnit* __restrict__ units, long long end,
                        unsigned long long* next, int* err, unsigned long long wait_ns, int need_extra) {
   extern __shared__ __align__(128) unsigned char smem[];
-  unsigned char* slice = smem + size_t(threadIdx.x >> 5) * kQueueSlice;
-  const int lane = threadIdx.x & 31;
-  unsigned long long p = 0;
-  if (lane == 0) p = atomicAdd(next, 1ull);
-  p = __shfl_sync(kFull, p, 0);
-  while (p < (unsigned long long)end) {
+  // The warp's current unit, kept in shared memory while its march runs so
+  // that the march has the registers to itself.
+  __shared__ unsigned long long cur[kStepWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned long long q = 0;
+  if (lane == 0) q = atomicAdd(next, 1ull);
+  q = __shfl_sync(kFull, q, 0);
+  for (;;) {
+    if (lane == 0) cur[warp] = q;
+    __syncwarp();
+    const unsigned long long p = q;
+    if (p >= (unsigned long long)end) return;
     // Claim the next unit now: the atomic's latency overlaps this unit.
     // Units are run in the order they are claimed.
-    unsigned long long q = 0;
     if (lane == 0) q = atomicAdd(next, 1ull);
-    const QueueUnit U = units[p];
-    const JobDesc& J = jobs[U.job];
-    const QueueOp op = J.qops[U.op];
-    const int nstrips = (op.kind == kFwd2Psv || op.kind == kFwd2Sh) ? J.g2.nstrips : J.g.nstrips;
-    const int chunk = op.kind == kMisfit ? 0 : int(U.unit) / nstrips;
-    const int c0 = op.kind == kMisfit ? 0 : max(0, chunk - J.qreach);
-    const int c1 = op.kind == kMisfit ? J.g.nchunks : min(J.g.nchunks, chunk + J.qreach + 1);
-    if (op.need > 0 && !wait_counters(J.qcnt, c0, c1, op.need + need_extra, wait_ns, err)) {
-      if (lane == 0) atomicOr(err, kErrWaitTimeout);
-      return;
+    {
+      const QueueUnit U = units[p];
+      const JobDesc& J = jobs[U.job];
+      const QueueOp op = J.qops[U.op];
+      const int nstrips = (op.kind == kFwd2Psv || op.kind == kFwd2Sh) ? J.g2.nstrips : J.g.nstrips;
+      const int chunk = op.kind == kMisfit ? 0 : int(U.unit) / nstrips;
+      const int c0 = op.kind == kMisfit ? 0 : max(0, chunk - J.qreach);
+      const int c1 = op.kind == kMisfit ? J.g.nchunks : min(J.g.nchunks, chunk + J.qreach + 1);
+      if (op.need > 0 && !wait_counters(J.qcnt, c0, c1, op.need + need_extra, wait_ns, err)) {
+        if (lane == 0) atomicOr(err, kErrWaitTimeout);
+        return;
+      }
+      __syncwarp();
+      fence_proxy_async_all();
+      if (!run_unit<TMA>(jobs, U.job, op, U.unit, smem + size_t(warp) * kQueueSlice)) return;
     }
-    __syncwarp();
-    fence_proxy_async_all();
-    if (!run_unit<TMA>(J, op, U.unit, slice)) return;
     // Finished: publish the unit's writes, then count it on its chunk (on
     // every chunk, for the misfit).
     __threadfence();
     __syncwarp();
-    if (op.kind == kMisfit) {
-      for (int c = lane; c < J.g.nchunks; c += 32) red_release_add(J.qcnt + c, 1);
-    } else if (lane == 0) {
-      red_release_add(J.qcnt + chunk, 1);
+    {
+      const QueueUnit U = units[*(volatile unsigned long long*)&cur[warp]];
+      const JobDesc& J = jobs[U.job];
+      const QueueOp op = J.qops[U.op];
+      if (op.kind == kMisfit) {
+        for (int c = lane; c < J.g.nchunks; c += 32) red_release_add(J.qcnt + c, 1);
+      } else if (lane == 0) {
+        const int nstrips = (op.kind == kFwd2Psv || op.kind == kFwd2Sh) ? J.g2.nstrips : J.g.nstrips;
+        red_release_add(J.qcnt + int(U.unit) / nstrips, 1);
+      }
     }
-    p = __shfl_sync(kFull, q, 0);
+    q = __shfl_sync(kFull, q, 0);
   }
 }
 
