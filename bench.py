@@ -280,6 +280,8 @@ def run_ours(args, rank, world):
         sim.set_option("two_step_rows", args.two_step_rows)
     if args.tma >= 0:
         sim.set_option("tma", args.tma)
+    if args.pdl >= 0:
+        sim.set_option("pdl", args.pdl)
     two_step = args.two_step != 0   # the engine's default for PSV alone and SH alone is on
     sim.upload_model("vp", W["vp"])
     sim.upload_model("vs", W["vs"])
@@ -494,6 +496,8 @@ def run_secondary(args):
     if args.workload in ("c1", "c3"):
         W = configs.c1_sh_forward() if args.workload == "c1" else configs.c3_spin_forward(nt=args.nt or 3000)
         sim = W.make_sim()
+        if args.pdl >= 0:
+            sim.set_option("pdl", args.pdl)
         if args.autotune:
             sim.set_option("autotune", 50)
         stream = torch.cuda.ExternalStream(sim.stream)
@@ -534,6 +538,8 @@ def run_secondary(args):
         sim = W.make_sim()
         if args.tma >= 0:
             sim.set_option("tma", args.tma)
+        if args.pdl >= 0:
+            sim.set_option("pdl", args.pdl)
         if args.checkpoint_slots:
             sim.set_option("checkpoint_slots", args.checkpoint_slots)
         if args.checkpoint_budget_mb:
@@ -705,6 +711,8 @@ def run_secondary(args):
             batch.set_option("tma", args.tma)
         if args.queue_band >= 0:
             batch.set_option("queue_band", args.queue_band)
+        if args.pdl >= 0:
+            batch.set_option("pdl", args.pdl)
         if args.checkpoint_slots:
             batch.set_option("checkpoint_slots", args.checkpoint_slots)
         tune_ms = None
@@ -789,6 +797,9 @@ def main():
     ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--tma", type=int, default=-1,
                     help="c2, c4, c5: rows of the two-step and reverse kernels by tensor copies (1) or bulk copies (0)")
+    ap.add_argument("--pdl", type=int, default=-1,
+                    help="c2-c5: step launches may start while the previous one finishes (1, the engine's "
+                         "default) or not (0)")
     ap.add_argument("--count", type=int, default=48, help="c5: number of problems (48 = the configuration)")
     ap.add_argument("--c5-hi", type=int, default=1536,
                     help="c5: largest grid edge (1536 = the configuration; smaller for profiling captures)")

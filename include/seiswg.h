@@ -224,7 +224,9 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * steps, else binomial checkpointing with as many states as fit),
  * "checkpoint_budget_mb" (the memory that default choice may give to
  * checkpoints; 0: half of the free HBM), "stability_check" (0/1, default 1: see
- * seiswg_sim_prepare), "wait_polls" (polls of a kernel's bounded wait for
+ * seiswg_sim_prepare), "pdl" (0/1, default 1: step and reverse launches may
+ * start while the previous launch in the stream finishes -- programmatic
+ * dependent launch; the same results), "wait_polls" (polls of a kernel's bounded wait for
  * its row pipeline before it gives up and the run fails with
  * SEISWG_ETIMEOUT; 0: the built-in 2^20), "test_arm_extra" (a test hook for
  * that failure path: bytes armed on the first stage of every warp's row
@@ -280,7 +282,11 @@ int seiswg_batch_run(seiswg_batch* batch);
  * groups with their own launches (and streams in order 2); "tma" (0/1,
  * default 1): the grouped two-step forward and PSV reverse launches fetch
  * rows with 3-D tensor copies through each job's table of tensor maps, or
- * with one bulk copy per field (the same bits); "checkpoint_slots" (S >= 1:
+ * with one bulk copy per field (the same bits); "pdl" (0/1, default 1): the
+ * grouped forward and reverse launches may start while the previous launch
+ * of their stream finishes (programmatic dependent launch: a launch's CTAs
+ * set up their row pipelines on the SMs the previous launch leaves and wait
+ * for it before their first read; the same bits); "checkpoint_slots" (S >= 1:
  * every job keeps S + 2 states and follows the binomial checkpointing
  * schedule of seiswg_sim_checkpoint_plan; 0: back to the uniform checkpoints
  * of seiswg_batch_create), which reallocates the jobs' state pools.  Each

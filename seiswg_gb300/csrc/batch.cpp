@@ -474,6 +474,13 @@ void Batch::set_queue_wait_ns(unsigned long long ns) {
   graph_ = nullptr;
 }
 
+void Batch::set_pdl(bool on) {
+  SW_CUDA(cudaStreamSynchronize(stream_));
+  pdl_ = on;
+  if (graph_) cudaGraphExecDestroy(graph_);
+  graph_ = nullptr;
+}
+
 void Batch::set_queue_band(int slots) {
   if (slots < 0) throw std::invalid_argument("queue_band must be >= 0");
   queue_band_ = slots;
@@ -573,12 +580,12 @@ void Batch::enqueue_slots(int t0, int t1) {
 void Batch::launch_kind(const Launch& l, cudaStream_t s) {
   const GroupOp* ops = d_ops_ + l.offset;
   switch (l.kind) {
-    case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, s)); break;
-    case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, s)); break;
-    case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, s)); break;
-    case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, s)); break;
-    case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, s)); break;
-    case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, s)); break;
+    case kFwdSh: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, false, pdl_, s)); break;
+    case kFwdPsv: SW_CUDA(launch_grouped_forward(d_jobs_, ops, l.count, l.warps, true, pdl_, s)); break;
+    case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, pdl_, s)); break;
+    case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, pdl_, s)); break;
+    case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, pdl_, s)); break;
+    case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, pdl_, s)); break;
     case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, s)); break;
   }
   ++launches_per_run_;

@@ -75,6 +75,11 @@ class Batch {
   // bulk copy per field; the same results.  Drops the captured graph.
   void set_tma(bool on);
   bool tma() const { return tma_; }
+  // Grouped forward and reverse launches may start while the previous launch
+  // in their stream finishes (programmatic dependent launch; default on).
+  // Drops the captured graph.
+  void set_pdl(bool on);
+  bool pdl() const { return pdl_; }
   // Jobs whose grouped launches fetch rows by tensor copies: all with a map
   // table while the option is on (a job whose fields do not lie at uniform
   // strides has none), 0 while it is off.
@@ -142,6 +147,7 @@ class Batch {
   bool own_stream_ = false;
   int concurrent_ = 2;
   bool tma_ = true;   // grouped launches fetch rows by tensor copies where the job has a map table
+  bool pdl_ = true;   // grouped launches with programmatic dependent launch
   int groups_ = 1;
   std::vector<cudaStream_t> aux_;   // mode 1: forked streams for a slot's other kinds
   cudaEvent_t fork_ = nullptr;

@@ -484,6 +484,7 @@ int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
     else if (k == "tma") sim.set_use_tma(value != 0);
     else if (k == "autotune") sim.autotune(int(value));
     else if (k == "stability_check") sim.set_stability_check(value != 0);
+    else if (k == "pdl") sim.set_pdl(value != 0);
     else if (k == "checkpoint_slots") {
       if (value < 0 || value > (1 << 30)) throw std::invalid_argument("checkpoint_slots out of range");
       sim.set_checkpoint_slots(int(value));
@@ -544,6 +545,7 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "concurrent") b->batch->set_concurrent(int(value));
     else if (k == "stream_groups") b->batch->set_stream_groups(int(value));
     else if (k == "tma") b->batch->set_tma(value != 0);
+    else if (k == "pdl") b->batch->set_pdl(value != 0);
     else if (k == "queue_wait_us") {
       if (value < 1 || value > (int64_t(1) << 40)) throw std::invalid_argument("queue_wait_us out of range");
       b->batch->set_queue_wait_ns((unsigned long long)value * 1000ull);

@@ -101,6 +101,7 @@ Sim::Sim(const SimDesc& d, cudaStream_t stream) : d_(d), stream_(stream) {
   den_x_ = 8.0f * d.dx;
   den_z_ = 8.0f * d.dz;
   geom_.loader = kLoaderBulk;
+  geom_.pdl = 1;
   set_chunk_rows(model_chunk_rows());
   // PSV alone runs its forward passes two steps per launch by default.
   if ((d.psv && !d.sh && !d.spin) || (d.sh && !d.psv)) set_two_step(true);
@@ -399,6 +400,12 @@ double Sim::autotune(int steps) {
 
 void Sim::set_wait_polls(unsigned polls) {
   geom_.wait_polls = geom2_.wait_polls = polls;
+  for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+  graphs_.clear();
+}
+
+void Sim::set_pdl(bool on) {
+  geom_.pdl = geom2_.pdl = on ? 1u : 0u;
   for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
   graphs_.clear();
 }

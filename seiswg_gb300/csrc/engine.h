@@ -234,6 +234,9 @@ class Sim {
   // launch's first wait runs out (0 for normal runs).
   void set_wait_polls(unsigned polls);
   void set_arm_extra(unsigned bytes);
+  // Step and reverse launches may start while the previous one finishes
+  // (programmatic dependent launch; default on).  Drops the captured graphs.
+  void set_pdl(bool on);
   int chunk_rows() const { return geom_.lx; }
   uint64_t kernel_launches() const { return launches_; }
   void synchronize() const;

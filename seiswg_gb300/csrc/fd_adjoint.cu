@@ -74,8 +74,7 @@ cudaError_t launch_psv_adj(const PsvAdjoint& p, cudaStream_t s) {
   const size_t smem = asmem<L>();
   static const cudaError_t attr = aprep(psv_adjoint_kernel<L>, smem);
   if (attr != cudaSuccess) return attr;
-  psv_adjoint_kernel<L><<<ablocks(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(psv_adjoint_kernel<L>, p.g.pdl != 0, ablocks(p.g), smem, s, p);
 }
 
 template <class L>
@@ -83,8 +82,7 @@ cudaError_t launch_sh_adj(const ShAdjoint& p, cudaStream_t s) {
   const size_t smem = asmem<L>();
   static const cudaError_t attr = aprep(sh_adjoint_kernel<L>, smem);
   if (attr != cudaSuccess) return attr;
-  sh_adjoint_kernel<L><<<ablocks(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(sh_adjoint_kernel<L>, p.g.pdl != 0, ablocks(p.g), smem, s, p);
 }
 
 }  // namespace
@@ -116,19 +114,19 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_adjoint_kernel(con
 }
 
 cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
-                                   cudaStream_t s) {
+                                   bool pdl, cudaStream_t s) {
   if (nops <= 0 || warps <= 0) return cudaSuccess;
   const unsigned blocks = unsigned((warps + kStepWarps - 1) / kStepWarps);
   if (psv) {
     const size_t smem = asmem<ABulk<PA_NSEG>>();
     static const cudaError_t attr = aprep(grouped_adjoint_kernel<true>, smem);
     if (attr != cudaSuccess) return attr;
-    grouped_adjoint_kernel<true><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+    return launch_step(grouped_adjoint_kernel<true>, pdl, blocks, smem, s, jobs, ops, nops);
   } else {
     const size_t smem = asmem<ABulk<SA_NSEG>>();
     static const cudaError_t attr = aprep(grouped_adjoint_kernel<false>, smem);
     if (attr != cudaSuccess) return attr;
-    grouped_adjoint_kernel<false><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+    return launch_step(grouped_adjoint_kernel<false>, pdl, blocks, smem, s, jobs, ops, nops);
   }
   return cudaGetLastError();
 }
@@ -168,8 +166,7 @@ cudaError_t launch_psv_adjoint_tma(const PsvAdjoint& p, const TmaAdj& t, cudaStr
   const size_t smem = asmem<ATma>();
   static const cudaError_t attr = aprep(psv_adjoint_tma_kernel, smem);
   if (attr != cudaSuccess) return attr;
-  psv_adjoint_tma_kernel<<<ablocks(p.g), kStepWarps * 32, smem, s>>>(p, t);
-  return cudaGetLastError();
+  return launch_step(psv_adjoint_tma_kernel, p.g.pdl != 0, ablocks(p.g), smem, s, p, t);
 }
 
 cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s) {

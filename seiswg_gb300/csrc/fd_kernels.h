@@ -244,13 +244,13 @@ __device__ __forceinline__ int group_op_of(const GroupOp* __restrict__ ops, int 
 #endif
 
 cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
-                                   cudaStream_t s);
+                                   bool pdl, cudaStream_t s);
 cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
-                                   cudaStream_t s);
+                                   bool pdl, cudaStream_t s);
 // Two PSV (psv) or SH steps (op.it, op.it + 1) of every op's job, with the
 // jobs' g2.
 cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
-                                    cudaStream_t s);
+                                    bool pdl, cudaStream_t s);
 // Misfit of one problem's assembled traces against obs [ncomp][nrec][nt];
 // writes J per trace and the adjoint-source table dt * U.
 cudaError_t launch_sim_misfit(const float* syn, const float* obs, float* u_tab, double* J, int nrec, int nt,

@@ -150,6 +150,25 @@ size_t smem_for() {
   return L::kStages ? size_t(kStepWarps) * L::smem_bytes_per_warp() : 0;
 }
 
+// Launches a step or reverse kernel of kStepWarps warps per CTA; with pdl
+// it is allowed to start while the previous launch in the stream finishes
+// (its loaders wait for that launch, pdl_wait).
+template <typename... P, typename... A>
+cudaError_t launch_step(void (*kernel)(P...), bool pdl, unsigned blocks, size_t smem, cudaStream_t s,
+                        A&&... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(blocks);
+  cfg.blockDim = dim3(kStepWarps * 32);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<A&&>(args)...);
+}
+
 template <typename K>
 cudaError_t prepare_kernel(K kernel, size_t smem) {
   // Opt in to more than 48 KB of dynamic shared memory.

@@ -79,6 +79,18 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
       : "memory");
 }
 
+// Programmatic dependent launch.  A step kernel launched with the
+// programmatic-serialization attribute may start while the launch before it
+// in the stream finishes: its CTAs take the SMs that launch's CTAs leave, set
+// up their row pipelines, and wait (pdl_wait) for that launch to complete,
+// and for its writes to be visible, before their first read of state.  Every
+// CTA first signals (pdl_trigger) that the next such launch may start.  In a
+// kernel launched without the attribute both are no-ops.  The loaders' start()
+// does both, before their first copy: everything a march does before start()
+// touches only data no launch of the stream writes.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // A warp's slice of the CTA's dynamic shared memory: the S stages of its row
 // ring, then S mbarriers, rounded up to 128 bytes so that the stages of every
 // warp stay 128-byte aligned, as tensor copies require.  Warp w's slice
@@ -118,7 +130,10 @@ struct DirectRows {
   __device__ DirectRows(const Segs<NSEG>& segs, size_t ld_, int c0_, int ib_, int, float*, uint64_t*, int)
       : s(segs), ld(ld_), c0(c0_), ib(ib_) {}
   __device__ __forceinline__ void configure(const Geom&) {}
-  __device__ __forceinline__ void start() {}
+  __device__ __forceinline__ void start() {
+    pdl_trigger();
+    pdl_wait();
+  }
   // Loads the stage of iteration k (row i = ib - 1 + k).
   __device__ __forceinline__ bool acquire(int k) {
     const int i = ib - 1 + k;
@@ -204,6 +219,8 @@ struct BulkRows {
   // armed for `extra` bytes more than its copies bring, so that the wait of
   // iteration 0 runs out although every copy lands.
   __device__ __forceinline__ void start() {
+    pdl_trigger();
+    pdl_wait();
     if (lane == 0) {
       for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
       fence_mbar_init();

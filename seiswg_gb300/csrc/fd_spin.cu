@@ -201,8 +201,7 @@ cudaError_t launch_spin(const PsvStep& p, cudaStream_t s) {
   const size_t smem = smem_for<L>();
   static const cudaError_t attr = prepare_kernel(psv_spin_step_kernel<L>, smem);
   if (attr != cudaSuccess) return attr;
-  psv_spin_step_kernel<L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(psv_spin_step_kernel<L>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
 }
 
 }  // namespace

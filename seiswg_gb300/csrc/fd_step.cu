@@ -51,8 +51,7 @@ cudaError_t launch_sh(const ShStep& p, cudaStream_t s) {
   const size_t smem = smem_for<L>();
   static const cudaError_t attr = prepare_kernel(sh_step_kernel<L>, smem);
   if (attr != cudaSuccess) return attr;
-  sh_step_kernel<L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(sh_step_kernel<L>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
 }
 
 template <class L>
@@ -60,8 +59,7 @@ cudaError_t launch_psv(const PsvStep& p, cudaStream_t s) {
   const size_t smem = smem_for<L>();
   static const cudaError_t attr = prepare_kernel(psv_step_kernel<L>, smem);
   if (attr != cudaSuccess) return attr;
-  psv_step_kernel<L><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(psv_step_kernel<L>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
 }
 
 }  // namespace
@@ -85,19 +83,19 @@ __global__ void __launch_bounds__(kStepWarps * 32) grouped_forward_kernel(const 
 }
 
 cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
-                                   cudaStream_t s) {
+                                   bool pdl, cudaStream_t s) {
   if (nops <= 0 || warps <= 0) return cudaSuccess;
   const unsigned blocks = unsigned((warps + kStepWarps - 1) / kStepWarps);
   if (psv) {
     const size_t smem = smem_for<BulkL<PV_NSEG>>();
     static const cudaError_t attr = prepare_kernel(grouped_forward_kernel<true>, smem);
     if (attr != cudaSuccess) return attr;
-    grouped_forward_kernel<true><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+    return launch_step(grouped_forward_kernel<true>, pdl, blocks, smem, s, jobs, ops, nops);
   } else {
     const size_t smem = smem_for<BulkL<SH_NSEG>>();
     static const cudaError_t attr = prepare_kernel(grouped_forward_kernel<false>, smem);
     if (attr != cudaSuccess) return attr;
-    grouped_forward_kernel<false><<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+    return launch_step(grouped_forward_kernel<false>, pdl, blocks, smem, s, jobs, ops, nops);
   }
   return cudaGetLastError();
 }

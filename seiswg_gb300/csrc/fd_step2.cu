@@ -67,19 +67,19 @@ __global__ void __launch_bounds__(kStepWarps * 32, 3) grouped_forward2_sh_kernel
 }
 
 cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
-                                    cudaStream_t s) {
+                                    bool pdl, cudaStream_t s) {
   if (nops <= 0 || warps <= 0) return cudaSuccess;
   const unsigned blocks = unsigned((warps + kStepWarps - 1) / kStepWarps);
   if (psv) {
     const size_t smem = smem_for<Bulk2>();
     static const cudaError_t attr = prepare_kernel(grouped_forward2_kernel, smem);
     if (attr != cudaSuccess) return attr;
-    grouped_forward2_kernel<<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+    return launch_step(grouped_forward2_kernel, pdl, blocks, smem, s, jobs, ops, nops);
   } else {
     const size_t smem = smem_for<ShBulk2>();
     static const cudaError_t attr = prepare_kernel(grouped_forward2_sh_kernel, smem);
     if (attr != cudaSuccess) return attr;
-    grouped_forward2_sh_kernel<<<blocks, kStepWarps * 32, smem, s>>>(jobs, ops, nops);
+    return launch_step(grouped_forward2_sh_kernel, pdl, blocks, smem, s, jobs, ops, nops);
   }
   return cudaGetLastError();
 }
@@ -96,8 +96,7 @@ cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s
   const size_t smem = smem_for<TmaRows2>();
   static const cudaError_t attr = prepare_kernel(psv_step2_tma_kernel, smem);
   if (attr != cudaSuccess) return attr;
-  psv_step2_tma_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p, t);
-  return cudaGetLastError();
+  return launch_step(psv_step2_tma_kernel, p.g.pdl != 0, blocks_for(p.g), smem, s, p, t);
 }
 
 // SH two-step kernel: fewer registers than the PSV one (three CTAs per SM).
@@ -117,8 +116,7 @@ cudaError_t launch_sh_step2_tma(const ShStep& p, const Tma2& t, cudaStream_t s) 
   const size_t smem = smem_for<TmaRows<ShTmaPlan, 6, 3>>();
   static const cudaError_t attr = prepare_kernel(sh_step2_tma_kernel, smem);
   if (attr != cudaSuccess) return attr;
-  sh_step2_tma_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p, t);
-  return cudaGetLastError();
+  return launch_step(sh_step2_tma_kernel, p.g.pdl != 0, blocks_for(p.g), smem, s, p, t);
 }
 
 int sh_step2_blocks_per_sm() {
@@ -133,8 +131,7 @@ cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s) {
   const size_t smem = smem_for<ShBulk2>();
   static const cudaError_t attr = prepare_kernel(sh_step2_kernel, smem);
   if (attr != cudaSuccess) return attr;
-  sh_step2_kernel<<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(sh_step2_kernel, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
 }
 
 size_t step2_smem_bytes() { return smem_for<Bulk2>(); }
@@ -152,8 +149,7 @@ cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s) {
   const size_t smem = smem_for<Bulk2>();
   static const cudaError_t attr = prepare_kernel(psv_step2_kernel<Bulk2>, smem);
   if (attr != cudaSuccess) return attr;
-  psv_step2_kernel<Bulk2><<<blocks_for(p.g), kStepWarps * 32, smem, s>>>(p);
-  return cudaGetLastError();
+  return launch_step(psv_step2_kernel<Bulk2>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
 }
 
 }  // namespace seiswg

@@ -60,6 +60,8 @@ struct TmaRows {
     extra = g.arm_extra;
   }
   __device__ __forceinline__ void start() {
+    pdl_trigger();
+    pdl_wait();
     if (lane == 0) {
       for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
       fence_mbar_init();

@@ -63,6 +63,8 @@ struct Geom {
   unsigned wait_polls;  // polls of a bounded row-pipeline wait (0: kWaitLimit)
   unsigned arm_extra;   // test hook: bytes armed on the first stage of every warp's
                         // ring beyond its copies, so that its wait runs out (0 normally)
+  unsigned pdl;         // single-problem launches may start while the stream's previous
+                        // launch finishes (programmatic dependent launch, fd_pipe.cuh)
 };
 
 // Row loaders of the step kernels (fd_pipe.cuh).
