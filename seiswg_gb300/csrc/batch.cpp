@@ -294,7 +294,12 @@ double Batch::autotune(int slots) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  SW_CUDA(cudaMemsetAsync(err_, 0, sizeof(int), stream_));
+  // The windows compute on whatever the slots before them left, so only a
+  // wait that ran out is an error here.
+  int e = 0;
+  SW_CUDA(cudaMemcpy(&e, err_, sizeof(int), cudaMemcpyDeviceToHost));
+  SW_CUDA(cudaMemset(err_, 0, sizeof(int)));
+  if (e & kErrWaitTimeout) throw WaitTimeout("a batched kernel gave up waiting during the autotuner's windows");
   two_step_ = best_two;
   set_chunk_rows(best_lx);
   return double(best);
@@ -452,15 +457,18 @@ void Batch::enqueue_queue(int t0, int t1) {
     SW_CUDA(cudaMemsetAsync(d_qcnt_, 0, std::max(1, ncnt_) * sizeof(int), stream_));
     SW_CUDA(cudaMemsetAsync(d_next_, 0, sizeof(unsigned long long), stream_));
   } else {
-    std::vector<int> cnt(size_t(std::max(1, ncnt_)), 0);
+    // Copied in stream order from buffers that outlive the copies.
+    window_cnt_.assign(size_t(std::max(1, ncnt_)), 0);
     for (size_t q = 0; q < jobs_.size(); ++q) {
       const std::vector<int>& n = need_at_[q];
       const int v = n[std::min(size_t(t0), n.size() - 1)];
-      std::fill(cnt.begin() + cnt_off_[q], cnt.begin() + cnt_off_[q] + descs_[q].g.nchunks, v);
+      std::fill(window_cnt_.begin() + cnt_off_[q], window_cnt_.begin() + cnt_off_[q] + descs_[q].g.nchunks, v);
     }
-    const unsigned long long first = (unsigned long long)slot_begin_[size_t(t0)];
-    SW_CUDA(cudaMemcpy(d_qcnt_, cnt.data(), cnt.size() * sizeof(int), cudaMemcpyHostToDevice));
-    SW_CUDA(cudaMemcpy(d_next_, &first, sizeof(first), cudaMemcpyHostToDevice));
+    window_next_ = (unsigned long long)slot_begin_[size_t(t0)];
+    SW_CUDA(cudaMemcpyAsync(d_qcnt_, window_cnt_.data(), window_cnt_.size() * sizeof(int), cudaMemcpyHostToDevice,
+                            stream_));
+    SW_CUDA(cudaMemcpyAsync(d_next_, &window_next_, sizeof(window_next_), cudaMemcpyHostToDevice, stream_));
+    SW_CUDA(cudaStreamSynchronize(stream_));  // the host buffers are reused by the next window
   }
   SW_CUDA(launch_batch_queue(d_jobs_, d_units_, slot_begin_[size_t(t1)], d_next_, err_, queue_tma_, queue_wait_ns_,
                              queue_need_extra_, queue_blocks_, stream_));

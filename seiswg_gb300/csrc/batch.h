@@ -187,6 +187,8 @@ class Batch {
   std::vector<long long> slot_begin_;       // first unit of each slot
   std::vector<std::vector<int>> need_at_;   // per job: need of each operation, then the total
   std::vector<int> cnt_off_;                // per job: its first counter
+  std::vector<int> window_cnt_;             // the counters a window of slots starts from (enqueue_queue)
+  unsigned long long window_next_ = 0;
   int ncnt_ = 0;
   int queue_blocks_ = 0;
   bool queue_tma_ = false;

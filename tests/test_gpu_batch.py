@@ -229,6 +229,17 @@ def test_batch_binomial_checkpointing_gives_the_same_gradients():
     for i in range(len(probs)):
         for p in ("mu", "buoyancy"):
             assert rel_l2(batch.gradient(i, p), ref[i][p]) <= 1e-5
+    # the same through the device queue: binomial against uniform, bit for bit
+    batch.set_option("two_step", 0)
+    batch.set_option("concurrent", 3)
+    batch.run()
+    qref = [{p: batch.gradient(i, p) for p in ("mu", "buoyancy")} for i in range(len(probs))]
+    batch.set_option("checkpoint_slots", 0)
+    batch.run()
+    for i in range(len(probs)):
+        for p in ("mu", "buoyancy"):
+            assert np.array_equal(batch.gradient(i, p), qref[i][p]), ("queue", i, p)
+            assert rel_l2(qref[i][p], ref[i][p]) <= 1e-5
     batch.close()
     for s in sims:
         s.close()
@@ -259,6 +270,44 @@ def test_queue_wait_expiry_reports_a_timeout_and_the_batch_recovers():
         batch.run()
         for i in range(len(probs)):
             assert np.array_equal(batch.gradient(i, "mu"), ref[i]), i
+    finally:
+        batch.close()
+        for s in sims:
+            s.close()
+
+
+def test_queue_autotune_windows_and_chunk_rows():
+    """The device queue's autotuner runs windows of slots in the middle of the
+    schedule, each job's counters set as if the slots before had run: every
+    window must finish (a dependency wait that ran out would make the autotune
+    call fail with SEISWG_ETIMEOUT) and leave a batch whose next runs give the
+    queue's own gradients, for every chunk-row setting."""
+    import time
+
+    import seiswg_gb300 as sw
+
+    probs = _problems()[:3]
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    try:
+        batch.set_option("concurrent", 3)
+        batch.set_option("queue_wait_us", 200000)   # a stuck window fails the test in 0.2 s
+        batch.run()
+        ref = [batch.gradient(i, "mu") for i in range(len(probs))]
+        t0 = time.perf_counter()
+        batch.set_option("autotune", 4)
+        assert time.perf_counter() - t0 < 60
+        info = batch.info()
+        assert info["concurrent"] == 3 and info["chunk_rows"] in (0, 32, 48, 64, 96, 128)
+        batch.run()
+        for i in range(len(probs)):                  # one- or two-step recording: the same to rounding
+            assert rel_l2(batch.gradient(i, "mu"), ref[i]) <= 1e-5
+        for lx in (32, 0):
+            batch.set_option("chunk_rows", lx)
+            batch.set_option("two_step", 1)
+            batch.run()
+            for i in range(len(probs)):
+                assert np.array_equal(batch.gradient(i, "mu"), ref[i]), (lx, i)
     finally:
         batch.close()
         for s in sims:
