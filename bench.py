@@ -16,6 +16,9 @@ e2e    the reference-facing C ABI with host buffers: per step
        bounded sample of the same workload.
 N > 1: independent replicas, one per GPU (shots are independent; no
        collective on the data path); value = total cell-updates / max time.
+other_configs  (N = 1) after the headline, C1, C3, C4 and C5 each measured by
+       its own `bench.py --workload cX --no-cpu` process and summarised in the
+       same line (--no-others skips them).
 """
 from __future__ import annotations
 
@@ -383,7 +386,45 @@ def run_ours(args, rank, world):
             line["cpu_baseline"] = cpu
         if parity:
             line["parity"] = parity
+        if world == 1 and not args.no_others:
+            line["other_configs"] = run_others()
         print(json.dumps(line), flush=True)
+
+
+# The other configurations, measured after the headline in the same run (one
+# process each, outside the headline's timed region): C1 and C3 forward, the
+# C4 gradient, the C5 batch (autotuned) against its plain per-shot path.
+OTHERS = [("c1", ["--steps", "5", "--warmup", "3"], 300),
+          ("c3", ["--steps", "2", "--warmup", "3"], 300),
+          ("c4", ["--steps", "1", "--warmup", "2"], 600),
+          ("c5", ["--steps", "1", "--warmup", "2", "--autotune"], 900)]
+
+
+def run_others():
+    out = {}
+    for name, extra, limit in OTHERS:
+        cmd = [sys.executable, os.path.abspath(__file__), "--workload", name, "--no-cpu"] + extra
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=limit)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            if r.returncode != 0 or not lines:
+                out[name] = {"error": f"exit {r.returncode}: " + (r.stderr or r.stdout)[-300:]}
+                continue
+            d = json.loads(lines[-1])
+        except Exception as e:  # noqa: BLE001 - a failed secondary must not lose the headline line
+            out[name] = {"error": repr(e)[-300:]}
+            continue
+        keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "speedup", "max_rel_l2_mu_vs_plain",
+                "gcell_updates_per_s", "clocks")
+        o = {k: d[k] for k in keep if k in d}
+        o["workload"] = d.get("config", {}).get("workload")
+        if "roofline" in d:
+            o["roofline_frac"] = d["roofline"].get("frac")
+        if "plain" in d:
+            o["plain_problem_gradients_per_s"] = d["plain"].get("problem_gradients_per_s")
+        o["command"] = "bench.py --workload " + name + " --no-cpu " + " ".join(extra)
+        out[name] = o
+    return out
 
 
 def short_parity(W, phys, nt_p):
@@ -790,6 +831,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-others", action="store_true",
+                    help="c2: skip the other configurations' lines embedded after the headline (other_configs)")
     ap.add_argument("--parity-nt", type=int, default=60, help="c2: steps of the parity run outside the timed region")
     ap.add_argument("--autotune", action="store_true", help="empirical loader/chunk tuning before timing")
     ap.add_argument("--two-step", type=int, default=-1,
