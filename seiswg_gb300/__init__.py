@@ -429,6 +429,9 @@ class Sim:
         _check(lib().seiswg_sim_release_workspace(self._h))
 
     def set_option(self, key: str, value: int):
+        """The options of seiswg_sim_set_option (include/seiswg.h): "graphs", "chunk_rows", "loader",
+        "two_step", "two_step_rows", "cluster", "tma", "pdl", "autotune", "stability_check",
+        "checkpoint_slots", "checkpoint_budget_mb", "wait_polls", "test_arm_extra"."""
         _check(lib().seiswg_sim_set_option(self._h, key.encode(), int(value)))
 
     def synchronize(self):
@@ -481,7 +484,8 @@ class Batch:
     def set_option(self, key: str, value: int):
         """"chunk_rows" (0: per-problem model), "two_step" (0/1), "concurrent" (0, 1, 2: grouped
         launches in that order; 3: one persistent launch over a device queue), "stream_groups" (1..4),
-        "tma" (0/1: rows of the two-step and reverse marches by tensor copies or bulk copies),
+        "tma" (0/1: rows of the two-step and reverse marches by tensor copies or bulk copies), "pdl" (0/1:
+        programmatic dependent launch of the grouped launches),
         "queue_wait_us" (bound of a queue dependency wait), "queue_band" (slots per band of the queue's
         order, 0: slot-major), "test_queue_need_extra" (test hook),
         "checkpoint_slots" or "autotune" (slots per timing window)."""
