@@ -9,6 +9,10 @@ sizes, with fewer time steps so that the CPU oracles finish in seconds:
       rho gradients against central differences of the FP64 misfit on 16
       seeded cells of the illuminated zone
 
+and, at the full sizes and step counts, properties that need no oracle: the
+whole C2 run is deterministic and linear in the source, and one whole C4
+shot gradient is deterministic.
+
 Traces and final states are held to relative L2 <= 1e-5 against the FP32
 oracle (the spin rotation yi to 3x the oracle's own distance from FP64,
 tests/test_gpu_parity.py); the distance from the FP64 oracle is reported.
@@ -154,3 +158,69 @@ def test_c4_full_grid_gradient():
         errs.append(abs(fd - grads[name][i, j]) / abs(fd))
     errs = np.array(errs)
     assert np.median(errs) <= 2e-3 and errs.max() <= 2e-2, errs
+
+
+def test_c2_full_run_is_deterministic_and_linear_in_the_source():
+    """The whole C2 run (4096 x 4096, nt = 4000, the headline two-step kernel)
+    checked by properties that need no oracle at this size: two runs give the
+    same bits (no race between warps or launches), and the wavefield is linear
+    in the source.  With the amplitude doubled every operation on normal
+    numbers doubles its result exactly, but the leading edge of a wavefield
+    passes through the subnormal range, where a doubled value keeps more
+    significant bits, and traces of weak first arrivals carry that difference
+    (measured: 4.2e-7 on the deep receivers' ux): the doubled run is held to
+    2x the first to the parity tolerance, relative L2 1e-5."""
+    from seiswg_gb300 import configs
+
+    w = configs.c2_psv_forward()
+    si, sj = w.sources[0][0], w.sources[0][1]
+    deep_i = np.arange(si - 600, si + 601, 40, dtype=np.int32)
+    rec_i = np.concatenate([w.rec_i, deep_i])
+    rec_j = np.concatenate([w.rec_j, np.full(deep_i.size, sj + 300, np.int32)])
+    fields = ("vx", "vz", "sxx", "szz", "sxz")
+
+    def run(workload):
+        sim = workload.make_sim()
+        sim.set_receivers(rec_i, rec_j)
+        sim.forward(-1)
+        out = [sim.traces()[0], sim.traces()[2]] + [sim.state(f) for f in fields]
+        sim.close()
+        return out
+
+    a, b = run(w), run(w)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert np.abs(a[0][w.rec_i.size:]).max() > 0          # the deep line records the wavefield
+    w2 = configs.c2_psv_forward()
+    w2.sources = [s[:5] + (2.0 * s[5],) for s in w2.sources]
+    d = run(w2)
+    for x, y in zip(a, d):
+        assert np.all(np.isfinite(y))
+        assert rel_l2(y, 2.0 * x) <= 1e-5
+
+
+def test_c4_full_shot_gradient_is_deterministic():
+    """One shot of the C4 gradient at full size (2048 x 2048, nt = 3000:
+    two-step recording, checkpoints every second step, recomputation and
+    3000 reverse steps): two runs give the same bits."""
+    import seiswg_gb300 as sw
+    from seiswg_gb300 import configs
+
+    w = configs.c4_psv_adjoint()
+    w.sources = w.sources[:1]
+    st = w.make_sim(model=w.extra["true_model"])
+    st.forward(0)
+    obs = st.traces()[[0, 2]]
+    st.close()
+    sim = w.make_sim()
+    grads = []
+    for _ in range(2):
+        sim.gradient_clear()
+        sim.forward_op(0, 0)
+        _, adj = sw.l2_misfit(sim.traces()[[0, 2]], obs, w.dt)
+        sim.backward_op(adj)
+        grads.append([sim.gradient(p) for p in ("lambda", "mu", "buoyancy")])
+    sim.close()
+    for x, y in zip(*grads):
+        assert np.abs(x).max() > 0
+        assert np.array_equal(x, y)
