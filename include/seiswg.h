@@ -165,7 +165,8 @@ int seiswg_sim_kernel(seiswg_sim* sim, float* host);
 /* Exact discrete adjoint (no counterpart in the reference, which has only the
  * SH imaging condition above, solver.rs:1386-1498).  The pair
  * behaves like an autograd function: forward_op runs source isrc (-1: all)
- * and stores the wavefield every ckpt_every steps (0: ceil(sqrt(nt))); the
+ * and stores the wavefield every ckpt_every steps (0: the scheme of the
+ * "checkpoint_slots" option below); the
  * traces are then available through seiswg_sim_traces.  backward_op takes
  * dJ/dd of the recorded displacement traces, [ncomp][nrec][nt] with ncomp 1
  * (SH: uy) or 2 (PSV: ux, uz), and accumulates the gradients of J with
@@ -219,11 +220,13 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * fields lie at uniform strides, default on; 0: one bulk copy per field;
  * the same results either way), "checkpoint_slots" (forward_op with
  * ckpt_every = 0 uses binomial checkpointing with this many stored states,
- * 1 or more; 0, the default: uniform checkpoints every second step where half
- * of the free HBM (or the budget below) holds them, else every ceil(sqrt(nt))
- * steps, else binomial checkpointing with as many states as fit),
- * "checkpoint_budget_mb" (the memory that default choice may give to
- * checkpoints; 0: half of the free HBM), "stability_check" (0/1, default 1: see
+ * 1 or more; 0, the default: every state kept where the budget below holds
+ * nt + 1 states (no recomputation; two-step launches store the state between
+ * their steps), else uniform checkpoints every second step, else every
+ * ceil(sqrt(nt)) steps, else binomial checkpointing with as many states as
+ * fit), "checkpoint_budget_mb" (the memory that default choice may give to
+ * checkpoints; 0: the free HBM less a tenth of the device's memory, at
+ * least 2 GiB, kept in reserve), "stability_check" (0/1, default 1: see
  * seiswg_sim_prepare), "pdl" (0/1, default 1: step and reverse launches may
  * start while the previous launch in the stream finishes -- programmatic
  * dependent launch; the same results), "wait_polls" (polls of a kernel's bounded wait for

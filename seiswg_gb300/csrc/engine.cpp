@@ -291,12 +291,13 @@ void Sim::set_use_tma(bool on) {
 }
 
 void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList& inj_in,
-                        const ProbeList& probes_in) {
+                        const ProbeList& probes_in, const State* mid) {
   if (d_.sh) {
     ShStep p{};
     p.g = geom2_;
     p.vy0 = a.vy; p.sxy0 = a.sxy; p.szy0 = a.szy;
     p.vy1 = o.vy; p.sxy1 = o.sxy; p.szy1 = o.szy;
+    if (mid) { p.vym = mid->vy; p.sxym = mid->sxy; p.szym = mid->szy; }
     p.rho = rdt_; p.mu = mdt_;  // dt/rho, dt*mu
     p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
     p.inj = inj_in;
@@ -319,6 +320,7 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
   p.g = geom2_;
   p.vx0 = a.vx; p.vz0 = a.vz; p.sxx0 = a.sxx; p.szz0 = a.szz; p.sxz0 = a.sxz;
   p.vx1 = o.vx; p.vz1 = o.vz; p.sxx1 = o.sxx; p.szz1 = o.szz; p.sxz1 = o.sxz;
+  if (mid) { p.vxm = mid->vx; p.vzm = mid->vz; p.sxxm = mid->sxx; p.szzm = mid->szz; p.sxzm = mid->sxz; }
   p.rho = rdt_; p.lam = ldt_; p.mu = mdt_;  // dt/rho, dt*lambda, dt*mu
   p.taper_x = taper_x_; p.taper_zb = taper_zb_; p.taper_zt = taper_zt_;
   p.inj = inj_in;
@@ -1158,14 +1160,16 @@ void Sim::gradient_clear() {
   SW_CUDA(cudaMemsetAsync(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols, 0, 3 * fb, stream_));
 }
 
-// The checkpoint scheme of a forward_op with ckpt_every = 0: uniform
-// checkpoints every second step where the budget holds them (with the
-// forward pass running two steps per launch this recomputes half a forward
-// pass per gradient), else every ceil(sqrt(nt)) steps (one forward pass),
-// else binomial checkpointing with as many slots as the budget holds.
-// Budget: the "checkpoint_budget_mb" option, or half of the free memory plus
-// what the current checkpoints hold.  Returns k > 0 (uniform interval) or
-// -S (binomial, S slots).
+// The checkpoint scheme of a forward_op with ckpt_every = 0: every state
+// kept where the budget holds them (no recomputation: the reverse sweep only
+// runs reverse steps; with two steps per launch the forward launches store
+// the state between their two steps as well), else uniform checkpoints every
+// second step (half a forward pass recomputed per gradient), else every
+// ceil(sqrt(nt)) steps (one forward pass), else binomial checkpointing with
+// as many slots as the budget holds.  Budget: the "checkpoint_budget_mb"
+// option, or the free device memory less a reserve of a tenth of the
+// device's memory (at least 2 GiB), plus what the current checkpoints hold.
+// Returns k > 0 (uniform interval) or -S (binomial, S slots).
 int Sim::default_checkpoint_interval() const {
   const int nt = std::max(d_.nt, 1);
   const int k_sqrt = std::max(1, int(std::ceil(std::sqrt(double(nt)))));
@@ -1174,8 +1178,10 @@ int Sim::default_checkpoint_interval() const {
   if (ck_budget_ == 0) {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return k_sqrt;
-    budget = 0.5 * double(free_b) + double(ck_bytes_);
+    const double reserve = std::max(0.1 * double(total_b), double(size_t(2) << 30));
+    budget = std::max(0.0, double(free_b) - reserve) + double(ck_bytes_);
   }
+  if ((double(nt) + 1.0) * state_b <= budget) return 1;
   const int k2 = std::min(2, nt);
   if ((double((nt + k2 - 1) / k2) + k2) * state_b <= budget) return k2;
   if ((double((nt + k_sqrt - 1) / k_sqrt) + k_sqrt) * state_b <= budget) return k_sqrt;
@@ -1273,15 +1279,18 @@ void Sim::forward_op(int isrc, int ckpt_every) {
   if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
   // Steps write straight into the checkpoint they end on; the others
   // alternate between the two state buffers.  Two steps per launch wherever
-  // no checkpoint falls between them.
+  // no checkpoint falls between them, and with every state kept (k = 1) two
+  // steps per launch throughout, the launch storing the state between its
+  // two steps as well.
   auto ckpt = [&](int c) { return slot_state(ck_store_ + size_t(c) * state_elems); };
+  const bool keep_mid = two_step_ && k == 1;
   int last = -1;
-  auto plan = [&](const std::function<void(int, int, const State&, const State&)>& step) {
+  auto plan = [&](const std::function<void(int, int, const State&, const State&, const State*)>& step) {
     State cur = ckpt(0);
     int pp = 0;
     last = -1;
     for (int it = 0; it < nt;) {
-      const int n = (two_step_ && it + 1 < nt && (it + 1) % k != 0) ? 2 : 1;
+      const int n = (two_step_ && it + 1 < nt && ((it + 1) % k != 0 || keep_mid)) ? 2 : 1;
       const int e = it + n;
       State dst;
       if (e % k == 0 && e < nt) {
@@ -1291,20 +1300,22 @@ void Sim::forward_op(int isrc, int ckpt_every) {
         last = pp;
         pp ^= 1;
       }
-      step(it, n, cur, dst);
+      const State mid = keep_mid && n == 2 ? ckpt(it + 1) : State{};
+      step(it, n, cur, dst, keep_mid && n == 2 ? &mid : nullptr);
       cur = dst;
       it = e;
     }
   };
   const std::string key = "fop/" + std::to_string(inj.n) + "/" + std::to_string(k) + (two_step_ ? "/2" : "");
   run_loop(key, [&] {
-    plan([&](int it, int n, const State& a, const State& o) {
-      if (n == 2) enqueue_step2(it, a, o, inj, pl);
+    plan([&](int it, int n, const State& a, const State& o, const State* mid) {
+      if (n == 2) enqueue_step2(it, a, o, inj, pl, mid);
       else enqueue_step_states(it, a, o, inj, pl, false);
     });
     enqueue_traces();
   });
-  plan([](int, int, const State&, const State&) {});  // the buffer of the final state (graph replays skip the body)
+  // the buffer of the final state (graph replays skip the body)
+  plan([](int, int, const State&, const State&, const State*) {});
   cur_buf_ = last < 0 ? 0 : last;
   ck_isrc_ = isrc;
 }

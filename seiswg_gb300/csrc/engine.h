@@ -267,7 +267,9 @@ class Sim {
   void run_loop(const std::string& key, const std::function<void()>& body);
   void copy_field_to_host(const float* dev, float* host) const;
   int chunk_rows_for(int blocks_per_sm, int strip_cols, int extra_rows) const;
-  void enqueue_step2(int it, const State& a, const State& o, const InjectList& inj, const ProbeList& probes);
+  // mid: where not null, the state after step `it` is stored there too.
+  void enqueue_step2(int it, const State& a, const State& o, const InjectList& inj, const ProbeList& probes,
+                     const State* mid = nullptr);
   int default_checkpoint_interval() const;
   int final_buffer(int snap_every) const;  // buffer holding the state after run_forward
 

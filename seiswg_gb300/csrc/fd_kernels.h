@@ -33,6 +33,7 @@ struct ShStep {
   Geom g;
   const float *vy0, *sxy0, *szy0;
   float *vy1, *sxy1, *szy1;
+  float *vym, *sxym, *szym;  // two-step kernels: the state after the first step (null: not stored)
   const float *rho, *mu;
   const float *taper_x, *taper_zb, *taper_zt;
   InjectList inj;
@@ -44,6 +45,7 @@ struct PsvStep {
   Geom g;
   const float *vx0, *vz0, *sxx0, *szz0, *sxz0;
   float *vx1, *vz1, *sxx1, *szz1, *sxz1;
+  float *vxm, *vzm, *sxxm, *szzm, *sxzm;  // two-step kernels: the state after the first step (null: not stored)
   const float *vyc0, *syx0, *syy0, *syz0;
   float *vyc1, *syx1, *syy1, *syz1;
   const float *rho, *lam, *mu;
@@ -90,8 +92,10 @@ size_t sh_cluster_smem_bytes(int nx, int nz, int ctas);
 cudaError_t launch_sh_cluster(const ShCluster& p, int ctas, cudaStream_t s);
 
 // Two PSV steps (inj.it and inj.it + 1; no spin) from the *0 state to the *1
-// state.  p.g describes the two-step decomposition: nstrips over
-// kStripCols2-column strips, lx / nchunks its own chunk rows.
+// state, and, where p.vxm is not null, the state after step inj.it to the *m
+// fields (all five).  p.g describes the two-step decomposition: nstrips over
+// kStripCols2-column strips, lx / nchunks its own chunk rows.  The same for
+// the SH launchers below with p.vym.
 cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s);
 size_t step2_smem_bytes();
 int step2_blocks_per_sm();

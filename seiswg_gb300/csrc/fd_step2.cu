@@ -19,10 +19,13 @@
 namespace seiswg {
 
 
-template <class Loader>
+// MID (here and below): the kernel also stores the state after the first of
+// its two steps (p.vxm .., p.vym ..), for a gradient's forward pass that
+// keeps every state.
+template <class Loader, bool MID = false>
 __global__ void __launch_bounds__(kStepWarps * 32, 2) psv_step2_kernel(const PsvStep p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  psv2_march<Loader>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<Loader>(smem));
+  psv2_march<Loader, Tma2, MID>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<Loader>(smem));
 }
 
 // Grouped two-step launch (batched gradients): the warp's job and op as in
@@ -85,53 +88,72 @@ cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int
 }
 
 // The two-step PSV kernel with its rows fetched by tensor copies.
+template <bool MID>
 __global__ void __launch_bounds__(kStepWarps * 32, 2) psv_step2_tma_kernel(const __grid_constant__ PsvStep p,
                                                                            const __grid_constant__ Tma2 t) {
   extern __shared__ __align__(128) unsigned char smem[];
-  psv2_march<TmaRows2>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<TmaRows2>(smem),
-                       &t);
+  psv2_march<TmaRows2, Tma2, MID>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5),
+                                  warp_slice<TmaRows2>(smem), &t);
+}
+
+template <bool MID>
+cudaError_t launch_psv2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s) {
+  const size_t smem = smem_for<TmaRows2>();
+  static const cudaError_t attr = prepare_kernel(psv_step2_tma_kernel<MID>, smem);
+  if (attr != cudaSuccess) return attr;
+  return launch_step(psv_step2_tma_kernel<MID>, p.g.pdl != 0, blocks_for(p.g), smem, s, p, t);
 }
 
 cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s) {
-  const size_t smem = smem_for<TmaRows2>();
-  static const cudaError_t attr = prepare_kernel(psv_step2_tma_kernel, smem);
-  if (attr != cudaSuccess) return attr;
-  return launch_step(psv_step2_tma_kernel, p.g.pdl != 0, blocks_for(p.g), smem, s, p, t);
+  return p.vxm ? launch_psv2_tma<true>(p, t, s) : launch_psv2_tma<false>(p, t, s);
 }
 
 // SH two-step kernel: fewer registers than the PSV one (three CTAs per SM).
+template <bool MID>
 __global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_kernel(const ShStep p) {
   extern __shared__ __align__(128) unsigned char smem[];
-  sh2_march<ShBulk2>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<ShBulk2>(smem));
+  sh2_march<ShBulk2, Tma2, MID>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<ShBulk2>(smem));
 }
 
+template <bool MID>
 __global__ void __launch_bounds__(kStepWarps * 32, 3) sh_step2_tma_kernel(const __grid_constant__ ShStep p,
                                                                           const __grid_constant__ Tma2 t) {
   extern __shared__ __align__(128) unsigned char smem[];
   using L = TmaRows<ShTmaPlan, 6, 3>;
-  sh2_march<L>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<L>(smem), &t);
+  sh2_march<L, Tma2, MID>(p, blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), warp_slice<L>(smem), &t);
+}
+
+template <bool MID>
+cudaError_t launch_sh2_tma(const ShStep& p, const Tma2& t, cudaStream_t s) {
+  const size_t smem = smem_for<TmaRows<ShTmaPlan, 6, 3>>();
+  static const cudaError_t attr = prepare_kernel(sh_step2_tma_kernel<MID>, smem);
+  if (attr != cudaSuccess) return attr;
+  return launch_step(sh_step2_tma_kernel<MID>, p.g.pdl != 0, blocks_for(p.g), smem, s, p, t);
 }
 
 cudaError_t launch_sh_step2_tma(const ShStep& p, const Tma2& t, cudaStream_t s) {
-  const size_t smem = smem_for<TmaRows<ShTmaPlan, 6, 3>>();
-  static const cudaError_t attr = prepare_kernel(sh_step2_tma_kernel, smem);
-  if (attr != cudaSuccess) return attr;
-  return launch_step(sh_step2_tma_kernel, p.g.pdl != 0, blocks_for(p.g), smem, s, p, t);
+  return p.vym ? launch_sh2_tma<true>(p, t, s) : launch_sh2_tma<false>(p, t, s);
 }
 
 int sh_step2_blocks_per_sm() {
   int n = 0;
   const size_t smem = smem_for<ShBulk2>();
-  cudaError_t e = prepare_kernel(sh_step2_kernel, smem);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step2_kernel, kStepWarps * 32, smem);
+  cudaError_t e = prepare_kernel(sh_step2_kernel<false>, smem);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, sh_step2_kernel<false>, kStepWarps * 32, smem);
   return e == cudaSuccess ? n : 0;
 }
 
-cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s) {
+template <bool MID>
+cudaError_t launch_sh2(const ShStep& p, cudaStream_t s) {
   const size_t smem = smem_for<ShBulk2>();
-  static const cudaError_t attr = prepare_kernel(sh_step2_kernel, smem);
+  static const cudaError_t attr = prepare_kernel(sh_step2_kernel<MID>, smem);
   if (attr != cudaSuccess) return attr;
-  return launch_step(sh_step2_kernel, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
+  return launch_step(sh_step2_kernel<MID>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
+}
+
+cudaError_t launch_sh_step2(const ShStep& p, cudaStream_t s) {
+  return p.vym ? launch_sh2<true>(p, s) : launch_sh2<false>(p, s);
 }
 
 size_t step2_smem_bytes() { return smem_for<Bulk2>(); }
@@ -145,11 +167,16 @@ int step2_blocks_per_sm() {
   return e == cudaSuccess ? n : 0;
 }
 
-cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s) {
+template <bool MID>
+cudaError_t launch_psv2(const PsvStep& p, cudaStream_t s) {
   const size_t smem = smem_for<Bulk2>();
-  static const cudaError_t attr = prepare_kernel(psv_step2_kernel<Bulk2>, smem);
+  static const cudaError_t attr = prepare_kernel(psv_step2_kernel<Bulk2, MID>, smem);
   if (attr != cudaSuccess) return attr;
-  return launch_step(psv_step2_kernel<Bulk2>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
+  return launch_step(psv_step2_kernel<Bulk2, MID>, p.g.pdl != 0, blocks_for(p.g), smem, s, p);
+}
+
+cudaError_t launch_psv_step2(const PsvStep& p, cudaStream_t s) {
+  return p.vxm ? launch_psv2<true>(p, s) : launch_psv2<false>(p, s);
 }
 
 }  // namespace seiswg

@@ -140,8 +140,10 @@ __device__ __forceinline__ void stress(const f4& u0, const f4& u1, const f4& u2,
 // EDGE: derivatives masked by index and level-1 values outside the grid
 // zeroed.  (A second, test-free instantiation for interior warps executed 17 %
 // fewer instructions but ran 8 % slower: two bodies of this size no longer
-// fit the instruction cache.)
-template <class Loader, bool EDGE, class M>
+// fit the instruction cache.)  MID: the level-1 rows the warp owns are
+// stored too (p.vxm .. p.sxzm: the state after step `it`, which a gradient's
+// forward pass keeps as a checkpoint; a separate kernel, not a second body).
+template <class Loader, bool EDGE, class M, bool MID = false>
 __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, const LaneCols& L, int valid,
                                           unsigned char* smem, const M* tm) {
   const Geom& g = p.g;
@@ -250,9 +252,14 @@ __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, cons
         xd = in_grid(xd, row_ok, valid);
         zd = in_grid(zd, row_ok, valid);
       }
-      if (i >= m.ib && i < m.ie)
+      if (i >= m.ib && i < m.ie) {
+        if constexpr (MID) {
+          st4_masked(at(p.vxm, i), xd, L.own);
+          st4_masked(at(p.vzm, i), zd, L.own);
+        }
         probe_at(p.probes, i, L, pi1, dt,
                  [&](int comp, int e) { return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e); });
+      }
     }
 
     // ---- level 1, stress of row i-2 (step it)
@@ -265,6 +272,13 @@ __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, cons
         sx3 = in_grid(sx3, row_ok, valid);
         sz3 = in_grid(sz3, row_ok, valid);
         sq3 = in_grid(sq3, row_ok, valid);
+      }
+      if constexpr (MID) {
+        if (r >= m.ib && r < m.ie) {
+          st4_masked(at(p.sxxm, r), sx3, L.own);
+          st4_masked(at(p.szzm, r), sz3, L.own);
+          st4_masked(at(p.sxzm, r), sq3, L.own);
+        }
       }
     }
 
@@ -316,14 +330,14 @@ __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, cons
   return true;
 }
 
-template <class Loader, class M = Tma2>
+template <class Loader, class M = Tma2, bool MID = false>
 __device__ __forceinline__ bool psv2_march(const PsvStep& p, int gw, unsigned char* smem,
                                            const M* tm = nullptr) {
   const March m = march_of(p.g, gw);
   if (!m.active) return true;
   int valid;
   const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
-  return psv2_body<Loader, true, M>(p, m, L, valid, smem, tm);
+  return psv2_body<Loader, true, M, MID>(p, m, L, valid, smem, tm);
 }
 
 // --------------------------------------------------------------------------
@@ -367,7 +381,8 @@ __device__ __forceinline__ void inject_add_y(const InjectList& inj, int i, int c
   inject_at<false, true, false>(inj, i, c0, cur, ds, ds, ds);
 }
 
-template <class Loader, class M>
+// MID: the level-1 rows the warp owns are stored too (p.vym, p.sxym, p.szym).
+template <class Loader, class M, bool MID = false>
 __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const LaneCols& L, int valid,
                                          unsigned char* smem, const M* tm) {
   const Geom& g = p.g;
@@ -456,7 +471,10 @@ __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const 
       for (int e = 0; e < 4; ++e) vd.v[e] = (bx1 * tbt.v[e]) * fmaf(ds.v[e], rho.v[e], vo.v[e]);
       const bool row_ok = (i >= 0 && i < nx);
       if (!row_ok || cols_out) vd = in_grid(vd, row_ok, valid);
-      if (i >= m.ib && i < m.ie) probe_at(p.probes, i, L, pi1, dt, [&](int, int e) { return pick4(vd, e); });
+      if (i >= m.ib && i < m.ie) {
+        if constexpr (MID) st4_masked(at(p.vym, i), vd, L.own);
+        probe_at(p.probes, i, L, pi1, dt, [&](int, int e) { return pick4(vd, e); });
+      }
     }
 
     // ---- level 1, stress of row i-2 (step it): div_vy, add_sy_sh
@@ -474,6 +492,12 @@ __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const 
       if (!row_ok || cols_out) {
         sx3 = in_grid(sx3, row_ok, valid);
         sz3 = in_grid(sz3, row_ok, valid);
+      }
+      if constexpr (MID) {
+        if (r >= m.ib && r < m.ie) {
+          st4_masked(at(p.sxym, r), sx3, L.own);
+          st4_masked(at(p.szym, r), sz3, L.own);
+        }
       }
     }
 
@@ -521,13 +545,13 @@ __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const 
   return true;
 }
 
-template <class Loader, class M = Tma2>
+template <class Loader, class M = Tma2, bool MID = false>
 __device__ __forceinline__ bool sh2_march(const ShStep& p, int gw, unsigned char* smem, const M* tm = nullptr) {
   const March m = march_of(p.g, gw);
   if (!m.active) return true;
   int valid;
   const LaneCols L = lane_cols2(p.g, m.strip, m.lane, valid);
-  return sh2_body<Loader, M>(p, m, L, valid, smem, tm);
+  return sh2_body<Loader, M, MID>(p, m, L, valid, smem, tm);
 }
 
 }  // namespace

@@ -363,22 +363,26 @@ def test_binomial_checkpointing_gives_the_uniform_gradient(phys):
 
 
 def test_checkpoint_budget_selects_the_scheme():
-    """The default scheme under a memory budget: every second step where it
-    fits, every ceil(sqrt(nt)) steps where that fits, else binomial
-    checkpointing with as many states as fit (the same gradient)."""
+    """The default scheme under a memory budget: every state where nt + 1
+    fit (nothing recomputed; the two-step launches store the state between
+    their steps), every second step where that fits, every ceil(sqrt(nt))
+    steps where that fits, else binomial checkpointing with as many states as
+    fit (the same gradient)."""
     vp, vs, rho, flags, src, rec = _problem("psv", 4)
     obs = _observed(vp, vs, rho, flags, src, rec, 0)
     sim, _ = _sim(vp, vs, rho, flags, src, rec)
     ref = _gpu_gradient(sim, flags, obs, 0, 1)[2]
     g0 = _gpu_gradient(sim, flags, obs, 0, 0)[2]
     plan = sim.checkpoint_plan()
-    assert plan["interval"] == 2 and plan["slots"] == 0     # the test grid fits every second step
-    state = plan["bytes"] / (NT // 2 + 2)
-    for states, want in ((40, "sqrt"), (12, "binomial")):
+    assert plan["interval"] == 1 and plan["slots"] == 0 and plan["recomputed"] == 0, plan  # every state fits
+    state = plan["bytes"] / (NT + 1)
+    for states, want in ((NT // 2 + 8, "second"), (40, "sqrt"), (12, "binomial")):
         sim.set_option("checkpoint_budget_mb", max(1, int(states * state) >> 20))
         g = _gpu_gradient(sim, flags, obs, 0, 0)[2]
         plan = sim.checkpoint_plan()
-        if want == "sqrt":
+        if want == "second":
+            assert plan["interval"] == 2 and plan["slots"] == 0, plan
+        elif want == "sqrt":
             assert plan["interval"] == int(np.ceil(np.sqrt(NT))) and plan["slots"] == 0, plan
         else:
             assert plan["slots"] >= 1 and plan["interval"] == 0 and plan["bytes"] <= states * state, plan
