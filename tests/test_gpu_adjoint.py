@@ -109,6 +109,45 @@ def test_checkpoint_interval_does_not_change_the_gradient(phys):
     sim.close()
 
 
+@pytest.mark.parametrize("phys,nt", [("psv", 259), ("psv", 260), ("sh", 259)])
+def test_every_state_kept_by_the_two_step_recording(phys, nt):
+    """Every state kept (k = 1) with two steps per recording launch: the
+    launches store the state between their two steps, an odd last step runs
+    alone, nothing is recomputed, and the gradient is the one of one-step
+    recording with every state kept to FP32 rounding (the two-step kernel
+    contracts multiply-adds), the same bits on a second run."""
+    import seiswg_gb300 as sw
+
+    vp, vs, rho, flags, src, rec = _problem(phys, 3)
+    stf = np.stack([sw.ricker(nt, DT, s[2], s[3], s[4], 1.0e10) for s in src], axis=1)
+    sim = sw.Sim(NX, NZ, nt, DX, DX, DT, **flags)
+    for k, v in (("vp", vp), ("vs", vs), ("rho", rho)):
+        sim.upload_model(k, v)
+    sim.prepare()
+    sim.set_sources([s[0] for s in src], [s[1] for s in src], stf)
+    sim.set_receivers([r[0] for r in rec], [r[1] for r in rec])
+    sim.forward(-1)
+    obs = 0.8 * sim.traces()[_comps(flags)]
+    out = {}
+    for two in (0, 1, 1):
+        sim.set_option("two_step", two)
+        sim.gradient_clear()
+        sim.forward_op(-1, 1)
+        plan = sim.checkpoint_plan()
+        assert plan["interval"] == 1 and plan["recomputed"] == 0, plan
+        _, adj = sw.l2_misfit(sim.traces()[_comps(flags)], obs, DT)
+        sim.backward_op(adj)
+        g = {p: sim.gradient(p) for p in (("lambda", "mu", "buoyancy") if phys == "psv" else ("mu", "buoyancy"))}
+        if two in out:
+            for p in g:
+                assert np.array_equal(g[p], out[two][p]), p
+        out[two] = g
+    sim.close()
+    for p, ref in out[0].items():
+        assert np.abs(ref).max() > 0
+        assert rel_l2(out[1][p], ref) <= 1e-5, (p, rel_l2(out[1][p], ref))
+
+
 def test_psv_gradient_matches_finite_differences_of_fp32_misfit():
     import seiswg_gb300 as sw
 
