@@ -66,6 +66,42 @@ inline std::vector<HostOp> job_ops(int nt, int k, bool psv, bool two) {
   return L;
 }
 
+// One launch of a single problem's recording pass (Sim::forward_op, uniform
+// checkpoints every k steps): steps [it, it + n) from slot a to slot b, and
+// where mid >= 0 the state after step `it` stored in slot mid as well.
+// Slots: c >= 0 checkpoint c (checkpoint 0 the zero initial state), -1 and
+// -2 the two state buffers.
+struct RecordLaunch {
+  int it, n, a, b, mid;
+};
+
+// A step that ends on a checkpoint writes the checkpoint's slot, the others
+// alternate between the two state buffers; two steps per launch (`two`)
+// wherever no checkpoint falls between them, and with every state kept
+// (k = 1) two steps per launch throughout, each launch storing the state
+// between its steps into that step's checkpoint.  An odd last step runs
+// alone.
+inline std::vector<RecordLaunch> record_plan(int nt, int k, bool two) {
+  std::vector<RecordLaunch> L;
+  const bool keep_mid = two && k == 1;
+  int cur = 0, pp = 0;
+  for (int it = 0; it < nt;) {
+    const int n = (two && it + 1 < nt && ((it + 1) % k != 0 || keep_mid)) ? 2 : 1;
+    const int e = it + n;
+    int dst;
+    if (e % k == 0 && e < nt) {
+      dst = e / k;
+    } else {
+      dst = -1 - pp;
+      pp ^= 1;
+    }
+    L.push_back(RecordLaunch{it, n, cur, dst, keep_mid && n == 2 ? it + 1 : -1});
+    cur = dst;
+    it = e;
+  }
+  return L;
+}
+
 // ---------------------------------------------------------------------------
 // Binomial checkpointing (Griewank and Walther, "Algorithm 799: revolve",
 // ACM TOMS 26(1), 2000), restated for a job with S state slots.

@@ -1277,45 +1277,28 @@ void Sim::forward_op(int isrc, int ckpt_every) {
   ProbeList pl = probe_list();
   zero_state();
   if (nprobe_) SW_CUDA(cudaMemsetAsync(probe_acc_, 0, size_t(nprobe_) * sizeof(float), stream_));
-  // Steps write straight into the checkpoint they end on; the others
-  // alternate between the two state buffers.  Two steps per launch wherever
-  // no checkpoint falls between them, and with every state kept (k = 1) two
-  // steps per launch throughout, the launch storing the state between its
-  // two steps as well.
-  auto ckpt = [&](int c) { return slot_state(ck_store_ + size_t(c) * state_elems); };
-  const bool keep_mid = two_step_ && k == 1;
-  int last = -1;
-  auto plan = [&](const std::function<void(int, int, const State&, const State&, const State*)>& step) {
-    State cur = ckpt(0);
-    int pp = 0;
-    last = -1;
-    for (int it = 0; it < nt;) {
-      const int n = (two_step_ && it + 1 < nt && ((it + 1) % k != 0 || keep_mid)) ? 2 : 1;
-      const int e = it + n;
-      State dst;
-      if (e % k == 0 && e < nt) {
-        dst = ckpt(e / k);
-      } else {
-        dst = st_[pp];
-        last = pp;
-        pp ^= 1;
-      }
-      const State mid = keep_mid && n == 2 ? ckpt(it + 1) : State{};
-      step(it, n, cur, dst, keep_mid && n == 2 ? &mid : nullptr);
-      cur = dst;
-      it = e;
-    }
-  };
+  // The launches of record_plan (batch_plan.h): steps write straight into
+  // the checkpoint they end on, the others alternate between the two state
+  // buffers; with every state kept, two-step launches store the state
+  // between their steps as well.
+  const std::vector<RecordLaunch> plan = record_plan(nt, k, two_step_);
+  auto slot = [&](int q) { return q >= 0 ? slot_state(ck_store_ + size_t(q) * state_elems) : st_[-1 - q]; };
   const std::string key = "fop/" + std::to_string(inj.n) + "/" + std::to_string(k) + (two_step_ ? "/2" : "");
   run_loop(key, [&] {
-    plan([&](int it, int n, const State& a, const State& o, const State* mid) {
-      if (n == 2) enqueue_step2(it, a, o, inj, pl, mid);
-      else enqueue_step_states(it, a, o, inj, pl, false);
-    });
+    for (const RecordLaunch& o : plan) {
+      if (o.n == 2) {
+        const State mid = o.mid >= 0 ? slot(o.mid) : State{};
+        enqueue_step2(o.it, slot(o.a), slot(o.b), inj, pl, o.mid >= 0 ? &mid : nullptr);
+      } else {
+        enqueue_step_states(o.it, slot(o.a), slot(o.b), inj, pl, false);
+      }
+    }
     enqueue_traces();
   });
   // the buffer of the final state (graph replays skip the body)
-  plan([](int, int, const State&, const State&, const State*) {});
+  int last = -1;
+  for (const RecordLaunch& o : plan)
+    if (o.b < 0) last = -1 - o.b;
   cur_buf_ = last < 0 ? 0 : last;
   ck_isrc_ = isrc;
 }

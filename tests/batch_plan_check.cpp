@@ -45,6 +45,11 @@
 // cover only the unit's own chunk must be reported, and so must a queue with
 // a unit moved ahead of one it depends on, which deadlocks one warp.  The
 // queues are laid out slot-major or in diagonal bands of 1 to 64 slots.
+// A single problem's recording pass (record_plan, Sim::forward_op): every nt
+// up to 160 and every interval, one- and two-step launches, replayed on the
+// checkpoints and the two state buffers; with every state kept the two-step
+// launches must store the state between their steps (planted: a dropped
+// middle store, a two-step launch across a checkpoint).
 // Prints "ok <cases> <mixes> <revolve cases> <queue mixes>" and exits 0, or
 // prints the first violation and exits 1.
 #include <algorithm>
@@ -205,6 +210,45 @@ static int check_revolve(int& cases) {
   return 0;
 }
 
+// A single problem's recording pass (record_plan): replayed on its slots
+// (checkpoints and the two state buffers), every launch must read the state
+// of its first step and write the state after its last, a middle state only
+// from a two-step launch and into that step's checkpoint; at the end every
+// checkpoint c holds the state of step c*k, the last launch's buffer holds
+// step nt, and with every state kept and two-step launches all but an odd
+// last step run two per launch.
+static int replay_record(int nt, int k, bool two, const std::vector<RecordLaunch>& L) {
+  const int ncp = (nt + k - 1) / k;
+  std::vector<int> ck(size_t(std::max(ncp, 1)), -1), buf(2, -1);
+  ck[0] = 0;
+  auto at = [&](int s) -> int& { return s >= 0 ? ck[size_t(s)] : buf[size_t(-1 - s)]; };
+  int next = 0, twos = 0;
+  for (size_t q = 0; q < L.size(); ++q) {
+    const RecordLaunch& o = L[q];
+    if (o.it != next || (o.n != 1 && o.n != 2) || o.it + o.n > nt) return fail(nt, k, two, q, "steps out of order");
+    if (o.a >= ncp || o.b >= ncp || o.a < -2 || o.b < -2 || o.a == o.b) return fail(nt, k, two, q, "bad slot");
+    if (at(o.a) != o.it) return fail(nt, k, two, q, "reads a state of another step");
+    if (o.n == 2 && !two) return fail(nt, k, two, q, "two steps without two-step launches");
+    if (o.b >= 0 && o.b * k != o.it + o.n) return fail(nt, k, two, q, "writes a checkpoint of another step");
+    if (o.mid >= 0 && (o.n != 2 || o.mid != o.it + 1 || o.mid * k != o.it + 1 || o.mid >= ncp))
+      return fail(nt, k, two, q, "bad middle state");
+    if (o.n == 2 && (o.it + 1) % k == 0 && o.mid < 0) return fail(nt, k, two, q, "skips a checkpoint");
+    at(o.b) = o.it + o.n;
+    if (o.mid >= 0) at(o.mid) = o.it + 1;
+    twos += o.n == 2;
+    next = o.it + o.n;
+  }
+  if (next != nt) return fail(nt, k, two, L.size(), "the pass does not end at nt");
+  for (int c = 0; c < ncp; ++c)
+    if (ck[size_t(c)] != c * k) return fail(nt, k, two, L.size(), "a checkpoint is missing");
+  if (nt > 0 && (L.back().b >= 0 || at(L.back().b) != nt)) return fail(nt, k, two, L.size(), "final state");
+  if (two && k == 1 && twos != nt / 2) return fail(nt, k, two, L.size(), "one-step launches with every state kept");
+  return 0;
+}
+
+static int check_record(int nt, int k, bool two) { return replay_record(nt, k, two, record_plan(nt, k, two)); }
+
+
 static bool catches_planted_mistakes() {
   const int nt = 23, k = 5;
   quiet = true;
@@ -227,6 +271,18 @@ static bool catches_planted_mistakes() {
       if (o.kind != kMisfit) nomisfit.push_back(o);
     ok = ok && replay(nt, k, true, two != 0, nomisfit) == 1;
   }
+  // A recording pass with every state kept whose middle-state store is
+  // dropped, and one whose two-step launch skips a checkpoint.
+  std::vector<RecordLaunch> R = record_plan(12, 1, true);
+  R[2].mid = -1;
+  ok = ok && replay_record(12, 1, true, R) == 1;
+  R = record_plan(12, 3, true);
+  for (RecordLaunch& o : R)
+    if (o.n == 1 && o.it + 1 < 12) {
+      o.n = 2;  // two steps across the checkpoint at it + 1, written nowhere
+      break;
+    }
+  ok = ok && replay_record(12, 3, true, R) == 1;
   quiet = false;
   return ok;
 }
@@ -582,6 +638,19 @@ int main() {
     for (int k : {2, 3, 31, 32, 55, 63, 64})
       for (int two = 0; two < 2; ++two) {
         if (check(nt, k, true, two != 0)) return 1;
+        ++cases;
+      }
+  // Single-problem recording passes, every interval including every state.
+  for (int nt = 1; nt <= 160; ++nt)
+    for (int k = 1; k <= nt; ++k)
+      for (int two = 0; two < 2; ++two) {
+        if (check_record(nt, k, two != 0)) return 1;
+        ++cases;
+      }
+  for (int nt : {1000, 1001, 3000, 4000})
+    for (int k : {1, 2, 55, 64})
+      for (int two = 0; two < 2; ++two) {
+        if (check_record(nt, k, two != 0)) return 1;
         ++cases;
       }
   int mixes = 0;

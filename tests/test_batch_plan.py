@@ -15,7 +15,11 @@ exactly the optimal number of steps.  The device queue of launch order 3
 (plan_queue): 1500 random mixes run by a discrete-event model of the queue
 kernel's warps (claiming units in order, waiting on the per-chunk counters)
 with every unit's reads and writes, at the rows the marches really touch,
-checked against each job's sequential order, and no deadlock.  The program
+checked against each job's sequential order, and no deadlock.  A single
+problem's recording pass (record_plan, Sim::forward_op) for every nt up to 160
+and every interval: every launch reads the state of its step, checkpoints and
+the final state hold theirs, and with every state kept the two-step launches
+store the state between their steps.  The program
 first shows that it reports planted mistakes (a dropped dependency bit, a
 queue dependency that does not cover the rows read, a unit queued ahead of
 its dependency).  CPU only (g++)."""
