@@ -756,6 +756,8 @@ def run_secondary(args):
             batch.set_option("pdl", args.pdl)
         if args.checkpoint_slots:
             batch.set_option("checkpoint_slots", args.checkpoint_slots)
+        if args.two_step_recompute >= 0:
+            batch.set_option("two_step_recompute", args.two_step_recompute)
         tune_ms = None
         if args.autotune:
             t0 = time.perf_counter()
@@ -838,6 +840,8 @@ def main():
     ap.add_argument("--two-step", type=int, default=-1,
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
+    ap.add_argument("--two-step-recompute", type=int, default=-1,
+                    help="c5: grouped launches recompute two steps per operation (1) or one (0); -1: the default")
     ap.add_argument("--tma", type=int, default=-1,
                     help="c2, c4, c5: rows of the two-step and reverse kernels by tensor copies (1) or bulk copies (0)")
     ap.add_argument("--pdl", type=int, default=-1,

@@ -260,7 +260,10 @@ int seiswg_batch_run(seiswg_batch* batch);
 /* key "chunk_rows": rows per warp chunk of every job (0: each problem's own
  * chunk model); "two_step" (0/1): jobs whose problem runs two steps per
  * launch (PSV alone, SH alone) record their forward pass that way (default
- * 1); "autotune": tries
+ * 1); "two_step_recompute" (0/1, default 1): such jobs also recompute the
+ * states of each checkpoint interval two steps per grouped launch, each
+ * launch storing both states (launch order 3 recomputes one step per
+ * operation); "autotune": tries
  * chunk rows 0, 16 (not in order 3), 32, 48, 64, 96 and 128 with and without two-step
  * recording, timing `value` slots of the recording pass and of the reverse
  * sweep each, and keeps the one whose times, scaled to the slot counts of

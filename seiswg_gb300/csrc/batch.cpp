@@ -255,6 +255,11 @@ void Batch::set_two_step(bool on) {
   set_chunk_rows(chunk_rows_);  // rebuilds the schedule
 }
 
+void Batch::set_two_step_recompute(bool on) {
+  pair_ = on;
+  set_chunk_rows(chunk_rows_);  // rebuilds the schedule
+}
+
 double Batch::autotune(int slots) {
   if (slots < 1) slots = 1;
   // The device queue counts units per chunk: short chunks multiply its units
@@ -331,7 +336,10 @@ void Batch::build_schedule() {
   for (size_t q = 0; q < jobs_.size(); ++q) {
     const Job& j = jobs_[q];
     const bool two = two_step_ && descs_[q].g2.lx > 0;
-    lists[q] = j.S > 0 ? job_ops_revolve(j.nt, j.S, j.psv, two) : job_ops(j.nt, j.k, j.psv, two);
+    // Grouped launches recompute two steps per operation as well (the queue
+    // kernel's marches store no middle state).
+    lists[q] = j.S > 0 ? job_ops_revolve(j.nt, j.S, j.psv, two)
+                       : job_ops(j.nt, j.k, j.psv, two, /*pair=*/pair_ && concurrent_ != 3);
   }
   size_t T = 0;
   rec_slots_ = 0;

@@ -53,6 +53,10 @@ class Batch {
   // tries both.
   void set_two_step(bool on);
   bool two_step() const { return two_step_; }
+  // With two-step recording, grouped launches also recompute two steps per
+  // operation, storing both states (default on; launch order 3 always
+  // recomputes one step per operation); rebuilds the schedule.
+  void set_two_step_recompute(bool on);
   // How the schedule runs.  0: one grouped launch per (slot, kind), one
   // after another on the batch's stream.  1: the launches of one slot run
   // concurrently on forked streams that join before the next slot.  2: one
@@ -139,6 +143,7 @@ class Batch {
   std::vector<Geom> model_geom2_;  // ... of its two-step kernel (lx 0: none)
   int chunk_rows_ = 0;
   bool two_step_ = true;
+  bool pair_ = true;  // two-step recomputation (set_two_step_recompute)
   size_t ops_bytes_ = 0;
 
   std::vector<BatchProblem> problems_;

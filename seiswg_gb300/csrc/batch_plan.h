@@ -19,8 +19,10 @@ namespace seiswg {
 
 
 // Forward: step `it` (two steps for kFwd2*) from slot a to slot b, flags & 1
-// records the probes.  Reverse: reverse step `it` with the forward state of
-// step `it` in slot a, the incoming adjoint state in adjoint slot b.
+// records the probes, flags & kOpMid (two-step operations) stores the state
+// after step `it` in slot b - 1 as well.  Reverse: reverse step `it` with the
+// forward state of step `it` in slot a, the incoming adjoint state in
+// adjoint slot b.
 struct HostOp {
   int kind, it, a, b, flags;
 };
@@ -29,8 +31,11 @@ struct HostOp {
 // (ncp = ceil(nt / k)): the recording pass (two steps per operation where
 // `two` and no checkpoint falls between them), the misfit, then for each
 // interval from the last a recomputation of its states followed by its
-// reverse steps, newest first.
-inline std::vector<HostOp> job_ops(int nt, int k, bool psv, bool two) {
+// reverse steps, newest first.  With `pair` (and `two`) the recomputation
+// runs two steps per operation, each storing both states (kOpMid: the
+// interval slots of consecutive steps are consecutive), and an odd last
+// step alone.
+inline std::vector<HostOp> job_ops(int nt, int k, bool psv, bool two, bool pair = false) {
   std::vector<HostOp> L;
   const int ncp = (nt + k - 1) / k;
   auto seg = [&](int m) { return ncp + m - 1; };  // interval slot, m >= 1
@@ -57,7 +62,16 @@ inline std::vector<HostOp> job_ops(int nt, int k, bool psv, bool two) {
   int parity = 0;
   for (int c = ncp - 1; c >= 0; --c) {
     const int n0 = c * k, n1 = nt < n0 + k ? nt : n0 + k;
-    for (int m = 1; m <= n1 - n0 - 1; ++m) L.push_back(HostOp{fwd, n0 + m - 1, m == 1 ? c : seg(m - 1), seg(m), 0});
+    for (int m = 1; m <= n1 - n0 - 1;) {
+      const int a = m == 1 ? c : seg(m - 1);
+      if (two && pair && m + 1 <= n1 - n0 - 1) {
+        L.push_back(HostOp{fwd2, n0 + m - 1, a, seg(m + 1), kOpMid});
+        m += 2;
+      } else {
+        L.push_back(HostOp{fwd, n0 + m - 1, a, seg(m), 0});
+        ++m;
+      }
+    }
     for (int n = n1 - 1; n >= n0; --n) {
       L.push_back(HostOp{adj, n, n == n0 ? c : seg(n - n0), parity, 0});
       parity ^= 1;

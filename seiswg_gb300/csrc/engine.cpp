@@ -1443,7 +1443,8 @@ void Sim::run_backward() {
     return;
   }
 
-  const std::string key = "bop/" + std::to_string(src.n) + "/" + std::to_string(rec.n) + "/" + std::to_string(k);
+  const std::string key = "bop/" + std::to_string(src.n) + "/" + std::to_string(rec.n) + "/" + std::to_string(k) +
+                          (two_step_ ? "/2" : "");
   run_loop(key, [&] {
     int cur = 0;
     for (int seg = ck_n_ - 1; seg >= 0; --seg) {
@@ -1454,7 +1455,18 @@ void Sim::run_backward() {
         return n == n0 ? slot_state(ck_store_ + size_t(seg) * state_elems)
                        : slot_state(seg_store_ + size_t(n - n0) * state_elems);
       };
-      for (int n = n0; n < n1 - 1; ++n) enqueue_step_states(n, fstate(n), fstate(n + 1), src, none, false);
+      // Two steps per launch where the forward pass runs them, each launch
+      // storing both states.
+      for (int n = n0; n < n1 - 1;) {
+        if (two_step_ && n + 2 <= n1 - 1) {
+          const State mid = fstate(n + 1);
+          enqueue_step2(n, fstate(n), fstate(n + 2), src, none, &mid);
+          n += 2;
+        } else {
+          enqueue_step_states(n, fstate(n), fstate(n + 1), src, none, false);
+          ++n;
+        }
+      }
       for (int n = n1 - 1; n >= n0; --n) {
         enqueue_reverse(n, fstate(n), adj[cur], adj[1 - cur], src, rec, ga);
         cur ^= 1;

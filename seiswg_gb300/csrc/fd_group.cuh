@@ -53,12 +53,18 @@ __device__ __forceinline__ ShStep job_sh_step(const JobDesc& J, int it, int a, i
 }
 
 // Steps it and it + 1 with the two-step geometry g2 and the dt-scaled
-// material (dt/rho, dt*lambda, dt*mu at the material's field stride).
+// material (dt/rho, dt*lambda, dt*mu at the material's field stride);
+// flags & kOpMid: the state after step `it` into slot b - 1 as well.
 __device__ __forceinline__ PsvStep job_psv_step2(const JobDesc& J, int it, int a, int b, int flags) {
   PsvStep p = job_psv_step(J, it, a, b, flags);
   p.g = J.g2;
   const long long dm = J.lam - J.rho;
   p.rho = J.rho_dt; p.lam = J.rho_dt + dm; p.mu = J.rho_dt + 2 * dm;
+  if (flags & kOpMid) {
+    p.vxm = job_field(J.pool, J, b - 1, 0); p.vzm = job_field(J.pool, J, b - 1, 1);
+    p.sxxm = job_field(J.pool, J, b - 1, 2); p.szzm = job_field(J.pool, J, b - 1, 3);
+    p.sxzm = job_field(J.pool, J, b - 1, 4);
+  }
   return p;
 }
 
@@ -66,6 +72,10 @@ __device__ __forceinline__ ShStep job_sh_step2(const JobDesc& J, int it, int a, 
   ShStep p = job_sh_step(J, it, a, b, flags);
   p.g = J.g2;
   p.rho = J.rho_dt; p.mu = J.rho_dt + 2 * (J.lam - J.rho);
+  if (flags & kOpMid) {
+    p.vym = job_field(J.pool, J, b - 1, 0); p.sxym = job_field(J.pool, J, b - 1, 1);
+    p.szym = job_field(J.pool, J, b - 1, 2);
+  }
   return p;
 }
 

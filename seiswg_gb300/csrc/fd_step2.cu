@@ -29,7 +29,8 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) psv_step2_kernel(const Psv
 }
 
 // Grouped two-step launch (batched gradients): the warp's job and op as in
-// grouped_forward_kernel (fd_step.cu), then the two-step march.
+// grouped_forward_kernel (fd_step.cu), then the two-step march, which also
+// stores the middle state of operations flagged kOpMid (recomputation).
 __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(const JobDesc* __restrict__ jobs,
                                                                               const GroupOp* __restrict__ ops,
                                                                               int nops) {
@@ -43,9 +44,9 @@ __global__ void __launch_bounds__(kStepWarps * 32, 2) grouped_forward2_kernel(co
   if (J.tm) {
     const Tma2Ptrs mp = job_psv2_maps(J, op.a);
     using L = TmaRows<PsvTmaPlan, 6, 3, Tma2Ptrs>;
-    psv2_march<L, Tma2Ptrs>(p, lw, warp_slice<L>(smem), &mp);
+    psv2_march<L, Tma2Ptrs, true>(p, lw, warp_slice<L>(smem), &mp);
   } else {
-    psv2_march<Bulk2>(p, lw, warp_slice<Bulk2>(smem));
+    psv2_march<Bulk2, Tma2, true>(p, lw, warp_slice<Bulk2>(smem));
   }
 }
 
@@ -63,9 +64,9 @@ __global__ void __launch_bounds__(kStepWarps * 32, 3) grouped_forward2_sh_kernel
   if (J.tm) {
     const Tma2Ptrs mp = job_sh2_maps(J, op.a);
     using L = TmaRows<ShTmaPlan, 6, 3, Tma2Ptrs>;
-    sh2_march<L, Tma2Ptrs>(p, lw, warp_slice<L>(smem), &mp);
+    sh2_march<L, Tma2Ptrs, true>(p, lw, warp_slice<L>(smem), &mp);
   } else {
-    sh2_march<ShBulk2>(p, lw, warp_slice<ShBulk2>(smem));
+    sh2_march<ShBulk2, Tma2, true>(p, lw, warp_slice<ShBulk2>(smem));
   }
 }
 

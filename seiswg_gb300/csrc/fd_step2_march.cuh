@@ -140,9 +140,9 @@ __device__ __forceinline__ void stress(const f4& u0, const f4& u1, const f4& u2,
 // EDGE: derivatives masked by index and level-1 values outside the grid
 // zeroed.  (A second, test-free instantiation for interior warps executed 17 %
 // fewer instructions but ran 8 % slower: two bodies of this size no longer
-// fit the instruction cache.)  MID: the level-1 rows the warp owns are
-// stored too (p.vxm .. p.sxzm: the state after step `it`, which a gradient's
-// forward pass keeps as a checkpoint; a separate kernel, not a second body).
+// fit the instruction cache.)  MID: where p.vxm is set, the level-1 rows
+// the warp owns are stored too (p.vxm .. p.sxzm: the state after step `it`,
+// which a gradient keeps; a separate kernel, not a second body).
 template <class Loader, bool EDGE, class M, bool MID = false>
 __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, const LaneCols& L, int valid,
                                           unsigned char* smem, const M* tm) {
@@ -254,8 +254,10 @@ __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, cons
       }
       if (i >= m.ib && i < m.ie) {
         if constexpr (MID) {
-          st4_masked(at(p.vxm, i), xd, L.own);
-          st4_masked(at(p.vzm, i), zd, L.own);
+          if (p.vxm) {
+            st4_masked(at(p.vxm, i), xd, L.own);
+            st4_masked(at(p.vzm, i), zd, L.own);
+          }
         }
         probe_at(p.probes, i, L, pi1, dt,
                  [&](int comp, int e) { return comp == kProbeVX ? pick4(xd, e) : pick4(zd, e); });
@@ -274,7 +276,7 @@ __device__ __forceinline__ bool psv2_body(const PsvStep& p, const March& m, cons
         sq3 = in_grid(sq3, row_ok, valid);
       }
       if constexpr (MID) {
-        if (r >= m.ib && r < m.ie) {
+        if (p.vxm && r >= m.ib && r < m.ie) {
           st4_masked(at(p.sxxm, r), sx3, L.own);
           st4_masked(at(p.szzm, r), sz3, L.own);
           st4_masked(at(p.sxzm, r), sq3, L.own);
@@ -381,7 +383,8 @@ __device__ __forceinline__ void inject_add_y(const InjectList& inj, int i, int c
   inject_at<false, true, false>(inj, i, c0, cur, ds, ds, ds);
 }
 
-// MID: the level-1 rows the warp owns are stored too (p.vym, p.sxym, p.szym).
+// MID: where p.vym is set, the level-1 rows the warp owns are stored too
+// (p.vym, p.sxym, p.szym).
 template <class Loader, class M, bool MID = false>
 __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const LaneCols& L, int valid,
                                          unsigned char* smem, const M* tm) {
@@ -472,7 +475,9 @@ __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const 
       const bool row_ok = (i >= 0 && i < nx);
       if (!row_ok || cols_out) vd = in_grid(vd, row_ok, valid);
       if (i >= m.ib && i < m.ie) {
-        if constexpr (MID) st4_masked(at(p.vym, i), vd, L.own);
+        if constexpr (MID) {
+          if (p.vym) st4_masked(at(p.vym, i), vd, L.own);
+        }
         probe_at(p.probes, i, L, pi1, dt, [&](int, int e) { return pick4(vd, e); });
       }
     }
@@ -494,7 +499,7 @@ __device__ __forceinline__ bool sh2_body(const ShStep& p, const March& m, const 
         sz3 = in_grid(sz3, row_ok, valid);
       }
       if constexpr (MID) {
-        if (r >= m.ib && r < m.ie) {
+        if (p.vym && r >= m.ib && r < m.ie) {
           st4_masked(at(p.sxym, r), sx3, L.own);
           st4_masked(at(p.szym, r), sz3, L.own);
         }

@@ -78,6 +78,9 @@ enum { kErrWaitTimeout = 1, kErrNonFiniteTraces = 2, kErrNonFiniteGradient = 4 }
 // Kinds of work of a batched job (batch_plan.h): one grouped launch per
 // (schedule slot, kind), or the kind of a queue operation.
 enum BatchKind { kFwdSh = 0, kFwdPsv, kFwd2Sh, kFwd2Psv, kAdjSh, kAdjPsv, kMisfit, kKinds };
+// Flag of a two-step operation: the state after its first step is stored in
+// slot b - 1 as well (flags & 1: the probes are recorded).
+constexpr int kOpMid = 2;
 
 // The batch's device work queue (batch_plan.h, fd_queue.cu).  QueueOp: one
 // operation of a job -- its kind (BatchKind), step, slots and flags as in

@@ -45,6 +45,10 @@
 // cover only the unit's own chunk must be reported, and so must a queue with
 // a unit moved ahead of one it depends on, which deadlocks one warp.  The
 // queues are laid out slot-major or in diagonal bands of 1 to 64 slots.
+// With two-step recomputation (job_ops with `pair`) the same replay, the
+// middle state of each two-step recomputation landing in slot b - 1, and
+// ceil(m / 2) operations per interval of m recomputed steps (planted: a
+// dropped middle store).
 // A single problem's recording pass (record_plan, Sim::forward_op): every nt
 // up to 160 and every interval, one- and two-step launches, replayed on the
 // checkpoints and the two state buffers; with every state kept the two-step
@@ -72,7 +76,7 @@ static int fail(int nt, int k, bool two, size_t op, const char* what) {
   return 1;
 }
 
-static int replay(int nt, int k, bool psv, bool two, const std::vector<HostOp>& L) {
+static int replay(int nt, int k, bool psv, bool two, const std::vector<HostOp>& L, bool pair = false) {
   const int ncp = (nt + k - 1) / k, nslot = ncp + k + 1;
   std::vector<int> slot(nslot, -1);
   slot[0] = 0;  // the initial (zero) state
@@ -94,8 +98,14 @@ static int replay(int nt, int k, bool psv, bool two, const std::vector<HostOp>& 
         if (o.it != rec || !(o.flags & 1)) return fail(nt, k, two, q, "recording pass out of order");
         rec += n;
       } else {
-        if (o.kind != fwd) return fail(nt, k, two, q, "recomputation in two-step launches");
+        if (o.kind != fwd && !(pair && o.kind == fwd2 && (o.flags & kOpMid)))
+          return fail(nt, k, two, q, "recomputation in two-step launches that do not keep both states");
         if (o.flags & 1) return fail(nt, k, two, q, "recomputation records probes");
+      }
+      if (o.flags & kOpMid) {
+        if (o.kind != fwd2 || !misfit) return fail(nt, k, two, q, "a middle state outside a two-step recomputation");
+        if (o.b - 1 < ncp || o.b - 1 == o.a) return fail(nt, k, two, q, "the middle state overwrites a checkpoint");
+        slot[o.b - 1] = o.it + 1;
       }
       if (o.b < ncp && o.it + n != o.b * k) return fail(nt, k, two, q, "checkpoint slot gets another step");
       slot[o.b] = o.it + n;
@@ -119,7 +129,32 @@ static int replay(int nt, int k, bool psv, bool two, const std::vector<HostOp>& 
   return 0;
 }
 
-static int check(int nt, int k, bool psv, bool two) { return replay(nt, k, psv, two, job_ops(nt, k, psv, two)); }
+static int check(int nt, int k, bool psv, bool two) {
+  if (replay(nt, k, psv, two, job_ops(nt, k, psv, two))) return 1;
+  if (!two) return 0;
+  // Two-step recomputation: the same steps, half the operations.
+  const std::vector<HostOp> P = job_ops(nt, k, psv, true, true);
+  if (replay(nt, k, psv, two, P, true)) return 1;
+  size_t fwd_ops = 0, fwd_ops1 = 0;
+  bool after = false;
+  for (const HostOp& o : P) {
+    if (o.kind == kMisfit) after = true;
+    else if (after && o.kind != kAdjPsv && o.kind != kAdjSh) ++fwd_ops;
+  }
+  after = false;
+  for (const HostOp& o : job_ops(nt, k, psv, true)) {
+    if (o.kind == kMisfit) after = true;
+    else if (after && o.kind != kAdjPsv && o.kind != kAdjSh) ++fwd_ops1;
+  }
+  const int ncp = (nt + k - 1) / k;
+  size_t want = 0;  // per interval of m recomputed steps, ceil(m / 2) operations
+  for (int c = 0; c < ncp; ++c) {
+    const int n0 = c * k, n1 = nt < n0 + k ? nt : n0 + k;
+    want += size_t(n1 - n0 - 1 + 1) / 2;
+  }
+  if (fwd_ops != want || fwd_ops1 < fwd_ops) return fail(nt, k, two, P.size(), "two-step recomputation op count");
+  return 0;
+}
 
 // Each planted mistake must be reported.
 // Replays a binomial schedule on S + 2 slots; *recomputed = forward steps of
@@ -270,6 +305,16 @@ static bool catches_planted_mistakes() {
     for (const HostOp& o : L)
       if (o.kind != kMisfit) nomisfit.push_back(o);
     ok = ok && replay(nt, k, true, two != 0, nomisfit) == 1;
+  }
+  // A two-step recomputation whose middle-state store is dropped.
+  {
+    std::vector<HostOp> P = job_ops(nt, k, true, true, true);
+    for (HostOp& o : P)
+      if (o.flags & kOpMid) {
+        o.flags &= ~kOpMid;
+        break;
+      }
+    ok = ok && replay(nt, k, true, true, P, true) == 1;
   }
   // A recording pass with every state kept whose middle-state store is
   // dropped, and one whose two-step launch skips a checkpoint.
