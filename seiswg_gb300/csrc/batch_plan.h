@@ -163,7 +163,9 @@ inline int revolve_split(int n, int s) {
 // checkpoint slots: slots 0..S-1 (slot 0 holds S^0, the zero state that no
 // step writes), then the working pair S and S+1.  The recording pass stores
 // the states of the recursion's right spine; the reverse phase then walks the
-// recursion, recomputing with one-step operations.  When the free slots run
+// recursion, recomputing with one-step operations (two-step ones with `two`,
+// where two steps lead to the next state needed: no state between them is
+// read).  When the free slots run
 // out before the spine reaches step nt-1, the recording pass ends with a
 // one-step operation so that S^(nt-1) stays in a working slot for the first
 // reverse step.  The HostOp vocabulary and slot conventions are those of
@@ -211,16 +213,19 @@ inline std::vector<HostOp> job_ops_revolve(int nt, int S, bool psv, bool two) {
     L.push_back(HostOp{adj, n, slot, parity, 0});
     parity ^= 1;
   };
-  // S^b from S^a in slot src, one step per operation, into slot dst (or, when
-  // dst is a working slot, into whichever working slot the alternation ends
-  // in); returns the slot holding S^b.
+  // S^b from S^a in slot src, one step per operation (two with `two`, the
+  // last one alone when b - a is odd), into slot dst (or, when dst is a
+  // working slot, into whichever working slot the alternation ends in);
+  // returns the slot holding S^b.
   auto advance = [&](int src, int a, int b, int dst) {
     int from = src, w = 0;
-    for (int it = a; it < b; ++it) {
-      int to = (it + 1 == b && dst < S) ? dst : pp(w++);
+    for (int it = a; it < b;) {
+      const int n = (two && it + 2 <= b) ? 2 : 1;
+      int to = (it + n == b && dst < S) ? dst : pp(w++);
       if (to == from) to = pp(w++);
-      L.push_back(HostOp{fwd, it, from, to, 0});
+      L.push_back(HostOp{n == 2 ? fwd2 : fwd, it, from, to, 0});
       from = to;
+      it += n;
     }
     return from;
   };

@@ -1222,7 +1222,8 @@ void Sim::forward_op_binomial(int isrc, int S) {
   rv_ops_ = job_ops_revolve(nt, S, d_.psv, two_step_);
   recompute_steps_ = 0;
   for (const HostOp& o : rv_ops_)
-    if (!(o.flags & 1) && (o.kind == kFwdPsv || o.kind == kFwdSh)) ++recompute_steps_;
+    if (!(o.flags & 1) && o.kind != kMisfit && o.kind != kAdjPsv && o.kind != kAdjSh)
+      recompute_steps_ += (o.kind == kFwd2Psv || o.kind == kFwd2Sh) ? 2 : 1;
   if (!g_mu_) gradient_clear();
   InjectList inj = source_injections(isrc);
   ProbeList pl = probe_list();
@@ -1434,6 +1435,7 @@ void Sim::run_backward() {
         if (o.kind == kMisfit) { after = true; continue; }
         if (!after) continue;
         if (o.kind == kFwdPsv || o.kind == kFwdSh) enqueue_step_states(o.it, rv_slot(o.a), rv_slot(o.b), src, none, false);
+        else if (o.kind == kFwd2Psv || o.kind == kFwd2Sh) enqueue_step2(o.it, rv_slot(o.a), rv_slot(o.b), src, none);
         else enqueue_reverse(o.it, rv_slot(o.a), adj[o.b], adj[1 - o.b], src, rec, ga);
       }
       SW_CUDA(launch_check_finite(g_lam_ - size_t(kHaloRows) * ld_ - kHaloCols, 3 * (d_.nx + 2 * kHaloRows), ld_,

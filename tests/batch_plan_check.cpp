@@ -179,8 +179,9 @@ static int replay_revolve(int nt, int S, bool psv, bool two, const std::vector<H
         if (o.it != rec || !(o.flags & 1)) return fail(nt, S, two, q, "revolve: recording out of order");
         rec += n;
       } else {
-        if (o.kind != fwd || (o.flags & 1)) return fail(nt, S, two, q, "revolve: recomputation not one plain step");
-        *recomputed += 1;
+        if ((o.kind != fwd && !(two && o.kind == fwd2)) || (o.flags & 1))
+          return fail(nt, S, two, q, "revolve: recomputation not a plain step (or two with two-step launches)");
+        *recomputed += n;
       }
       slot[o.b] = o.it + n;
     } else if (o.kind == kMisfit) {
