@@ -1,6 +1,7 @@
-"""Batched gradients of uneven problems (by default one persistent launch over
-a device work queue, else grouped launches; one CUDA graph per run, misfit on
-the device) against the plain per-shot path, problem by problem.  The
+"""Batched gradients of uneven problems (grouped launches by default, one per
+schedule slot and kind of work, or one persistent launch over a device work
+queue; one CUDA graph per run, misfit on the device) against the plain
+per-shot path, problem by problem.  The
 tolerance is the gradient accuracy the batched configuration asks for,
 relative L2 1e-4; the two paths share their marches, so they agree far
 closer."""
@@ -118,6 +119,44 @@ def test_chunk_rows_and_autotune_leave_gradients_unchanged():
             assert np.array_equal(batch.gradient(i, "mu"), ref[i] if info["two_step"] else one[i]), ("autotune", i)
         with pytest.raises(sw.SeiswgError):
             batch.set_option("chunk_rows", 2)
+    finally:
+        batch.close()
+        for s in sims:
+            s.close()
+
+
+def test_two_step_recomputation_keeps_the_gradient_to_rounding():
+    """Recomputing the intervals' states two steps per grouped launch (the
+    default with two-step recording; each launch stores both states) runs the
+    same steps in fewer schedule slots and launches; the gradients agree with
+    one-step recomputation to FP32 rounding (the two-step kernel contracts
+    multiply-adds), bitwise from run to run, and with the plain path."""
+    import seiswg_gb300 as sw
+
+    probs = _problems()[:3]
+    plain = [_plain(w, obs, comps) for (w, obs, comps) in probs]
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    try:
+        out = {}
+        for pair in (1, 0, 1):
+            batch.set_option("two_step_recompute", pair)
+            info = batch.info()
+            batch.run()
+            g = [{p: batch.gradient(i, p) for p in ("lambda", "mu", "buoyancy")} for i in range(len(probs))]
+            if pair in out:
+                for i in range(len(probs)):
+                    for p in g[i]:
+                        assert np.array_equal(g[i][p], out[pair][1][i][p]), (i, p)
+            out[pair] = (info, g)
+        assert out[1][0]["slots"] < out[0][0]["slots"]
+        assert out[1][0]["launches_per_run"] < out[0][0]["launches_per_run"]
+        assert batch.checkpoint_plan()["recomputed_steps"] > 0
+        for i, (_, gp) in enumerate(plain):
+            params = ("lambda", "mu", "buoyancy") if probs[i][0].flags["psv"] else ("mu", "buoyancy")
+            for p in params:
+                assert rel_l2(out[1][1][i][p], out[0][1][i][p]) <= 1e-5, (i, p)
+                assert rel_l2(out[1][1][i][p], gp[p]) <= 1e-4, (i, p)
     finally:
         batch.close()
         for s in sims:
