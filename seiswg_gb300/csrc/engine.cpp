@@ -1170,7 +1170,7 @@ void Sim::gradient_clear() {
 // option, or the free device memory less a reserve of a tenth of the
 // device's memory (at least 2 GiB), plus what the current checkpoints hold.
 // Returns k > 0 (uniform interval) or -S (binomial, S slots).
-int Sim::default_checkpoint_interval() const {
+int Sim::default_checkpoint_interval(double cap) const {
   const int nt = std::max(d_.nt, 1);
   const int k_sqrt = std::max(1, int(std::ceil(std::sqrt(double(nt)))));
   const double state_b = double(nstate()) * double(field_elems_) * sizeof(float);
@@ -1181,6 +1181,7 @@ int Sim::default_checkpoint_interval() const {
     const double reserve = std::max(0.1 * double(total_b), double(size_t(2) << 30));
     budget = std::max(0.0, double(free_b) - reserve) + double(ck_bytes_);
   }
+  if (cap >= 0.0) budget = std::min(budget, cap);
   if ((double(nt) + 1.0) * state_b <= budget) return 1;
   const int k2 = std::min(2, nt);
   if ((double((nt + k2 - 1) / k2) + k2) * state_b <= budget) return k2;
@@ -1252,25 +1253,42 @@ void Sim::forward_op(int isrc, int ckpt_every) {
   if (d_.spin) throw std::invalid_argument("the exact adjoint is defined for SH or PSV without spin");
   if (d_.sh && d_.psv) throw std::invalid_argument("the exact adjoint runs one of SH or PSV at a time");
   const int nt = d_.nt;
-  int k = ckpt_every > 0 ? ckpt_every : rv_force_ > 0 ? -rv_force_ : default_checkpoint_interval();
+  const size_t state_elems = size_t(nstate()) * field_elems_;
+  // The scheme the budget allows; should its allocation fail (memory taken
+  // meanwhile, or too fragmented for one block), the next scheme that needs
+  // less.  An explicit interval or slot count fails instead.
+  const bool chosen = ckpt_every <= 0 && rv_force_ <= 0;
+  double cap = -1.0;
+  int k = 0, ncp = 0;
+  for (;;) {
+    k = ckpt_every > 0 ? ckpt_every : rv_force_ > 0 ? -rv_force_ : default_checkpoint_interval(cap);
+    if (k < 0) break;
+    k = std::max(1, std::min(k, std::max(nt, 1)));
+    ncp = (nt + k - 1) / k;
+    if (k == ck_k_ && ncp == ck_n_ && !rv_slots_) break;
+    free_checkpoints();
+    const size_t a = size_t(std::max(1, ncp)) * state_elems * sizeof(float);
+    const size_t b = size_t(k) * state_elems * sizeof(float);
+    const cudaError_t ea = cudaMalloc(&ck_store_, a);
+    const cudaError_t eb = ea == cudaSuccess ? cudaMalloc(&seg_store_, b) : ea;
+    if (eb == cudaSuccess) {
+      // Halos of every stored state stay zero; so does checkpoint 0 (the
+      // zero initial state), which no step writes.
+      SW_CUDA(cudaMemsetAsync(ck_store_, 0, a, stream_));
+      SW_CUDA(cudaMemsetAsync(seg_store_, 0, b, stream_));
+      ck_k_ = k;
+      ck_n_ = ncp;
+      ck_bytes_ = a + b;
+      break;
+    }
+    (void)cudaGetLastError();  // the failed allocation's error, not sticky
+    free_checkpoints();
+    if (!chosen || eb != cudaErrorMemoryAllocation || k >= nt) SW_CUDA(eb);
+    cap = double(a + b) - 1.0;
+  }
   if (k < 0) {
     forward_op_binomial(isrc, -k);
     return;
-  }
-  k = std::max(1, std::min(k, std::max(nt, 1)));
-  const int ncp = (nt + k - 1) / k;
-  const size_t state_elems = size_t(nstate()) * field_elems_;
-  if (k != ck_k_ || ncp != ck_n_ || rv_slots_) {
-    free_checkpoints();
-    SW_CUDA(cudaMalloc(&ck_store_, std::max(1, ncp) * state_elems * sizeof(float)));
-    SW_CUDA(cudaMalloc(&seg_store_, size_t(k) * state_elems * sizeof(float)));
-    // Halos of every stored state stay zero; so does checkpoint 0 (the zero
-    // initial state), which no step writes.
-    SW_CUDA(cudaMemsetAsync(ck_store_, 0, std::max(1, ncp) * state_elems * sizeof(float), stream_));
-    SW_CUDA(cudaMemsetAsync(seg_store_, 0, size_t(k) * state_elems * sizeof(float), stream_));
-    ck_k_ = k;
-    ck_n_ = ncp;
-    ck_bytes_ = (size_t(ncp) + size_t(k)) * state_elems * sizeof(float);
   }
   recompute_steps_ = nt - ncp;  // every interval but its checkpoint, once
   if (!g_mu_) gradient_clear();

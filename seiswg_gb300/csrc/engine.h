@@ -270,7 +270,9 @@ class Sim {
   // mid: where not null, the state after step `it` is stored there too.
   void enqueue_step2(int it, const State& a, const State& o, const InjectList& inj, const ProbeList& probes,
                      const State* mid = nullptr);
-  int default_checkpoint_interval() const;
+  // cap >= 0: a scheme needing at most `cap` bytes (after an allocation of a
+  // larger one failed).
+  int default_checkpoint_interval(double cap = -1.0) const;
   int final_buffer(int snap_every) const;  // buffer holding the state after run_forward
 
   SimDesc d_;

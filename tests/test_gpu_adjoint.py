@@ -148,6 +148,38 @@ def test_every_state_kept_by_the_two_step_recording(phys, nt):
         assert rel_l2(out[1][p], ref) <= 1e-5, (p, rel_l2(out[1][p], ref))
 
 
+def test_checkpoint_allocation_failure_falls_back_to_a_smaller_scheme():
+    """A budget above the device's memory: the every-state scheme of a 2048^2
+    PSV run of 4000 steps (about 344 GB) fails to allocate -- an error return
+    of the allocator, nothing on the device -- and forward_op takes the next
+    scheme that fits (every second state, about 172 GB); the reverse sweep
+    then runs on it."""
+    import seiswg_gb300 as sw
+
+    n, nt, dt = 2048, 4000, 5e-4
+    sim = sw.Sim(n, n, nt, 5.0, 5.0, dt, psv=True, abs_left=True, abs_right=True, abs_bottom=True, abs_width=20)
+    try:
+        sim.upload_model("vp", np.full((n, n), 3000.0, np.float32))
+        sim.upload_model("vs", np.full((n, n), 1732.0, np.float32))
+        sim.upload_model("rho", np.full((n, n), 2600.0, np.float32))
+        sim.prepare()
+        sim.set_sources([n // 2], [60], sw.ricker(nt, dt, 15.0, 0.08, 0.0, 1.0e10)[:, None, :])
+        sim.set_receivers(list(range(100, n - 100, 64)), [40] * len(range(100, n - 100, 64)))
+        sim.set_option("checkpoint_budget_mb", 10 << 20)  # 10 TiB
+        sim.gradient_clear()
+        sim.forward_op(0, 0)
+        plan = sim.checkpoint_plan()
+        assert plan["interval"] == 2 and plan["slots"] == 0, plan
+        syn = sim.traces()[[0, 2]]
+        assert np.isfinite(syn).all() and np.abs(syn).max() > 0
+        _, adj = sw.l2_misfit(syn, 0.5 * syn, dt)
+        sim.backward_op(adj)
+        g = sim.gradient("mu")
+        assert np.isfinite(g).all() and np.abs(g).max() > 0
+    finally:
+        sim.close()
+
+
 def test_psv_gradient_matches_finite_differences_of_fp32_misfit():
     import seiswg_gb300 as sw
 
