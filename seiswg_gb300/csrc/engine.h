@@ -134,8 +134,9 @@ class Sim {
 
   // ---- exact discrete adjoint with checkpointing --------------------------
   // forward_op: one forward run of source isrc (-1: all) that also stores the
-  // full wavefield state every `ckpt_every` steps (0: every second step when
-  // half of the free HBM holds those states, else ceil(sqrt(nt))).
+  // full wavefield state every `ckpt_every` steps (0: the scheme the budget
+  // allows -- every state, every second one, every ceil(sqrt(nt)), else
+  // binomial checkpointing; default_checkpoint_interval).
   // backward_op: the reverse sweep for the adjoint source adj = dJ/dd of the
   // recorded traces, [ncomp][nrec][nt] (SH: uy; PSV: ux, uz), rebuilding the
   // forward states of each checkpoint interval by recomputation; gradients
@@ -161,7 +162,7 @@ class Sim {
   long long recompute_steps() const { return recompute_steps_; }
   // Options of the checkpoint scheme: binomial checkpointing with S slots
   // (0: the default choice), and the memory the default choice may use for
-  // checkpoints (0: half of the free HBM).
+  // checkpoints (0: the free HBM less a reserve of a tenth of the device).
   void set_checkpoint_slots(int S) { rv_force_ = S > 0 ? S : 0; }
   void set_checkpoint_budget(size_t bytes) { ck_budget_ = bytes; }
   // Frees the checkpoint, interval, adjoint and snapshot buffers (they are
