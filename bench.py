@@ -285,6 +285,8 @@ def run_ours(args, rank, world):
         sim.set_option("tma", args.tma)
     if args.pdl >= 0:
         sim.set_option("pdl", args.pdl)
+    if args.two_step_producer >= 0 and phys == "psv":
+        sim.set_option("two_step_producer", args.two_step_producer)
     two_step = args.two_step != 0   # the engine's default for PSV alone and SH alone is on
     sim.upload_model("vp", W["vp"])
     sim.upload_model("vs", W["vs"])
@@ -333,6 +335,8 @@ def run_ours(args, rank, world):
     # (two-step rows are fetched by tensor copies unless --tma 0)
     kernel = (f"{phys}_step2_tma_kernel" if args.tma != 0 else f"{phys}_step2_kernel") if two_step \
         else f"{phys}_step_kernel"
+    if two_step and args.tma != 0 and args.two_step_producer != 0 and phys == "psv":
+        kernel = "psv_step2_pc_kernel"   # the default: rows from producer warps
     per_launch = 2 if two_step else 1
     launch_s = ms_per_step / 1e3 / (nt / per_launch)
     achieved = BYTES_PER_CELL[phys] * nx * nz / launch_s / 1e9
@@ -840,6 +844,8 @@ def main():
     ap.add_argument("--two-step", type=int, default=-1,
                     help="c2: two time steps per launch (1), one (0), or the engine's default (-1: two)")
     ap.add_argument("--two-step-rows", type=int, default=0)
+    ap.add_argument("--two-step-producer", type=int, default=-1,
+                    help="c2 (PSV): two-step rows fetched by producer warps (1, the default) or by every march (0)")
     ap.add_argument("--two-step-recompute", type=int, default=-1,
                     help="c5: grouped launches recompute two steps per operation (1) or one (0); -1: the default")
     ap.add_argument("--tma", type=int, default=-1,

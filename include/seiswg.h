@@ -212,7 +212,10 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * runs advance two time steps per launch; PSV alone (no SH, no spin) or SH
  * alone, and on by default there; multiply-add contraction, so results
  * match the one-step kernel to rounding), "two_step_rows" (rows per march of
- * the two-step kernel; 0: its occupancy model), "cluster" (0/1: SH grids
+ * the two-step kernel; 0: its occupancy model), "two_step_producer" (0/1,
+ * default 1: PSV two-step launches with tensor copies take their rows from
+ * producer warps, one per march, instead of each march issuing its own
+ * copies; the same results), "cluster" (0/1: SH grids
  * whose state and material fit one thread-block cluster's shared memory run
  * each forward pass in one launch with the wavefield on chip; default on;
  * results are the one-step kernel's bits), "tma" (0/1: the two-step and the

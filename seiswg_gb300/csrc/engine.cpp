@@ -339,7 +339,8 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
   if (tma_ready() && a.sxx - a.vz == ds && a.szz - a.sxx == ds && a.sxz - a.szz == ds &&
       encode_fields(&tma_.sig, a.vx, ds, 5, ld_, rows_alloc, 3) &&
       encode_fields(&tma_.vel, a.vx, ds, 5, ld_, rows_alloc, 2)) {
-    SW_CUDA(launch_psv_step2_tma(p, tma_, stream_));
+    if (two_step_pc_) SW_CUDA(launch_psv_step2_pc(p, tma_, stream_));
+    else SW_CUDA(launch_psv_step2_tma(p, tma_, stream_));
   } else {
     SW_CUDA(launch_psv_step2(p, stream_));
   }

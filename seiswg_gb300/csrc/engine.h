@@ -210,6 +210,10 @@ class Sim {
   void set_two_step(bool on);
   void set_two_step_rows(int lx);
   bool two_step() const { return two_step_; }
+  // Two-step PSV launches with tensor copies take their rows from producer
+  // warps (launch_psv_step2_pc; default on) or issue the copies in every
+  // march (launch_psv_step2_tma); the same bits.
+  void set_two_step_producer(bool on) { two_step_pc_ = on; }
   // Small SH grids run whole forward passes in one thread-block cluster when
   // state and material fit its shared memory (default on).
   void set_use_cluster(bool on) { use_cluster_ = on; }
@@ -284,6 +288,7 @@ class Sim {
   Geom geom_{};
   Geom geom2_{};            // decomposition of the two-step kernel (lx 0: not yet modelled)
   bool two_step_ = false;
+  bool two_step_pc_ = true;
   bool use_cluster_ = true;
   bool use_tma_ = true;
   int tma_mat_ = -1;   // material tensor maps: -1 not yet encoded, 0 unavailable, 1 in tma_

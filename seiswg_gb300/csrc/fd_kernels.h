@@ -111,6 +111,10 @@ struct Tma2 {
   CUtensorMap sig, vel, rho, lm;
 };
 cudaError_t launch_psv_step2_tma(const PsvStep& p, const Tma2& t, cudaStream_t s);
+// The same launch with every row copy issued by a producer warpgroup
+// (fd_step2pc.cu): eight marches of p.g per CTA; bitwise the results of
+// launch_psv_step2_tma.
+cudaError_t launch_psv_step2_pc(const PsvStep& p, const Tma2& t, cudaStream_t s);
 // Tensor maps of the PSV reverse step: the forward state (vx, vz, sxx, szz,
 // sxz) with boxes of 1 and 2 fields, the incoming adjoint state (same field
 // order) with boxes of 3 and 2, the material (1/rho, lambda, mu) with boxes of

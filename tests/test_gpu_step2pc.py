@@ -1,0 +1,118 @@
+"""The two-step PSV kernel with its rows fetched by a producer warpgroup (the
+Sim option "two_step_producer") against the kernel whose marches issue their
+own copies: the marches are the same code on the same rows, so traces,
+snapshots, the final state and the exact gradient (whose recording launches
+also store the state between their two steps) are bitwise equal.  Cases:
+those of the two-step tests (grids narrower than one strip, strip and chunk
+boundaries, odd nt, snapshot steps that split a pair, receivers and sources
+on the edges, every taper edge, chunks shorter than the two-step reach), a
+grid of many strips and chunks, and an expired row wait, reported as a
+timeout with the handle usable afterwards."""
+import numpy as np
+import pytest
+
+from tests.test_gpu_parity import _model
+from tests.test_gpu_two_step import CASES, FIELDS, SNAP
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim(sw, nx, nz, nt, src, rec, pc, rows=0, **flags):
+    dt = 1.2e-3
+    stf = np.stack([sw.ricker(nt, dt, s[2], s[3], s[4], 1.0e10) for s in src], axis=1)
+    sim = sw.Sim(nx, nz, nt, 10.0, 10.0, dt, psv=True, **flags)
+    for k, v in _model(nx, nz, 0).items():
+        sim.upload_model(k, v)
+    sim.prepare()
+    sim.set_sources([s[0] for s in src], [s[1] for s in src], stf)
+    sim.set_receivers([r[0] for r in rec], [r[1] for r in rec])
+    sim.set_option("two_step", 1)
+    sim.set_option("two_step_producer", pc)
+    if rows:
+        sim.set_option("two_step_rows", rows)
+    return sim
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_forward_is_bitwise_the_self_issuing_kernel(case):
+    import seiswg_gb300 as sw
+
+    nx, nz, nt, src, rec, rows, snap, flags = CASES[case]
+    out = []
+    for pc in (0, 1):
+        with _sim(sw, nx, nz, nt, src, rec, pc, rows, **flags) as sim:
+            snaps = sim.forward(-1, snap, SNAP["psv"] if snap else [])
+            out.append((sim.traces(), snaps, [sim.state(f) for f in FIELDS["psv"]]))
+    (t0, s0, f0), (t1, s1, f1) = out
+    assert np.abs(t0).max() > 0
+    assert np.array_equal(t0, t1)
+    assert (s0 is None and s1 is None) or np.array_equal(s0, s1)
+    for a, b in zip(f0, f1):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("rows", [0, 6, 40])
+def test_large_grid_forward_is_bitwise_the_self_issuing_kernel(rows):
+    """A grid of many strips and chunks (the model chunk rows, chunks shorter
+    than the reach, long chunks), a source in the interior."""
+    import seiswg_gb300 as sw
+
+    nx, nz, nt = 700, 900, 60
+    src = [(350, 450, 20.0, 0.03, 0.0), (120, 800, 25.0, 0.03, 30.0)]
+    rec = [(i, 300) for i in range(3, 700, 17)] + [(350, j) for j in range(0, 900, 23)]
+    flags = dict(abs_left=True, abs_right=True, abs_bottom=True, abs_width=20)
+    out = []
+    for pc in (0, 1):
+        with _sim(sw, nx, nz, nt, src, rec, pc, rows, **flags) as sim:
+            sim.forward(-1)
+            out.append((sim.traces(), [sim.state(f) for f in FIELDS["psv"]]))
+    assert np.array_equal(out[0][0], out[1][0])
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.abs(a).max() > 0
+        assert np.array_equal(a, b)
+
+
+def test_gradient_is_bitwise_the_self_issuing_kernel():
+    """The exact gradient: every state kept, the recording launches storing
+    the state between their two steps (the producer kernel's MID
+    instantiation)."""
+    import seiswg_gb300 as sw
+
+    nx, nz, nt = 140, 200, 150
+    src = [(70, 60, 20.0, 0.05, 30.0)]
+    rec = [(i, 100) for i in range(2, nx - 2, 7)]
+    grads = []
+    for pc in (0, 1):
+        with _sim(sw, nx, nz, nt, src, rec, pc, abs_left=True, abs_bottom=True, abs_width=10) as sim:
+            sim.gradient_clear()
+            sim.forward_op(0, 0)
+            syn = sim.traces()[[0, 2]]
+            _, adj = sw.l2_misfit(syn, 0.9 * syn, 1.2e-3)
+            sim.backward_op(adj)
+            grads.append([sim.gradient(p) for p in ("lambda", "mu", "buoyancy")])
+    for a, b in zip(grads[0], grads[1]):
+        assert np.abs(a).max() > 0
+        assert np.array_equal(a, b)
+
+
+def test_expired_wait_reports_timeout_and_the_handle_recovers():
+    """Row 0 of every march armed for 16 bytes more than its copies: each
+    march gives up at its first row, its producer at the stage it can no
+    longer refill (after counting the extra bytes and waiting for its copies),
+    the run reports a timeout, and the same handle then runs normally."""
+    import seiswg_gb300 as sw
+
+    nx, nz, nt, src, rec, _, _, flags = CASES[1]
+    with _sim(sw, nx, nz, nt, src, rec, 0, **flags) as clean:
+        clean.forward(-1)
+        want = clean.traces()
+    with _sim(sw, nx, nz, nt, src, rec, 1, **flags) as sim:
+        sim.set_option("wait_polls", 4096)
+        sim.set_option("test_arm_extra", 16)
+        with pytest.raises(sw.SeiswgError) as e:
+            sim.forward(-1)
+        assert e.value.code == sw.ETIMEOUT and "bounded wait" in str(e.value)
+        sim.set_option("test_arm_extra", 0)
+        sim.set_option("wait_polls", 0)
+        sim.forward(-1)
+        assert np.array_equal(sim.traces(), want)
