@@ -828,7 +828,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nt", type=int, default=4000)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--ref-sample", type=int, default=600, help="oracle steps in the CPU sample (~10 s)")
     ap.add_argument("--chunk-rows", type=int, default=0)
     ap.add_argument("--grid", type=int, default=4096, help="grid edge (4096 = the headline workload)")
