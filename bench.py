@@ -585,6 +585,8 @@ def run_secondary(args):
             sim.set_option("tma", args.tma)
         if args.pdl >= 0:
             sim.set_option("pdl", args.pdl)
+        if args.reverse_producer >= 0:
+            sim.set_option("reverse_producer", args.reverse_producer)
         if args.checkpoint_slots:
             sim.set_option("checkpoint_slots", args.checkpoint_slots)
         if args.checkpoint_budget_mb:
@@ -846,6 +848,8 @@ def main():
     ap.add_argument("--two-step-rows", type=int, default=0)
     ap.add_argument("--two-step-producer", type=int, default=-1,
                     help="c2 (PSV): two-step rows fetched by producer warps (1, the default) or by every march (0)")
+    ap.add_argument("--reverse-producer", type=int, default=-1,
+                    help="c4: PSV reverse-step rows fetched by producer warps (1, the default) or by every march (0)")
     ap.add_argument("--two-step-recompute", type=int, default=-1,
                     help="c5: grouped launches recompute two steps per operation (1) or one (0); -1: the default")
     ap.add_argument("--tma", type=int, default=-1,

@@ -215,7 +215,8 @@ int seiswg_sim_release_workspace(seiswg_sim* sim);
  * the two-step kernel; 0: its occupancy model), "two_step_producer" (0/1,
  * default 1: PSV two-step launches with tensor copies take their rows from
  * producer warps, one per march, instead of each march issuing its own
- * copies; the same results), "cluster" (0/1: SH grids
+ * copies; the same results), "reverse_producer" (0/1, default 1: the same
+ * for the PSV reverse step), "cluster" (0/1: SH grids
  * whose state and material fit one thread-block cluster's shared memory run
  * each forward pass in one launch with the wavefield on chip; default on;
  * results are the one-step kernel's bits), "tma" (0/1: the two-step and the

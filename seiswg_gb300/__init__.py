@@ -430,7 +430,7 @@ class Sim:
 
     def set_option(self, key: str, value: int):
         """The options of seiswg_sim_set_option (include/seiswg.h): "graphs", "chunk_rows", "loader",
-        "two_step", "two_step_rows", "two_step_producer", "cluster", "tma", "pdl", "autotune", "stability_check",
+        "two_step", "two_step_rows", "two_step_producer", "reverse_producer", "cluster", "tma", "pdl", "autotune", "stability_check",
         "checkpoint_slots", "checkpoint_budget_mb", "wait_polls", "test_arm_extra"."""
         _check(lib().seiswg_sim_set_option(self._h, key.encode(), int(value)))
 

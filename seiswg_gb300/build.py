@@ -34,11 +34,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-
 # The reverse step (no counterpart in the reference), the two-step forward
 # kernel and the spin kernel are issue-bound, so they contract multiply-add
 # pairs.
-FMAD = {"fd_adjoint.cu": "true", "fd_step2.cu": "true", "fd_step2pc.cu": "true", "fd_spin.cu": "true", "fd_queue.cu": "true"}
+FMAD = {"fd_adjoint.cu": "true", "fd_step2.cu": "true", "fd_step2pc.cu": "true", "fd_adjointpc.cu": "true", "fd_spin.cu": "true", "fd_queue.cu": "true"}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fno-strict-aliasing", "-Wall", "-Wextra", f"-I{CUDA_HOME}/include",
              f"-I{os.path.join(ROOT, 'include')}"]
 
-CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_step2pc.cu", "fd_spin.cu", "fd_cluster.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_batch.cu", "fd_queue.cu", "noalloc.cu"]
+CU_SOURCES = ["fd_step.cu", "fd_step2.cu", "fd_step2pc.cu", "fd_spin.cu", "fd_cluster.cu", "fd_aux.cu", "fd_adjoint.cu", "fd_adjointpc.cu", "fd_batch.cu", "fd_queue.cu", "noalloc.cu"]
 CXX_SOURCES = ["engine.cpp", "host.cpp", "batch.cpp", "capi.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 

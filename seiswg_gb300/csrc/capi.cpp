@@ -481,6 +481,7 @@ int seiswg_sim_set_option(seiswg_sim* s, const char* key, int64_t value) {
     else if (k == "two_step") sim.set_two_step(value != 0);
     else if (k == "two_step_rows") sim.set_two_step_rows(int(value));
     else if (k == "two_step_producer") sim.set_two_step_producer(value != 0);
+    else if (k == "reverse_producer") sim.set_reverse_producer(value != 0);
     else if (k == "cluster") sim.set_use_cluster(value != 0);
     else if (k == "tma") sim.set_use_tma(value != 0);
     else if (k == "autotune") sim.autotune(int(value));

@@ -280,7 +280,8 @@ bool Sim::launch_adjoint_tma(const PsvAdjoint& p, const State& f, const State& a
       !encode_fields(&tma_adj_.a3, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 3) ||
       !encode_fields(&tma_adj_.a2, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 2))
     return false;
-  SW_CUDA(launch_psv_adjoint_tma(p, tma_adj_, stream_));
+  if (reverse_pc_) SW_CUDA(launch_psv_adjoint_pc(p, tma_adj_, stream_));
+  else SW_CUDA(launch_psv_adjoint_tma(p, tma_adj_, stream_));
   return true;
 }
 

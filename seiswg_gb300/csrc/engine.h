@@ -213,7 +213,19 @@ class Sim {
   // Two-step PSV launches with tensor copies take their rows from producer
   // warps (launch_psv_step2_pc; default on) or issue the copies in every
   // march (launch_psv_step2_tma); the same bits.
-  void set_two_step_producer(bool on) { two_step_pc_ = on; }
+  void set_two_step_producer(bool on) {
+    two_step_pc_ = on;
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+  }
+  // PSV reverse steps with tensor copies take their rows from producer warps
+  // (launch_psv_adjoint_pc; default on) or issue the copies in every march;
+  // the same bits.
+  void set_reverse_producer(bool on) {
+    reverse_pc_ = on;
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+  }
   // Small SH grids run whole forward passes in one thread-block cluster when
   // state and material fit its shared memory (default on).
   void set_use_cluster(bool on) { use_cluster_ = on; }
@@ -289,6 +301,7 @@ class Sim {
   Geom geom2_{};            // decomposition of the two-step kernel (lx 0: not yet modelled)
   bool two_step_ = false;
   bool two_step_pc_ = true;
+  bool reverse_pc_ = true;
   bool use_cluster_ = true;
   bool use_tma_ = true;
   int tma_mat_ = -1;   // material tensor maps: -1 not yet encoded, 0 unavailable, 1 in tma_

@@ -168,6 +168,10 @@ struct ShAdjoint {
 int adjoint_blocks_per_sm(bool psv, int loader);
 cudaError_t launch_psv_adjoint(const PsvAdjoint& p, cudaStream_t s);
 cudaError_t launch_psv_adjoint_tma(const PsvAdjoint& p, const TmaAdj& t, cudaStream_t s);
+// The same reverse step with every row copy issued by producer warps
+// (fd_adjointpc.cu): eight marches of p.g per CTA; bitwise the results of
+// launch_psv_adjoint_tma.
+cudaError_t launch_psv_adjoint_pc(const PsvAdjoint& p, const TmaAdj& t, cudaStream_t s);
 cudaError_t launch_sh_adjoint(const ShAdjoint& p, cudaStream_t s);
 
 // ---- grouped launches over many independent jobs (fd_step.cu, fd_adjoint.cu,

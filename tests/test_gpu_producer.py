@@ -1,13 +1,14 @@
-"""The two-step PSV kernel with its rows fetched by a producer warpgroup (the
-Sim option "two_step_producer") against the kernel whose marches issue their
-own copies: the marches are the same code on the same rows, so traces,
-snapshots, the final state and the exact gradient (whose recording launches
-also store the state between their two steps) are bitwise equal.  Cases:
-those of the two-step tests (grids narrower than one strip, strip and chunk
-boundaries, odd nt, snapshot steps that split a pair, receivers and sources
-on the edges, every taper edge, chunks shorter than the two-step reach), a
-grid of many strips and chunks, and an expired row wait, reported as a
-timeout with the handle usable afterwards."""
+"""Kernels whose rows are fetched by producer warps (fd_producer.cuh) against
+the kernels whose marches issue their own copies: the marches are the same
+code on the same rows, so the results are bitwise equal.  The two-step PSV
+kernel (the Sim option "two_step_producer"): traces, snapshots and the final
+state on the cases of the two-step tests (grids narrower than one strip,
+strip and chunk boundaries, odd nt, snapshot steps that split a pair,
+receivers and sources on the edges, every taper edge, chunks shorter than the
+two-step reach) and a grid of many strips and chunks, and the exact gradient,
+whose recording launches also store the state between their two steps.  The
+PSV reverse step ("reverse_producer"): the gradient.  Both: an expired row
+wait is reported as a timeout and the handle stays usable."""
 import numpy as np
 import pytest
 
@@ -116,3 +117,64 @@ def test_expired_wait_reports_timeout_and_the_handle_recovers():
         sim.set_option("wait_polls", 0)
         sim.forward(-1)
         assert np.array_equal(sim.traces(), want)
+
+
+@pytest.mark.parametrize("nt", [150, 151])
+def test_reverse_step_gradient_is_bitwise_the_self_issuing_kernel(nt):
+    """The PSV reverse step with producer warps: the same gradient bits,
+    every state kept or every second one (recomputation between)."""
+    import seiswg_gb300 as sw
+
+    nx, nz = 140, 230
+    src = [(70, 60, 20.0, 0.05, 30.0)]
+    rec = [(i, 100) for i in range(2, nx - 2, 7)]
+    for k in (0, 2):
+        grads = []
+        for rp in (0, 1):
+            with _sim(sw, nx, nz, nt, src, rec, 1, abs_left=True, abs_bottom=True, abs_width=10) as sim:
+                sim.set_option("reverse_producer", rp)
+                sim.gradient_clear()
+                sim.forward_op(0, k)
+                syn = sim.traces()[[0, 2]]
+                _, adj = sw.l2_misfit(syn, 0.9 * syn, 1.2e-3)
+                sim.backward_op(adj)
+                grads.append([sim.gradient(p) for p in ("lambda", "mu", "buoyancy")])
+        for a, b in zip(grads[0], grads[1]):
+            assert np.abs(a).max() > 0
+            assert np.array_equal(a, b), k
+
+
+def test_reverse_step_expired_wait_reports_timeout_and_the_handle_recovers():
+    """Row 0 of every reverse march armed for 16 bytes more than its copies:
+    the reverse sweep reports a timeout (read with the gradient), and the same
+    handle then gives the gradient of a clean run."""
+    import seiswg_gb300 as sw
+
+    nx, nz, nt = 96, 140, 40
+    src = [(48, 40, 25.0, 0.04, 30.0)]
+    rec = [(i, 70) for i in range(5, nx - 5, 9)]
+    with _sim(sw, nx, nz, nt, src, rec, 1, abs_left=True, abs_bottom=True, abs_width=10) as sim:
+        sim.set_option("reverse_producer", 1)
+        sim.gradient_clear()
+        sim.forward_op(0, 0)
+        syn = sim.traces()[[0, 2]]
+        _, adj = sw.l2_misfit(syn, 0.5 * syn, 1.2e-3)
+        sim.backward_op(adj)
+        want = sim.gradient("mu")
+        assert np.abs(want).max() > 0
+        sim.gradient_clear()
+        sim.forward_op(0, 0)
+        sim.traces()
+        sim.set_option("wait_polls", 4096)
+        sim.set_option("test_arm_extra", 16)
+        sim.backward_op(adj)
+        with pytest.raises(sw.SeiswgError) as e:
+            sim.gradient("mu")
+        assert e.value.code == sw.ETIMEOUT
+        sim.set_option("test_arm_extra", 0)
+        sim.set_option("wait_polls", 0)
+        sim.gradient_clear()
+        sim.forward_op(0, 0)
+        sim.traces()
+        sim.backward_op(adj)
+        assert np.array_equal(sim.gradient("mu"), want)
