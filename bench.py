@@ -764,6 +764,8 @@ def run_secondary(args):
             batch.set_option("checkpoint_slots", args.checkpoint_slots)
         if args.two_step_recompute >= 0:
             batch.set_option("two_step_recompute", args.two_step_recompute)
+        if args.reverse_producer >= 0:
+            batch.set_option("reverse_producer", args.reverse_producer)
         tune_ms = None
         if args.autotune:
             t0 = time.perf_counter()
@@ -849,7 +851,8 @@ def main():
     ap.add_argument("--two-step-producer", type=int, default=-1,
                     help="c2 (PSV): two-step rows fetched by producer warps (1, the default) or by every march (0)")
     ap.add_argument("--reverse-producer", type=int, default=-1,
-                    help="c4: PSV reverse-step rows fetched by producer warps (1, the default) or by every march (0)")
+                    help="c4, c5: PSV reverse-step rows fetched by producer warps (1; the default for c4, not c5) "
+                         "or by every march (0)")
     ap.add_argument("--two-step-recompute", type=int, default=-1,
                     help="c5: grouped launches recompute two steps per operation (1) or one (0); -1: the default")
     ap.add_argument("--tma", type=int, default=-1,

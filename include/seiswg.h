@@ -264,7 +264,9 @@ int seiswg_batch_run(seiswg_batch* batch);
 /* key "chunk_rows": rows per warp chunk of every job (0: each problem's own
  * chunk model); "two_step" (0/1): jobs whose problem runs two steps per
  * launch (PSV alone, SH alone) record their forward pass that way (default
- * 1); "two_step_recompute" (0/1, default 1): such jobs also recompute the
+ * 1); "reverse_producer" (0/1, default 0): grouped PSV reverse launches
+ * take their rows from producer warps (every job by tensor copies; the same
+ * results); "two_step_recompute" (0/1, default 1): such jobs also recompute the
  * states of each checkpoint interval two steps per grouped launch, each
  * launch storing both states (launch order 3 recomputes one step per
  * operation); "autotune": tries

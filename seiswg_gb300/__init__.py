@@ -482,7 +482,8 @@ class Batch:
         _check(lib().seiswg_batch_run(self._h))
 
     def set_option(self, key: str, value: int):
-        """"chunk_rows" (0: per-problem model), "two_step" (0/1), "two_step_recompute" (0/1: the
+        """"chunk_rows" (0: per-problem model), "two_step" (0/1), "reverse_producer" (0/1: grouped PSV
+        reverse launches with rows from producer warps), "two_step_recompute" (0/1: the
         intervals' states recomputed two steps per grouped launch), "concurrent" (0, 1, 2: grouped
         launches in that order; 3: one persistent launch over a device queue), "stream_groups" (1..4),
         "tma" (0/1: rows of the two-step and reverse marches by tensor copies or bulk copies), "pdl" (0/1:

@@ -601,7 +601,12 @@ void Batch::launch_kind(const Launch& l, cudaStream_t s) {
     case kFwd2Sh: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, false, pdl_, s)); break;
     case kFwd2Psv: SW_CUDA(launch_grouped_forward2(d_jobs_, ops, l.count, l.warps, true, pdl_, s)); break;
     case kAdjSh: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, false, pdl_, s)); break;
-    case kAdjPsv: SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, pdl_, s)); break;
+    case kAdjPsv:
+      if (reverse_pc_ && tma_jobs() == int(descs_.size()))
+        SW_CUDA(launch_grouped_adjoint_pc(d_jobs_, ops, l.count, l.warps, pdl_, s));
+      else
+        SW_CUDA(launch_grouped_adjoint(d_jobs_, ops, l.count, l.warps, true, pdl_, s));
+      break;
     case kMisfit: SW_CUDA(launch_grouped_misfit(d_jobs_, ops, l.count, s)); break;
   }
   ++launches_per_run_;

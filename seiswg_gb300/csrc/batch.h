@@ -57,6 +57,15 @@ class Batch {
   // operation, storing both states (default on; launch order 3 always
   // recomputes one step per operation); rebuilds the schedule.
   void set_two_step_recompute(bool on);
+  // Grouped PSV reverse launches take their rows from producer warps when
+  // every job fetches by tensor copies (default off: a producer CTA takes a
+  // whole SM, which packs worse beside the other kinds' launches); drops the
+  // graph.
+  void set_reverse_producer(bool on) {
+    reverse_pc_ = on;
+    if (graph_) cudaGraphExecDestroy(graph_);
+    graph_ = nullptr;
+  }
   // How the schedule runs.  0: one grouped launch per (slot, kind), one
   // after another on the batch's stream.  1: the launches of one slot run
   // concurrently on forked streams that join before the next slot.  2: one
@@ -144,6 +153,7 @@ class Batch {
   int chunk_rows_ = 0;
   bool two_step_ = true;
   bool pair_ = true;  // two-step recomputation (set_two_step_recompute)
+  bool reverse_pc_ = false;
   size_t ops_bytes_ = 0;
 
   std::vector<BatchProblem> problems_;

@@ -545,6 +545,7 @@ int seiswg_batch_set_option(seiswg_batch* b, const char* key, int64_t value) {
     else if (k == "autotune") b->batch->autotune(int(value));
     else if (k == "two_step") b->batch->set_two_step(value != 0);
     else if (k == "two_step_recompute") b->batch->set_two_step_recompute(value != 0);
+    else if (k == "reverse_producer") b->batch->set_reverse_producer(value != 0);
     else if (k == "concurrent") b->batch->set_concurrent(int(value));
     else if (k == "stream_groups") b->batch->set_stream_groups(int(value));
     else if (k == "tma") b->batch->set_tma(value != 0);

@@ -259,6 +259,10 @@ cudaError_t launch_grouped_forward(const JobDesc* jobs, const GroupOp* ops, int 
                                    bool pdl, cudaStream_t s);
 cudaError_t launch_grouped_adjoint(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,
                                    bool pdl, cudaStream_t s);
+// The grouped PSV reverse launch with every row copy issued by producer
+// warps (fd_adjointpc.cu); every job of the launch needs its map table.
+cudaError_t launch_grouped_adjoint_pc(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool pdl,
+                                      cudaStream_t s);
 // Two PSV (psv) or SH steps (op.it, op.it + 1) of every op's job, with the
 // jobs' g2.
 cudaError_t launch_grouped_forward2(const JobDesc* jobs, const GroupOp* ops, int nops, int warps, bool psv,

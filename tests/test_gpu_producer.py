@@ -7,8 +7,9 @@ strip and chunk boundaries, odd nt, snapshot steps that split a pair,
 receivers and sources on the edges, every taper edge, chunks shorter than the
 two-step reach) and a grid of many strips and chunks, and the exact gradient,
 whose recording launches also store the state between their two steps.  The
-PSV reverse step ("reverse_producer"): the gradient.  Both: an expired row
-wait is reported as a timeout and the handle stays usable."""
+PSV reverse step ("reverse_producer" of a Sim and of a Batch): the gradient.
+Both: an expired row wait is reported as a timeout and the handle stays
+usable."""
 import numpy as np
 import pytest
 
@@ -178,3 +179,35 @@ def test_reverse_step_expired_wait_reports_timeout_and_the_handle_recovers():
         sim.traces()
         sim.backward_op(adj)
         assert np.array_equal(sim.gradient("mu"), want)
+
+
+def test_batch_reverse_launches_are_bitwise_the_self_issuing_kernel():
+    """The batch's grouped PSV reverse launches with producer warps (the
+    Batch option "reverse_producer"; each producer warp finds its march's job
+    and op as the march does): the same gradients and misfits, in every
+    grouped launch order."""
+    import seiswg_gb300 as sw
+    from tests.test_gpu_batch import _problems
+
+    probs = _problems()
+    sims = [w.make_sim() for (w, _, _) in probs]
+    batch = sw.Batch(sims, [obs for (_, obs, _) in probs])
+    try:
+        ref = None
+        for mode, rp in ((2, 0), (2, 1), (0, 1), (1, 1)):
+            batch.set_option("concurrent", mode)
+            batch.set_option("reverse_producer", rp)
+            batch.run()
+            g = [batch.gradient(i, p) for i in range(len(probs)) for p in ("lambda", "mu", "buoyancy")]
+            J = [batch.misfit(i) for i in range(len(probs))]
+            if ref is None:
+                ref = (g, J)
+                assert any(np.abs(a).max() > 0 for a in g)
+                continue
+            assert J == ref[1], (mode, rp)
+            for a, b in zip(g, ref[0]):
+                assert np.array_equal(a, b), (mode, rp)
+    finally:
+        batch.close()
+        for s in sims:
+            s.close()
