@@ -1,6 +1,6 @@
 // fd_producer.cuh -- row rings filled by producer warps (warp specialisation
 // of the copies, not of the arithmetic), shared by the two-step kernel
-// (fd_step2pc.cu) and the PSV reverse step (fd_adjointpc.cu).
+// (fd_step2pc.cu) and the PSV reverse steps (fd_adjointpc.cu).
 //
 // In the self-issuing kernels every march issues its own row copies: each
 // iteration lane 0 arms the stage's barrier and issues the row's tensor
@@ -118,11 +118,12 @@ __device__ __forceinline__ void pc_init(unsigned char* smem) {
   __syncthreads();
 }
 
-// One producer lane: the copies of rows 0 .. nk-1 of a march, row k at
-// padded row y0 + k and padded column x0 (Plan::issue), into ring `slice`.
-template <class Rows, class Plan, class M>
-__device__ __forceinline__ void pc_produce(const M* tm, unsigned char* slice, int x0, int y0, int nk, const Geom& g,
-                                           int* err) {
+// One producer lane: the copies of rows 0 .. nk-1 of a march into ring
+// `slice`, issue(stage buffer, k, barrier) issuing row k's (after the barrier
+// is armed with the stage's bytes).
+template <class Rows, class Issue>
+__device__ __forceinline__ void pc_produce_with(unsigned char* slice, int nk, const Geom& g, int* err,
+                                                const Issue& issue) {
   constexpr int S = Rows::S;
   float* buf = reinterpret_cast<float*>(slice);
   uint64_t* full = reinterpret_cast<uint64_t*>(slice + size_t(S) * Rows::kStageBytes);
@@ -140,12 +141,21 @@ __device__ __forceinline__ void pc_produce(const M* tm, unsigned char* slice, in
     }
     fence_proxy_async();  // the consumer's reads of the stage before the copies that refill it
     mbar_expect_tx(&full[s], Rows::kStageBytes + (k == 0 ? extra : 0u));
-    Plan::issue(buf + size_t(s) * Rows::NSEG * kSegFloats, tm, x0, y0 + k, &full[s]);
+    issue(buf + size_t(s) * Rows::NSEG * kSegFloats, k, &full[s]);
   }
   // Row 0 never completes with the test hook's extra bytes (its consumer and
   // then this loop give up): count them, then wait for every issued copy.
   if (extra && k > 0) mbar_complete_tx(&full[0], extra);
   for (int r = k > S ? k - S : 0; r < k; ++r) (void)mbar_wait(&full[r % S], uint32_t(r / S) & 1u, lim);
+}
+
+// The same with a tensor-copy plan: row k at padded row y0 + k and padded
+// column x0 (Plan::issue).
+template <class Rows, class Plan, class M>
+__device__ __forceinline__ void pc_produce(const M* tm, unsigned char* slice, int x0, int y0, int nk, const Geom& g,
+                                           int* err) {
+  pc_produce_with<Rows>(slice, nk, g, err,
+                        [&](float* sb, int k, uint64_t* bar) { Plan::issue(sb, tm, x0, y0 + k, bar); });
 }
 
 // The register split of the CTA's warpgroups: true in a consumer warp.
