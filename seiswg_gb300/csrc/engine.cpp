@@ -280,8 +280,17 @@ bool Sim::launch_adjoint_tma(const PsvAdjoint& p, const State& f, const State& a
       !encode_fields(&tma_adj_.a3, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 3) ||
       !encode_fields(&tma_adj_.a2, a.vx, a.vz - a.vx, 5, ld_, rows_alloc, 2))
     return false;
-  if (reverse_pc_) SW_CUDA(launch_psv_adjoint_pc(p, tma_adj_, stream_));
-  else SW_CUDA(launch_psv_adjoint_tma(p, tma_adj_, stream_));
+  // A producer kernel whose launch register count differs from its register
+  // split's is refused before any launch (pc_kernel_ready): the march then
+  // issues its own copies.
+  const cudaError_t e = reverse_pc_ ? launch_psv_adjoint_pc(p, tma_adj_, stream_) : cudaErrorInvalidConfiguration;
+  if (e == cudaErrorInvalidConfiguration) {
+    (void)cudaGetLastError();
+    reverse_pc_ = false;
+    SW_CUDA(launch_psv_adjoint_tma(p, tma_adj_, stream_));
+  } else {
+    SW_CUDA(e);
+  }
   return true;
 }
 
@@ -340,8 +349,14 @@ void Sim::enqueue_step2(int it, const State& a, const State& o, const InjectList
   if (tma_ready() && a.sxx - a.vz == ds && a.szz - a.sxx == ds && a.sxz - a.szz == ds &&
       encode_fields(&tma_.sig, a.vx, ds, 5, ld_, rows_alloc, 3) &&
       encode_fields(&tma_.vel, a.vx, ds, 5, ld_, rows_alloc, 2)) {
-    if (two_step_pc_) SW_CUDA(launch_psv_step2_pc(p, tma_, stream_));
-    else SW_CUDA(launch_psv_step2_tma(p, tma_, stream_));
+    const cudaError_t e = two_step_pc_ ? launch_psv_step2_pc(p, tma_, stream_) : cudaErrorInvalidConfiguration;
+    if (e == cudaErrorInvalidConfiguration) {  // refused before any launch, as above
+      (void)cudaGetLastError();
+      two_step_pc_ = false;
+      SW_CUDA(launch_psv_step2_tma(p, tma_, stream_));
+    } else {
+      SW_CUDA(e);
+    }
   } else {
     SW_CUDA(launch_psv_step2(p, stream_));
   }
