@@ -12,8 +12,8 @@
 // arms its `full` barrier and issues its copies (Plan::issue), S - 1 - KEEP
 // rows ahead of the march, as the self-issuing ring; a producer that waits
 // holds up no other march.  The consumer waits on `full` and, once past a
-// stage's last read (KEEP rows kept for reads further back), arrives on
-// `empty`.  The marches are the self-issuing kernels' own code, reading the
+// stage's last read (KEEP rows kept for reads further back), its 32 lanes
+// arrive on `empty`.  The marches are the self-issuing kernels' own code, reading the
 // same rows, so the results are their bits.
 //
 // Registers: such a CTA is launched with 128 per thread (512 threads, one
@@ -78,8 +78,8 @@ struct PcRows {
       par ^= 1u;
     }
     // Row k - 1 - KEEP was last read (directly or as a kept row) in
-    // iteration k - 1.
-    if (lane == 0 && k > KEEP) {
+    // iteration k - 1; every lane arrives (no divergent branch per row).
+    if (k > KEEP) {
       const int rel = cur - 1 - KEEP;
       mbar_arrive_pc(&empty[rel < 0 ? rel + S : rel]);
     }
@@ -110,7 +110,7 @@ __device__ __forceinline__ void pc_init(unsigned char* smem) {
                                                   size_t(Rows::S) * Rows::kStageBytes);
       for (int s = 0; s < Rows::S; ++s) {
         mbar_init(&bar[s], 1);            // full: the producer's arming arrival and the copies' bytes
-        mbar_init(&bar[Rows::S + s], 1);  // empty: the consumer's lane 0
+        mbar_init(&bar[Rows::S + s], 32);  // empty: the consumer's 32 lanes
       }
     }
     fence_mbar_init();
