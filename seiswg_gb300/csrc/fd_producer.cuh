@@ -69,8 +69,10 @@ struct PcRows {
     pdl_wait();  // the rows a march loads itself come from the previous launch
     __syncwarp();
   }
+  // Each lane releases a stage after its own last read of it (its arrival
+  // orders its reads before the producer's refill), so no warp barrier is
+  // needed per row.
   __device__ __forceinline__ bool acquire(int k) {
-    __syncwarp();  // the previous iteration's reads are done
     cur = nxt;
     const uint32_t ph = par;
     if (++nxt == S) {
@@ -93,7 +95,7 @@ struct PcRows {
     return r;
   }
   __device__ __forceinline__ f4 seg(int q) const { return seg_back(q, 0); }
-  __device__ __forceinline__ void release() { __syncwarp(); }
+  __device__ __forceinline__ void release() {}
   __device__ __forceinline__ void drain(int) { __syncwarp(); }  // the producer drains the copies
   __host__ __device__ static constexpr size_t smem_bytes_per_warp() {
     return (size_t(S) * kStageBytes + 2 * size_t(S) * 8 + 127) / 128 * 128;
