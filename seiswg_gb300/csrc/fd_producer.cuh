@@ -13,8 +13,8 @@
 // rows ahead of the march, as the self-issuing ring; a producer that waits
 // holds up no other march.  The consumer waits on `full` and, once past a
 // stage's last read (KEEP rows kept for reads further back), its 32 lanes
-// arrive on `empty`.  The marches are the self-issuing kernels' own code, reading the
-// same rows, so the results are their bits.
+// arrive on `empty`.  The marches are the self-issuing kernels' own code,
+// reading the same rows, so the results are their bits.
 //
 // Registers: such a CTA is launched with 128 per thread (512 threads, one
 // CTA per SM, the whole register file); the producer warpgroups give back all
